@@ -1,0 +1,158 @@
+"""flibs-shaped facade over the FP64 oracle (test infrastructure only).
+
+Same function names, argument order and Python array layouts as the pyrpa
+ctypes wrappers (``libs/flibs/*.py``), so a parity test can call the oracle
+and the CUDA library through identical calls.  Conversions: a Python array
+of shape [A,B,...] is the Fortran array of shape (...,B,A); the oracle works
+on the Fortran view (``x.T`` for the 4-D tensors).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import flex_oracle as O
+
+
+def gen_irr_k_TRS(Nx, Ny, Nz):
+    return O.generate_irr_kpoint_inv(Nx, Ny, Nz)
+
+
+def gen_kpoint_weight(invk, Nk):
+    return O.get_kweight(np.asarray(invk), Nk)
+
+
+def gen_ham(klist, ham_r, rvec):
+    return np.ascontiguousarray(O.gen_ham_F(klist, ham_r, rvec).transpose(0, 2, 1))
+
+
+def get_eig(hamk):
+    w, v = O.get_eig_F(hamk.transpose(0, 2, 1))
+    return w, np.ascontiguousarray(v.transpose(0, 2, 1))
+
+
+def get_ffermi(eig, mu, temp):
+    return O.get_ffermi(eig, mu, temp)
+
+
+def gen_SCmatrix(olist, site, U, J):
+    return O.get_scmat(np.asarray(olist), np.asarray(site), U, J)
+
+
+def gen_SCmatrix_orb(olist, site, Umat, Jmat):
+    return O.get_scmat_orb(np.asarray(olist), np.asarray(site), Umat, Jmat)
+
+
+def get_chi_orb_list(Norb, site_prof=(1,)):
+    return O.get_chi_orb_list(Norb, site_prof)
+
+
+def gen_Green0(eig, uni, mu, temp, Nw):
+    return np.ascontiguousarray(O.gen_green0_F(eig, uni.transpose(0, 2, 1), mu, temp, Nw).T)
+
+
+def gen_green(selfen, hamk, mu, temp):
+    return np.ascontiguousarray(O.gen_green_F(selfen.T, hamk.transpose(0, 2, 1), mu, temp).T)
+
+
+def _grid(kmap, invk, Nx, Ny, Nz):
+    return O.KGrid(np.asarray(kmap), np.asarray(invk), Nx, Ny, Nz)
+
+
+def get_chi0_conv(Gk, kmap, invk, olist, temp, Nx, Ny, Nz):
+    chi = O.get_chi0_conv(Gk.T, _grid(kmap, invk, Nx, Ny, Nz), np.asarray(olist), temp)
+    return np.ascontiguousarray(chi.T)
+
+
+def get_chi0(Smat, Cmat, Gk, olist, kmap, invk, temp, Nx, Ny, Nz):
+    chi = O.get_chi0_conv(Gk.T, _grid(kmap, invk, Nx, Ny, Nz), np.asarray(olist), temp)
+    st = O.ckchi(chi, Smat.T, Cmat.T)[0]
+    return np.ascontiguousarray(chi.T), st
+
+
+def get_chi0_tail(Smat, Cmat, Gk, eig, uni, olist, kmap, invk, mu, temp, Nx, Ny, Nz):
+    chi = O.chi0_tail(Gk.T, eig, uni.transpose(0, 2, 1), mu, _grid(kmap, invk, Nx, Ny, Nz),
+                      np.asarray(olist), temp)
+    st = O.ckchi(chi, Smat.T, Cmat.T)[0]
+    return np.ascontiguousarray(chi.T), st
+
+
+def get_chis(chi0, Smat):
+    X = chi0.transpose(0, 2, 1)
+    return np.ascontiguousarray(O.get_chis_F(X, Smat.T).transpose(0, 2, 1))
+
+
+def get_chis_chic(chi, Smat, Cmat):
+    s, c = O.get_chis_chic_F(chi.T, Smat.T, Cmat.T)
+    return np.ascontiguousarray(s.T), np.ascontiguousarray(c.T)
+
+
+def get_eig_or_tr_chi(chi, invk, sw_eig):
+    return O.get_eig_or_tr_chi(chi.T, np.asarray(invk), sw_eig)
+
+
+def _fortran_view(a, shape):
+    """Memory of a C-contiguous array read as a Fortran array of ``shape``."""
+    return np.ascontiguousarray(a).reshape(-1).reshape(shape, order="F")
+
+
+def get_Vsigma_nosoc_flex(chi, Smat, Cmat):
+    """The reference wrapper passes Nk=len(chi), Nw=len(chi[0]) and lets the
+    library read the buffer as (Nk,Nw,Nchi,Nchi) (libs/flibs/_selfenergy.py:60-73)."""
+    Nk, Nw, Nchi = len(chi), len(chi[0]), len(Smat)
+    X = _fortran_view(chi, (Nk, Nw, Nchi, Nchi))
+    V = O.vsigma_flex_nosoc(X, Smat.T, Cmat.T)
+    return V.reshape(-1, order="F").reshape(chi.shape)
+
+
+def mkself(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, mu, fill, temp, Nw, Nx, Ny, Nz,
+           sw_out=False, sw_in=False, sub_sigma=1, scf_loop=300, eps=1.0e-4, pp=0.3, m_diis=5,
+           sw_rescale=False, sw_tail=False, sigma_scale=1.0, full=False):
+    r = O.mkself(Smat.T, Cmat.T, np.asarray(kmap), np.asarray(invk), np.asarray(olist),
+                 hamk.transpose(0, 2, 1), eig, uni.transpose(0, 2, 1), mu, fill, temp, scf_loop,
+                 pp, eps, Nx, Ny, Nz, Nw, sub_sigma=sub_sigma, m_diis=m_diis,
+                 sw_rescale=sw_rescale, sw_tail=sw_tail)
+    sig = np.ascontiguousarray(r.sigma.T)
+    return (sig, r.mu, r) if full else (sig, r.mu)
+
+
+def linearized_eliashberg(chi, Gk, uni, init_delta, Smat, Cmat, olist, plist, kmap, invk,
+                          Nx, Ny, Nz, temp, gap_sym, eps=1.0e-5, itemax=300, arnoldi_m=10,
+                          full=False):
+    r = O.lin_eliash(chi.T, Gk.T, uni.transpose(0, 2, 1), np.asarray(init_delta).T,
+                     Smat.T, Cmat.T, np.asarray(olist), np.asarray(plist), np.asarray(kmap),
+                     np.asarray(invk), temp, eps, Nx, Ny, Nz, itemax, gap_sym, arnoldi_m)
+    gap = np.ascontiguousarray(r.delta.T)
+    return (gap, r.lam, r) if full else (gap, r.lam)
+
+
+def get_initial_gap(klist, Norb, gap_sym):
+    """Band-basis initial gap [Norb, Nk] (libs/plibs/_response.py:413-462)."""
+    A = 2 * np.pi
+    kx, ky, kz = klist[:, 0], klist[:, 1], klist[:, 2]
+    rows = {0: np.ones(len(klist)), 1: np.cos(A * kx) - np.cos(A * ky),
+            2: 2 * np.cos(A * kx) * np.cos(A * ky), 3: 2 * np.sin(A * kx) * np.sin(A * ky),
+            4: 2 * np.sin(A * kx) * np.sin(A * kz), 5: 2 * np.sin(A * ky) * np.sin(A * kz),
+            -1: 2 * np.sin(A * kx), -2: 2 * np.sin(A * ky)}
+    row = rows.get(gap_sym, np.zeros(len(klist)))
+    return np.tile(row, (Norb, 1))
+
+
+def mkfk_trs_nsoc(Gk, delta):
+    return np.ascontiguousarray(O.mkfk_F(Gk.T, delta.T).T)
+
+
+def get_initial_delta(init_delta, uni, invk, Nw, gap_sym):
+    d = O.get_initial_delta(np.asarray(init_delta).T, uni.transpose(0, 2, 1), np.asarray(invk),
+                            Nw, gap_sym)
+    return np.ascontiguousarray(d.T)
+
+
+def conv_delta_orb_to_band(delta, uni, invk, plist, gap_sym):
+    out = O.conv_delta_orb_to_band_F(delta.T, uni.transpose(0, 2, 1), np.asarray(plist),
+                                     np.asarray(invk), gap_sym)
+    return np.ascontiguousarray(out.T)
+
+
+def get_plist(rvec, ham_r):
+    P = O.get_parity_prop(rvec, ham_r)
+    return np.sign(P.T[0, :])
