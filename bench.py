@@ -1,0 +1,291 @@
+#!/usr/bin/env python
+"""Time to a converged FLEX self-energy plus the linearized-Eliashberg
+eigenvalue on one GB300, for the 5-orbital 64x64x2048 model (config c2).
+
+One step = one full solve of the reference's calc_lin_eliashberg_eq path
+(mkself to the residual eps -> G -> tail-corrected chi0 -> lin_eliash), run
+through the engine's C ABI (pyrpa_gb_flex_eliash, host buffers in and out).
+  value        device seconds of the solve with the inputs already in HBM
+               (CUDA events on the library stream, between upload and download)
+  e2e          wall seconds of the whole ABI call from host buffers, copies included
+  roofline     the FFT pass kernel (the dominant kernel), timed live per launch
+               with CUDA events during the timed steps
+  cpu_baseline the oracle's per-orbital-pair FFT convolution at full size on
+               all host cores, extrapolated to one solve with this run's
+               iteration and Eliashberg-application counts
+Inputs are larger than L2 (every FFT array is >= 134 MB), so no L2 flush is
+needed between steps.  `--impl reference` prints the CPU line only.
+Under torchrun every rank solves its own copy of the model (replicas, no
+collective on the data path); the reported time is the maximum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+METRIC = "time-to-converged FLEX Σ+λ, 5-orb 64²×2048: FP32+warm-start vs plain FP64"
+# FLEX iterations and Eliashberg operator applications of one c2 solve as
+# measured by the GPU engine (FP32 bulk, eps 1e-4, DIIS 5, Arnoldi 10); the
+# CPU-only reference arm extrapolates with them.
+DEFAULT_COUNTS = {"c2": (30, 20), "c1": (30, 20), "c5": (30, 20)}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
+    p.add_argument("--precision", type=int, default=32, choices=[32, 64])
+    p.add_argument("--eps", type=float, default=1.0e-4)
+    p.add_argument("--scf-loop", type=int, default=300)
+    p.add_argument("--no-tail", action="store_true")
+    p.add_argument("--cpu-pairs", type=int, default=0, help="orbital pairs in the CPU sample (0: one per core)")
+    p.add_argument("--flex-iters", type=int, default=0)
+    p.add_argument("--applies", type=int, default=0)
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------- CPU baseline
+def _cpu_pair_worker(args):
+    """One reference orbital-pair convolution at full grid size with the
+    oracle (pad G on the full grid, two forward 4-D FFTs, the G(r,t)G(-r,-t)
+    product, one backward FFT, gather to the irreducible mesh) on random data:
+    the unit of work of chi0_conv_acc / calc_sigma / mkdelta_nsoc."""
+    Nx, Ny, Nz, Nw, reps, seed = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    sys.path.insert(0, str(ROOT))
+    from oracle import flex_oracle as FO
+    klist, kmap, invk = FO.generate_irr_kpoint_inv(Nx, Ny, Nz)
+    grid = FO.KGrid(kmap, invk, Nx, Ny, Nz)
+    rng = np.random.default_rng(seed)
+    G = (rng.standard_normal((len(klist), Nw, 1, 1)) + 1j * rng.standard_normal((len(klist), Nw, 1, 1)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        A = np.fft.fftn(grid.pad_green(G, 0, 0))
+        B = np.fft.fftn(grid.pad_green(G, 0, 0))
+        tmp = np.fft.ifftn(-A * FO._reverse_all(B))
+        grid.gather_irr(tmp, Nw)
+    return time.perf_counter() - t0, reps
+
+
+def cpu_pair_rate(cfg, npairs: int):
+    """Pairs per second on all host cores (spawned workers, one pair each)."""
+    cores = os.cpu_count() or 1
+    npairs = npairs or cores
+    work = [(cfg["Nx"], cfg["Ny"], cfg["Nz"], cfg["Nw"], 1, i) for i in range(npairs)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(processes=min(cores, npairs)) as pool:
+        res = pool.map(_cpu_pair_worker, work)
+    wall = time.perf_counter() - t0
+    return npairs / wall, min(cores, npairs), npairs, wall
+
+
+def pair_counts(cfg, tail: bool):
+    Nchi = cfg["Norb"] ** 2
+    nirr = Nchi * (Nchi + 1) // 2
+    per_iter = (3 * nirr if tail else nirr) + Nchi * Nchi
+    no = cfg["Norb"]
+    per_apply = sum(1 for a in range(no) for c in range(no) for b in range(no) for d in range(no) if a >= b)
+    final_chi0 = 3 * nirr if tail else nirr
+    return per_iter, per_apply, final_chi0
+
+
+def cpu_seconds(cfg, tail, iters, applies, rate):
+    per_iter, per_apply, final_chi0 = pair_counts(cfg, tail)
+    return (iters * per_iter + final_chi0 + applies * per_apply) / rate
+
+
+# ------------------------------------------------------------------ main
+def main():
+    a = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    sys.path.insert(0, str(ROOT))
+    from pyrpa_gb300 import models
+
+    cfg = dict(models.CONFIGS[a.config])
+    tail = not a.no_tail
+    config = {"workload": f"{a.config}: {cfg['Norb']}-orbital {cfg['Nx']}x{cfg['Ny']}x{cfg['Nz']} k-mesh, "
+                          f"{cfg['Nw']} Matsubara, FLEX+linearized Eliashberg",
+              "Norb": cfg["Norb"], "k_mesh": [cfg["Nx"], cfg["Ny"], cfg["Nz"]], "Nw": cfg["Nw"],
+              "U": cfg["U"], "J": cfg["J"], "T": cfg["temp"], "fill_per_spin": cfg["fill"], "eps": a.eps,
+              "chi0": "tail-corrected" if tail else "sharp cutoff", "warm_start": "none (cold G0 start)",
+              "parallelism": f"replicas x{a.gpus}" if a.gpus > 1 else "single GPU",
+              "l2": "inputs larger than L2 (FFT arrays >= 134 MB); no flush"}
+
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        iters, applies = (a.flex_iters or DEFAULT_COUNTS[a.config][0]), (a.applies or DEFAULT_COUNTS[a.config][1])
+        vals = []
+        for i in range(a.warmup + a.steps):
+            rate, cores, npairs, wall = cpu_pair_rate(cfg, a.cpu_pairs)
+            if i >= a.warmup:
+                vals.append(cpu_seconds(cfg, tail, iters, applies, rate))
+        v = statistics.mean(vals)
+        sample = (f"{npairs} full-size orbital-pair FFT convolutions per step on {cores} spawned numpy workers, "
+                  f"extrapolated with {iters} FLEX iterations and {applies} Eliashberg applications")
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": 0, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "c128", "data": "synthetic seeded tight-binding model",
+                "config": config,
+                "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+                "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return 0
+
+    from pyrpa_gb300 import flibs as F
+
+    F.load_library()
+    F.set_verbose(0)
+    F.set_precision(a.precision)
+    m = models.prepare(a.config)
+    c = m["cfg"]
+    call = dict(mu=m["mu"], fill=c["fill"], temp=c["temp"], Nw=c["Nw"], Nx=c["Nx"], Ny=c["Ny"], Nz=c["Nz"],
+                gap_sym=c["gap_sym"], eps=a.eps, scf_loop=a.scf_loop, sw_tail=tail, sw_rescale=True)
+
+    def solve():
+        return F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
+                             m["init"], m["plist"], **call)
+
+    for _ in range(a.warmup):
+        solve()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        dist.barrier()
+    F.fft_profile(True)
+    F.fft_stats()
+    k0 = F.kernel_launches()
+    dev, wall, res = [], [], None
+    with ClockSampler(local if world == 1 else 0) as clk:
+        for _ in range(a.steps):
+            t0 = time.perf_counter()
+            res = solve()
+            wall.append(time.perf_counter() - t0)
+            dev.append(res["compute_ms"] / 1e3)
+    F.fft_profile(False)
+    fft = F.fft_stats()
+    launches = F.kernel_launches() - k0
+    stats = F.last_stats()
+    value, e2e = max(dev), max(wall)
+    if dist is not None:
+        import torch
+        t = torch.tensor([value, e2e], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        value, e2e = float(t[0]), float(t[1])
+        dist.barrier()
+    if rank != 0:
+        return 0
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = (fft["bytes"] / (fft["ms"] / 1e3) / 1e9) if fft["ms"] > 0 else None
+    per_launch_bytes = fft["bytes"] / max(1, fft["launches"])
+    in_bytes = sum(x.nbytes for x in (m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"],
+                                        m["uni"], m["init"], m["plist"]))
+    out_bytes = res["sigmak"].nbytes + res["gap"].nbytes
+    iters, applies = int(stats["iterations"]), int(stats["applies"])
+    rate, cores, npairs, cwall = cpu_pair_rate(c, a.cpu_pairs)
+    cpu_v = cpu_seconds(c, tail, iters, applies, rate)
+    config.update({"flex_iterations": iters, "eliashberg_applications": applies, "lambda": res["lam"],
+                   "stoner": res["stoner"], "mu": res["mu"], "precision": f"fp{a.precision} bulk"})
+    line = {
+        "metric": METRIC, "value": value, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c64" if a.precision == 32 else "c128", "data": "synthetic seeded tight-binding model",
+        "config": config,
+        "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "fft_pass_kernel", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
+                     "bytes_per_launch": per_launch_bytes, "launches": fft["launches"],
+                     "avg_launch_ms": fft["ms"] / max(1, fft["launches"]), "traffic": None},
+        "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": cores, "kind": "port",
+                         "sample": f"{npairs} full-size orbital-pair FFT convolutions (oracle, numpy) in {cwall:.1f} s "
+                                   f"on {cores} spawned workers, extrapolated with this run's {iters} FLEX iterations "
+                                   f"and {applies} Eliashberg applications (FFT-pair work only)"},
+        "clocks": clk.summary(),
+        "stages_ms": {k: v for k, v in stats.items() if k.startswith("t_")},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

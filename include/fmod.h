@@ -1,0 +1,196 @@
+/* C ABI of the GB300 FLEX / RPA / linearized-Eliashberg engine (libfmod.so).
+ *
+ * Each declaration replaces the Fortran bind(C) subroutine of the pyrpa
+ * reference library cited beside it, with the same symbol name, argument
+ * order and meaning, so pyrpa's ctypes wrappers (libs/flibs/*.py) bind it
+ * unchanged.  Conventions, as in the reference:
+ *   - every argument is passed by reference (scalars included);
+ *   - int64_t = integer(c_int64_t), double = real(c_double),
+ *     double _Complex arrays are passed as double[2*n] (re, im);
+ *   - bool = logical(1) / ctypes c_bool (1 byte);
+ *   - arrays are Fortran column-major: the Fortran shape is the reverse of
+ *     the numpy shape the wrappers allocate, e.g. Gk(Nk,Nw,Norb,Norb) is the
+ *     numpy [Norb,Norb,Nw,Nk] array;
+ *   - kmap(3,Nkall) holds 0-based grid coordinates, invk(3,Nkall) the 1-based
+ *     irreducible index, the 0/1 (direct / via -k) flag and the index of -k;
+ *     olist(Nchi,2) the 1-based orbitals of each orbital pair.
+ * Every call is synchronous.  Failures print a message, fill the outputs
+ * with NaN and are reported by pyrpa_gb_last_error (the reference stops the
+ * process instead).  The hot path runs on the GPU only; without a visible
+ * CUDA device every entry point reports an error.
+ */
+#ifndef PYRPA_GB300_FMOD_H
+#define PYRPA_GB300_FMOD_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ setup --- */
+/* fmod.f90:7-20 openmp_params: reports no OpenMP (0, false) in this build */
+void openmp_params(int64_t* omp_num, bool* omp_check);
+/* finv.f90:1-290 generate_irr_kpoint_inv: klist(3,Nk), kmap(3,Nkall), invk(3,Nkall) */
+void generate_irr_kpoint_inv(double* klist, int64_t* kmap, int64_t* invk, const int64_t* Nk,
+                             const int64_t* Nx, const int64_t* Ny, const int64_t* Nz);
+/* finv.f90:292-305 get_kweight */
+void get_kweight(double* weight, const int64_t* invk, const int64_t* Nk, const int64_t* Nkall);
+/* fmod.f90:162-207 gen_ham: ham_k(Norb,Norb,Nk) = sum_R H(R) exp(-2 pi i k.R), Hermitized */
+void gen_ham(double* ham_k, const double* klist, const double* ham_r, const double* rvec,
+             const int64_t* Nk, const int64_t* Nr, const int64_t* Norb);
+/* fmod.f90:209-248 get_eig: eig(Norb,Nk) ascending, uni(Norb,Norb,Nk) eigenvectors in columns */
+void get_eig(double* eig, double* uni, const double* ham_k, const int64_t* Nk, const int64_t* Norb);
+/* fmod.f90:312-340 get_ffermi */
+void get_ffermi(double* ffermi, const double* eig, const double* mu, const double* temp,
+                const int64_t* Nk, const int64_t* Norb);
+/* fmod.f90:657-716 get_parity_prop: Pmn(Norb,Norb) = +-1 */
+void get_parity_prop(double* Pmn, const double* rvec, const double* ham_r, const int64_t* Norb,
+                     const int64_t* Nr);
+/* fUJ.f90:1-57 get_scmat: Kanamori S and C (Nchi,Nchi), U' = U - 2J */
+void get_scmat(double* Smat, double* Cmat, const int64_t* ol, const int64_t* site, const double* Uval,
+               const double* Jval, const int64_t* Nchi);
+/* fUJ.f90:59-107 get_scmat_orb: orbital-dependent Umat/Jmat (Norb,Norb) */
+void get_scmat_orb(double* Smat, double* Cmat, const int64_t* ol, const int64_t* site,
+                   const double* Umat, const double* Jmat, const int64_t* Nchi, const int64_t* Norb);
+
+/* ------------------------------------------------------------ Green --- */
+/* fself.f90:1-41 gen_green0 (gen_green0_): Gk(Nk,Nw,Norb,Norb) */
+void gen_green0_(double* Gk, const double* eig, const double* uni, const double* mu, const double* temp,
+                 const int64_t* Nk, const int64_t* Nw, const int64_t* Norb);
+/* fself.f90:43-79 gen_green_inv (gen_green_inv_): Gk = iw + mu - H - Sigma */
+void gen_green_inv_(double* Gk, const double* self, const double* hamk, const double* mu,
+                    const double* temp, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb);
+/* fself.f90:134-157 getinv (getinv_): in-place inverse of each Norb x Norb block */
+void getinv_(double* Gk, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb);
+
+/* ------------------------------------------------------ susceptibility --- */
+/* fchi.f90:615-635 get_chi0_conv (get_chi0_conv_): irr_chi(Nchi(Nchi+1)/2,2), chi_map(Nchi,Nchi,2) int32 */
+void get_chi0_conv_(double* chi, const double* Gk, const int64_t* kmap, const int64_t* invk,
+                    const int32_t* irr_chi, const int32_t* chi_map, const int64_t* olist,
+                    const double* temp, const int64_t* Nx, const int64_t* Ny, const int64_t* Nz,
+                    const int64_t* Nw, const int64_t* Nk, const int64_t* Nkall, const int64_t* Norb,
+                    const int64_t* Nchi);
+/* fchi.f90:401-419 get_chi0: chi(Nk,Nw,Nchi,Nchi) by FFT convolution, plus the Stoner factor */
+void get_chi0(double* chi, const double* Smat, const double* Cmat, const double* Gk,
+              const int64_t* kmap, const int64_t* invk, const int64_t* olist, const double* temp,
+              const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* Nw,
+              const int64_t* Nk, const int64_t* Nkall, const int64_t* Norb, const int64_t* Nchi,
+              double* maxchi0s_out);
+/* fchi.f90:894-918 get_chi0_tail: conv[G] - conv[G0] + analytic tau reference */
+void get_chi0_tail(double* chi, const double* Smat, const double* Cmat, const double* Gk,
+                   const double* eig, const double* uni, const int64_t* kmap, const int64_t* invk,
+                   const int64_t* olist, const double* mu, const double* temp, const int64_t* Nx,
+                   const int64_t* Ny, const int64_t* Nz, const int64_t* Nw, const int64_t* Nk,
+                   const int64_t* Nkall, const int64_t* Norb, const int64_t* Nchi,
+                   double* maxchi0s_out);
+/* fchi.f90:319-350 get_chis: chis(Nchi,Nchi,Nw) = (I - chi0 S)^-1 chi0 */
+void get_chis(double* chis, const double* chi0, const double* Smat, const int64_t* Nchi,
+              const int64_t* Nw);
+/* fself.f90:783-816 get_chis_chic: nu = 0 RPA spin/charge susceptibilities (Nk,Nchi,Nchi) */
+void get_chis_chic(double* chis, double* chic, const double* chi, const double* Smat,
+                   const double* Cmat, const int64_t* Nk, const int64_t* Nw, const int64_t* Nchi);
+/* fself.f90:818-851 get_eig_or_tr_chi: max Re eigenvalue or trace on the full grid.
+ * The Fortran dummy sw_eig is a default logical; the wrappers pass a 1-byte
+ * c_bool, which is what this declaration reads. */
+void get_eig_or_tr_chi(double* chiqout, const double* chi, const int64_t* invk,
+                       const int64_t* Nkall, const int64_t* Nk, const int64_t* Nchi,
+                       const bool* sw_eig);
+/* fUJ.f90:318-365 get_vsigma_flex_nosoc (get_vsigma_flex_nosoc_): V_sigma in place */
+void get_vsigma_flex_nosoc_(double* chi, const double* Smat, const double* Cmat, const int64_t* Nk,
+                            const int64_t* Nw, const int64_t* Nchi);
+
+/* ------------------------------------------------------------- FLEX --- */
+/* fself.f90:287-781 mkself: FLEX self-consistency; sigmak(Nk,Nw,Norb,Norb), mu.
+ * sw_out / sw_in write / read sigma.bin in the working directory. */
+void mkself(double* sigmak, double* mu, const double* Smat, const double* Cmat, const int64_t* kmap,
+            const int64_t* invk, const int64_t* olist, const double* hamk, const double* eig,
+            const double* uni, const double* mu_init, const double* rfill, const double* temp,
+            const int64_t* scf_loop, const double* pp, const double* eps, const int64_t* Nkall,
+            const int64_t* Nk, const int64_t* Nw, const int64_t* Norb, const int64_t* Nchi,
+            const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* sub_sigma,
+            const bool* sw_out, const bool* sw_in, const int64_t* m_diis, const bool* sw_rescale,
+            const bool* sw_tail, const double* sigma_scale);
+
+/* ------------------------------------------------------- Eliashberg --- */
+/* feliash.f90:1-443 lin_eliash: leading eigenvalue lambda_out and gap delta(Nk,Nw,Norb,Norb);
+ * chi is overwritten with the pairing vertex V_Delta as in the reference. */
+void lin_eliash(double* delta, double* chi, const double* Gk, const double* uni,
+                const double* init_delta, const double* Smat, const double* Cmat,
+                const int64_t* olist, const double* prt, const int64_t* kmap, const int64_t* invk,
+                const double* temp, const double* eps, const int64_t* Nkall, const int64_t* Nk,
+                const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nx,
+                const int64_t* Ny, const int64_t* Nz, const int64_t* itemax, const int64_t* gap_sym,
+                const int64_t* arnoldi_m, double* lambda_out);
+/* feliash.f90:445-484 mkfk_trs_nsoc (mkfk_trs_nsoc_): F = -G Delta G^dagger, Hermitized */
+void mkfk_trs_nsoc_(double* fk, const double* Gk, const double* delta, const int64_t* Nk,
+                    const int64_t* Nw, const int64_t* Norb);
+/* feliash.f90:637-731 get_initial_delta (get_initial_delta_) */
+void get_initial_delta_(double* delta, const double* init_delta, const double* uni, const int64_t* kmap,
+                        const int64_t* invk, const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw,
+                        const int64_t* Norb, const int64_t* gap_sym);
+/* feliash.f90:787-821 remap_delta (remap_delta_): delta(Nkall,Nw,Norb,Norb) */
+void remap_delta_(double* delta, const double* delta0, const double* prt, const int64_t* invk,
+                  const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb,
+                  const int64_t* gap_sym);
+/* feliash.f90:733-785 conv_delta_orb_to_band: deltab(Nkall,Norb,Norb) at the first frequency */
+void conv_delta_orb_to_band(double* deltab, const double* delta, const double* uni, const double* prt,
+                            const int64_t* invk, const int64_t* Norb, const int64_t* Nkall,
+                            const int64_t* Nk, const int64_t* Nw, const int64_t* gap_sym);
+
+/* ------------------------------------- additions without a reference counterpart --- */
+/* 64: FP64 everywhere (default, the reference's arithmetic); 32: complex FP32 FFTs,
+ * contractions and vertex solves with G, Sigma, mu, DIIS and lambda kept in FP64.
+ * The environment variable PYRPA_GB_PRECISION=fp32 sets 32 at first use. */
+void pyrpa_gb_set_precision(const int64_t* bits);
+void pyrpa_gb_get_precision(int64_t* bits);
+/* 0 silences the progress lines the reference prints to stdout */
+void pyrpa_gb_set_verbose(const int64_t* level);
+/* message of the last failure (NUL-terminated, at most len bytes) and 1/0 */
+void pyrpa_gb_last_error(char* buf, const int64_t* len, int64_t* code);
+void pyrpa_gb_clear_error(void);
+/* kernels this process has launched (all engine kernels, FFT passes included) */
+void pyrpa_gb_kernel_launches(int64_t* n);
+/* statistics of the last mkself / lin_eliash: iterations, esterr, Stoner, mu, lambda,
+ * Eliashberg applications, then device milliseconds of chi0, vertex, Sigma, DIIS,
+ * mu, Dyson, Eliashberg applications (14 doubles) */
+void pyrpa_gb_last_stats(double* out);
+void pyrpa_gb_device_info(int64_t* num_sms, int64_t* device);
+/* live timing of the FFT pass kernel: when on, every pass launch is bracketed
+ * by CUDA events on the library stream; pyrpa_gb_fft_stats returns and resets
+ * {launches, summed ms, algorithmic bytes (one read and one write per element)} */
+void pyrpa_gb_fft_profile(const int64_t* on);
+void pyrpa_gb_fft_stats(double* out);
+
+/* The reference's linearized-Eliashberg driver with the FLEX self-energy
+ * (libs/plibs/_calc.py:370-405: mkself -> gen_green -> get_chi0(_tail) ->
+ * lin_eliash) as one call whose intermediates (G, chi0, V_Delta) stay in HBM.
+ * Arguments as in mkself and lin_eliash; sigma_seed (may be NULL) replaces the
+ * G0 start by a given Sigma with chemical potentials seed_mu / seed_mu_old
+ * (the sw_in path without a file).  times_ms[3] (may be NULL) receives the
+ * host-to-device, device compute and device-to-host milliseconds measured
+ * with CUDA events on the library stream.  No counterpart in the reference. */
+void pyrpa_gb_flex_eliash(double* sigmak, double* mu, double* delta, double* lambda_out, double* stoner,
+                          double* times_ms, const double* Smat, const double* Cmat, const int64_t* kmap,
+                          const int64_t* invk, const int64_t* olist, const double* hamk, const double* eig,
+                          const double* uni, const double* init_delta, const double* prt,
+                          const double* sigma_seed, const double* seed_mu, const double* seed_mu_old,
+                          const double* mu_init, const double* rfill, const double* temp,
+                          const int64_t* scf_loop, const double* pp, const double* eps, const int64_t* Nkall,
+                          const int64_t* Nk, const int64_t* Nw, const int64_t* Norb, const int64_t* Nchi,
+                          const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* sub_sigma,
+                          const int64_t* m_diis, const bool* sw_rescale, const bool* sw_tail,
+                          const int64_t* gap_sym, const int64_t* arnoldi_m, const int64_t* itemax,
+                          const double* eps_eliash);
+
+/* Symbols outside the accelerated path (transport, impurity, SOC, Eilenberger,
+ * real-frequency maps, Pade, nonlinear Eliashberg ...) are exported with no
+ * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"
+ * so that `import libs.flibs` binds every name it expects. */
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYRPA_GB300_FMOD_H */

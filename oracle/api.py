@@ -99,9 +99,11 @@ def get_Vsigma_nosoc_flex(chi, Smat, Cmat):
     """The reference wrapper passes Nk=len(chi), Nw=len(chi[0]) and lets the
     library read the buffer as (Nk,Nw,Nchi,Nchi) (libs/flibs/_selfenergy.py:60-73)."""
     Nk, Nw, Nchi = len(chi), len(chi[0]), len(Smat)
-    X = _fortran_view(chi, (Nk, Nw, Nchi, Nchi))
-    V = O.vsigma_flex_nosoc(X, Smat.T, Cmat.T)
-    return V.reshape(-1, order="F").reshape(chi.shape)
+    flat = np.ascontiguousarray(chi).reshape(-1).copy()
+    n = Nk * Nw * Nchi * Nchi
+    X = flat[:n].reshape((Nk, Nw, Nchi, Nchi), order="F")
+    flat[:n] = O.vsigma_flex_nosoc(X, Smat.T, Cmat.T).reshape(-1, order="F")
+    return flat.reshape(chi.shape)
 
 
 def mkself(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, mu, fill, temp, Nw, Nx, Ny, Nz,

@@ -1,0 +1,914 @@
+// C ABI of the GB300 engine: the symbols of the reference libfmod.so that the
+// pyrpa ctypes wrappers (libs/flibs/*.py) bind, with the same argument order
+// and meaning (every argument by reference, Fortran column-major arrays).
+// Declarations and the reference interface each one replaces: include/fmod.h.
+//
+// Differences from the reference on purpose: a failure prints a message,
+// records it for pyrpa_gb_last_error() and fills the outputs with NaN instead
+// of terminating the process (the Fortran code calls `stop`).
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "drivers.cuh"
+#include "flex.cuh"
+#include "linalg.cuh"
+
+namespace pgb {
+
+Context& ctx() {
+  static Context c;
+  return c;
+}
+
+void ensure_context() {
+  Context& c = ctx();
+  if (c.ready) return;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    throw Error("no CUDA device is visible: this library runs the FLEX/RPA path only on the GPU");
+  PGB_CUDA(cudaGetDevice(&c.device));
+  cudaDeviceProp prop;
+  PGB_CUDA(cudaGetDeviceProperties(&prop, c.device));
+  c.num_sms = prop.multiProcessorCount;
+  PGB_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  cudaMemPool_t pool;
+  PGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, c.device));
+  uint64_t thr = std::numeric_limits<uint64_t>::max();
+  PGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  if (const char* s = std::getenv("PYRPA_GB_PRECISION")) {
+    std::string v(s);
+    if (v == "32" || v == "fp32" || v == "FP32") c.precision = 32;
+  }
+  if (const char* s = std::getenv("PYRPA_GB_VERBOSE")) c.verbose = std::atoi(s);
+  c.ready = true;
+}
+
+}  // namespace pgb
+
+using namespace pgb;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_last_error;
+int64_t g_last_code = 0;
+
+void report(const char* fn, const char* what) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_last_error = std::string(fn) + ": " + what;
+  g_last_code = 1;
+  fprintf(stderr, "pyrpa_gb300 error in %s: %s\n", fn, what);
+  fflush(stderr);
+}
+
+template <typename T> void nan_fill(T* p, size_t n) {
+  if (!p) return;
+  const double q = std::numeric_limits<double>::quiet_NaN();
+  double* d = reinterpret_cast<double*>(p);
+  for (size_t i = 0; i < n * sizeof(T) / sizeof(double); ++i) d[i] = q;
+}
+
+bool fp32() { return ctx().precision == 32; }
+
+// --------------------------------------------------------- setup kernels
+__global__ void k_gen_ham(double2* hk, const double* klist, const double2* hr, const double* rvec, int64_t Nk,
+                          int64_t Nr, int No) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nk; i += (long long)gridDim.x * blockDim.x) {
+    double2 acc[kMaxOrb * kMaxOrb];
+    for (int e = 0; e < No * No; ++e) acc[e] = make_double2(0, 0);
+    for (long long j = 0; j < Nr; ++j) {
+      const double d = klist[3 * i] * rvec[3 * j] + klist[3 * i + 1] * rvec[3 * j + 1] + klist[3 * i + 2] * rvec[3 * j + 2];
+      double s, c;
+      sincospi(2.0 * d, &s, &c);
+      const double2 ph = make_double2(c, -s);
+      for (int l = 0; l < No; ++l)
+        for (int m = l; m < No; ++m) acc[m + No * l] += hr[m + No * (l + (long long)No * j)] * ph;
+    }
+    double2* out = hk + (long long)No * No * i;
+    for (int l = 0; l < No; ++l) {
+      out[l + No * l] = make_double2(acc[l + No * l].x, 0.0);
+      for (int m = l + 1; m < No; ++m) {
+        out[m + No * l] = acc[m + No * l];
+        out[l + No * m] = conj(acc[m + No * l]);
+      }
+    }
+  }
+}
+
+__global__ void k_get_eig(double* eig, double2* uni, const double2* hk, int64_t Nk, int No) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nk; i += (long long)gridDim.x * blockDim.x) {
+    double2 A[kMaxOrb * kMaxOrb], V[kMaxOrb * kMaxOrb];
+    double w[kMaxOrb];
+    const double2* h = hk + (long long)No * No * i;
+    for (int m = 0; m < No; ++m)
+      for (int l = 0; l < No; ++l) A[m * No + l] = h[m + No * l];
+    jacobi_herm(A, No, w, V);
+    for (int n = 0; n < No; ++n) {
+      eig[n + (long long)No * i] = w[n];
+      for (int m = 0; m < No; ++m) uni[m + No * (n + (long long)No * i)] = V[m * No + n];
+    }
+  }
+}
+
+__global__ void k_ffermi(double* f, const double* eig, double mu, double itemp, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    f[i] = 0.5 - 0.5 * tanh((eig[i] - mu) * itemp);
+}
+
+__global__ void k_extract_nu0(double2* out, const double2* chi, long long Nk, long long K, int nel) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nk * nel; i += (long long)gridDim.x * blockDim.x) {
+    const long long k = i % Nk, e = i / Nk;
+    out[i] = chi[k + K * e];
+  }
+}
+
+__global__ void k_eig_or_tr(double2* vals, const double2* chi, int64_t Nk, int n, int sw_eig) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < Nk; k += (long long)gridDim.x * blockDim.x) {
+    if (!sw_eig) {
+      double2 t = make_double2(0, 0);
+      for (int l = 0; l < n; ++l) t += chi[k + Nk * (l + (long long)n * l)];
+      vals[k] = t;
+      continue;
+    }
+    double2 A[kMaxChi * kMaxChi], w[kMaxChi];
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) A[a * n + b] = chi[k + Nk * (a + (long long)n * b)];
+    double best = -1e300;
+    if (eigvals_general(A, n, w) < 0) best = nan("");
+    else
+      for (int i = 0; i < n; ++i) best = fmax(best, w[i].x);
+    vals[k] = make_double2(best, 0.0);
+  }
+}
+
+__global__ void k_map_full(double2* out, const double2* vals, const int64_t* invk, int64_t Nkall) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nkall; i += (long long)gridDim.x * blockDim.x)
+    out[i] = vals[invk[3 * i] - 1];
+}
+
+__global__ void k_remap_delta(double2* out, const double2* d0, const double* prt, const int64_t* invk, int64_t Nkall,
+                              int64_t Nk, int64_t Nw, int No, double dprt) {
+  const long long N = Nkall * Nw * No * No;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N; idx += (long long)gridDim.x * blockDim.x) {
+    const long long i = idx % Nkall;
+    const long long j = (idx / Nkall) % Nw;
+    const int m = (int)((idx / (Nkall * Nw)) % No), l = (int)(idx / (Nkall * Nw * No));
+    const long long k = invk[3 * i] - 1;
+    double2 v = d0[k + Nk * (j + Nw * (m + (long long)No * l))];
+    if (invk[3 * i + 1] == 1) v = (dprt * prt[m] * prt[l]) * v;
+    else if (invk[3 * i + 1] != 0) v = make_double2(0, 0);
+    out[idx] = v;
+  }
+}
+
+__global__ void k_orb_to_band(double2* out, const double2* delta, const double2* uni, const double* prt,
+                              const int64_t* invk, int64_t Nkall, int64_t Nk, int No, double dprt) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nkall; i += (long long)gridDim.x * blockDim.x) {
+    const long long k = invk[3 * i] - 1;
+    const int fl = (int)invk[3 * i + 1];
+    const double2* U = uni + (long long)No * No * k;
+    double2 D[kMaxOrb * kMaxOrb], T[kMaxOrb * kMaxOrb];
+    // compact first-Matsubara slice: element (a,b) of k at k + Nk*(a + No*b)
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) D[a * No + b] = delta[k + Nk * (long long)(a + No * b)];
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 acc = make_double2(0, 0);
+        for (int c = 0; c < No; ++c) {
+          // L = U^H (direct) or U^T diag(prt) (via -k); L[a][c]
+          double2 L = fl == 0 ? conj(U[c + No * a]) : U[c + No * a] * prt[c];
+          acc += L * D[c * No + b];
+        }
+        T[a * No + b] = fl == 0 ? acc : acc * (dprt * prt[b]);
+      }
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 acc = make_double2(0, 0);
+        for (int c = 0; c < No; ++c) {
+          double2 Rm = fl == 0 ? U[c + No * b] : conj(U[c + No * b]);
+          acc += T[a * No + c] * Rm;
+        }
+        if (fl != 0 && fl != 1) acc = make_double2(0, 0);
+        out[i + Nkall * (a + (long long)No * b)] = acc;
+      }
+  }
+}
+
+unsigned g1(long long n, int t) { return (unsigned)std::max(1LL, std::min<long long>((n + t - 1) / t, 65536)); }
+
+// ------------------------------------------------------- irreducible k mesh
+int64_t irr_count(int64_t Nx, int64_t Ny, int64_t Nz) {
+  const int64_t N = Nx * Ny * Nz;
+  if (N % 2 == 0) {
+    if (Nz % 2 == 0) {
+      if (Nx % 2 == 0 && Ny % 2 == 0) return N / 2 + 4;
+      if (Nx % 2 == 0 || Ny % 2 == 0) return N / 2 + 2;
+      return N / 2 + 1;
+    }
+    if (Nx % 2 == 0 && Ny % 2 == 0) return N / 2 + 2;
+    return N / 2 + 1;
+  }
+  return (N + 1) / 2;
+}
+
+// irreducible list in the reference's order (finv.f90:117-288)
+std::vector<std::array<int64_t, 3>> irr_grid(int64_t Nx, int64_t Ny, int64_t Nz, int64_t Nk) {
+  std::vector<std::array<int64_t, 3>> kl(Nk, {0, 0, 0});
+  auto put = [&](int64_t it, int64_t i, int64_t j, int64_t k) {
+    PGB_CHECK(it >= 1 && it <= Nk, "irreducible k index outside the list");
+    kl[it - 1] = {i, j, k};
+  };
+  auto half_plane = [&](int64_t ini, int64_t k) -> int64_t {
+    if (Nx % 2 == 0 && Ny % 2 == 0) {
+      for (int64_t j = 0; j <= Ny / 2; ++j)
+        for (int64_t i = 0; i <= Nx / 2; ++i) put(ini + i + (Nx / 2 + 1) * j, i, j, k);
+      const int64_t ini2 = ini + (Nx / 2 + 1) * (Ny / 2 + 1) - 1;
+      for (int64_t j = Ny / 2 + 1; j < Ny; ++j)
+        for (int64_t i = 1; i < Nx / 2; ++i) put(ini2 + i + (Nx / 2 - 1) * (j - Ny / 2 - 1), i, j, k);
+      return ini + Nx * Ny / 2 + 2;
+    }
+    int64_t it = ini;
+    if ((Nx * Ny) % 2 == 0) {
+      PGB_CHECK(Nx % 2 == 0, "odd Nx with even Ny: the irreducible k list is undefined for this mesh");
+      for (int64_t j = 0; j <= (Ny - 1) / 2; ++j)
+        for (int64_t i = 0; i <= Nx / 2; ++i) put(it++, i, j, k);
+      for (int64_t j = (Ny + 1) / 2; j < Ny; ++j)
+        for (int64_t i = 1; i < Nx / 2; ++i) put(it++, i, j, k);
+      return it;
+    }
+    for (int64_t j = 0; j <= (Ny - 1) / 2; ++j)
+      for (int64_t i = 0; i <= (Nx - 1) / 2; ++i) put(it++, i, j, k);
+    for (int64_t j = (Ny + 1) / 2; j < Ny; ++j)
+      for (int64_t i = 1; i <= (Nx - 1) / 2; ++i) put(it++, i, j, k);
+    return it;
+  };
+  int64_t ini = half_plane(1, 0);
+  if (Nz > 1) {
+    const int64_t nfull = (Nz % 2 == 0) ? Nz / 2 - 1 : (Nz - 1) / 2;
+    for (int64_t k = 1; k <= nfull; ++k)
+      for (int64_t j = 0; j < Ny; ++j)
+        for (int64_t i = 0; i < Nx; ++i) put(ini + i + Nx * j + Nx * Ny * (k - 1), i, j, k);
+    ini += Nx * Ny * nfull;
+    if (Nz % 2 == 0) half_plane(ini, Nz / 2);
+  }
+  return kl;
+}
+
+}  // namespace
+
+// chi0 entry shared by get_chi0 / get_chi0_tail / get_chi0_conv_
+namespace {
+template <typename R>
+double chi0_entry(double2* chi_out, const double* Smat, const double* Cmat, const double2* Gk, const int64_t* kmap,
+                  const int64_t* invk, const int64_t* olist, double temp, int64_t Nx, int64_t Ny, int64_t Nz, int64_t Nw,
+                  int64_t Nk, int64_t Nkall, int64_t Norb, int64_t Nchi, const double* eig, const double2* uni,
+                  double mu, bool tail, bool with_stoner, const int32_t* irr_chi, const int32_t* chi_map) {
+  PGB_CHECK(Nkall == Nx * Ny * Nz, "Nkall differs from Nx*Ny*Nz");
+  Geom g;
+  build_geom(g, kmap, invk, Nx, Ny, Nz, Nk, Nw, Norb, Nchi);
+  Pairs p;
+  build_pairs(p, olist, (int)Norb, (int)Nchi, irr_chi, chi_map);
+  const long long KE = g.K * Norb * Norb, KC = g.K * Nchi * Nchi;
+  DBuf<double2> G(KE);
+  G.upload(Gk, KE);
+  DBuf<double> e, S, C;
+  DBuf<double2> u;
+  TailRef tr;
+  if (tail) {
+    e.alloc(Norb * Nk);
+    e.upload(eig, Norb * Nk);
+    u.alloc(Norb * Norb * Nk);
+    u.upload(uni, Norb * Norb * Nk);
+    tr.eig = e.p;
+    tr.uni = u.p;
+    tr.mu = mu;
+  }
+  DBuf<cx<R>> chi(KC);
+  chi0<R>(g, p, G.p, temp, tail ? &tr : nullptr, chi.p);
+  G.release();
+  double sdw = 0;
+  if (with_stoner) {
+    S.alloc(Nchi * Nchi);
+    C.alloc(Nchi * Nchi);
+    S.upload(Smat, Nchi * Nchi);
+    C.upload(Cmat, Nchi * Nchi);
+    double cdw = 0;
+    int qs = 0, qc = 0;
+    stoner<R>(g, chi.p, S.p, C.p, &sdw, &cdw, &qs, &qc);
+    ckchi_print(g, sdw, cdw, qs, qc);
+  }
+  if (sizeof(R) == 8) {
+    chi.download(chi_out, KC);
+  } else {
+    DBuf<double2> w(KC);
+    widen<R>(w.p, chi.p, KC);
+    w.download(chi_out, KC);
+  }
+  sync();
+  return sdw;
+}
+}  // namespace
+
+#define ABI_TRY try {
+#define ABI_CATCH(name, onerr)            \
+  }                                       \
+  catch (const std::exception& e) {       \
+    report(name, e.what());               \
+    onerr;                                \
+  }
+
+extern "C" {
+
+// ============================================================== extras ==
+void pyrpa_gb_set_precision(const int64_t* bits) {
+  ctx().precision = (*bits == 32) ? 32 : 64;
+}
+void pyrpa_gb_get_precision(int64_t* bits) {
+  ABI_TRY ensure_context(); ABI_CATCH("pyrpa_gb_get_precision", (void)0)
+  *bits = ctx().precision;
+}
+void pyrpa_gb_set_verbose(const int64_t* v) { ctx().verbose = (int)*v; }
+void pyrpa_gb_last_error(char* buf, const int64_t* len, int64_t* code) {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  if (buf && len && *len > 0) {
+    const size_t n = std::min<size_t>((size_t)*len - 1, g_last_error.size());
+    memcpy(buf, g_last_error.data(), n);
+    buf[n] = 0;
+  }
+  if (code) *code = g_last_code;
+}
+void pyrpa_gb_clear_error() {
+  std::lock_guard<std::mutex> lk(g_err_mu);
+  g_last_error.clear();
+  g_last_code = 0;
+}
+void pyrpa_gb_kernel_launches(int64_t* n) { *n = ctx().kernel_launches; }
+void pyrpa_gb_last_stats(double* out) {
+  const LastStats& s = last_stats();
+  const double v[14] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
+                        s.t_vertex, s.t_sigma, s.t_diis, s.t_mu, s.t_dyson, s.t_apply, 0.0};
+  memcpy(out, v, sizeof(v));
+}
+void pyrpa_gb_fft_profile(const int64_t* on) { fft_profile_enable(*on != 0); }
+void pyrpa_gb_fft_stats(double* out) {
+  ABI_TRY fft_profile_collect(&out[0], &out[1], &out[2]);
+  ABI_CATCH("pyrpa_gb_fft_stats", (out[0] = out[1] = out[2] = 0))
+}
+void pyrpa_gb_device_info(int64_t* num_sms, int64_t* device) {
+  ABI_TRY ensure_context(); *num_sms = ctx().num_sms; *device = ctx().device;
+  ABI_CATCH("pyrpa_gb_device_info", (*num_sms = 0, *device = -1))
+}
+
+// ================================================================ setup ==
+void openmp_params(int64_t* omp_num, bool* omp_check) {
+  // no OpenMP in this build: the work runs on the GPU
+  *omp_num = 0;
+  *omp_check = false;
+}
+
+void generate_irr_kpoint_inv(double* klist, int64_t* kmap, int64_t* invk, const int64_t* Nk, const int64_t* Nx,
+                             const int64_t* Ny, const int64_t* Nz) {
+  ABI_TRY
+  const int64_t nx = *Nx, ny = *Ny, nz = *Nz, nk = *Nk, N = nx * ny * nz;
+  PGB_CHECK(nx > 0 && ny > 0 && nz > 0, "non-positive mesh");
+  PGB_CHECK(nk == irr_count(nx, ny, nz), "Nk differs from the irreducible count of this mesh");
+  auto irr = irr_grid(nx, ny, nz, nk);
+  std::unordered_map<int64_t, int64_t> direct, inverse;
+  auto key = [&](int64_t x, int64_t y, int64_t z) { return x + nx * (y + ny * z); };
+  for (int64_t j = 0; j < nk; ++j) {
+    const auto& c = irr[j];
+    klist[3 * j] = (double)c[0] / (double)nx;
+    klist[3 * j + 1] = (double)c[1] / (double)ny;
+    klist[3 * j + 2] = (double)c[2] / (double)nz;
+    direct.emplace(key(c[0], c[1], c[2]), j);
+    inverse.emplace(key((nx - c[0]) % nx, (ny - c[1]) % ny, (nz - c[2]) % nz), j);
+  }
+  for (int64_t z = 0; z < nz; ++z)
+    for (int64_t y = 0; y < ny; ++y)
+      for (int64_t x = 0; x < nx; ++x) {
+        const int64_t i = key(x, y, z);
+        kmap[3 * i] = x;
+        kmap[3 * i + 1] = y;
+        kmap[3 * i + 2] = z;
+        auto d = direct.find(i), v = inverse.find(i);
+        PGB_CHECK(d != direct.end() || v != inverse.end(), "k point without irreducible partner");
+        if (d != direct.end() && (v == inverse.end() || d->second <= v->second)) {
+          invk[3 * i] = d->second + 1;
+          invk[3 * i + 1] = 0;
+        } else {
+          invk[3 * i] = v->second + 1;
+          invk[3 * i + 1] = 1;
+        }
+        invk[3 * i + 2] = key((nx - x) % nx, (ny - y) % ny, (nz - z) % nz) + 1;
+      }
+  (void)N;
+  ABI_CATCH("generate_irr_kpoint_inv", (void)0)
+}
+
+void get_kweight(double* weight, const int64_t* invk, const int64_t* Nk, const int64_t* Nkall) {
+  ABI_TRY
+  for (int64_t k = 0; k < *Nk; ++k) weight[k] = 0.0;
+  for (int64_t i = 0; i < *Nkall; ++i) {
+    const int64_t k = invk[3 * i] - 1;
+    PGB_CHECK(k >= 0 && k < *Nk, "invk(1,:) outside [1,Nk]");
+    weight[k] += 1.0;
+  }
+  ABI_CATCH("get_kweight", (void)0)
+}
+
+void get_scmat(double* Smat, double* Cmat, const int64_t* ol, const int64_t* site, const double* Uval,
+               const double* Jval, const int64_t* Nchi) {
+  const int64_t n = *Nchi;
+  const double U = *Uval, J = *Jval, Up = U - 2 * J;
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = 0; j < n; ++j) {
+      double s = 0, c = 0;
+      const int64_t i1 = ol[i], i2 = ol[n + i], j1 = ol[j], j2 = ol[n + j];
+      if (site[i] == site[j]) {
+        if (i1 == i2 && j1 == j2) {
+          if (i1 == j1) { s = U; c = U; }
+          else { s = J; c = 2 * Up - J; }
+        } else if (i1 == j1 && i2 == j2) {
+          s = Up; c = -Up + 2 * J;
+        } else if (i1 == j2 && i2 == j1) {
+          s = J; c = J;
+        }
+      }
+      Smat[j + n * i] = s;
+      Cmat[j + n * i] = c;
+    }
+}
+
+void get_scmat_orb(double* Smat, double* Cmat, const int64_t* ol, const int64_t* site, const double* Umat,
+                   const double* Jmat, const int64_t* Nchi, const int64_t* Norb) {
+  const int64_t n = *Nchi, no = *Norb;
+  auto Uf = [&](int64_t a, int64_t b) { return Umat[(a - 1) + no * (b - 1)]; };
+  auto Jf = [&](int64_t a, int64_t b) { return Jmat[(a - 1) + no * (b - 1)]; };
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = 0; j < n; ++j) {
+      double s = 0, c = 0;
+      const int64_t i1 = ol[i], i2 = ol[n + i], j1 = ol[j], j2 = ol[n + j];
+      if (site[i] == site[j]) {
+        if (i1 == i2 && j1 == j2) {
+          if (i1 == j1) { s = Uf(i1, i1); c = s; }
+          else { s = Jf(i1, j1); c = 2 * Uf(i1, j1) - Jf(i1, j1); }
+        } else if (i1 == j1 && i2 == j2) {
+          s = Uf(i1, i2); c = -Uf(i1, i2) + 2 * Jf(i1, i2);
+        } else if (i1 == j2 && i2 == j1) {
+          s = Jf(i1, i2); c = s;
+        }
+      }
+      Smat[j + n * i] = s;
+      Cmat[j + n * i] = c;
+    }
+}
+
+void get_parity_prop(double* Pmn, const double* rvec, const double2* ham_r, const int64_t* Norb, const int64_t* Nr) {
+  const int64_t no = *Norb, nr = *Nr;
+  std::vector<double> num(no * no, 0.0), den(no * no, 0.0);
+  for (int64_t i = 0; i < nr; ++i)
+    for (int64_t j = i + 1; j < nr; ++j) {
+      const double d = std::fabs(rvec[3 * i] + rvec[3 * j]) + std::fabs(rvec[3 * i + 1] + rvec[3 * j + 1]) +
+                       std::fabs(rvec[3 * i + 2] + rvec[3 * j + 2]);
+      if (d < 1e-6) {
+        for (int64_t e = 0; e < no * no; ++e) {
+          const double2 a = ham_r[e + no * no * j], b = ham_r[e + no * no * i];
+          num[e] += a.x * b.x + a.y * b.y;
+          den[e] += b.x * b.x + b.y * b.y;
+        }
+        break;
+      }
+    }
+  for (int64_t e = 0; e < no * no; ++e) {
+    const double p = den[e] > 1e-10 ? num[e] / den[e] : 0.0;
+    Pmn[e] = p >= 0.0 ? 1.0 : -1.0;
+  }
+}
+
+void gen_ham(double2* ham_k, const double* klist, const double2* ham_r, const double* rvec, const int64_t* Nk,
+             const int64_t* Nr, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, nr = *Nr, no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  DBuf<double2> hk(no * no * nk), hr(no * no * nr);
+  DBuf<double> kl(3 * nk), rv(3 * nr);
+  hr.upload(ham_r, no * no * nr);
+  kl.upload(klist, 3 * nk);
+  rv.upload(rvec, 3 * nr);
+  k_gen_ham<<<g1(nk, 64), 64, 0, ctx().stream>>>(hk.p, kl.p, hr.p, rv.p, nk, nr, (int)no);
+  launch_check("gen_ham");
+  hk.download(ham_k, no * no * nk);
+  sync();
+  ABI_CATCH("gen_ham", nan_fill(ham_k, (size_t)(*Norb) * (*Norb) * (*Nk)))
+}
+
+void get_eig(double* eig, double2* uni, const double2* ham_k, const int64_t* Nk, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  DBuf<double2> hk(no * no * nk), u(no * no * nk);
+  DBuf<double> e(no * nk);
+  hk.upload(ham_k, no * no * nk);
+  k_get_eig<<<g1(nk, 64), 64, 0, ctx().stream>>>(e.p, u.p, hk.p, nk, (int)no);
+  launch_check("get_eig");
+  e.download(eig, no * nk);
+  u.download(uni, no * no * nk);
+  sync();
+  ABI_CATCH("get_eig", (nan_fill(eig, (size_t)(*Norb) * (*Nk)), nan_fill(uni, (size_t)(*Norb) * (*Norb) * (*Nk))))
+}
+
+void get_ffermi(double* ffermi, const double* eig, const double* mu, const double* temp, const int64_t* Nk,
+                const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const long long n = (*Nk) * (*Norb);
+  DBuf<double> e(n), f(n);
+  e.upload(eig, n);
+  const double t = std::max(*temp, 1.0e-12);
+  k_ffermi<<<g1(n, 256), 256, 0, ctx().stream>>>(f.p, e.p, *mu, 0.5 / t, n);
+  launch_check("ffermi");
+  f.download(ffermi, n);
+  sync();
+  ABI_CATCH("get_ffermi", nan_fill(ffermi, (size_t)(*Nk) * (*Norb)))
+}
+
+// ================================================================ green ==
+void gen_green0_(double2* Gk, const double* eig, const double2* uni, const double* mu, const double* temp,
+                 const int64_t* Nk, const int64_t* Nw, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, nw = *Nw, no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  DBuf<double> e(no * nk);
+  DBuf<double2> u(no * no * nk), G(nk * nw * no * no);
+  e.upload(eig, no * nk);
+  u.upload(uni, no * no * nk);
+  green0(G.p, e.p, u.p, *mu, *temp, (int)nk, (int)nw, (int)no);
+  G.download(Gk, nk * nw * no * no);
+  sync();
+  ABI_CATCH("gen_green0_", nan_fill(Gk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+void gen_green_inv_(double2* Gk, const double2* self, const double2* hamk, const double* mu, const double* temp,
+                    const int64_t* Nk, const int64_t* Nw, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, nw = *Nw, no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  const long long KE = nk * nw * no * no;
+  DBuf<double2> s(KE), h(no * no * nk), G(KE);
+  s.upload(self, KE);
+  h.upload(hamk, no * no * nk);
+  green_inv_only(G.p, s.p, h.p, *mu, *temp, (int)nk, (int)nw, (int)no);
+  G.download(Gk, KE);
+  sync();
+  ABI_CATCH("gen_green_inv_", nan_fill(Gk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+void getinv_(double2* Gk, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, nw = *Nw, no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  const long long K = nk * nw, KE = K * no * no;
+  DBuf<double2> G(KE);
+  G.upload(Gk, KE);
+  PGB_CHECK(invert_blocks(G.p, K, (int)no, 1, K), "zgetrf failed in getinv: singular matrix");
+  G.download(Gk, KE);
+  sync();
+  ABI_CATCH("getinv_", nan_fill(Gk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+// ================================================================== chi ==
+
+void get_chi0(double2* chi, const double* Smat, const double* Cmat, const double2* Gk, const int64_t* kmap,
+              const int64_t* invk, const int64_t* olist, const double* temp, const int64_t* Nx, const int64_t* Ny,
+              const int64_t* Nz, const int64_t* Nw, const int64_t* Nk, const int64_t* Nkall, const int64_t* Norb,
+              const int64_t* Nchi, double* maxchi0s_out) {
+  ABI_TRY
+  ensure_context();
+  auto f = fp32() ? chi0_entry<float> : chi0_entry<double>;
+  *maxchi0s_out = f(chi, Smat, Cmat, Gk, kmap, invk, olist, *temp, *Nx, *Ny, *Nz, *Nw, *Nk, *Nkall, *Norb, *Nchi,
+                    nullptr, nullptr, 0.0, false, true, nullptr, nullptr);
+  ABI_CATCH("get_chi0", (nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)), *maxchi0s_out = NAN))
+}
+
+void get_chi0_tail(double2* chi, const double* Smat, const double* Cmat, const double2* Gk, const double* eig,
+                   const double2* uni, const int64_t* kmap, const int64_t* invk, const int64_t* olist, const double* mu,
+                   const double* temp, const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* Nw,
+                   const int64_t* Nk, const int64_t* Nkall, const int64_t* Norb, const int64_t* Nchi,
+                   double* maxchi0s_out) {
+  ABI_TRY
+  ensure_context();
+  auto f = fp32() ? chi0_entry<float> : chi0_entry<double>;
+  *maxchi0s_out = f(chi, Smat, Cmat, Gk, kmap, invk, olist, *temp, *Nx, *Ny, *Nz, *Nw, *Nk, *Nkall, *Norb, *Nchi,
+                    eig, uni, *mu, true, true, nullptr, nullptr);
+  ABI_CATCH("get_chi0_tail", (nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)), *maxchi0s_out = NAN))
+}
+
+void get_chi0_conv_(double2* chi, const double2* Gk, const int64_t* kmap, const int64_t* invk, const int32_t* irr_chi,
+                    const int32_t* chi_map, const int64_t* olist, const double* temp, const int64_t* Nx,
+                    const int64_t* Ny, const int64_t* Nz, const int64_t* Nw, const int64_t* Nk, const int64_t* Nkall,
+                    const int64_t* Norb, const int64_t* Nchi) {
+  ABI_TRY
+  ensure_context();
+  auto f = fp32() ? chi0_entry<float> : chi0_entry<double>;
+  f(chi, nullptr, nullptr, Gk, kmap, invk, olist, *temp, *Nx, *Ny, *Nz, *Nw, *Nk, *Nkall, *Norb, *Nchi, nullptr,
+    nullptr, 0.0, false, false, irr_chi, chi_map);
+  ABI_CATCH("get_chi0_conv_", nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)))
+}
+
+void get_chis(double2* chis, const double2* chi0, const double* Smat, const int64_t* Nchi, const int64_t* Nw) {
+  ABI_TRY
+  ensure_context();
+  const int64_t n = *Nchi, nw = *Nw;
+  PGB_CHECK(n <= kMaxChi, "Nchi above the engine limit of 32 orbital pairs");
+  DBuf<double2> X(n * n * nw);
+  DBuf<double> S(n * n);
+  X.upload(chi0, n * n * nw);
+  S.upload(Smat, n * n);
+  PGB_CHECK(vertex<double>(X.p, nw, -1, (int)n, S.p, S.p, 3), "zgesv failed: singular (I - chi0 S)");
+  X.download(chis, n * n * nw);
+  sync();
+  ABI_CATCH("get_chis", nan_fill(chis, (size_t)(*Nchi) * (*Nchi) * (*Nw)))
+}
+
+void get_chis_chic(double2* chis, double2* chic, const double2* chi, const double* Smat, const double* Cmat,
+                   const int64_t* Nk, const int64_t* Nw, const int64_t* Nchi) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, nw = *Nw, n = *Nchi;
+  PGB_CHECK(n <= kMaxChi, "Nchi above the engine limit of 32 orbital pairs");
+  const long long K = nk * nw;
+  DBuf<double2> X(K * n * n), A(nk * n * n), B(nk * n * n);
+  DBuf<double> S(n * n), C(n * n);
+  X.upload(chi, K * n * n);
+  S.upload(Smat, n * n);
+  C.upload(Cmat, n * n);
+  k_extract_nu0<<<g1(nk * n * n, 256), 256, 0, ctx().stream>>>(A.p, X.p, nk, K, (int)(n * n));
+  launch_check("extract_nu0");
+  X.release();
+  PGB_CUDA(cudaMemcpyAsync(B.p, A.p, A.bytes(), cudaMemcpyDeviceToDevice, ctx().stream));
+  PGB_CHECK(vertex<double>(A.p, nk, nk, (int)n, S.p, C.p, 3), "zgesv failed: singular (I - chi0 S)");
+  PGB_CHECK(vertex<double>(B.p, nk, nk, (int)n, S.p, C.p, 4), "zgesv failed: singular (I + chi0 C)");
+  A.download(chis, nk * n * n);
+  B.download(chic, nk * n * n);
+  sync();
+  ABI_CATCH("get_chis_chic", (nan_fill(chis, (size_t)(*Nk) * (*Nchi) * (*Nchi)),
+                              nan_fill(chic, (size_t)(*Nk) * (*Nchi) * (*Nchi))))
+}
+
+void get_eig_or_tr_chi(double2* chiqout, const double2* chi, const int64_t* invk, const int64_t* Nkall,
+                       const int64_t* Nk, const int64_t* Nchi, const bool* sw_eig) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, n = *Nchi, nkall = *Nkall;
+  PGB_CHECK(n <= kMaxChi, "Nchi above the engine limit of 32 orbital pairs");
+  for (int64_t i = 0; i < nkall; ++i) PGB_CHECK(invk[3 * i] >= 1 && invk[3 * i] <= nk, "invk(1,:) outside [1,Nk]");
+  DBuf<double2> X(nk * n * n), v(nk), out(nkall);
+  DBuf<int64_t> iv(3 * nkall);
+  X.upload(chi, nk * n * n);
+  iv.upload(invk, 3 * nkall);
+  k_eig_or_tr<<<g1(nk, 32), 32, 0, ctx().stream>>>(v.p, X.p, nk, (int)n, (*sw_eig) ? 1 : 0);
+  launch_check("eig_or_tr");
+  k_map_full<<<g1(nkall, 256), 256, 0, ctx().stream>>>(out.p, v.p, iv.p, nkall);
+  launch_check("map_full");
+  out.download(chiqout, nkall);
+  sync();
+  ABI_CATCH("get_eig_or_tr_chi", nan_fill(chiqout, (size_t)(*Nkall)))
+}
+
+void get_vsigma_flex_nosoc_(double2* chi, const double* Smat, const double* Cmat, const int64_t* Nk,
+                            const int64_t* Nw, const int64_t* Nchi) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, nw = *Nw, n = *Nchi;
+  PGB_CHECK(n <= kMaxChi, "Nchi above the engine limit of 32 orbital pairs");
+  const long long K = nk * nw;
+  DBuf<double2> X(K * n * n);
+  DBuf<double> S(n * n), C(n * n);
+  X.upload(chi, K * n * n);
+  S.upload(Smat, n * n);
+  C.upload(Cmat, n * n);
+  PGB_CHECK(vertex<double>(X.p, K, K, (int)n, S.p, C.p, 0), "zgesv failed in V_sigma");
+  X.download(chi, K * n * n);
+  sync();
+  ABI_CATCH("get_vsigma_flex_nosoc_", nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)))
+}
+
+// ================================================================= flex ==
+void mkself(double2* sigmak, double* mu, const double* Smat, const double* Cmat, const int64_t* kmap,
+            const int64_t* invk, const int64_t* olist, const double2* hamk, const double* eig, const double2* uni,
+            const double* mu_init, const double* rfill, const double* temp, const int64_t* scf_loop, const double* pp,
+            const double* eps, const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb,
+            const int64_t* Nchi, const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* sub_sigma,
+            const bool* sw_out, const bool* sw_in, const int64_t* m_diis, const bool* sw_rescale, const bool* sw_tail,
+            const double* sigma_scale) {
+  ABI_TRY
+  ensure_context();
+  MkselfArgs a{sigmak, mu, Smat, Cmat, kmap, invk, olist, hamk, eig, uni, *mu_init, *rfill, *temp, *scf_loop, *pp,
+               *eps, *Nkall, *Nk, *Nw, *Norb, *Nchi, *Nx, *Ny, *Nz, *sub_sigma, *sw_out, *sw_in, *m_diis,
+               *sw_rescale, *sw_tail, *sigma_scale};
+  if (fp32()) run_mkself<float>(a);
+  else run_mkself<double>(a);
+  ABI_CATCH("mkself", (nan_fill(sigmak, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)), *mu = NAN))
+}
+
+void lin_eliash(double2* delta, double2* chi, const double2* Gk, const double2* uni, const double* init_delta,
+                const double* Smat, const double* Cmat, const int64_t* olist, const double* prt, const int64_t* kmap,
+                const int64_t* invk, const double* temp, const double* eps, const int64_t* Nkall, const int64_t* Nk,
+                const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nx, const int64_t* Ny,
+                const int64_t* Nz, const int64_t* itemax, const int64_t* gap_sym, const int64_t* arnoldi_m,
+                double* lambda_out) {
+  ABI_TRY
+  ensure_context();
+  LinEliashArgs a{delta, chi, Gk, uni, init_delta, Smat, Cmat, olist, prt, kmap, invk, *temp, *eps, *Nkall, *Nk, *Nw,
+                  *Nchi, *Norb, *Nx, *Ny, *Nz, *itemax, *gap_sym, *arnoldi_m, lambda_out};
+  if (fp32()) run_lin_eliash<float>(a);
+  else run_lin_eliash<double>(a);
+  ABI_CATCH("lin_eliash", (nan_fill(delta, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)), *lambda_out = NAN))
+}
+
+void pyrpa_gb_flex_eliash(double2* sigmak, double* mu, double2* delta, double* lambda_out, double* stoner,
+                          double* times_ms, const double* Smat, const double* Cmat, const int64_t* kmap,
+                          const int64_t* invk, const int64_t* olist, const double2* hamk, const double* eig,
+                          const double2* uni, const double* init_delta, const double* prt, const double2* sigma_seed,
+                          const double* seed_mu, const double* seed_mu_old, const double* mu_init,
+                          const double* rfill, const double* temp, const int64_t* scf_loop, const double* pp,
+                          const double* eps, const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw,
+                          const int64_t* Norb, const int64_t* Nchi, const int64_t* Nx, const int64_t* Ny,
+                          const int64_t* Nz, const int64_t* sub_sigma, const int64_t* m_diis, const bool* sw_rescale,
+                          const bool* sw_tail, const int64_t* gap_sym, const int64_t* arnoldi_m,
+                          const int64_t* itemax, const double* eps_eliash) {
+  ABI_TRY
+  ensure_context();
+  PipelineArgs a{sigmak, mu, delta, lambda_out, stoner, times_ms, Smat, Cmat, kmap, invk, olist, hamk, eig, uni,
+                 init_delta, prt, sigma_seed, seed_mu ? *seed_mu : 0.0, seed_mu_old ? *seed_mu_old : 0.0, *mu_init,
+                 *rfill, *temp, *scf_loop, *pp, *eps, *Nkall, *Nk, *Nw, *Norb, *Nchi, *Nx, *Ny, *Nz, *sub_sigma,
+                 *m_diis, *sw_rescale, *sw_tail, *gap_sym, *arnoldi_m, *itemax, *eps_eliash};
+  if (fp32()) run_pipeline<float>(a);
+  else run_pipeline<double>(a);
+  ABI_CATCH("pyrpa_gb_flex_eliash", (nan_fill(sigmak, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)),
+                                     nan_fill(delta, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)), *mu = NAN,
+                                     *lambda_out = NAN))
+}
+
+void mkfk_trs_nsoc_(double2* fk, const double2* Gk, const double2* delta, const int64_t* Nk, const int64_t* Nw,
+                    const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  const long long K = (*Nk) * (*Nw), KE = K * no * no;
+  DBuf<double2> G(KE), D(KE), F(KE);
+  G.upload(Gk, KE);
+  D.upload(delta, KE);
+  mkfk(F.p, G.p, D.p, K, (int)no);
+  F.download(fk, KE);
+  sync();
+  ABI_CATCH("mkfk_trs_nsoc_", nan_fill(fk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+void get_initial_delta_(double2* delta, const double* init_delta, const double2* uni, const int64_t* kmap,
+                        const int64_t* invk, const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw,
+                        const int64_t* Norb, const int64_t* gap_sym) {
+  ABI_TRY
+  ensure_context();
+  (void)kmap;
+  const int64_t nk = *Nk, nw = *Nw, no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  const long long KE = nk * nw * no * no;
+  std::vector<double> w(nk, 0.0);
+  for (int64_t i = 0; i < *Nkall; ++i) {
+    const int64_t k = invk[3 * i] - 1;
+    PGB_CHECK(k >= 0 && k < nk, "invk(1,:) outside [1,Nk]");
+    w[k] += 1.0;
+  }
+  DBuf<double> kw(nk), init(nk * no);
+  DBuf<double2> u(no * no * nk), D(KE);
+  kw.upload(w.data(), nk);
+  init.upload(init_delta, nk * no);
+  u.upload(uni, no * no * nk);
+  initial_delta(D.p, init.p, u.p, (int)nk, (int)nw, (int)no, (int)*gap_sym);
+  const double nrm = inner_w(D.p, D.p, kw.p, (int)nk, KE).x;
+  PGB_CHECK(nrm > 0, "Error: get_initial_delta norm <= 0");
+  scal(D.p, 1.0 / std::sqrt(2.0 * nrm), KE);
+  D.download(delta, KE);
+  sync();
+  ABI_CATCH("get_initial_delta_", nan_fill(delta, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+void remap_delta_(double2* delta, const double2* delta0, const double* prt, const int64_t* invk, const int64_t* Nkall,
+                  const int64_t* Nk, const int64_t* Nw, const int64_t* Norb, const int64_t* gap_sym) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nkall = *Nkall, nk = *Nk, nw = *Nw, no = *Norb;
+  for (int64_t i = 0; i < nkall; ++i) PGB_CHECK(invk[3 * i] >= 1 && invk[3 * i] <= nk, "invk(1,:) outside [1,Nk]");
+  DBuf<double2> d0(nk * nw * no * no), out(nkall * nw * no * no);
+  DBuf<double> pr(no);
+  DBuf<int64_t> iv(3 * nkall);
+  d0.upload(delta0, nk * nw * no * no);
+  pr.upload(prt, no);
+  iv.upload(invk, 3 * nkall);
+  k_remap_delta<<<g1(nkall * nw * no * no, 256), 256, 0, ctx().stream>>>(out.p, d0.p, pr.p, iv.p, nkall, nk, nw,
+                                                                         (int)no, (*gap_sym < 0) ? -1.0 : 1.0);
+  launch_check("remap_delta");
+  out.download(delta, nkall * nw * no * no);
+  sync();
+  ABI_CATCH("remap_delta_", nan_fill(delta, (size_t)(*Nkall) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+void conv_delta_orb_to_band(double2* deltab, const double2* delta, const double2* uni, const double* prt,
+                            const int64_t* invk, const int64_t* Norb, const int64_t* Nkall, const int64_t* Nk,
+                            const int64_t* Nw, const int64_t* gap_sym) {
+  ABI_TRY
+  ensure_context();
+  const int64_t no = *Norb, nkall = *Nkall, nk = *Nk;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  for (int64_t i = 0; i < nkall; ++i) PGB_CHECK(invk[3 * i] >= 1 && invk[3 * i] <= nk, "invk(1,:) outside [1,Nk]");
+  // only the first Matsubara slice is used: copy delta(:,1,:,:) compactly
+  std::vector<double2> d0((size_t)nk * no * no);
+  for (int64_t e = 0; e < no * no; ++e)
+    memcpy(&d0[(size_t)nk * e], delta + (size_t)nk * (*Nw) * e, sizeof(double2) * nk);
+  DBuf<double2> d(nk * no * no), u(no * no * nk), out(nkall * no * no);
+  DBuf<double> pr(no);
+  DBuf<int64_t> iv(3 * nkall);
+  d.upload(d0.data(), nk * no * no);
+  u.upload(uni, no * no * nk);
+  pr.upload(prt, no);
+  iv.upload(invk, 3 * nkall);
+  k_orb_to_band<<<g1(nkall, 64), 64, 0, ctx().stream>>>(out.p, d.p, u.p, pr.p, iv.p, nkall, nk, (int)no,
+                                                        (*gap_sym < 0) ? -1.0 : 1.0);
+  launch_check("orb_to_band");
+  out.download(deltab, nkall * no * no);
+  sync();
+  ABI_CATCH("conv_delta_orb_to_band", nan_fill(deltab, (size_t)(*Nkall) * (*Norb) * (*Norb)))
+}
+
+// ============================================== outside the FLEX/RPA path ==
+// Present so that `import libs.flibs` binds every symbol; each reports that
+// it is not part of this engine.
+#define PGB_STUB(name)                                                                                    \
+  void name() {                                                                                            \
+    report(#name, "not part of the GB300 FLEX/RPA/Eliashberg engine (outside the accelerated path)");      \
+  }
+PGB_STUB(calc_kn)
+PGB_STUB(calc_lij)
+PGB_STUB(calc_lij_wl)
+PGB_STUB(calc_sigma_hall)
+PGB_STUB(calc_tau_epa)
+PGB_STUB(calc_tdf)
+PGB_STUB(chiq_map)
+PGB_STUB(conv_delta_orb_to_band_soc)
+PGB_STUB(eliashberg)
+PGB_STUB(gen_dos)
+PGB_STUB(gen_green_inv_from_eig)
+PGB_STUB(gen_imp_ham)
+PGB_STUB(gen_tr_greenw_0)
+PGB_STUB(get_a_)
+PGB_STUB(get_band_to_orb_delta)
+PGB_STUB(get_chi0_soc)
+PGB_STUB(get_chi_irr)
+PGB_STUB(get_chi_irr_sc)
+PGB_STUB(get_chis_chic_soc)
+PGB_STUB(get_dft_imp_ham)
+PGB_STUB(get_eig_mlo)
+PGB_STUB(get_imass0)
+PGB_STUB(get_imassk)
+PGB_STUB(get_iqshift_)
+PGB_STUB(get_phi_irr)
+PGB_STUB(get_qp_)
+PGB_STUB(get_qshift_)
+PGB_STUB(get_spectrum_spaghetti)
+PGB_STUB(get_tau)
+PGB_STUB(get_tr_chi)
+PGB_STUB(get_tr_phi)
+PGB_STUB(get_veloc)
+PGB_STUB(get_vlm0)
+PGB_STUB(get_vmat_soc)
+PGB_STUB(get_vmat_soc_orb)
+PGB_STUB(get_vnm)
+PGB_STUB(lin_eliash_soc)
+PGB_STUB(matrix_riccati_batch)
+PGB_STUB(matrix_riccati_chords)
+PGB_STUB(mkbdghamk)
+PGB_STUB(mkfk_trs_soc_)
+PGB_STUB(mkself_soc)
+PGB_STUB(pade_with_trace)
+PGB_STUB(phiq_map)
+PGB_STUB(riccati_chords)
+PGB_STUB(solve_cpa_array)
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+// Common device/host helpers of the GB300 FLEX engine: complex arithmetic on
+// float2/double2, error reporting, the per-process CUDA context.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace pgb {
+
+// ---------------------------------------------------------------- complex --
+template <typename R> struct cvec;
+template <> struct cvec<float> { using type = float2; };
+template <> struct cvec<double> { using type = double2; };
+template <typename R> using cx = typename cvec<R>::type;
+
+__host__ __device__ __forceinline__ float2 mkc(float a, float b) { return make_float2(a, b); }
+__host__ __device__ __forceinline__ double2 mkc(double a, double b) { return make_double2(a, b); }
+template <typename R> __host__ __device__ __forceinline__ cx<R> cmk(R a, R b) { return mkc(a, b); }
+
+__host__ __device__ __forceinline__ float2 operator+(float2 a, float2 b) { return mkc(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ double2 operator+(double2 a, double2 b) { return mkc(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 operator-(float2 a, float2 b) { return mkc(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ double2 operator-(double2 a, double2 b) { return mkc(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 operator-(float2 a) { return mkc(-a.x, -a.y); }
+__host__ __device__ __forceinline__ double2 operator-(double2 a) { return mkc(-a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 operator*(float2 a, float2 b) {
+  return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ double2 operator*(double2 a, double2 b) {
+  return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 operator*(float a, float2 b) { return mkc(a * b.x, a * b.y); }
+__host__ __device__ __forceinline__ double2 operator*(double a, double2 b) { return mkc(a * b.x, a * b.y); }
+__host__ __device__ __forceinline__ float2 operator*(float2 b, float a) { return mkc(a * b.x, a * b.y); }
+__host__ __device__ __forceinline__ double2 operator*(double2 b, double a) { return mkc(a * b.x, a * b.y); }
+__host__ __device__ __forceinline__ float2& operator+=(float2& a, float2 b) { a.x += b.x; a.y += b.y; return a; }
+__host__ __device__ __forceinline__ double2& operator+=(double2& a, double2 b) { a.x += b.x; a.y += b.y; return a; }
+__host__ __device__ __forceinline__ float2& operator-=(float2& a, float2 b) { a.x -= b.x; a.y -= b.y; return a; }
+__host__ __device__ __forceinline__ double2& operator-=(double2& a, double2 b) { a.x -= b.x; a.y -= b.y; return a; }
+
+__host__ __device__ __forceinline__ float2 conj(float2 a) { return mkc(a.x, -a.y); }
+__host__ __device__ __forceinline__ double2 conj(double2 a) { return mkc(a.x, -a.y); }
+__host__ __device__ __forceinline__ float abs2(float2 a) { return a.x * a.x + a.y * a.y; }
+__host__ __device__ __forceinline__ double abs2(double2 a) { return a.x * a.x + a.y * a.y; }
+// a * (s i), s = +-1
+__host__ __device__ __forceinline__ float2 muli(float2 a, float s) { return mkc(-s * a.y, s * a.x); }
+__host__ __device__ __forceinline__ double2 muli(double2 a, double s) { return mkc(-s * a.y, s * a.x); }
+// complex division a / b (scaled to avoid overflow for large |b|)
+__host__ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  double s = fabs(b.x) + fabs(b.y);
+  double bx = b.x / s, by = b.y / s;
+  double d = bx * bx + by * by;
+  double ax = a.x / s, ay = a.y / s;
+  return mkc((ax * bx + ay * by) / d, (ay * bx - ax * by) / d);
+}
+__host__ __device__ __forceinline__ float2 cdiv(float2 a, float2 b) {
+  float s = fabsf(b.x) + fabsf(b.y);
+  float bx = b.x / s, by = b.y / s;
+  float d = bx * bx + by * by;
+  float ax = a.x / s, ay = a.y / s;
+  return mkc((ax * bx + ay * by) / d, (ay * bx - ax * by) / d);
+}
+__host__ __device__ __forceinline__ double cabs_(double2 a) { return hypot(a.x, a.y); }
+__host__ __device__ __forceinline__ float cabs_(float2 a) { return hypotf(a.x, a.y); }
+
+template <typename D, typename S> __host__ __device__ __forceinline__ cx<D> ccast(S a) {
+  return cmk<D>((D)a.x, (D)a.y);
+}
+
+// ---------------------------------------------------------------- errors --
+struct Error : std::runtime_error {
+  explicit Error(const std::string& s) : std::runtime_error(s) {}
+};
+
+#define PGB_CUDA(call)                                                               \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      throw ::pgb::Error(std::string(#call) + ": " + cudaGetErrorString(e_));        \
+  } while (0)
+
+#define PGB_CHECK(cond, msg)                     \
+  do {                                           \
+    if (!(cond)) throw ::pgb::Error(msg);        \
+  } while (0)
+
+inline void launch_check(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw Error(std::string("launch ") + what + ": " + cudaGetErrorString(e));
+}
+
+inline unsigned nblocks(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+// -------------------------------------------------------------- context --
+// One CUDA stream per process; every entry point of the library runs on it and
+// synchronizes it before returning (the C ABI is synchronous like the
+// reference's Fortran subroutines).
+struct Context {
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int num_sms = 0;
+  bool ready = false;
+  int precision = 64;          // 64: FP64 bulk; 32: complex FP32 bulk with FP64 steps
+  int verbose = 1;             // progress prints like the reference's stdout
+  long long kernel_launches = 0;
+};
+Context& ctx();
+void ensure_context();
+
+// Device allocation through the stream-ordered pool (memory stays cached in
+// the pool between calls, so repeated calls of one shape do not re-map HBM).
+template <typename T> struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t count) { alloc(count); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  void alloc(size_t count) {
+    release();
+    n = count;
+    if (count) PGB_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), ctx().stream));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, ctx().stream);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+  size_t bytes() const { return n * sizeof(T); }
+  void zero() {
+    if (n) PGB_CUDA(cudaMemsetAsync(p, 0, bytes(), ctx().stream));
+  }
+  void upload(const void* h, size_t count) {
+    PGB_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, ctx().stream));
+  }
+  void download(void* h, size_t count) const {
+    PGB_CUDA(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, ctx().stream));
+  }
+};
+
+inline void sync() { PGB_CUDA(cudaStreamSynchronize(ctx().stream)); }
+
+void log(const char* fmt, ...);
+
+}  // namespace pgb

@@ -1,0 +1,830 @@
+// FLEX self-consistency loop and linearized-Eliashberg solver on the GPU.
+//
+// Host code here only orchestrates: every array operation is a kernel of
+// flex.cu; the host keeps the scalar control flow of the reference (DIIS
+// coefficient solve of a (m+1)^2 system, the Brent/bisection search for mu,
+// the m x m Hessenberg eigenproblem of Arnoldi), all in FP64.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <vector>
+
+#include "drivers.cuh"
+#include "linalg.cuh"
+
+namespace pgb {
+
+namespace {
+
+LastStats g_stats;
+
+struct Timer {
+  cudaEvent_t a, b;
+  Timer() {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+  }
+  ~Timer() {
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+  void start() { cudaEventRecord(a, ctx().stream); }
+  double stop() {
+    cudaEventRecord(b, ctx().stream);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+};
+
+__global__ void k_sub(double2* out, const double2* a, const double2* b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = a[i] - b[i];
+}
+
+struct DiisTerms {
+  const double2* x[16];
+  double c[16];
+};
+
+// sigma_diis = sum c_i x_i; relative change estimate; mixing (fself.f90:494-532)
+__global__ void k_diis_mix(double2* sig, const double2* sig0, DiisTerms t, int n, double pp, int use_diis,
+                           double* partmax, long long N) {
+  __shared__ double red[256];
+  double mx = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    double2 sd = mkc(0.0, 0.0);
+    for (int h = 0; h < n; ++h) sd += t.c[h] * t.x[h][i];
+    const double2 s0 = sig0[i];
+    const double asd = hypot(sd.x, sd.y);
+    if (asd > 1.0e-10) {
+      const double2 d = s0 - sd;
+      mx = fmax(mx, hypot(d.x, d.y) / asd);
+    }
+    sig[i] = use_diis ? sd : (pp * sd + (1.0 - pp) * s0);
+  }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partmax[blockIdx.x] = red[0];
+}
+
+__global__ void k_max_parts(double* out, const double* part, int n) {
+  __shared__ double red[256];
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, part[i]);
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+// real (n x n) solve with partial pivoting; false if singular (dgesv semantics)
+bool solve_real(std::vector<double> A, std::vector<double>& b, int n) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(A[i * n + k]) > std::fabs(A[p * n + k])) p = i;
+    if (A[p * n + k] == 0.0) return false;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) std::swap(A[k * n + j], A[p * n + j]);
+      std::swap(b[k], b[p]);
+    }
+    for (int i = k + 1; i < n; ++i) {
+      const double l = A[i * n + k] / A[k * n + k];
+      for (int j = k; j < n; ++j) A[i * n + j] -= l * A[k * n + j];
+      b[i] -= l * b[k];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    double s = b[k];
+    for (int j = k + 1; j < n; ++j) s -= A[k * n + j] * b[j];
+    b[k] = s / A[k * n + k];
+  }
+  return true;
+}
+
+// ----------------------------------------------------------- sigma.bin --
+// gfortran sequential unformatted records (4-byte length markers), written
+// and read like io_sigma / ck_sigma_meta (fself.f90:742-780).
+void write_record(std::ofstream& f, const void* data, size_t bytes) {
+  PGB_CHECK(bytes < 2147483639ULL, "sigma.bin record above 2 GiB is not supported");
+  const int32_t n = (int32_t)bytes;
+  f.write((const char*)&n, 4);
+  f.write((const char*)data, (std::streamsize)bytes);
+  f.write((const char*)&n, 4);
+}
+bool read_record(std::ifstream& f, void* data, size_t bytes) {
+  int32_t n = 0, m = 0;
+  if (!f.read((char*)&n, 4)) return false;
+  if ((size_t)n != bytes) throw Error("sigma.bin record of " + std::to_string(n) + " bytes, expected " +
+                                      std::to_string(bytes));
+  f.read((char*)data, (std::streamsize)bytes);
+  f.read((char*)&m, 4);
+  PGB_CHECK(f && m == n, "sigma.bin record markers do not match");
+  return true;
+}
+
+void write_sigma_bin(double mu, double mu_old, const std::vector<double2>& sig, double temp, int Nw, int Norb,
+                     int Nk) {
+  std::ofstream f("sigma.bin", std::ios::binary | std::ios::trunc);
+  PGB_CHECK(f.good(), "cannot open sigma.bin for writing");
+  write_record(f, &mu, 8);
+  write_record(f, &mu_old, 8);
+  write_record(f, sig.data(), sig.size() * sizeof(double2));
+  const double meta[4] = {temp, (double)Nw, (double)Norb, (double)Nk};
+  write_record(f, meta, sizeof(meta));
+}
+
+void read_sigma_bin(double& mu, double& mu_old, std::vector<double2>& sig, double temp, int Nw, int Norb, int Nk) {
+  std::ifstream f("sigma.bin", std::ios::binary);
+  PGB_CHECK(f.good(), "sigma.bin not found in the working directory");
+  PGB_CHECK(read_record(f, &mu, 8), "sigma.bin: missing mu record");
+  PGB_CHECK(read_record(f, &mu_old, 8), "sigma.bin: missing mu_old record");
+  // peek the length of the sigma record to report a mesh mismatch clearly
+  int32_t n = 0;
+  std::streampos pos = f.tellg();
+  f.read((char*)&n, 4);
+  f.seekg(pos);
+  if ((size_t)n != sig.size() * sizeof(double2)) {
+    throw Error("io_sigma: sigma.bin was written on a different mesh (record of " + std::to_string(n) +
+                " bytes); convert the seed with plibs.regrid_sigma_bin first");
+  }
+  read_record(f, sig.data(), sig.size() * sizeof(double2));
+  double meta[4];
+  int32_t m = 0;
+  if (f.read((char*)&m, 4) && m == 32) {
+    f.read((char*)meta, 32);
+    if ((int)std::lround(meta[1]) != Nw || (int)std::lround(meta[2]) != Norb || (int)std::lround(meta[3]) != Nk)
+      throw Error("io_sigma: sigma.bin was written on a different mesh; convert the seed with "
+                  "plibs.regrid_sigma_bin first");
+    if (std::fabs(meta[0] - temp) > 1e-10)
+      log("io_sigma: seed was written at T=%10.6f eV, reused raw at T=%10.6f eV (T-annealing)\n", meta[0], temp);
+  }
+}
+
+// ------------------------------------------------------- host eigen (m x m)
+// eigenvalues and the zgeev-normalized eigenvector of eigenvalue idx
+void eig_small(const std::vector<double2>& H, int m, std::vector<double2>& w) {
+  std::vector<double2> A(H);
+  w.assign(m, make_double2(0, 0));
+  PGB_CHECK(eigvals_general(A.data(), m, w.data()) >= 0, "Hessenberg eigenvalue iteration did not converge");
+}
+
+std::vector<double2> eigvec(const std::vector<double2>& H, int m, double2 lam) {
+  std::vector<double2> x(m, make_double2(1.0, 0.0));
+  const double sc = 1e-13 * (std::fabs(lam.x) + std::fabs(lam.y) + 1.0);
+  for (int it = 0; it < 4; ++it) {
+    std::vector<double2> A(m * m), b(x);
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) A[i * m + j] = H[i * m + j] - ((i == j) ? (lam + make_double2(sc, 0)) : make_double2(0, 0));
+    // complex LU with partial pivoting
+    for (int k = 0; k < m; ++k) {
+      int p = k;
+      for (int i = k + 1; i < m; ++i)
+        if (cabs1(A[i * m + k]) > cabs1(A[p * m + k])) p = i;
+      if (cabs1(A[p * m + k]) == 0) A[p * m + k] = make_double2(1e-300, 0);
+      if (p != k) {
+        for (int j = 0; j < m; ++j) std::swap(A[k * m + j], A[p * m + j]);
+        std::swap(b[k], b[p]);
+      }
+      for (int i = k + 1; i < m; ++i) {
+        double2 l = cdiv(A[i * m + k], A[k * m + k]);
+        for (int j = k; j < m; ++j) A[i * m + j] -= l * A[k * m + j];
+        b[i] -= l * b[k];
+      }
+    }
+    for (int k = m - 1; k >= 0; --k) {
+      double2 s = b[k];
+      for (int j = k + 1; j < m; ++j) s -= A[k * m + j] * b[j];
+      b[k] = cdiv(s, A[k * m + k]);
+    }
+    double nrm = 0;
+    for (auto& v : b) nrm += abs2(v);
+    nrm = std::sqrt(nrm);
+    for (int i = 0; i < m; ++i) x[i] = b[i] * (1.0 / nrm);
+  }
+  // largest component real and positive (zgeev normalization)
+  int kmax = 0;
+  for (int i = 1; i < m; ++i)
+    if (abs2(x[i]) > abs2(x[kmax])) kmax = i;
+  const double a = std::sqrt(abs2(x[kmax]));
+  const double2 ph = conj(x[kmax]) * (1.0 / a);
+  for (auto& v : x) v = v * ph;
+  return x;
+}
+
+}  // namespace
+
+const LastStats& last_stats() { return g_stats; }
+
+// ================================================================ inputs ==
+void upload_inputs(Inputs& in, const int64_t* kmap, const int64_t* invk, const int64_t* olist, int64_t Nx, int64_t Ny,
+                   int64_t Nz, int64_t Nkall, int64_t Nk, int64_t Nw, int64_t Norb, int64_t Nchi, const double* Smat,
+                   const double* Cmat, const double2* hamk, const double* eig, const double2* uni) {
+  PGB_CHECK(Nkall == Nx * Ny * Nz, "Nkall differs from Nx*Ny*Nz");
+  in.Norb = (int)Norb;
+  in.Nchi = (int)Nchi;
+  in.Nk = (int)Nk;
+  in.Nw = (int)Nw;
+  build_geom(in.g, kmap, invk, Nx, Ny, Nz, Nk, Nw, Norb, Nchi);
+  build_pairs(in.p, olist, (int)Norb, (int)Nchi);
+  in.S.alloc(Nchi * Nchi);
+  in.C.alloc(Nchi * Nchi);
+  in.S.upload(Smat, Nchi * Nchi);
+  in.C.upload(Cmat, Nchi * Nchi);
+  if (eig) {
+    in.eig.alloc(Norb * Nk);
+    in.eig.upload(eig, Norb * Nk);
+  }
+  if (hamk) {
+    in.H.alloc(Norb * Norb * Nk);
+    in.H.upload(hamk, Norb * Norb * Nk);
+  }
+  if (uni) {
+    in.uni.alloc(Norb * Norb * Nk);
+    in.uni.upload(uni, Norb * Norb * Nk);
+  }
+}
+
+// ================================================================ mkself ==
+template <typename R>
+void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_out, const double2* seed,
+                 double seed_mu, double seed_mu_old) {
+  cudaStream_t st = ctx().stream;
+  const Geom& g = in.g;
+  const Pairs& p = in.p;
+  const int Norb = in.Norb, Nchi = in.Nchi, Nk = in.Nk, Nw = in.Nw;
+  PGB_CHECK(a.m_diis >= 1 && a.m_diis <= 16, "m_diis outside 1..16");
+  const long long K = g.K, No2 = (long long)Norb * Norb, KE = K * No2;
+  DBuf<double>& S = in.S;
+  DBuf<double>& C = in.C;
+  DBuf<double>& eig = in.eig;
+  DBuf<double2>& H = in.H;
+  DBuf<double2>& uni = in.uni;
+  DBuf<double2> G(KE), sig(KE), sig0(KE), eg((size_t)K * Norb);
+  DBuf<cx<R>> chi((size_t)K * Nchi * Nchi);
+  std::vector<DBuf<double2>> xout(a.m_diis), res(a.m_diis);
+  for (int i = 0; i < a.m_diis; ++i) {
+    xout[i].alloc(KE);
+    res[i].alloc(KE);
+  }
+  double mu = a.mu_init, mu_old = 0.0, esterr = 0.0, maxchi0s = 0.0;
+  if (a.sw_in || seed) {
+    if (seed) {
+      mu = seed_mu;
+      mu_old = seed_mu_old;
+      PGB_CUDA(cudaMemcpyAsync(sig.p, seed, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    } else {
+      log(" load self\n");
+      std::vector<double2> hs(KE);
+      read_sigma_bin(mu, mu_old, hs, a.temp, Nw, Norb, Nk);
+      sig.upload(hs.data(), KE);
+    }
+    if (a.sigma_scale != 1.0) {
+      log("[FLEX] scale loaded sigma seed by%10.6f\n", a.sigma_scale);
+      scal(sig.p, a.sigma_scale, KE);
+    }
+    PGB_CUDA(cudaMemcpyAsync(sig0.p, sig.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    PGB_CHECK(dyson(G.p, sig.p, H.p, mu, a.temp, Nk, Nw, Norb), "singular G^-1 in the Dyson step");
+  } else {
+    mu_old = mu * 1.2;
+    sig0.zero();
+    green0(G.p, eig.p, uni.p, mu, a.temp, Nk, Nw, Norb);
+  }
+  // DIIS state
+  int n_hist = 0, i_hist = 0;
+  std::vector<double> Bc((size_t)a.m_diis * a.m_diis, 0.0);
+  // mu bracket cache
+  bool bracket_valid = false;
+  double muS_cache = 0, muL_cache = 0;
+  DBuf<double> partmax(1024), dmax(1);
+
+  auto compare_sigma = [&]() {
+    i_hist = i_hist % a.m_diis + 1;
+    n_hist = std::min(n_hist + 1, (int)a.m_diis);
+    const int slot = i_hist - 1;
+    PGB_CUDA(cudaMemcpyAsync(xout[slot].p, sig.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    k_sub<<<nblocks(KE, 256) > 65536 ? 65536 : nblocks(KE, 256), 256, 0, st>>>(res[slot].p, sig.p, sig0.p, KE);
+    launch_check("diis_residual");
+    ctx().kernel_launches++;
+    const int n = n_hist;
+    std::vector<int> idx(n);
+    for (int h = 1; h <= n; ++h) idx[h - 1] = (((i_hist - n + h - 1) % a.m_diis) + a.m_diis) % a.m_diis;
+    for (int h = 0; h < n; ++h) {
+      const double v = dot_re(res[slot].p, res[idx[h]].p, KE);
+      Bc[slot * a.m_diis + idx[h]] = v;
+      Bc[idx[h] * a.m_diis + slot] = v;
+    }
+    const int nn = n + 1;
+    std::vector<double> B((size_t)nn * nn, 0.0), c(nn, 0.0);
+    for (int i = 0; i < n; ++i) {
+      for (int j = 0; j < n; ++j) B[i * nn + j] = Bc[idx[i] * a.m_diis + idx[j]];
+      B[i * nn + n] = 1.0;
+      B[n * nn + i] = 1.0;
+      B[i * nn + i] += 1.0e-12;
+    }
+    c[n] = 1.0;
+    if (!solve_real(B, c, nn)) {
+      log(" DIIS: dgesv failed, fallback to most-recent entry\n");
+      std::fill(c.begin(), c.end(), 0.0);
+      c[n - 1] = 1.0;
+    }
+    DiisTerms t{};
+    for (int h = 0; h < n; ++h) {
+      t.x[h] = xout[idx[h]].p;
+      t.c[h] = c[h];
+    }
+    k_diis_mix<<<1024, 256, 0, st>>>(sig.p, sig0.p, t, n, a.pp, n >= 2 ? 1 : 0, partmax.p, KE);
+    launch_check("diis_mix");
+    k_max_parts<<<1, 256, 0, st>>>(dmax.p, partmax.p, 1024);
+    launch_check("max_parts");
+    ctx().kernel_launches += 2;
+    dmax.download(&esterr, 1);
+    sync();
+    log("esterr=%9.2E\n", esterr);
+  };
+
+  auto get_rn = [&](double rmu) { return filling(eg.p, eig.p, Nk, Nw, Norb, rmu, a.temp); };
+
+  auto renew_mu = [&]() {
+    PGB_CHECK(eig_gkinv(eg.p, H.p, sig.p, Nk, Nw, Norb), "eigenvalues of H+Sigma did not converge");
+    const double eps = (esterr > 1.0e-2) ? 1.0e-8 : esterr * 1.0e-1;
+    double dmu = std::fabs(mu - mu_old) * 2.0;
+    if (dmu < eps * 4.0) dmu = eps * 4.0;
+    mu_old = mu;
+    const double fill = a.fill;
+    double muS = 0, muL = 0, rnS = 0, rnL = 0;
+    bool found = false;
+    if (bracket_valid) {
+      rnS = get_rn(muS_cache);
+      rnL = get_rn(muL_cache);
+      if (rnS < fill && rnL > fill) {
+        muS = muS_cache;
+        muL = muL_cache;
+        found = true;
+        log("[mu] cached bracket valid\n");
+      } else {
+        log("[mu] cached bracket invalid, re-searching\n");
+      }
+    }
+    if (!found) {
+      muL = mu + dmu;
+      muS = mu - dmu;
+      for (int it = 1; it <= 100; ++it) {
+        mu = muL;
+        rnL = get_rn(mu);
+        if (rnL < fill) {
+          if (std::fabs(fill - rnL) > 0.5) muL += 1.0;
+          else if (std::fabs(fill - rnL) > dmu) muL += 0.5;
+          else muL += dmu;
+        } else {
+          break;
+        }
+        PGB_CHECK(it < 100, "Too many");
+      }
+      for (int it = 1; it <= 100; ++it) {
+        mu = muS;
+        rnS = get_rn(mu);
+        if (rnS > fill) {
+          if (std::fabs(rnS - fill) > 0.5) muS -= 1.0;
+          else if (std::fabs(rnS - fill) > dmu) muS -= 0.5;
+          else muS -= dmu;
+        } else {
+          break;
+        }
+        PGB_CHECK(it < 100, "Too many");
+      }
+    }
+    muS_cache = muS;
+    muL_cache = muL;
+    bracket_valid = true;
+    rnL -= fill;
+    rnS -= fill;
+    double rnc = rnS, muc = muS, mud = 0.0, muM = 0.0, rnM = 0.0;
+    bool flag = false;
+    // inverse quadratic interpolation / bisection hybrid (fself.f90:623-654)
+    for (int it = 1; it <= 100; ++it) {
+      if (rnc != rnS && rnc != rnL)
+        muM = (muL * rnS * rnc * (rnS - rnc) + muS * rnL * rnc * (rnc - rnL) + muc * rnL * rnS * (rnL - rnS)) /
+              ((rnL - rnS) * (rnc - rnL) * (rnc - rnS));
+      else
+        muM = muL - rnL * (muL - muS) / (rnL - rnS);
+      if ((0.25 * (3.0 * muS + muL) > muM || muM > muL) || (flag && std::fabs(muM - muL) >= std::fabs(muL - muc) * 0.5) ||
+          (!flag && std::fabs(muM - muL) >= std::fabs(muc - mud) * 0.5) || (flag && std::fabs(muL - muc) < 1.0e-8) ||
+          (!flag && std::fabs(muc - mud) < 1.0e-8)) {
+        muM = (muL + muS) * 0.5;
+        flag = true;
+      } else {
+        flag = false;
+      }
+      if (std::fabs(muL - muM) < eps) break;
+      mu = muM;
+      rnM = get_rn(muM);
+      mud = muc;
+      muc = muL;
+      rnc = rnL;
+      if (rnS * (rnM - fill) < 0) {
+        muL = muM;
+        rnL = rnM - fill;
+      } else {
+        muS = muM;
+        rnS = rnM - fill;
+      }
+      if (std::fabs(rnS) < std::fabs(rnL)) {
+        std::swap(muL, muS);
+        std::swap(rnL, rnS);
+      }
+      PGB_CHECK(it < 100, "Too many loop!");
+    }
+    mu = (rnL == rnS) ? (muS + muL) * 0.5 : (muS * rnL - muL * rnS) / (rnL - rnS);
+    rnM = get_rn(mu);
+    mu_old = mu;
+    log("mu  =%8.4f filling =%8.4f\n", mu, rnM);
+  };
+
+  Timer tm;
+  TailRef tail{eig.p, uni.p, mu};
+  int it = 0;
+  for (it = 1; it <= a.scf_loop; ++it) {
+    log("iter=%5d\n", it);
+    tm.start();
+    tail.mu = mu;
+    chi0<R>(g, p, G.p, a.temp, a.sw_tail ? &tail : nullptr, chi.p);
+    g_stats.t_chi0 += tm.stop();
+    double sdw = 0, cdw = 0;
+    int qs = 0, qc = 0;
+    tm.start();
+    stoner<R>(g, chi.p, S.p, C.p, &sdw, &cdw, &qs, &qc);
+    ckchi_print(g, sdw, cdw, qs, qc);
+    maxchi0s = sdw;
+    if (a.sw_rescale && maxchi0s >= 1.0) {
+      const double rt = 1.0 - 1.0e-4;
+      log("[FLEX] Stoner factor=%10.6f >= 1: rescaling chi0 to%7.4f\n", maxchi0s, rt);
+      scale_chi<R>(chi.p, K * Nchi * Nchi, rt / maxchi0s);
+    }
+    PGB_CHECK(vertex<R>(chi.p, K, K, Nchi, S.p, C.p, 0), "zgesv failed in V_sigma");
+    g_stats.t_vertex += tm.stop();
+    tm.start();
+    sigma<R>(g, p, G.p, chi.p, S.p, C.p, a.temp, sig.p);
+    g_stats.t_sigma += tm.stop();
+    tm.start();
+    if (a.sub_sigma > 0) hf_subtract(sig.p, Nk, Nw, Norb, (int)a.sub_sigma);
+    compare_sigma();
+    g_stats.t_diis += tm.stop();
+    g_stats.esterr = esterr;
+    g_stats.iterations = it;
+    g_stats.stoner = maxchi0s;
+    if (esterr < a.eps) break;
+    tm.start();
+    renew_mu();
+    g_stats.t_mu += tm.stop();
+    tm.start();
+    PGB_CHECK(dyson(G.p, sig.p, H.p, mu, a.temp, Nk, Nw, Norb), "singular G^-1 in the Dyson step");
+    PGB_CUDA(cudaMemcpyAsync(sig0.p, sig.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    g_stats.t_dyson += tm.stop();
+  }
+  if (maxchi0s >= 1.0) {
+    log("[FLEX] WARNING: Stoner factor >= 1 at the final iteration:\n");
+    log("[FLEX]   max eig[chi0*S] =%10.6f -> the normal state is magnetically unstable at this T/U.\n", maxchi0s);
+  }
+  std::vector<double2> hs(KE);
+  if (a.sw_out) {
+    sig.download(hs.data(), KE);
+    sync();
+    write_sigma_bin(mu, mu_old, hs, a.temp, Nw, Norb, Nk);
+  }
+  tm.start();
+  renew_mu();
+  g_stats.t_mu += tm.stop();
+  PGB_CUDA(cudaMemcpyAsync(sig_out, sig.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  sync();
+  *mu_out = mu;
+  g_stats.mu = mu;
+}
+
+template <typename R>
+void run_mkself(const MkselfArgs& a) {
+  g_stats = LastStats{};
+  Inputs in;
+  upload_inputs(in, a.kmap, a.invk, a.olist, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Smat, a.Cmat,
+                a.hamk, a.eig, a.uni);
+  FlexParams prm{a.mu_init, a.fill, a.temp, a.scf_loop, a.pp, a.eps, a.sub_sigma, a.sw_out, a.sw_in, a.m_diis,
+                 a.sw_rescale, a.sw_tail, a.sigma_scale};
+  const long long KE = in.g.K * a.Norb * a.Norb;
+  DBuf<double2> sig(KE);
+  mkself_core<R>(in, prm, sig.p, a.mu_out, nullptr, 0.0, 0.0);
+  sig.download(a.sigmak, KE);
+  sync();
+}
+
+// ============================================================ lin_eliash ==
+// chi (device, cx<R>) is overwritten with the pairing vertex V_Delta; if
+// chi_host is given, V_Delta is also copied back there (feliash.f90:61).
+template <typename R>
+double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init, const double* prt,
+                   const EliashParams& a, double2* delta_out, double2* chi_host) {
+  cudaStream_t st = ctx().stream;
+  const Geom& g = in.g;
+  const Pairs& p = in.p;
+  const int Norb = in.Norb, Nchi = in.Nchi, Nk = in.Nk, Nw = in.Nw;
+  const long long K = g.K, KE = K * Norb * Norb, KC = K * Nchi * Nchi;
+  const bool singlet = a.gap_sym >= 0;
+  log(singlet ? "singlet\n" : "triplet\n");
+  DBuf<double>& S = in.S;
+  DBuf<double>& C = in.C;
+  DBuf<double2>& uni = in.uni;
+  {
+    Timer tv;
+    tv.start();
+    PGB_CHECK(vertex<R>(chi, K, K, Nchi, S.p, C.p, singlet ? 1 : 2), "zgesv failed in V_delta");
+    g_stats.t_vertex += tv.stop();
+    if (chi_host) {
+      DBuf<double2> tmp(KC);
+      if (sizeof(R) == 8) PGB_CUDA(cudaMemcpyAsync(tmp.p, chi, KC * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      else widen<R>(tmp.p, chi, KC);
+      tmp.download(chi_host, KC);
+      sync();
+    }
+  }
+  const double weight = a.temp / (double)g.Nkall;
+  const double scale = weight / (double)g.P;
+  DeltaKernelCache<R> cache;
+  DBuf<double2> F(KE), w(KE);
+  Timer ta;
+  auto apply_op = [&](double2* out, const double2* v) {
+    ta.start();
+    mkfk(F.p, G, v, K, Norb);
+    mkdelta<R>(g, p, F.p, chi, S.p, C.p, prt, singlet, scale, out, &cache);
+    g_stats.t_apply += ta.stop();
+    g_stats.applies += 1;
+  };
+  auto inner = [&](const double2* u, const double2* v) {
+    double2 s = inner_w(u, v, g.kweight.p, Nk, KE);
+    return make_double2(2.0 * s.x, 2.0 * s.y);
+  };
+  auto norm = [&](const double2* f) { return std::sqrt(2.0 * inner_w(f, f, g.kweight.p, Nk, KE).x); };
+  auto init_vec = [&](double2* d) {
+    initial_delta(d, init, uni.p, Nk, Nw, Norb, (int)a.gap_sym);
+    const double nrm = inner_w(d, d, g.kweight.p, Nk, KE).x;
+    PGB_CHECK(nrm > 0, "Error: get_initial_delta norm <= 0");
+    scal(d, 1.0 / std::sqrt(2.0 * nrm), KE);
+  };
+  double lambda_out = 0.0;
+  const int m = (int)a.arnoldi_m;
+  if (m > 0) {
+    PGB_CHECK(m <= 64, "arnoldi_m above 64 is not supported");
+    std::vector<DBuf<double2>> V(m);
+    for (auto& v : V) v.alloc(KE);
+    auto arnoldi = [&](double shift, const double2* defl, std::vector<double2>& Hm, int& m_act) {
+      Hm.assign((size_t)(m + 1) * m, make_double2(0, 0));
+      m_act = m;
+      for (int j = 0; j < m; ++j) {
+        apply_op(w.p, V[j].p);
+        if (defl) {
+          axpy(w.p, make_double2(shift, 0), V[j].p, KE);
+          double2 h = inner(defl, w.p);
+          axpy(w.p, make_double2(-h.x, -h.y), defl, KE);
+        }
+        for (int ii = 0; ii <= j; ++ii) {
+          double2 h = inner(V[ii].p, w.p);
+          Hm[ii * m + j] = h;
+          axpy(w.p, make_double2(-h.x, -h.y), V[ii].p, KE);
+        }
+        const double beta = norm(w.p);
+        Hm[(j + 1) * m + j] = make_double2(beta, 0);
+        if (beta < 1.0e-14) {
+          m_act = j + 1;
+          break;
+        }
+        if (j < m - 1) {
+          PGB_CUDA(cudaMemcpyAsync(V[j + 1].p, w.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+          scal(V[j + 1].p, 1.0 / beta, KE);
+        }
+      }
+    };
+    auto ritz = [&](double2* out, const std::vector<double2>& Hm, int m_act, double2 lam) {
+      std::vector<double2> Hs((size_t)m_act * m_act);
+      for (int i = 0; i < m_act; ++i)
+        for (int j = 0; j < m_act; ++j) Hs[i * m_act + j] = Hm[i * m + j];
+      std::vector<double2> y = eigvec(Hs, m_act, lam);
+      std::vector<const double2*> xs(m_act);
+      for (int i = 0; i < m_act; ++i) xs[i] = V[i].p;
+      lincomb(out, xs.data(), y.data(), m_act, KE);
+      scal(out, 1.0 / norm(out), KE);
+    };
+    auto ritz_values = [&](const std::vector<double2>& Hm, int m_act) {
+      std::vector<double2> Hs((size_t)m_act * m_act), ev;
+      for (int i = 0; i < m_act; ++i)
+        for (int j = 0; j < m_act; ++j) Hs[i * m_act + j] = Hm[i * m + j];
+      eig_small(Hs, m_act, ev);
+      return ev;
+    };
+    // pass 1: no shift
+    init_vec(V[0].p);
+    log("Arnoldi pass 1 (no shift): Krylov dim =%4d ...\n", m);
+    std::vector<double2> Hm;
+    int m_act = m;
+    arnoldi(0.0, nullptr, Hm, m_act);
+    std::vector<double2> ev = ritz_values(Hm, m_act);
+    int imin = 0, imax = 0;
+    for (int i = 1; i < m_act; ++i) {
+      if (ev[i].x < ev[imin].x) imin = i;
+      if (ev[i].x > ev[imax].x) imax = i;
+    }
+    const double lambda1 = ev[imin].x;
+    for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x);
+    log("  lambda_- =%12.6f\n", lambda1);
+    DBuf<double2> D(KE);
+    if (ev[imax].x >= 0.1) {
+      lambda_out = ev[imax].x;
+      log("  eliash   =%12.6f\n", lambda_out);
+      ritz(D.p, Hm, m_act, ev[imax]);
+    } else {
+      DBuf<double2> delta1(KE);
+      ritz(delta1.p, Hm, m_act, ev[imin]);
+      const double shift = -lambda1;
+      init_vec(V[0].p);
+      double2 h = inner(delta1.p, V[0].p);
+      axpy(V[0].p, make_double2(-h.x, -h.y), delta1.p, KE);
+      const double b0 = norm(V[0].p);
+      if (!(b0 >= 1.0e-14)) {
+        // the operator has no component outside the pass-1 direction
+        lambda_out = lambda1;
+        PGB_CUDA(cudaMemcpyAsync(D.p, delta1.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      } else {
+        scal(V[0].p, 1.0 / b0, KE);
+        log("Arnoldi pass 2 (shift=%10.6f): Krylov dim =%4d ...\n", shift, m);
+        arnoldi(shift, delta1.p, Hm, m_act);
+        ev = ritz_values(Hm, m_act);
+        imax = 0;
+        for (int i = 1; i < m_act; ++i)
+          if (ev[i].x > ev[imax].x) imax = i;
+        for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x - shift);
+        lambda_out = ev[imax].x - shift;
+        log("  eliash   =%12.6f\n", lambda_out);
+        ritz(D.p, Hm, m_act, ev[imax]);
+      }
+    }
+    PGB_CUDA(cudaMemcpyAsync(delta_out, D.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    sync();
+  } else {
+    // shifted power method with deflation (feliash.f90:66-140)
+    DBuf<double2> D(KE), nd(KE), d1(KE), tmp(KE);
+    double lambda1 = 0.0, lam_phys = 0.0, lam_rq = 0.0, inrm = 1.0;
+    for (int i_eig = 1; i_eig <= 2; ++i_eig) {
+      init_vec(D.p);
+      if (i_eig == 2) {
+        const double proj = inner(d1.p, D.p).x;
+        axpy(D.p, make_double2(-proj, 0), d1.p, KE);
+        scal(D.p, 1.0 / norm(D.p), KE);
+      }
+      double lam_prev = 0.0;
+      for (int it = 1; it <= a.itemax; ++it) {
+        apply_op(nd.p, D.p);
+        if (i_eig == 2) {
+          axpy(nd.p, make_double2(-lambda1, 0), D.p, KE);
+          const double proj = inner(d1.p, nd.p).x;
+          axpy(nd.p, make_double2(-proj, 0), d1.p, KE);
+        }
+        const double nrm = norm(nd.p);
+        PGB_CHECK(nrm > 0, "Error: norm <= 0 in iter_loop");
+        inrm = 1.0 / nrm;
+        lam_rq = inner(D.p, nd.p).x;
+        lam_phys = lam_rq + lambda1;
+        // vector error: min(||nd/|nd| - D||, ||nd/|nd| + D||)
+        PGB_CUDA(cudaMemcpyAsync(tmp.p, nd.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal(tmp.p, inrm, KE);
+        axpy(tmp.p, make_double2(-1, 0), D.p, KE);
+        const double ep = norm(tmp.p);
+        axpy(tmp.p, make_double2(2, 0), D.p, KE);
+        const double en = norm(tmp.p);
+        const double verr = std::min(ep, en);
+        log("%4d lambda_elsh=%16.8E%16.8E  vec_err=%12.4E\n", it, lam_phys, std::fabs(lam_phys - lam_prev), verr);
+        if (lam_phys < 0.0 && verr < a.eps) break;
+        if (verr < a.eps && std::fabs(lam_phys - lam_prev) < a.eps * (std::fabs(lam_phys) + 1e-10)) break;
+        lam_prev = lam_phys;
+        PGB_CUDA(cudaMemcpyAsync(D.p, nd.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal(D.p, inrm, KE);
+      }
+      if (i_eig == 1) {
+        if (lam_phys > 0.0) {
+          lambda_out = lam_phys;
+          break;
+        }
+        lambda1 = lam_rq;
+        PGB_CUDA(cudaMemcpyAsync(d1.p, nd.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal(d1.p, inrm, KE);
+      } else {
+        lambda_out = lam_phys;
+      }
+    }
+    scal(nd.p, 1.0 / norm(nd.p), KE);
+    PGB_CUDA(cudaMemcpyAsync(delta_out, nd.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    sync();
+  }
+  g_stats.lambda = lambda_out;
+  return lambda_out;
+}
+
+template <typename R>
+void run_lin_eliash(const LinEliashArgs& a) {
+  Inputs in;
+  upload_inputs(in, a.kmap, a.invk, a.olist, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Smat, a.Cmat,
+                nullptr, nullptr, a.uni);
+  const long long KE = in.g.K * a.Norb * a.Norb, KC = in.g.K * a.Nchi * a.Nchi;
+  DBuf<double> prt(a.Norb), init(a.Nk * a.Norb);
+  prt.upload(a.prt, a.Norb);
+  init.upload(a.init_delta, a.Nk * a.Norb);
+  DBuf<double2> G(KE), D(KE);
+  G.upload(a.Gk, KE);
+  DBuf<cx<R>> chi(KC);
+  {
+    DBuf<double2> tmp(KC);
+    tmp.upload(a.chi, KC);
+    if (sizeof(R) == 8) PGB_CUDA(cudaMemcpyAsync(chi.p, tmp.p, KC * sizeof(double2), cudaMemcpyDeviceToDevice, ctx().stream));
+    else narrow<R>(chi.p, tmp.p, KC);
+  }
+  EliashParams prm{a.temp, a.eps, a.itemax, a.gap_sym, a.arnoldi_m};
+  *a.lambda_out = eliash_core<R>(in, chi.p, G.p, init.p, prt.p, prm, D.p, a.clobber_chi ? a.chi : nullptr);
+  D.download(a.delta, KE);
+  sync();
+}
+
+// ============================================================== pipeline ==
+// FLEX self-energy -> G -> chi0 -> linearized Eliashberg, device resident
+// between the stages (the reference's calc_lin_eliashberg_eq with
+// sw_self=True, libs/plibs/_calc.py:370-405, as one call).
+template <typename R>
+void run_pipeline(const PipelineArgs& a) {
+  g_stats = LastStats{};
+  cudaStream_t st = ctx().stream;
+  Timer t;
+  t.start();
+  Inputs in;
+  upload_inputs(in, a.kmap, a.invk, a.olist, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Smat, a.Cmat,
+                a.hamk, a.eig, a.uni);
+  const long long K = in.g.K, KE = K * a.Norb * a.Norb, KC = K * a.Nchi * a.Nchi;
+  DBuf<double> prt(a.Norb), init(a.Nk * a.Norb);
+  prt.upload(a.prt, a.Norb);
+  init.upload(a.init_delta, a.Nk * a.Norb);
+  DBuf<double2> seed;
+  if (a.sigma_seed) {
+    seed.alloc(KE);
+    seed.upload(a.sigma_seed, KE);
+  }
+  const double t_h2d = t.stop();
+  t.start();
+  FlexParams prm{a.mu_init, a.fill, a.temp, a.scf_loop, a.pp, a.eps, a.sub_sigma, false, false, a.m_diis,
+                 a.sw_rescale, a.sw_tail, 1.0};
+  DBuf<double2> sig(KE), G(KE), D(KE);
+  double mu = 0;
+  mkself_core<R>(in, prm, sig.p, &mu, a.sigma_seed ? seed.p : nullptr, a.seed_mu, a.seed_mu_old);
+  const int iters = g_stats.iterations;
+  seed.release();
+  PGB_CHECK(dyson(G.p, sig.p, in.H.p, mu, a.temp, in.Nk, in.Nw, in.Norb), "singular G^-1 in the Dyson step");
+  double stoner_v = 0;
+  {
+    DBuf<cx<R>> chi(KC);
+    TailRef tr{in.eig.p, in.uni.p, mu};
+    chi0<R>(in.g, in.p, G.p, a.temp, a.sw_tail ? &tr : nullptr, chi.p);
+    double cdw = 0;
+    int qs = 0, qc = 0;
+    stoner<R>(in.g, chi.p, in.S.p, in.C.p, &stoner_v, &cdw, &qs, &qc);
+    ckchi_print(in.g, stoner_v, cdw, qs, qc);
+    EliashParams ep{a.temp, a.eps_eliash, a.itemax, a.gap_sym, a.arnoldi_m};
+    *a.lambda_out = eliash_core<R>(in, chi.p, G.p, init.p, prt.p, ep, D.p, nullptr);
+  }
+  g_stats.iterations = iters;
+  const double t_compute = t.stop();
+  t.start();
+  sig.download(a.sigmak, KE);
+  D.download(a.delta, KE);
+  sync();
+  const double t_d2h = t.stop();
+  *a.mu_out = mu;
+  *a.stoner_out = stoner_v;
+  if (a.times_ms) {
+    a.times_ms[0] = t_h2d;
+    a.times_ms[1] = t_compute;
+    a.times_ms[2] = t_d2h;
+  }
+  g_stats.mu = mu;
+}
+
+template void run_mkself<float>(const MkselfArgs&);
+template void run_mkself<double>(const MkselfArgs&);
+template void run_lin_eliash<float>(const LinEliashArgs&);
+template void run_lin_eliash<double>(const LinEliashArgs&);
+template void run_pipeline<float>(const PipelineArgs&);
+template void run_pipeline<double>(const PipelineArgs&);
+
+}  // namespace pgb

@@ -1,0 +1,107 @@
+// Argument bundles of the two solver drivers (host pointers as the C ABI
+// receives them) and the statistics of the last solve.
+#pragma once
+
+#include <cstdint>
+
+#include "flex.cuh"
+
+namespace pgb {
+
+struct MkselfArgs {
+  double2* sigmak;                 // out (Nk,Nw,Norb,Norb)
+  double* mu_out;
+  const double *Smat, *Cmat;       // (Nchi,Nchi)
+  const int64_t *kmap, *invk, *olist;
+  const double2* hamk;             // (Norb,Norb,Nk)
+  const double* eig;               // (Norb,Nk)
+  const double2* uni;              // (Norb,Norb,Nk)
+  double mu_init, fill, temp;
+  int64_t scf_loop;
+  double pp, eps;
+  int64_t Nkall, Nk, Nw, Norb, Nchi, Nx, Ny, Nz, sub_sigma;
+  bool sw_out, sw_in;
+  int64_t m_diis;
+  bool sw_rescale, sw_tail;
+  double sigma_scale;
+};
+
+struct LinEliashArgs {
+  double2* delta;                  // out (Nk,Nw,Norb,Norb)
+  double2* chi;                    // in (Nk,Nw,Nchi,Nchi); overwritten with V_Delta
+  const double2 *Gk, *uni;
+  const double* init_delta;        // (Nk,Norb)
+  const double *Smat, *Cmat;
+  const int64_t* olist;
+  const double* prt;
+  const int64_t *kmap, *invk;
+  double temp, eps;
+  int64_t Nkall, Nk, Nw, Nchi, Norb, Nx, Ny, Nz, itemax, gap_sym, arnoldi_m;
+  double* lambda_out;
+  bool clobber_chi = true;
+};
+
+struct PipelineArgs {
+  double2* sigmak;                 // out (Nk,Nw,Norb,Norb)
+  double* mu_out;
+  double2* delta;                  // out (Nk,Nw,Norb,Norb)
+  double* lambda_out;
+  double* stoner_out;
+  double* times_ms;                // out [3]: H2D, device compute, D2H (CUDA events); may be null
+  const double *Smat, *Cmat;
+  const int64_t *kmap, *invk, *olist;
+  const double2* hamk;
+  const double* eig;
+  const double2* uni;
+  const double* init_delta;        // (Nk,Norb)
+  const double* prt;               // (Norb)
+  const double2* sigma_seed;       // optional starting Sigma (Nk,Nw,Norb,Norb); null: G0 start
+  double seed_mu, seed_mu_old;
+  double mu_init, fill, temp;
+  int64_t scf_loop;
+  double pp, eps;
+  int64_t Nkall, Nk, Nw, Norb, Nchi, Nx, Ny, Nz, sub_sigma, m_diis;
+  bool sw_rescale, sw_tail;
+  int64_t gap_sym, arnoldi_m, itemax;
+  double eps_eliash;
+};
+
+// uploaded model data shared by the solvers
+struct Inputs {
+  Geom g;
+  Pairs p;
+  DBuf<double> S, C, eig;
+  DBuf<double2> H, uni;
+  int Norb = 1, Nchi = 1, Nk = 1, Nw = 1;
+};
+
+struct FlexParams {
+  double mu_init, fill, temp;
+  int64_t scf_loop;
+  double pp, eps;
+  int64_t sub_sigma;
+  bool sw_out, sw_in;
+  int64_t m_diis;
+  bool sw_rescale, sw_tail;
+  double sigma_scale;
+};
+
+struct EliashParams {
+  double temp, eps;
+  int64_t itemax, gap_sym, arnoldi_m;
+};
+
+struct LastStats {
+  int iterations = 0;
+  double esterr = 0, stoner = 0, mu = 0, lambda = 0;
+  int applies = 0;
+  // milliseconds on the device (CUDA events on the library stream)
+  double t_chi0 = 0, t_vertex = 0, t_sigma = 0, t_diis = 0, t_mu = 0, t_dyson = 0, t_apply = 0;
+};
+
+template <typename R> void run_mkself(const MkselfArgs& a);
+template <typename R> void run_lin_eliash(const LinEliashArgs& a);
+template <typename R> void run_pipeline(const PipelineArgs& a);
+const LastStats& last_stats();
+
+}  // namespace pgb

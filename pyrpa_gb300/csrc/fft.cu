@@ -1,0 +1,450 @@
+// Mixed-radix Stockham FFT passes in shared memory (see fft.cuh).
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "fft.cuh"
+
+namespace pgb {
+
+namespace {
+
+// tab[t] = exp(-2 pi i t / L); sign < 0 uses it as is, sign > 0 its conjugate
+template <typename R>
+__device__ __forceinline__ cx<R> twid(const double2* tab, int t, int sign) {
+  double2 w = __ldg(tab + t);
+  return cmk<R>((R)w.x, (R)(sign < 0 ? w.y : -w.y));
+}
+
+template <typename R, int RAD> struct Dft {
+  // generic radix: direct O(RAD^2) evaluation with roots from the line table
+  __device__ static void run(cx<R>* v, int sign, const double2* tab, int L) {
+    cx<R> o[RAD];
+    const int step = L / RAD;
+#pragma unroll
+    for (int k = 0; k < RAD; ++k) {
+      cx<R> acc = v[0];
+#pragma unroll
+      for (int r = 1; r < RAD; ++r) acc += v[r] * twid<R>(tab, ((r * k) % RAD) * step, sign);
+      o[k] = acc;
+    }
+#pragma unroll
+    for (int k = 0; k < RAD; ++k) v[k] = o[k];
+  }
+};
+
+template <typename R> struct Dft<R, 2> {
+  __device__ static void run(cx<R>* v, int, const double2*, int) {
+    cx<R> a = v[0] + v[1], b = v[0] - v[1];
+    v[0] = a;
+    v[1] = b;
+  }
+};
+
+template <typename R> struct Dft<R, 4> {
+  __device__ static void run(cx<R>* v, int sign, const double2*, int) {
+    cx<R> a0 = v[0] + v[2], a1 = v[0] - v[2], a2 = v[1] + v[3];
+    cx<R> a3 = muli(v[1] - v[3], (R)sign);
+    v[0] = a0 + a2;
+    v[1] = a1 + a3;
+    v[2] = a0 - a2;
+    v[3] = a1 - a3;
+  }
+};
+
+template <typename R> struct Dft<R, 3> {
+  __device__ static void run(cx<R>* v, int sign, const double2*, int) {
+    const R h = (R)0.86602540378443864676372317075294;  // sqrt(3)/2
+    cx<R> t1 = v[1] + v[2], t2 = v[1] - v[2];
+    cx<R> m = v[0] - (R)0.5 * t1;
+    cx<R> u = h * muli(t2, (R)sign);
+    v[0] = v[0] + t1;
+    v[1] = m + u;
+    v[2] = m - u;
+  }
+};
+
+template <typename R> struct Dft<R, 5> {
+  __device__ static void run(cx<R>* v, int sign, const double2*, int) {
+    const R c1 = (R)0.30901699437494742410229341718282;   // cos(2 pi/5)
+    const R c2 = (R)-0.80901699437494742410229341718282;  // cos(4 pi/5)
+    const R s1 = (R)0.95105651629515357211643933337938;   // sin(2 pi/5)
+    const R s2 = (R)0.58778525229247312916870595463907;   // sin(4 pi/5)
+    cx<R> a1 = v[1] + v[4], b1 = v[1] - v[4], a2 = v[2] + v[3], b2 = v[2] - v[3];
+    cx<R> p1 = v[0] + c1 * a1 + c2 * a2, p2 = v[0] + c2 * a1 + c1 * a2;
+    cx<R> q1 = muli(s1 * b1 + s2 * b2, (R)sign), q2 = muli(s2 * b1 - s1 * b2, (R)sign);
+    v[0] = v[0] + a1 + a2;
+    v[1] = p1 + q1;
+    v[4] = p1 - q1;
+    v[2] = p2 + q2;
+    v[3] = p2 - q2;
+  }
+};
+
+template <typename R> struct Dft<R, 8> {
+  __device__ static void run(cx<R>* v, int sign, const double2* t, int L) {
+    const R h = (R)0.70710678118654752440084436210485;
+    cx<R> e[4] = {v[0], v[2], v[4], v[6]};
+    cx<R> o[4] = {v[1], v[3], v[5], v[7]};
+    Dft<R, 4>::run(e, sign, t, L);
+    Dft<R, 4>::run(o, sign, t, L);
+    const R s = (R)sign;
+    cx<R> w1 = cmk<R>(h, s * h), w3 = cmk<R>(-h, s * h);
+    cx<R> o1 = o[1] * w1, o2 = muli(o[2], s), o3 = o[3] * w3;
+    v[0] = e[0] + o[0];
+    v[4] = e[0] - o[0];
+    v[1] = e[1] + o1;
+    v[5] = e[1] - o1;
+    v[2] = e[2] + o2;
+    v[6] = e[2] - o2;
+    v[3] = e[3] + o3;
+    v[7] = e[3] - o3;
+  }
+};
+
+// One Stockham stage (Govindaraju et al., "High performance discrete Fourier
+// transforms on graphics processors", SC08, Fig. 2) over nl lines in smem.
+template <typename R, int RAD>
+__device__ void stage(const cx<R>* in, cx<R>* out, int L, int Ns, int nl, int sign,
+                      const double2* tab) {
+  const int nbf = L / RAD;
+  const int total = nl * nbf;
+  const int tstride = L / (Ns * RAD);
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int b = idx / nbf;
+    const int j = idx - b * nbf;
+    const cx<R>* li = in + (size_t)b * L;
+    cx<R>* lo = out + (size_t)b * L;
+    const int jj = j % Ns;
+    cx<R> v[RAD];
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) {
+      v[r] = li[j + r * nbf];
+      if (r > 0 && jj > 0) v[r] = v[r] * twid<R>(tab, r * jj * tstride, sign);
+    }
+    Dft<R, RAD>::run(v, sign, tab, L);
+    const int idxD = (j / Ns) * Ns * RAD + jj;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) lo[idxD + r * Ns] = v[r];
+  }
+}
+
+template <typename R>
+__device__ void four_step_twiddle(cx<R>* buf, const PassDesc& d, long long o, bool contig, int nl,
+                                  int sign) {
+  const int L = d.L;
+  for (int e = threadIdx.x; e < nl * L; e += blockDim.x) {
+    const int b = e / L, p = e - b * L;
+    const long long k1 = ((contig ? o + b : o) % d.tw_L1);
+    const int t = (int)(((long long)p * k1) % d.tw_Lfull);
+    if (t) buf[e] = buf[e] * twid<R>(d.tw_full, t, sign);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256) fft_pass_kernel(cx<R>* data, long long P, PassDesc d,
+                                                       int sign) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* buf0 = reinterpret_cast<cx<R>*>(smem_raw);
+  cx<R>* buf1 = buf0 + (size_t)d.B * d.L;
+  const int L = d.L;
+  cx<R>* arr = data + (long long)blockIdx.y * P;
+  const long long tile = blockIdx.x;
+  const bool contig = (d.S == 1);
+  long long o, base;
+  int nl;
+  if (contig) {
+    const long long line0 = tile * d.B;
+    nl = (int)min((long long)d.B, d.O - line0);
+    base = line0 * L;
+    o = line0;
+    for (int e = threadIdx.x; e < nl * L; e += blockDim.x) buf0[e] = arr[base + e];
+  } else {
+    const long long nsb = (d.S + d.B - 1) / d.B;
+    o = tile / nsb;
+    const long long s0 = (tile - o * nsb) * d.B;
+    nl = (int)min((long long)d.B, d.S - s0);
+    base = o * L * d.S + s0;
+    for (int e = threadIdx.x; e < nl * L; e += blockDim.x) {
+      const int p = e / nl, b = e - p * nl;
+      buf0[b * L + p] = arr[base + (long long)p * d.S + b];
+    }
+  }
+  __syncthreads();
+  if (d.tw_L1 > 0 && !d.tw_post) {
+    four_step_twiddle<R>(buf0, d, o, contig, nl, sign);
+    __syncthreads();
+  }
+  cx<R>* in = buf0;
+  cx<R>* out = buf1;
+  int Ns = 1;
+  for (int st = 0; st < d.nst; ++st) {
+    const int rad = d.radix[st];
+    switch (rad) {
+      case 2: stage<R, 2>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 3: stage<R, 3>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 4: stage<R, 4>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 5: stage<R, 5>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 7: stage<R, 7>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 8: stage<R, 8>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 11: stage<R, 11>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 13: stage<R, 13>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      default: break;
+    }
+    __syncthreads();
+    cx<R>* tmp = in;
+    in = out;
+    out = tmp;
+    Ns *= rad;
+  }
+  if (d.tw_L1 > 0 && d.tw_post) {
+    four_step_twiddle<R>(in, d, o, contig, nl, sign);
+    __syncthreads();
+  }
+  if (contig) {
+    for (int e = threadIdx.x; e < nl * L; e += blockDim.x) arr[base + e] = in[e];
+  } else {
+    for (int e = threadIdx.x; e < nl * L; e += blockDim.x) {
+      const int p = e / nl, b = e - p * nl;
+      arr[base + (long long)p * d.S + b] = in[b * L + p];
+    }
+  }
+}
+
+std::mutex g_mu;
+std::map<int, double2*> g_tables;
+
+struct PassEvent {
+  cudaEvent_t a, b;
+  double bytes;
+};
+bool g_prof = false;
+std::vector<PassEvent> g_prof_ev;
+std::vector<cudaEvent_t> g_ev_pool;
+cudaEvent_t take_event() {
+  if (!g_ev_pool.empty()) {
+    cudaEvent_t e = g_ev_pool.back();
+    g_ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  PGB_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+const double2* twiddle_table(int L) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_tables.find(L);
+  if (it != g_tables.end()) return it->second;
+  std::vector<double2> h(L);
+  const long double twopi = 6.283185307179586476925286766559005768L;
+  for (int t = 0; t < L; ++t) {
+    // reduce to the first octant-free form: exact values at quarter turns
+    long long q = (long long)t * 4;
+    if (q % L == 0) {
+      int quarter = (int)((q / L) % 4);
+      const double c[4] = {1.0, 0.0, -1.0, 0.0}, s[4] = {0.0, 1.0, 0.0, -1.0};
+      h[t] = make_double2(c[quarter], -s[quarter]);
+    } else {
+      long double a = twopi * (long double)t / (long double)L;
+      h[t] = make_double2((double)cosl(a), (double)(-sinl(a)));
+    }
+  }
+  double2* d = nullptr;
+  PGB_CUDA(cudaMalloc(&d, sizeof(double2) * L));
+  PGB_CUDA(cudaMemcpy(d, h.data(), sizeof(double2) * L, cudaMemcpyHostToDevice));
+  g_tables[L] = d;
+  return d;
+}
+
+bool factor_line(int L, int* radix, int* nst) {
+  int n = L, k = 0;
+  const int pref[] = {8, 4, 2, 3, 5, 7, 11, 13};
+  for (int r : pref) {
+    while (n % r == 0 && n > 1) {
+      if (k >= kMaxStages) return false;
+      radix[k++] = r;
+      n /= r;
+    }
+  }
+  *nst = k;
+  return n == 1;
+}
+
+PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
+  PassDesc d{};
+  d.L = L;
+  d.S = S;
+  d.O = O;
+  PGB_CHECK(factor_line(L, d.radix, &d.nst),
+            "FFT length " + std::to_string(L) + " has a prime factor above 13 (unsupported)");
+  long long B = std::max(1LL, 32768LL / ((long long)L * elem_bytes));
+  B = std::min(B, 64LL);
+  if (S == 1) B = std::min(B, O);
+  else B = std::min(B, S);
+  d.B = (int)std::max(1LL, B);
+  d.tw_line = twiddle_table(L);
+  return d;
+}
+
+int split_length(int n) {
+  // L1 * L2 = n with both <= kMaxLine, L1 as close to sqrt(n) as possible
+  int best = -1;
+  for (int a = 2; a <= kMaxLine; ++a) {
+    if (n % a) continue;
+    int b = n / a;
+    if (b > kMaxLine) continue;
+    if (best < 0 || std::abs(a - b) < std::abs(best - n / best)) best = a;
+  }
+  PGB_CHECK(best > 0, "FFT axis length " + std::to_string(n) + " cannot be split into passes");
+  return best;
+}
+
+}  // namespace
+
+FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
+  dims_[0] = nx;
+  dims_[1] = ny;
+  dims_[2] = nz;
+  dims_[3] = nt;
+  P_ = (long long)nx * ny * nz * nt;
+  std::vector<int> tables;
+  long long S = 1;
+  for (int a = 0; a < 4; ++a) {
+    const int n = dims_[a];
+    const long long O = P_ / (S * n);
+    AxisMap& m = maps_[a];
+    m.n = n;
+    m.pos.resize(n);
+    m.logical.resize(n);
+    m.rev.resize(n);
+    if (n > 1 && n <= kMaxLine) {
+      PassDesc p = make_pass(n, S, O, elem_bytes);
+      fwd_.push_back(p);
+      bwd_.push_back(p);
+      if (a < 3) fwd_space_.push_back(p);
+      for (int k = 0; k < n; ++k) m.pos[k] = k;
+    } else if (n > 1) {
+      const int L1 = split_length(n), L2 = n / L1;
+      PassDesc pb = make_pass(L1, S * L2, O, elem_bytes);
+      PassDesc pa = make_pass(L2, S, O * L1, elem_bytes);
+      pa.tw_L1 = L1;
+      pa.tw_Lfull = n;
+      pa.tw_full = twiddle_table(n);
+      PassDesc pa_inv = pa;
+      pa_inv.tw_post = 1;
+      fwd_.push_back(pb);
+      fwd_.push_back(pa);
+      bwd_.push_back(pa_inv);
+      bwd_.push_back(pb);
+      if (a < 3) {
+        fwd_space_.push_back(pb);
+        fwd_space_.push_back(pa);
+      }
+      for (int k = 0; k < n; ++k) m.pos[k] = (k / L1) + L2 * (k % L1);
+    } else {
+      m.pos[0] = 0;
+    }
+    for (int k = 0; k < n; ++k) m.logical[m.pos[k]] = k;
+    for (int p = 0; p < n; ++p) m.rev[p] = m.pos[(n - m.logical[p]) % n];
+    S *= n;
+  }
+  // device tables
+  std::vector<int> h;
+  for (int a = 0; a < 4; ++a) {
+    off_pos_[a] = (int)h.size();
+    h.insert(h.end(), maps_[a].pos.begin(), maps_[a].pos.end());
+    off_rev_[a] = (int)h.size();
+    h.insert(h.end(), maps_[a].rev.begin(), maps_[a].rev.end());
+    off_log_[a] = (int)h.size();
+    h.insert(h.end(), maps_[a].logical.begin(), maps_[a].logical.end());
+  }
+  PGB_CUDA(cudaMalloc(&d_tables_, sizeof(int) * h.size()));
+  PGB_CUDA(cudaMemcpy(d_tables_, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+}
+
+template <typename R>
+void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int sign,
+                cudaStream_t s) const {
+  static bool attr_set = false;
+  if (!attr_set) {
+    PGB_CUDA(cudaFuncSetAttribute(fft_pass_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  96 * 1024));
+    attr_set = true;
+  }
+  for (const PassDesc& d : passes) {
+    const long long tiles = (d.S == 1) ? (d.O + d.B - 1) / d.B : d.O * ((d.S + d.B - 1) / d.B);
+    const size_t smem = 2 * (size_t)d.B * d.L * sizeof(cx<R>);
+    for (int b0 = 0; b0 < nb; b0 += 65535) {
+      const int nbb = std::min(65535, nb - b0);
+      dim3 grid((unsigned)tiles, (unsigned)nbb);
+      PassEvent pe{};
+      if (g_prof) {
+        pe.a = take_event();
+        pe.b = take_event();
+        pe.bytes = 2.0 * (double)nbb * (double)P_ * sizeof(cx<R>);
+        PGB_CUDA(cudaEventRecord(pe.a, s));
+      }
+      fft_pass_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
+      launch_check("fft_pass");
+      if (g_prof) {
+        PGB_CUDA(cudaEventRecord(pe.b, s));
+        g_prof_ev.push_back(pe);
+      }
+      ctx().kernel_launches++;
+    }
+  }
+}
+
+template <typename R> void FFT4D::forward(cx<R>* data, int nb, cudaStream_t s) const {
+  run<R>(fwd_, data, nb, -1, s);
+}
+template <typename R> void FFT4D::backward(cx<R>* data, int nb, cudaStream_t s) const {
+  run<R>(bwd_, data, nb, +1, s);
+}
+template <typename R> void FFT4D::forward_space(cx<R>* data, int nb, cudaStream_t s) const {
+  run<R>(fwd_space_, data, nb, -1, s);
+}
+
+template void FFT4D::forward<float>(float2*, int, cudaStream_t) const;
+template void FFT4D::forward<double>(double2*, int, cudaStream_t) const;
+template void FFT4D::backward<float>(float2*, int, cudaStream_t) const;
+template void FFT4D::backward<double>(double2*, int, cudaStream_t) const;
+template void FFT4D::forward_space<float>(float2*, int, cudaStream_t) const;
+template void FFT4D::forward_space<double>(double2*, int, cudaStream_t) const;
+
+void fft_profile_enable(bool on) { g_prof = on; }
+
+void fft_profile_collect(double* launches, double* ms, double* bytes) {
+  double n = 0, t = 0, b = 0;
+  for (auto& e : g_prof_ev) {
+    PGB_CUDA(cudaEventSynchronize(e.b));
+    float x = 0;
+    PGB_CUDA(cudaEventElapsedTime(&x, e.a, e.b));
+    n += 1;
+    t += x;
+    b += e.bytes;
+    g_ev_pool.push_back(e.a);
+    g_ev_pool.push_back(e.b);
+  }
+  g_prof_ev.clear();
+  *launches = n;
+  *ms = t;
+  *bytes = b;
+}
+
+const FFT4D& fft_plan(int nx, int ny, int nz, int nt, int elem_bytes) {
+  static std::map<std::tuple<int, int, int, int, int>, FFT4D*> plans;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_tuple(nx, ny, nz, nt, elem_bytes);
+  auto it = plans.find(key);
+  if (it != plans.end()) return *it->second;
+  FFT4D* p = new FFT4D(nx, ny, nz, nt, elem_bytes);
+  plans[key] = p;
+  return *p;
+}
+
+}  // namespace pgb

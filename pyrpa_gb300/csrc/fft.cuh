@@ -1,0 +1,82 @@
+// Batched 4-D complex FFT over the (x, y, z, t) grid of the FLEX engine.
+//
+// The reference transforms each orbital-pair array with one serial FFTW/
+// pocketfft call on the CPU (libs/src/fmod.f90:67-116, fft_wrapper.cpp:32-87).
+// Here a transform is a short sequence of "axis passes": each pass reads a
+// tile of lines into shared memory (coalesced along the fastest index),
+// runs a mixed-radix Stockham FFT (radices 8,4,2,3,5,7 and a table-driven
+// generic radix for other primes <= 64) and writes the tile back in place.
+// Axes longer than kMaxLine are split four-step style into two passes
+// (L = L1*L2) with the twiddle multiply fused into the second pass; the
+// frequency index of such an axis is then stored digit-transposed, which
+// all pointwise kernels handle through the per-axis position tables below.
+// Forward is exp(-2 pi i jk/L) (FFTW sign -1), backward exp(+...), both
+// unnormalized: the callers fold 1/P into their weights.
+#pragma once
+
+#include "common.cuh"
+
+namespace pgb {
+
+constexpr int kMaxLine = 1024;
+constexpr int kMaxStages = 16;
+
+struct PassDesc {
+  int L;               // line length
+  long long S;         // element stride along the line
+  long long O;         // number of outer blocks (dims above the line)
+  int B;               // lines per CTA
+  int nst;             // number of Stockham stages
+  int radix[kMaxStages];
+  int tw_L1;           // four-step: modulus of the k1 digit (0: no twiddle)
+  int tw_Lfull;        // four-step: full axis length
+  int tw_post;         // 0: multiply before the line DFT, 1: after
+  const double2* tw_line;  // exp(-2 pi i t / L), t < L
+  const double2* tw_full;  // exp(-2 pi i t / Lfull), t < Lfull
+};
+
+// Position tables of one axis: pos[k] is where logical index k is stored,
+// rev[p] the position of logical -k for the value stored at position p.
+struct AxisMap {
+  int n = 1;
+  std::vector<int> pos, rev, logical;
+};
+
+class FFT4D {
+ public:
+  FFT4D() = default;
+  FFT4D(int nx, int ny, int nz, int nt, int elem_bytes);
+  long long P() const { return P_; }
+  const int* dims() const { return dims_; }
+  // in-place transform of nb arrays stored back to back (stride P)
+  template <typename R> void forward(cx<R>* data, int nb, cudaStream_t s) const;
+  template <typename R> void backward(cx<R>* data, int nb, cudaStream_t s) const;
+  // spatial-only (x,y,z) forward transform; the t axis is left untouched
+  template <typename R> void forward_space(cx<R>* data, int nb, cudaStream_t s) const;
+  const AxisMap& axis(int a) const { return maps_[a]; }
+  // device copies of the position tables (pos, rev, logical) of each axis
+  const int* d_pos(int a) const { return d_tables_ + off_pos_[a]; }
+  const int* d_rev(int a) const { return d_tables_ + off_rev_[a]; }
+  const int* d_logical(int a) const { return d_tables_ + off_log_[a]; }
+
+ private:
+  int dims_[4] = {1, 1, 1, 1};
+  long long P_ = 1;
+  std::vector<PassDesc> fwd_, bwd_, fwd_space_;
+  AxisMap maps_[4];
+  int* d_tables_ = nullptr;
+  int off_pos_[4] = {0, 0, 0, 0}, off_rev_[4] = {0, 0, 0, 0}, off_log_[4] = {0, 0, 0, 0};
+  template <typename R> void run(const std::vector<PassDesc>& passes, cx<R>* data, int nb,
+                                 int sign, cudaStream_t s) const;
+};
+
+// Cached FFT plan for a grid (plans and twiddle tables live for the process).
+const FFT4D& fft_plan(int nx, int ny, int nz, int nt, int elem_bytes);
+
+// Optional live timing of every FFT pass launch with CUDA events on the
+// launching stream: launches, summed milliseconds and algorithmic bytes
+// (each element read once and written once per pass).
+void fft_profile_enable(bool on);
+void fft_profile_collect(double* launches, double* ms, double* bytes);
+
+}  // namespace pgb

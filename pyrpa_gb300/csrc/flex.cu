@@ -1,0 +1,1236 @@
+// Kernels and stage drivers of the GB300 FLEX engine (see flex.cuh).
+#include <algorithm>
+#include <cstdarg>
+#include <cstring>
+#include <map>
+
+#include "flex.cuh"
+#include "linalg.cuh"
+
+namespace pgb {
+
+namespace {
+constexpr double kPi = 3.141592653589793238462643383279;
+constexpr double kThresh = 1.0e-9;  // small-part zeroing of chi0 and Sigma (fchi.f90:483-506)
+
+__host__ __device__ __forceinline__ long long fidx(long long k, long long j, long long a, long long b,
+                                                   long long Nk, long long Nw, long long n) {
+  return k + Nk * (j + Nw * (a + n * b));
+}
+
+template <typename T> __device__ __forceinline__ T thresh(T v) {
+  if (fabs((double)v.x) < kThresh) v.x = 0;
+  if (fabs((double)v.y) < kThresh) v.y = 0;
+  return v;
+}
+
+__device__ int g_err_dev = 0;
+
+void reset_err() {
+  int z = 0;
+  PGB_CUDA(cudaMemcpyToSymbolAsync(g_err_dev, &z, sizeof(int), 0, cudaMemcpyHostToDevice, ctx().stream));
+}
+int fetch_err() {
+  int e = 0;
+  PGB_CUDA(cudaMemcpyFromSymbolAsync(&e, g_err_dev, sizeof(int), 0, cudaMemcpyDeviceToHost, ctx().stream));
+  sync();
+  return e;
+}
+
+inline void count_launch(const char* what) {
+  launch_check(what);
+  ctx().kernel_launches++;
+}
+
+inline unsigned grid_1d(long long n, int threads, long long cap = 1LL << 30) {
+  long long b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return (unsigned)b;
+}
+}  // namespace
+
+void log(const char* fmt, ...) {
+  if (!ctx().verbose) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vfprintf(stdout, fmt, ap);
+  va_end(ap);
+  fflush(stdout);
+}
+
+// =============================================================== geometry ==
+void build_geom(Geom& g, const int64_t* kmap, const int64_t* invk, int64_t Nx, int64_t Ny, int64_t Nz,
+                int64_t Nk, int64_t Nw, int64_t Norb, int64_t Nchi) {
+  PGB_CHECK(Nx > 0 && Ny > 0 && Nz > 0 && Nk > 0 && Nw > 0 && Norb > 0 && Nchi > 0,
+            "non-positive mesh or orbital dimension");
+  PGB_CHECK(Norb <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  PGB_CHECK(Nchi <= kMaxChi, "Nchi above the engine limit of 32 orbital pairs");
+  g.Nx = (int)Nx; g.Ny = (int)Ny; g.Nz = (int)Nz; g.Nw = (int)Nw; g.Nk = (int)Nk;
+  g.Norb = (int)Norb; g.Nchi = (int)Nchi;
+  g.Nkall = Nx * Ny * Nz;
+  g.M = 2 * Nw;
+  g.P = g.Nkall * g.M;
+  g.K = Nk * Nw;
+  g.h_grid_irr.assign(g.Nkall, -1);
+  g.h_grid_flag.assign(g.Nkall, 0);
+  g.h_irr_grid.assign(Nk, -1);
+  g.h_kweight.assign(Nk, 0.0);
+  g.h_full_of_grid.assign(g.Nkall, -1);
+  g.h_kmap.assign(kmap, kmap + 3 * g.Nkall);
+  for (long long i = 0; i < g.Nkall; ++i) {
+    const int64_t x = kmap[3 * i], y = kmap[3 * i + 1], z = kmap[3 * i + 2];
+    PGB_CHECK(x >= 0 && x < Nx && y >= 0 && y < Ny && z >= 0 && z < Nz, "kmap entry outside the mesh");
+    const long long gi = x + Nx * (y + Ny * z);
+    PGB_CHECK(g.h_grid_irr[gi] < 0, "kmap maps two k points onto one mesh cell");
+    const int64_t k = invk[3 * i] - 1, fl = invk[3 * i + 1];
+    PGB_CHECK(k >= 0 && k < Nk, "invk(1,:) outside [1,Nk]");
+    PGB_CHECK(fl == 0 || fl == 1, "invk(2,:) must be 0 or 1");
+    g.h_grid_irr[gi] = (int)k;
+    g.h_grid_flag[gi] = (int)fl;
+    g.h_full_of_grid[gi] = (int)i;
+    g.h_kweight[k] += 1.0;
+    if (fl == 0) {
+      PGB_CHECK(g.h_irr_grid[k] < 0, "an irreducible k point has two direct images");
+      g.h_irr_grid[k] = (int)gi;
+    }
+  }
+  for (long long k = 0; k < Nk; ++k)
+    PGB_CHECK(g.h_irr_grid[k] >= 0, "an irreducible k point has no direct image in kmap/invk");
+  g.grid_irr.alloc(g.Nkall);
+  g.grid_irr.upload(g.h_grid_irr.data(), g.Nkall);
+  g.grid_flag.alloc(g.Nkall);
+  g.grid_flag.upload(g.h_grid_flag.data(), g.Nkall);
+  g.irr_grid.alloc(Nk);
+  g.irr_grid.upload(g.h_irr_grid.data(), Nk);
+  g.kweight.alloc(Nk);
+  g.kweight.upload(g.h_kweight.data(), Nk);
+}
+
+void build_pairs(Pairs& p, const int64_t* olist, int Norb, int Nchi, const int32_t* irr_chi,
+                 const int32_t* chi_map) {
+  p.Norb = Norb;
+  p.Nchi = Nchi;
+  p.o1.resize(Nchi);
+  p.o2.resize(Nchi);
+  for (int l = 0; l < Nchi; ++l) {
+    p.o1[l] = (int)olist[l] - 1;
+    p.o2[l] = (int)olist[Nchi + l] - 1;
+    PGB_CHECK(p.o1[l] >= 0 && p.o1[l] < Norb && p.o2[l] >= 0 && p.o2[l] < Norb,
+              "olist entry outside [1,Norb]");
+  }
+  // exchange-symmetry map chi_1234 = chi*_4321 (fchi.f90:421-481)
+  std::vector<int> cm_m(Nchi * Nchi, -1), cm_l(Nchi * Nchi, -1);
+  std::vector<std::pair<int, int>> irr;  // (l, m)
+  if (chi_map && irr_chi) {
+    for (int l = 0; l < Nchi; ++l)
+      for (int m = 0; m < Nchi; ++m) {
+        cm_m[m + Nchi * l] = chi_map[m + Nchi * l] - 1;
+        cm_l[m + Nchi * l] = chi_map[m + Nchi * (l + Nchi)] - 1;
+      }
+    const int nirr = Nchi * (Nchi + 1) / 2;
+    for (int it = 0; it < nirr; ++it) {
+      const int l = irr_chi[it] - 1, m = irr_chi[it + nirr] - 1;
+      if (l < 0 || m < 0) continue;
+      PGB_CHECK(l < Nchi && m < Nchi, "irr_chi entry outside [1,Nchi]");
+      irr.push_back({l, m});
+    }
+  } else {
+    std::vector<char> is_irr(Nchi * Nchi, 0);
+    for (int l1 = 0; l1 < Nchi; ++l1)
+      for (int m1 = 0; m1 < Nchi; ++m1) {
+        bool done = false;
+        for (int l2 = 0; l2 < Nchi && !done; ++l2)
+          for (int m2 = 0; m2 < Nchi; ++m2) {
+            if (p.o1[l1] == p.o2[m2] && p.o2[l1] == p.o1[m2] && p.o1[m1] == p.o2[l2] &&
+                p.o2[m1] == p.o1[l2]) {
+              cm_m[m1 + Nchi * l1] = m2;
+              cm_l[m1 + Nchi * l1] = l2;
+              if (!is_irr[m2 + Nchi * l2]) is_irr[m1 + Nchi * l1] = 1;
+              done = true;
+              break;
+            }
+          }
+      }
+    for (int l1 = 0; l1 < Nchi; ++l1)
+      for (int m1 = 0; m1 < Nchi; ++m1)
+        if (is_irr[m1 + Nchi * l1]) irr.push_back({l1, m1});
+  }
+  p.chi.clear();
+  for (auto& lm : irr) {
+    ChiPair c{};
+    c.l = lm.first;
+    c.m = lm.second;
+    c.m2 = cm_m[c.m + Nchi * c.l];
+    c.l2 = cm_l[c.m + Nchi * c.l];
+    PGB_CHECK(c.m2 >= 0 && c.l2 >= 0, "orbital pair without exchange partner in olist");
+    c.self = (c.m2 == c.m && c.l2 == c.l);
+    c.e13 = p.o1[c.l] + Norb * p.o1[c.m];
+    c.e42 = p.o2[c.m] + Norb * p.o2[c.l];
+    c.J = make_double2(0, 0);
+    p.chi.push_back(c);
+  }
+  p.sigma.assign(Norb * Norb, {});
+  p.delta.assign(Norb * Norb, {});
+  for (int l = 0; l < Nchi; ++l)
+    for (int m = 0; m < Nchi; ++m) {
+      p.sigma[p.o1[m] + Norb * p.o1[l]].push_back({m, l, p.o2[m] + Norb * p.o2[l]});
+      if (p.o1[l] >= p.o2[m]) p.delta[p.o1[l] + Norb * p.o2[m]].push_back({m, l, p.o2[l] + Norb * p.o1[m]});
+    }
+}
+
+// =============================================================== green ==
+__global__ void k_green0(double2* G, const double* eig, const double2* uni, double mu, double temp,
+                         int Nk, int Nw, int No) {
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
+    const double2 iw = mkc(mu, (2.0 * j + 1.0) * kPi * temp);
+    double2 den[kMaxOrb];
+    for (int n = 0; n < No; ++n) den[n] = cdiv(mkc(1.0, 0.0), iw - mkc(eig[n + (long long)No * k], 0.0));
+    const double2* U = uni + (long long)No * No * k;
+    for (int l = 0; l < No; ++l)
+      for (int m = 0; m < No; ++m) {
+        double2 acc = mkc(0.0, 0.0);
+        for (int n = 0; n < No; ++n) acc += U[m + No * n] * conj(U[l + No * n]) * den[n];
+        G[fidx(k, j, m, l, Nk, Nw, No)] = acc;
+      }
+  }
+}
+
+void green0(double2* G, const double* eig, const double2* uni, double mu, double temp, int Nk, int Nw,
+            int Norb) {
+  const long long K = (long long)Nk * Nw;
+  k_green0<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, eig, uni, mu, temp, Nk, Nw, Norb);
+  count_launch("green0");
+}
+
+__global__ void k_dyson(double2* G, const double2* sig, const double2* hamk, double mu, double temp,
+                        int Nk, int Nw, int No, int invert) {
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
+    const double2 iw = mkc(mu, (2.0 * j + 1.0) * kPi * temp);
+    double2 A[kMaxOrb * kMaxOrb];
+    for (int l = 0; l < No; ++l)
+      for (int m = 0; m < No; ++m) {
+        double2 v = -(hamk[m + No * (l + (long long)No * k)] + sig[fidx(k, j, m, l, Nk, Nw, No)]);
+        if (l == m) v += iw;
+        A[m * No + l] = v;
+      }
+    if (invert && !inv_small(A, No)) atomicExch(&g_err_dev, 1);
+    for (int l = 0; l < No; ++l)
+      for (int m = 0; m < No; ++m) G[fidx(k, j, m, l, Nk, Nw, No)] = A[m * No + l];
+  }
+}
+
+bool dyson(double2* G, const double2* sig, const double2* hamk, double mu, double temp, int Nk, int Nw,
+           int Norb) {
+  reset_err();
+  const long long K = (long long)Nk * Nw;
+  k_dyson<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, sig, hamk, mu, temp, Nk, Nw, Norb, 1);
+  count_launch("dyson");
+  return fetch_err() == 0;
+}
+
+void green_inv_only(double2* G, const double2* sig, const double2* hamk, double mu, double temp, int Nk,
+                    int Nw, int Norb) {
+  const long long K = (long long)Nk * Nw;
+  k_dyson<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, sig, hamk, mu, temp, Nk, Nw, Norb, 0);
+  count_launch("green_inv");
+}
+
+__global__ void k_invert_blocks(double2* G, long long nmat, int No, long long smat, long long sel) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nmat;
+       t += (long long)gridDim.x * blockDim.x) {
+    double2 A[kMaxOrb * kMaxOrb];
+    for (int l = 0; l < No; ++l)
+      for (int m = 0; m < No; ++m) A[m * No + l] = G[t * smat + sel * (m + No * l)];
+    if (!inv_small(A, No)) atomicExch(&g_err_dev, 1);
+    for (int l = 0; l < No; ++l)
+      for (int m = 0; m < No; ++m) G[t * smat + sel * (m + No * l)] = A[m * No + l];
+  }
+}
+
+bool invert_blocks(double2* G, long long nmat, int Norb, long long stride_mat, long long stride_el) {
+  reset_err();
+  k_invert_blocks<<<grid_1d(nmat, 128, 65536), 128, 0, ctx().stream>>>(G, nmat, Norb, stride_mat,
+                                                                         stride_el);
+  count_launch("invert_blocks");
+  return fetch_err() == 0;
+}
+
+// ========================================================== padded grids ==
+// Full-grid padded Green function of element e=(a,b) (fchi.f90:563-583):
+// slot n<Nw: G_ab(k,iw_n) (at -k: G_ba), slot 2Nw-1-j: conj G_ba(k,iw_j)
+// (at -k: conj G_ab).
+template <typename R>
+__global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, const int* grid_irr,
+                            const int* grid_flag, long long Nkall, int Nk, int Nw, int No, long long P) {
+  const int e = elems[blockIdx.y];
+  const int a = e % No, b = e / No;
+  cx<R>* o = out + (long long)blockIdx.y * P;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)(idx / Nkall);
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    double2 v;
+    if (n < Nw) {
+      v = fl ? G[fidx(k, n, b, a, Nk, Nw, No)] : G[fidx(k, n, a, b, Nk, Nw, No)];
+    } else {
+      const int j = 2 * Nw - 1 - n;
+      v = conj(fl ? G[fidx(k, j, a, b, Nk, Nw, No)] : G[fidx(k, j, b, a, Nk, Nw, No)]);
+    }
+    o[idx] = cmk<R>((R)v.x, (R)v.y);
+  }
+}
+
+// Padded bosonic array of pair (m,l) (fself.f90:201-223, feliash.f90:538-560):
+// slots 0..Nw-1 = nu_0..nu_{Nw-1} (at -q the transposed pair), slot Nw = the
+// static value, slot 2Nw-j = conj V_lm(nu_j) (at -q conj V_ml).
+struct BosonTerm {
+  int m, l;
+  double stat;
+};
+template <typename R>
+__global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, const int* grid_irr,
+                            const int* grid_flag, long long Nkall, int Nk, int Nw, int Nchi, long long P) {
+  const BosonTerm t = terms[blockIdx.y];
+  cx<R>* o = out + (long long)blockIdx.y * P;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)(idx / Nkall);
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    cx<R> v;
+    if (n < Nw) {
+      v = fl ? V[fidx(k, n, t.l, t.m, Nk, Nw, Nchi)] : V[fidx(k, n, t.m, t.l, Nk, Nw, Nchi)];
+    } else if (n == Nw) {
+      v = cmk<R>((R)t.stat, (R)0);
+    } else {
+      const int j = 2 * Nw - n;
+      v = conj(fl ? V[fidx(k, j, t.m, t.l, Nk, Nw, Nchi)] : V[fidx(k, j, t.l, t.m, Nk, Nw, Nchi)]);
+    }
+    o[idx] = v;
+  }
+}
+
+// Padded anomalous function of element (a,b) with the parity rules of
+// mkdelta_nsoc (feliash.f90:561-578).
+template <typename R>
+__global__ void k_pad_anomalous(cx<R>* out, const double2* F, const int* grid_irr, const int* grid_flag,
+                                long long Nkall, int Nk, int Nw, int No, long long P, const double* prt,
+                                double sgn, double dprt) {
+  const int e = blockIdx.y;
+  const int a = e % No, b = e / No;
+  const double pp = prt[a] * prt[b];
+  cx<R>* o = out + (long long)e * P;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)(idx / Nkall);
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    double2 v;
+    if (n < Nw) {
+      v = F[fidx(k, n, a, b, Nk, Nw, No)];
+      if (fl) v = (pp * dprt) * v;
+    } else {
+      const int j = 2 * Nw - 1 - n;
+      if (!fl) v = (sgn * dprt * pp) * conj(F[fidx(k, j, a, b, Nk, Nw, No)]);
+      else v = sgn * F[fidx(k, j, b, a, Nk, Nw, No)];
+    }
+    o[idx] = cmk<R>((R)v.x, (R)v.y);
+  }
+}
+
+template <typename R>
+void pad_green_all(const Geom& g, const double2* G, cx<R>* out) {
+  const int No2 = g.Norb * g.Norb;
+  std::vector<int> h(No2);
+  for (int e = 0; e < No2; ++e) h[e] = e;
+  DBuf<int> d(No2);
+  d.upload(h.data(), No2);
+  dim3 grid(grid_1d(g.P, 256, 4096), No2);
+  k_pad_green<R><<<grid, 256, 0, ctx().stream>>>(out, G, d.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk,
+                                                  g.Nw, g.Norb, g.P);
+  count_launch("pad_green");
+}
+
+// ================================================================== chi0 ==
+struct ChiDev {
+  int m, l, m2, l2, e13, e42, self, pad;
+  double2 J;
+};
+
+template <typename R>
+__global__ void k_chi0_product(cx<R>* out, const cx<R>* F, const cx<R>* F0, const cx<R>* A,
+                               const cx<R>* B, const ChiDev* pairs, long long P, int Nx, int Ny, int Nz,
+                               int M, const int* rx, const int* ry, const int* rz, const int* rt,
+                               const int* lt, R sc, R sr) {
+  const ChiDev pr = pairs[blockIdx.y];
+  const cx<R>* a13 = F + (long long)pr.e13 * P;
+  const cx<R>* b42 = F + (long long)pr.e42 * P;
+  cx<R>* o = out + (long long)blockIdx.y * P;
+  const long long Nxy = (long long)Nx * Ny, Nkall = Nxy * Nz;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long r = idx % Nkall;
+    const int t = (int)(idx / Nkall);
+    const int x = (int)(r % Nx), y = (int)((r / Nx) % Ny), z = (int)(r / Nxy);
+    const long long rr = rx[x] + Nx * (ry[y] + (long long)Ny * rz[z]);
+    const long long ir = rr + Nkall * rt[t];
+    cx<R> v = -(a13[idx] * b42[ir]);
+    if (F0) {
+      // The reference conjugates a self-partner pair after each of its three
+      // accumulations (fchi.f90:610, 845-846), which leaves conj(conv[G] + ref)
+      // - conv[G0]; conj(conv[G0]) enters here as the transform of
+      // conj(P0(-r,-t)) so that one backward FFT and a final conj give it.
+      if (pr.self) v += conj(F0[(long long)pr.e13 * P + ir] * F0[(long long)pr.e42 * P + idx]);
+      else v += F0[(long long)pr.e13 * P + idx] * F0[(long long)pr.e42 * P + ir];
+    }
+    v = sc * v;
+    if (A) {
+      const long long s = lt[t];
+      v -= sr * (A[(long long)pr.e13 * P + r + Nkall * s] * B[(long long)pr.e42 * P + rr + Nkall * s]);
+    }
+    o[idx] = v;
+  }
+}
+
+template <typename R>
+__global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs, const int* irr_grid,
+                               const double2* sawc, long long Nkall, int Nk, int Nw, int Nchi, long long P) {
+  const ChiDev pr = pairs[blockIdx.y];
+  const cx<R>* t = tmp + (long long)blockIdx.y * P;
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
+    double2 v = ccast<double>(t[irr_grid[k] + Nkall * j]);
+    if (sawc) v += pr.J * sawc[j];
+    if (pr.self) v = conj(v);
+    v = thresh(v);
+    chi[fidx(k, j, pr.m, pr.l, Nk, Nw, Nchi)] = cmk<R>((R)v.x, (R)v.y);
+    if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = cmk<R>((R)v.x, (R)-v.y);
+  }
+}
+
+// tau kernels of the analytic reference bubble (fchi.f90:703-729), laid out
+// [(s*Norb + n)*Nk + k]
+__global__ void k_gpm(double* gp, double* gm, double* ff, const double* eig, double mu, double temp,
+                      int Nk, int No, int M) {
+  const long long N = (long long)Nk * No * M;
+  const double beta = 1.0 / temp, dtau = beta / M;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk);
+    const int n = (int)((idx / Nk) % No);
+    const int s = (int)(idx / ((long long)Nk * No));
+    const double xi = eig[n + (long long)No * k] - mu;
+    const double tau = s * dtau;
+    double p, q;
+    if (xi >= 0) {
+      const double d = 1.0 + exp(-beta * xi);
+      p = -exp(-xi * tau) / d;
+      q = exp(-xi * (beta - tau)) / d;
+      if (s == 0) ff[n + (long long)No * k] = exp(-beta * xi) / d;
+    } else {
+      const double d = 1.0 + exp(beta * xi);
+      p = -exp(xi * (beta - tau)) / d;
+      q = exp(xi * tau) / d;
+      if (s == 0) ff[n + (long long)No * k] = 1.0 / d;
+    }
+    gp[idx] = p;
+    gm[idx] = q;
+  }
+}
+
+// A_ab(g,s) = sum_n U_an U*_bn gp (conjugated coefficient at -k), same for B with gm
+template <typename R>
+__global__ void k_ref_tau(cx<R>* A, cx<R>* B, const double* gp, const double* gm, const double2* uni,
+                          const int* grid_irr, const int* grid_flag, long long Nkall, int Nk, int No,
+                          int M, long long P) {
+  const int e = blockIdx.y;
+  const int a = e % No, b = e / No;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int s = (int)(idx / Nkall);
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    const double2* U = uni + (long long)No * No * k;
+    double2 sa = mkc(0.0, 0.0), sb = mkc(0.0, 0.0);
+    for (int n = 0; n < No; ++n) {
+      double2 c = U[a + No * n] * conj(U[b + No * n]);
+      if (fl) c = conj(c);
+      const long long gidx = ((long long)s * No + n) * Nk + k;
+      sa += gp[gidx] * c;
+      sb += gm[gidx] * c;
+    }
+    A[(long long)e * P + idx] = cmk<R>((R)sa.x, (R)sa.y);
+    B[(long long)e * P + idx] = cmk<R>((R)sb.x, (R)sb.y);
+  }
+}
+
+// rhobar(m,l) = (1/Nkall) sum_full [rho(m,l,k) | rho(l,m,k) at -k] (fchi.f90:731-755)
+__global__ void k_rhobar(double2* rhobar, const double2* uni, const double* ff, const int* grid_irr,
+                         const int* grid_flag, long long Nkall, int No) {
+  const int e = blockIdx.x;
+  const int m = e % No, l = e / No;
+  __shared__ double2 red[256];
+  double2 acc = mkc(0.0, 0.0);
+  for (long long gi = threadIdx.x; gi < Nkall; gi += blockDim.x) {
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    const int p = fl ? l : m, q = fl ? m : l;
+    const double2* U = uni + (long long)No * No * k;
+    double2 r = mkc(0.0, 0.0);
+    for (int n = 0; n < No; ++n) r += (U[p + No * n] * conj(U[q + No * n])) * mkc(ff[n + (long long)No * k], 0.0);
+    acc += r;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) rhobar[e] = (1.0 / (double)Nkall) * red[0];
+}
+
+// sawtooth correction: exact -1/(i nu) minus its rectangle-rule DFT (fchi.f90:757-772)
+__global__ void k_sawc(double2* sawc, int Nw, int M, double temp) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= Nw) return;
+  const double dtau = 1.0 / temp / M;
+  double2 v = mkc(0.0, 0.0);
+  if (j > 0) v = mkc(0.0, 1.0 / (2.0 * kPi * j * temp));
+  for (int s = 0; s < M; ++s) {
+    double sn, cs;
+    sincospi(2.0 * (double)(((long long)j * s) % M) / (double)M, &sn, &cs);
+    const double w = dtau * (0.5 - (double)s / (double)M);
+    v.x -= w * cs;
+    v.y -= w * sn;
+  }
+  sawc[j] = v;
+}
+
+template <typename R>
+void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const TailRef* tail, cx<R>* chi) {
+  cudaStream_t st = ctx().stream;
+  const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, (int)g.M, (int)sizeof(cx<R>));
+  const int No2 = g.Norb * g.Norb;
+  DBuf<cx<R>> F((size_t)No2 * g.P);
+  pad_green_all<R>(g, G, F.p);
+  fft.forward<R>(F.p, No2, st);
+  DBuf<cx<R>> F0, A, B;
+  DBuf<double2> sawc;
+  std::vector<ChiDev> hp(p.chi.size());
+  for (size_t i = 0; i < p.chi.size(); ++i) {
+    const ChiPair& c = p.chi[i];
+    hp[i] = ChiDev{c.m, c.l, c.m2, c.l2, c.e13, c.e42, c.self, 0, make_double2(0, 0)};
+  }
+  if (tail) {
+    DBuf<double2> G0((size_t)g.K * No2);
+    green0(G0.p, tail->eig, tail->uni, tail->mu, temp, g.Nk, g.Nw, g.Norb);
+    F0.alloc((size_t)No2 * g.P);
+    pad_green_all<R>(g, G0.p, F0.p);
+    G0.release();
+    fft.forward<R>(F0.p, No2, st);
+    DBuf<double> gp((size_t)g.Nk * g.Norb * g.M), gm((size_t)g.Nk * g.Norb * g.M), ff((size_t)g.Nk * g.Norb);
+    k_gpm<<<grid_1d((long long)g.Nk * g.Norb * g.M, 256, 65536), 256, 0, st>>>(
+        gp.p, gm.p, ff.p, tail->eig, tail->mu, temp, g.Nk, g.Norb, (int)g.M);
+    count_launch("gpm");
+    A.alloc((size_t)No2 * g.P);
+    B.alloc((size_t)No2 * g.P);
+    dim3 gr(grid_1d(g.P, 256, 4096), No2);
+    k_ref_tau<R><<<gr, 256, 0, st>>>(A.p, B.p, gp.p, gm.p, tail->uni, g.grid_irr.p, g.grid_flag.p, g.Nkall,
+                                      g.Nk, g.Norb, (int)g.M, g.P);
+    count_launch("ref_tau");
+    fft.forward_space<R>(A.p, No2, st);
+    fft.forward_space<R>(B.p, No2, st);
+    DBuf<double2> rb(No2);
+    k_rhobar<<<No2, 256, 0, st>>>(rb.p, tail->uni, ff.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Norb);
+    count_launch("rhobar");
+    std::vector<double2> hrb(No2);
+    rb.download(hrb.data(), No2);
+    sync();
+    auto RB = [&](int m, int l) { return hrb[m + g.Norb * l]; };
+    for (auto& c : hp) {
+      const int a13 = p.o1[c.l], b13 = p.o1[c.m], a42 = p.o2[c.m], b42 = p.o2[c.l];
+      double2 J = make_double2(0, 0);
+      if (a13 == b13) J = J + RB(a42, b42);
+      if (a42 == b42) J = J - RB(a13, b13);
+      c.J = J;
+    }
+    sawc.alloc(g.Nw);
+    k_sawc<<<grid_1d(g.Nw, 128), 128, 0, st>>>(sawc.p, g.Nw, (int)g.M, temp);
+    count_launch("sawc");
+  }
+  DBuf<ChiDev> dp(hp.size());
+  dp.upload(hp.data(), hp.size());
+  PGB_CUDA(cudaMemsetAsync(chi, 0, sizeof(cx<R>) * (size_t)g.K * g.Nchi * g.Nchi, st));
+  // chunk of pairs per backward batch: bounded by free memory
+  size_t freeb = 0, totb = 0;
+  PGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+  long long ch = (long long)((freeb / 3) / (sizeof(cx<R>) * (size_t)g.P));
+  ch = std::max(1LL, std::min<long long>(ch, (long long)hp.size()));
+  ch = std::min(ch, 64LL);
+  DBuf<cx<R>> T((size_t)ch * g.P);
+  const double sc = temp / (double)g.Nkall / (double)g.P;
+  const double sr = 1.0 / (temp * (double)g.Nkall) / (double)g.P;
+  for (long long c0 = 0; c0 < (long long)hp.size(); c0 += ch) {
+    const int nc = (int)std::min<long long>(ch, (long long)hp.size() - c0);
+    dim3 gr(grid_1d(g.P, 256, 4096), nc);
+    k_chi0_product<R><<<gr, 256, 0, st>>>(T.p, F.p, tail ? F0.p : nullptr, tail ? A.p : nullptr,
+                                          tail ? B.p : nullptr, dp.p + c0, g.P, g.Nx, g.Ny, g.Nz, (int)g.M,
+                                          fft.d_rev(0), fft.d_rev(1), fft.d_rev(2), fft.d_rev(3),
+                                          fft.d_logical(3), (R)sc, (R)sr);
+    count_launch("chi0_product");
+    fft.backward<R>(T.p, nc, st);
+    dim3 gs(grid_1d(g.K, 256, 4096), nc);
+    k_chi0_scatter<R><<<gs, 256, 0, st>>>(chi, T.p, dp.p + c0, g.irr_grid.p, tail ? sawc.p : nullptr,
+                                          g.Nkall, g.Nk, g.Nw, g.Nchi, g.P);
+    count_launch("chi0_scatter");
+  }
+}
+
+// ================================================================ stoner ==
+template <typename R>
+__global__ void k_stoner(double* out, const cx<R>* chi, const double* S, const double* C, int Nk, int Nw,
+                         int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * Nk) return;
+  const int k = t % Nk, which = t / Nk;
+  const double* V = which ? C : S;
+  const double sg = which ? -1.0 : 1.0;
+  double2 Mx[kMaxChi * kMaxChi];
+  double2 w[kMaxChi];
+  for (int a = 0; a < n; ++a)
+    for (int b = 0; b < n; ++b) {
+      double2 acc = mkc(0.0, 0.0);
+      for (int c = 0; c < n; ++c) acc += V[c + n * b] * ccast<double>(chi[fidx(k, 0, a, c, Nk, Nw, n)]);
+      Mx[a * n + b] = sg * acc;
+    }
+  const int rc = eigvals_general(Mx, n, w);
+  if (rc < 0) atomicExch(&g_err_dev, 2);
+  double best = -1e300;
+  for (int i = 0; i < n; ++i) best = fmax(best, w[i].x);
+  out[t] = best;
+}
+
+template <typename R>
+void stoner(const Geom& g, const cx<R>* chi, const double* S, const double* C, double* sdw, double* cdw,
+            int* q_sdw, int* q_cdw) {
+  reset_err();
+  DBuf<double> out(2 * (size_t)g.Nk);
+  k_stoner<R><<<grid_1d(2LL * g.Nk, 32), 32, 0, ctx().stream>>>(out.p, chi, S, C, g.Nk, g.Nw, g.Nchi);
+  count_launch("stoner");
+  std::vector<double> h(2 * (size_t)g.Nk);
+  out.download(h.data(), h.size());
+  const int e = fetch_err();
+  PGB_CHECK(e == 0, "eigenvalue iteration of chi0(q,0)S did not converge");
+  double s2 = -1.0e5, c2 = -1.0e5;
+  int qs = 0, qc = 0;
+  for (int k = 0; k < g.Nk; ++k) {
+    if (h[k] > s2) { s2 = h[k]; qs = k; }
+    if (h[g.Nk + k] > c2) { c2 = h[g.Nk + k]; qc = k; }
+  }
+  *sdw = s2;
+  *cdw = c2;
+  if (q_sdw) *q_sdw = qs;
+  if (q_cdw) *q_cdw = qc;
+}
+
+void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc) {
+  auto kc = [&](int k, int c) { return (long long)g.h_kmap[3 * (long long)g.h_full_of_grid[g.h_irr_grid[k]] + c]; };
+  log("SDW%4lld%4lld%4lld%12.8f\n", kc(qs, 0), kc(qs, 1), kc(qs, 2), sdw);
+  log("CDW%4lld%4lld%4lld%12.8f\n", kc(qc, 0), kc(qc, 1), kc(qc, 2), cdw);
+}
+
+// ================================================================ vertex ==
+template <typename R>
+__global__ void k_vertex(cx<R>* chi, long long nmat, long long mstride, long long estride, int n,
+                         const double* S, const double* C, int mode, int warps) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  double* sS = reinterpret_cast<double*>(sm);
+  double* sC = sS + n * n;
+  double* sSC = sC + n * n;
+  size_t off = ((size_t)3 * n * n * sizeof(double) + 15) / 16 * 16;
+  cx<R>* wb = reinterpret_cast<cx<R>*>(sm + off);
+  const int ld = n;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  cx<R>* X = wb + (size_t)w * 4 * n * ld;
+  cx<R>* Pm = X + n * ld;
+  cx<R>* Q = Pm + n * ld;
+  cx<R>* T = Q + n * ld;
+  for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+    const int a = e / n, b = e % n;
+    sS[a * n + b] = S[a + n * b];
+    sC[a * n + b] = C[a + n * b];
+    sSC[a * n + b] = S[a + n * b] + C[a + n * b];
+  }
+  __syncthreads();
+  for (long long mat = (long long)blockIdx.x * warps + w; mat < nmat; mat += (long long)gridDim.x * warps) {
+    cx<R>* base = chi + mat * mstride;
+    for (int e = lane; e < n * n; e += 32) X[(e % n) * ld + e / n] = base[estride * e];
+    __syncwarp();
+    wmm_cr<R>(Pm, X, sS, n, ld, (R)1);  // chi0 S
+    wmm_cr<R>(Q, X, sC, n, ld, (R)1);   // chi0 C
+    bool ok = true;
+    if (mode == 0) {
+      // V = 1.5S - 0.5C - 0.25 (S+C)(chi0S + chi0C) + 1.5 S Xs + 0.5 C Xc
+      if (lane < n)
+        for (int j = 0; j < n; ++j) {
+          cx<R> acc = cmk<R>(0, 0);
+          for (int k = 0; k < n; ++k) acc += (R)sSC[lane * n + k] * (Pm[k * ld + j] + Q[k * ld + j]);
+          X[lane * ld + j] = cmk<R>((R)(1.5 * sS[lane * n + j] - 0.5 * sC[lane * n + j]), (R)0) - (R)0.25 * acc;
+        }
+      __syncwarp();
+    } else if (mode == 1 || mode == 2) {
+      const double sg = (mode == 1) ? 1.0 : -1.0;
+      for (int e = lane; e < n * n; e += 32)
+        X[(e / n) * ld + e % n] = cmk<R>((R)(0.5 * (sS[e] + sg * sC[e])), (R)0);
+      __syncwarp();
+    }
+    if (mode <= 2) {
+      // T = I - chi0 S ; solve T Xs = chi0 S
+      for (int e = lane; e < n * n; e += 32) {
+        const int a = e / n, b = e % n;
+        T[a * ld + b] = cmk<R>((R)(a == b), (R)0) - Pm[a * ld + b];
+      }
+      __syncwarp();
+      ok &= wsolve<R>(T, Pm, n, ld);
+      const R cs = (mode == 2) ? (R)-0.5 : (R)1.5;
+      wmm_rc_acc<R>(X, sS, Pm, n, ld, cs);
+      for (int e = lane; e < n * n; e += 32) {
+        const int a = e / n, b = e % n;
+        T[a * ld + b] = cmk<R>((R)(a == b), (R)0) + Q[a * ld + b];
+      }
+      __syncwarp();
+      ok &= wsolve<R>(T, Q, n, ld);
+      const R cc = (mode == 0) ? (R)0.5 : (R)-0.5;
+      wmm_rc_acc<R>(X, sC, Q, n, ld, cc);
+    } else {
+      // chi_s = (I - chi0 S)^-1 chi0 (mode 3), chi_c = (I + chi0 C)^-1 chi0 (mode 4)
+      for (int e = lane; e < n * n; e += 32) {
+        const int a = e / n, b = e % n;
+        T[a * ld + b] = cmk<R>((R)(a == b), (R)0) + ((mode == 3) ? -Pm[a * ld + b] : Q[a * ld + b]);
+      }
+      __syncwarp();
+      ok &= wsolve<R>(T, X, n, ld);
+    }
+    if (!ok && lane == 0) atomicExch(&g_err_dev, 3);
+    for (int e = lane; e < n * n; e += 32) base[estride * e] = X[(e % n) * ld + e / n];
+    __syncwarp();
+  }
+}
+
+template <typename R>
+bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double* S, const double* C,
+            int mode) {
+  // stride: distance between the elements of one matrix (matrices are consecutive, mstride 1)
+  // stride < 0 selects compact matrices: mstride = Nchi^2, estride = 1
+  long long mstride = 1, estride = stride;
+  if (stride < 0) { mstride = (long long)Nchi * Nchi; estride = 1; }
+  const int n = Nchi;
+  const size_t head = ((size_t)3 * n * n * sizeof(double) + 15) / 16 * 16;
+  const size_t per_warp = (size_t)4 * n * n * sizeof(cx<R>);
+  int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - head) / per_warp));
+  const size_t smem = head + warps * per_warp;
+  static bool attr[2] = {false, false};
+  if (!attr[sizeof(R) == 8]) {
+    PGB_CUDA(cudaFuncSetAttribute(k_vertex<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+    attr[sizeof(R) == 8] = true;
+  }
+  reset_err();
+  const long long blocks = std::min<long long>((nmat + warps - 1) / warps, (long long)ctx().num_sms * 16);
+  k_vertex<R><<<(unsigned)std::max(1LL, blocks), 32 * warps, smem, ctx().stream>>>(chi, nmat, mstride, estride,
+                                                                                     n, S, C, mode, warps);
+  count_launch("vertex");
+  return fetch_err() == 0;
+}
+
+template <typename R> __global__ void k_scale(cx<R>* a, long long n, R s) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = s * a[i];
+}
+template <typename R> void scale_chi(cx<R>* chi, long long n, double s) {
+  k_scale<R><<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(chi, n, (R)s);
+  count_launch("scale");
+}
+
+// ================================================================= sigma ==
+template <typename R>
+__global__ void k_contract(cx<R>* out, const cx<R>* W, const cx<R>* F, const int* ef, int nt, long long P) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    cx<R> acc = cmk<R>(0, 0);
+    for (int t = 0; t < nt; ++t) acc += W[(long long)t * P + idx] * F[(long long)ef[t] * P + idx];
+    out[idx] = acc;
+  }
+}
+
+__global__ void k_scatter_out(double2* dst, const void* tmp, int is_double, const int* irr_grid, long long Nkall,
+                              int Nk, int Nw, double scale, int do_thresh) {
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
+    const long long src = irr_grid[k] + Nkall * j;
+    double2 v = is_double ? ((const double2*)tmp)[src] : ccast<double>(((const float2*)tmp)[src]);
+    v = scale * v;
+    if (do_thresh) v = thresh(v);
+    dst[idx] = v;
+  }
+}
+
+template <typename R>
+void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, const double* S, const double* C,
+           double temp, double2* sig) {
+  cudaStream_t st = ctx().stream;
+  const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, (int)g.M, (int)sizeof(cx<R>));
+  const int No2 = g.Norb * g.Norb;
+  DBuf<cx<R>> F((size_t)No2 * g.P);
+  pad_green_all<R>(g, G, F.p);
+  fft.forward<R>(F.p, No2, st);
+  std::vector<double> hS(g.Nchi * g.Nchi), hC(g.Nchi * g.Nchi);
+  PGB_CUDA(cudaMemcpyAsync(hS.data(), S, sizeof(double) * hS.size(), cudaMemcpyDeviceToHost, st));
+  PGB_CUDA(cudaMemcpyAsync(hC.data(), C, sizeof(double) * hC.size(), cudaMemcpyDeviceToHost, st));
+  sync();
+  size_t maxt = 0;
+  for (auto& v : p.sigma) maxt = std::max(maxt, v.size());
+  DBuf<cx<R>> W(std::max<size_t>(1, maxt) * g.P), T(g.P);
+  DBuf<BosonTerm> dterms(std::max<size_t>(1, maxt));
+  DBuf<int> def(std::max<size_t>(1, maxt));
+  PGB_CUDA(cudaMemsetAsync(sig, 0, sizeof(double2) * (size_t)g.K * No2, st));
+  const double scale = temp / (double)g.Nkall / (double)g.P;
+  for (int e = 0; e < No2; ++e) {
+    const auto& terms = p.sigma[e];
+    if (terms.empty()) continue;
+    const int nt = (int)terms.size();
+    std::vector<BosonTerm> ht(nt);
+    std::vector<int> hef(nt);
+    for (int t = 0; t < nt; ++t) {
+      const int m = terms[t].m, l = terms[t].l;
+      ht[t] = BosonTerm{m, l, 1.5 * hS[m + g.Nchi * l] - 0.5 * hC[m + g.Nchi * l]};
+      hef[t] = terms[t].ef;
+    }
+    dterms.upload(ht.data(), nt);
+    def.upload(hef.data(), nt);
+    dim3 gr(grid_1d(g.P, 256, 4096), nt);
+    k_pad_boson<R><<<gr, 256, 0, st>>>(W.p, V, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw,
+                                        g.Nchi, g.P);
+    count_launch("pad_boson");
+    fft.forward<R>(W.p, nt, st);
+    k_contract<R><<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(T.p, W.p, F.p, def.p, nt, g.P);
+    count_launch("contract");
+    fft.backward<R>(T.p, 1, st);
+    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)e * g.K, T.p, sizeof(R) == 8,
+                                                             g.irr_grid.p, g.Nkall, g.Nk, g.Nw, scale, 1);
+    count_launch("scatter_sigma");
+    sync();  // host term buffers are reused by the next element
+  }
+}
+
+__global__ void k_hf(double2* sig, int Nk, int Nw, int No, int mode, double2* sub) {
+  // sub(k,l,m) for m >= l then subtract from every frequency (fself.f90:384-416)
+  const long long N = (long long)Nk * No * No;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk);
+    const int l = (int)((idx / Nk) % No), m = (int)(idx / ((long long)Nk * No));
+    if (m < l) continue;
+    double2 v;
+    if (mode == 1) {
+      v = 0.5 * (sig[fidx(k, 0, l, m, Nk, Nw, No)] + conj(sig[fidx(k, 0, m, l, Nk, Nw, No)]));
+    } else {
+      double2 s = mkc(0.0, 0.0);
+      for (int j = 0; j < Nw; ++j) s += sig[fidx(k, j, l, m, Nk, Nw, No)] + conj(sig[fidx(k, j, m, l, Nk, Nw, No)]);
+      v = (0.5 / Nw) * s;
+    }
+    sub[k + (long long)Nk * (l + No * m)] = v;
+    if (l != m) sub[k + (long long)Nk * (m + No * l)] = conj(v);
+  }
+}
+__global__ void k_hf_apply(double2* sig, const double2* sub, int Nk, int Nw, int No) {
+  const long long N = (long long)Nk * Nw * No * No;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long k = idx % Nk;
+    const long long ab = idx / ((long long)Nk * Nw);
+    sig[idx] -= sub[k + Nk * ab];
+  }
+}
+void hf_subtract(double2* sig, int Nk, int Nw, int Norb, int mode) {
+  DBuf<double2> sub((size_t)Nk * Norb * Norb);
+  k_hf<<<grid_1d((long long)Nk * Norb * Norb, 128, 65536), 128, 0, ctx().stream>>>(sig, Nk, Nw, Norb, mode, sub.p);
+  count_launch("hf");
+  k_hf_apply<<<grid_1d((long long)Nk * Nw * Norb * Norb, 256, 65536), 256, 0, ctx().stream>>>(sig, sub.p, Nk, Nw, Norb);
+  count_launch("hf_apply");
+}
+
+// ============================================================ reductions ==
+namespace {
+constexpr int kRedBlocks = 1024;
+constexpr int kRedThreads = 256;
+
+__global__ void k_dot_re(double2* part, const double2* a, const double2* b, long long n) {
+  __shared__ double red[kRedThreads];
+  double acc = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += a[i].x * b[i].x + a[i].y * b[i].y;
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = mkc(red[0], 0.0);
+}
+
+__global__ void k_inner_w(double2* part, const double2* a, const double2* b, const double* kw, int Nk, long long n) {
+  __shared__ double2 red[kRedThreads];
+  double2 acc = mkc(0.0, 0.0);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += kw[i % Nk] * (conj(a[i]) * b[i]);
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void k_sum_parts(double2* out, const double2* part, int n) {
+  __shared__ double2 red[kRedThreads];
+  double2 acc = mkc(0.0, 0.0);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += part[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+__global__ void k_filling(double2* part, const double2* eg, const double* eig, int Nk, int Nw, int No, double mu,
+                          double temp) {
+  __shared__ double2 red[kRedThreads];
+  double2 acc = mkc(0.0, 0.0);  // x: self-energy correction sum, y: Fermi sum
+  const long long N = (long long)Nk * Nw * No;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N; i += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(i % No);
+    const long long kj = i / No;
+    const int k = (int)(kj % Nk), j = (int)(kj / Nk);
+    const double2 z = mkc(mu, (2.0 * j + 1.0) * kPi * temp);
+    const double e = eig[n + (long long)No * k];
+    const double2 t1 = cdiv(mkc(1.0, 0.0), z - eg[n + (long long)No * (k + (long long)Nk * j)]);
+    const double2 t2 = cdiv(mkc(1.0, 0.0), z - mkc(e, 0.0));
+    acc.x += t1.x - t2.x;
+    if (j == 0) acc.y += 0.5 * (1.0 - tanh(0.5 * (e - mu) / temp));
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+double2 finish(DBuf<double2>& part, int nparts) {
+  DBuf<double2> out(1);
+  k_sum_parts<<<1, kRedThreads, 0, ctx().stream>>>(out.p, part.p, nparts);
+  count_launch("sum_parts");
+  double2 h;
+  out.download(&h, 1);
+  sync();
+  return h;
+}
+}  // namespace
+
+double dot_re(const double2* a, const double2* b, long long n) {
+  DBuf<double2> part(kRedBlocks);
+  k_dot_re<<<kRedBlocks, kRedThreads, 0, ctx().stream>>>(part.p, a, b, n);
+  count_launch("dot_re");
+  return finish(part, kRedBlocks).x;
+}
+
+double2 inner_w(const double2* a, const double2* b, const double* kw, int Nk, long long n) {
+  DBuf<double2> part(kRedBlocks);
+  k_inner_w<<<kRedBlocks, kRedThreads, 0, ctx().stream>>>(part.p, a, b, kw, Nk, n);
+  count_launch("inner_w");
+  return finish(part, kRedBlocks);
+}
+
+double filling(const double2* eig_g, const double* eig, int Nk, int Nw, int Norb, double mu, double temp) {
+  DBuf<double2> part(kRedBlocks);
+  k_filling<<<kRedBlocks, kRedThreads, 0, ctx().stream>>>(part.p, eig_g, eig, Nk, Nw, Norb, mu, temp);
+  count_launch("filling");
+  const double2 s = finish(part, kRedBlocks);
+  return (s.y + 2.0 * temp * s.x) / (double)Nk;
+}
+
+__global__ void k_eig_gkinv(double2* eg, const double2* hamk, const double2* sig, int Nk, int Nw, int No) {
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
+    double2 A[kMaxOrb * kMaxOrb], w[kMaxOrb];
+    for (int l = 0; l < No; ++l)
+      for (int m = 0; m < No; ++m)
+        A[m * No + l] = hamk[m + No * (l + (long long)No * k)] + sig[fidx(k, j, m, l, Nk, Nw, No)];
+    if (eigvals_general(A, No, w) < 0) atomicExch(&g_err_dev, 4);
+    for (int n = 0; n < No; ++n) eg[n + (long long)No * idx] = w[n];
+  }
+}
+
+bool eig_gkinv(double2* eig_g, const double2* hamk, const double2* sig, int Nk, int Nw, int Norb) {
+  reset_err();
+  const long long K = (long long)Nk * Nw;
+  k_eig_gkinv<<<grid_1d(K, 64, 1 << 20), 64, 0, ctx().stream>>>(eig_g, hamk, sig, Nk, Nw, Norb);
+  count_launch("eig_gkinv");
+  return fetch_err() == 0;
+}
+
+// ============================================================ eliashberg ==
+__global__ void k_mkfk(double2* F, const double2* G, const double2* D, long long K, int No) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double2 g[kMaxOrb * kMaxOrb], d[kMaxOrb * kMaxOrb], t[kMaxOrb * kMaxOrb];
+    const long long s = K;
+    for (int b = 0; b < No; ++b)
+      for (int a = 0; a < No; ++a) {
+        g[a * No + b] = G[idx + s * (a + No * b)];
+        d[a * No + b] = D[idx + s * (a + No * b)];
+      }
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 acc = mkc(0.0, 0.0);
+        for (int c = 0; c < No; ++c) acc += g[a * No + c] * d[c * No + b];
+        t[a * No + b] = acc;
+      }
+    // F = -(G Delta) G^H, then diag real and upper = conj(lower) (feliash.f90:466-481)
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b <= a; ++b) {
+        double2 acc = mkc(0.0, 0.0);
+        for (int c = 0; c < No; ++c) acc += t[a * No + c] * conj(g[b * No + c]);
+        acc = -acc;
+        if (a == b) acc.y = 0;
+        F[idx + s * (a + No * b)] = acc;
+        if (a != b) F[idx + s * (b + No * a)] = conj(acc);
+      }
+  }
+}
+void mkfk(double2* F, const double2* G, const double2* D, long long K, int Norb) {
+  k_mkfk<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(F, G, D, K, Norb);
+  count_launch("mkfk");
+}
+
+__global__ void k_hermitize(double2* D, long long K, int No) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    for (int l = 0; l < No; ++l) {
+      D[idx + K * (l + No * l)].y = 0;
+      for (int m = l + 1; m < No; ++m) D[idx + K * (l + No * m)] = conj(D[idx + K * (m + No * l)]);
+    }
+  }
+}
+void hermitize(double2* D, long long K, int Norb) {
+  k_hermitize<<<grid_1d(K, 256, 65536), 256, 0, ctx().stream>>>(D, K, Norb);
+  count_launch("hermitize");
+}
+
+template <typename R>
+void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, const double* S, const double* C,
+             const double* prt, bool singlet, double scale, double2* out, DeltaKernelCache<R>* cache) {
+  cudaStream_t st = ctx().stream;
+  const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, (int)g.M, (int)sizeof(cx<R>));
+  const int No2 = g.Norb * g.Norb;
+  const double sgn = singlet ? 1.0 : -1.0, dprt = singlet ? 1.0 : -1.0;
+  DBuf<cx<R>> FF((size_t)No2 * g.P);
+  dim3 gp(grid_1d(g.P, 256, 4096), No2);
+  k_pad_anomalous<R><<<gp, 256, 0, st>>>(FF.p, F, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, g.Norb, g.P,
+                                          prt, sgn, dprt);
+  count_launch("pad_anomalous");
+  fft.forward<R>(FF.p, No2, st);
+  std::vector<double> hS(g.Nchi * g.Nchi), hC(g.Nchi * g.Nchi);
+  PGB_CUDA(cudaMemcpyAsync(hS.data(), S, sizeof(double) * hS.size(), cudaMemcpyDeviceToHost, st));
+  PGB_CUDA(cudaMemcpyAsync(hC.data(), C, sizeof(double) * hC.size(), cudaMemcpyDeviceToHost, st));
+  sync();
+  size_t maxt = 0, total = 0;
+  for (auto& v : p.delta) { maxt = std::max(maxt, v.size()); total += v.size(); }
+  auto terms_of = [&](int e, std::vector<BosonTerm>& ht, std::vector<int>& hef) {
+    const auto& terms = p.delta[e];
+    ht.resize(terms.size());
+    hef.resize(terms.size());
+    for (size_t t = 0; t < terms.size(); ++t) {
+      const int m = terms[t].m, l = terms[t].l;
+      ht[t] = BosonTerm{m, l, 0.5 * (hS[m + g.Nchi * l] + sgn * hC[m + g.Nchi * l])};
+      hef[t] = terms[t].ef;
+    }
+  };
+  DBuf<BosonTerm> dterms(std::max<size_t>(1, maxt));
+  DBuf<int> def(std::max<size_t>(1, maxt));
+  // cache the transformed pairing vertex across Arnoldi steps when it fits
+  if (cache && !cache->built) {
+    size_t freeb = 0, totb = 0;
+    PGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+    const size_t need = total * (size_t)g.P * sizeof(cx<R>);
+    cache->built = true;
+    if (need < freeb * 0.7) {
+      cache->W.alloc(total * (size_t)g.P);
+      cache->offset.assign(No2, 0);
+      long long off = 0;
+      for (int e = 0; e < No2; ++e) {
+        cache->offset[e] = off;
+        if (p.delta[e].empty()) continue;
+        std::vector<BosonTerm> ht;
+        std::vector<int> hef;
+        terms_of(e, ht, hef);
+        dterms.upload(ht.data(), ht.size());
+        dim3 gr(grid_1d(g.P, 256, 4096), (unsigned)ht.size());
+        k_pad_boson<R><<<gr, 256, 0, st>>>(cache->W.p + off * g.P, Vd, dterms.p, g.grid_irr.p, g.grid_flag.p,
+                                            g.Nkall, g.Nk, g.Nw, g.Nchi, g.P);
+        count_launch("pad_vdelta");
+        fft.forward<R>(cache->W.p + off * g.P, (int)ht.size(), st);
+        sync();
+        off += (long long)ht.size();
+      }
+    }
+  }
+  const bool use_cache = cache && cache->W.p;
+  DBuf<cx<R>> W, T(g.P);
+  if (!use_cache) W.alloc(std::max<size_t>(1, maxt) * g.P);
+  PGB_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)g.K * No2, st));
+  for (int e = 0; e < No2; ++e) {
+    if (p.delta[e].empty()) continue;
+    std::vector<BosonTerm> ht;
+    std::vector<int> hef;
+    terms_of(e, ht, hef);
+    const int nt = (int)ht.size();
+    def.upload(hef.data(), nt);
+    const cx<R>* Wp;
+    if (use_cache) {
+      Wp = cache->W.p + cache->offset[e] * g.P;
+    } else {
+      dterms.upload(ht.data(), nt);
+      dim3 gr(grid_1d(g.P, 256, 4096), nt);
+      k_pad_boson<R><<<gr, 256, 0, st>>>(W.p, Vd, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw,
+                                          g.Nchi, g.P);
+      count_launch("pad_vdelta");
+      fft.forward<R>(W.p, nt, st);
+      Wp = W.p;
+    }
+    k_contract<R><<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(T.p, Wp, FF.p, def.p, nt, g.P);
+    count_launch("contract");
+    fft.backward<R>(T.p, 1, st);
+    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(out + (size_t)e * g.K, T.p, sizeof(R) == 8, g.irr_grid.p,
+                                                             g.Nkall, g.Nk, g.Nw, scale, 0);
+    count_launch("scatter_delta");
+    sync();
+  }
+  hermitize(out, g.K, g.Norb);
+}
+
+__global__ void k_initial_delta(double2* D, const double* init, const double2* uni, int Nk, int Nw, int No,
+                                int gap_sym) {
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk);
+    if (gap_sym == 0) {
+      for (int b = 0; b < No; ++b)
+        for (int a = 0; a < No; ++a) D[idx + K * (a + No * b)] = mkc(a == b ? 1.0 : 0.0, 0.0);
+      continue;
+    }
+    const double2* U = uni + (long long)No * No * k;
+    // delta0 = U diag(init) U^H, lower triangle then Hermitian (feliash.f90:685-699)
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b <= a; ++b) {
+        double2 acc = mkc(0.0, 0.0);
+        for (int n = 0; n < No; ++n) acc += (init[k + (long long)Nk * n] * U[a + No * n]) * conj(U[b + No * n]);
+        if (a == b) acc.y = 0;
+        D[idx + K * (a + No * b)] = acc;
+        if (a != b) D[idx + K * (b + No * a)] = conj(acc);
+      }
+  }
+}
+void initial_delta(double2* D, const double* init, const double2* uni, int Nk, int Nw, int Norb, int gap_sym) {
+  const long long K = (long long)Nk * Nw;
+  k_initial_delta<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(D, init, uni, Nk, Nw, Norb, gap_sym);
+  count_launch("initial_delta");
+}
+
+__global__ void k_axpy(double2* y, double2 a, const double2* x, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+__global__ void k_scal(double2* y, double a, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] = a * y[i];
+}
+struct LinComb {
+  const double2* x[64];
+  double2 c[64];
+};
+__global__ void k_lincomb(double2* y, LinComb lc, int m, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double2 acc = mkc(0.0, 0.0);
+    for (int t = 0; t < m; ++t) acc += lc.c[t] * lc.x[t][i];
+    y[i] = acc;
+  }
+}
+void axpy(double2* y, double2 a, const double2* x, long long n) {
+  k_axpy<<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(y, a, x, n);
+  count_launch("axpy");
+}
+void scal(double2* y, double a, long long n) {
+  k_scal<<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(y, a, n);
+  count_launch("scal");
+}
+void lincomb(double2* y, const double2* const* xs, const double2* cs, int m, long long n) {
+  PGB_CHECK(m <= 64, "linear combination of more than 64 vectors");
+  LinComb lc{};
+  for (int i = 0; i < m; ++i) { lc.x[i] = xs[i]; lc.c[i] = cs[i]; }
+  k_lincomb<<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(y, lc, m, n);
+  count_launch("lincomb");
+}
+
+template <typename R> __global__ void k_widen(double2* out, const cx<R>* in, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = ccast<double>(in[i]);
+}
+template <typename R> __global__ void k_narrow(cx<R>* out, const double2* in, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = cmk<R>((R)in[i].x, (R)in[i].y);
+}
+template <typename R> void widen(double2* out, const cx<R>* in, long long n) {
+  k_widen<R><<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(out, in, n);
+  count_launch("widen");
+}
+template <typename R> void narrow(cx<R>* out, const double2* in, long long n) {
+  k_narrow<R><<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(out, in, n);
+  count_launch("narrow");
+}
+
+// ======================================================== instantiations ==
+#define PGB_INST(R)                                                                                        \
+  template void chi0<R>(const Geom&, const Pairs&, const double2*, double, const TailRef*, cx<R>*);        \
+  template void stoner<R>(const Geom&, const cx<R>*, const double*, const double*, double*, double*, int*, \
+                          int*);                                                                           \
+  template bool vertex<R>(cx<R>*, long long, long long, int, const double*, const double*, int);          \
+  template void scale_chi<R>(cx<R>*, long long, double);                                                   \
+  template void sigma<R>(const Geom&, const Pairs&, const double2*, const cx<R>*, const double*,           \
+                         const double*, double, double2*);                                                 \
+  template void mkdelta<R>(const Geom&, const Pairs&, const double2*, const cx<R>*, const double*,         \
+                           const double*, const double*, bool, double, double2*, DeltaKernelCache<R>*);    \
+  template void widen<R>(double2*, const cx<R>*, long long);                                               \
+  template void narrow<R>(cx<R>*, const double2*, long long);
+PGB_INST(float)
+PGB_INST(double)
+
+}  // namespace pgb

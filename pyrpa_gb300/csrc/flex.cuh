@@ -1,0 +1,133 @@
+// GB300 FLEX / RPA / linearized-Eliashberg engine: geometry, orbital-pair
+// tables and the stage drivers the C ABI (abi.cu) calls.
+//
+// Data layout in HBM.  Per-(k,iw) quantities keep the reference's Fortran
+// layout so the C ABI copies them without reshuffling:
+//   G, Sigma, Delta, F : (Nk, Nw, Norb, Norb) complex, k fastest
+//   chi, V             : (Nk, Nw, Nchi, Nchi), k fastest
+// The FFT work arrays are full-grid (x, y, z, t) arrays, x fastest, one
+// P = Nkall*2Nw block per orbital element; the t axis of a transformed array
+// may be stored digit-transposed (FFT4D position tables).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace pgb {
+
+struct Geom {
+  int Nx = 1, Ny = 1, Nz = 1, Nw = 1, Nk = 1, Norb = 1, Nchi = 1;
+  long long Nkall = 1, M = 2, P = 2, K = 1;
+  std::vector<int> h_grid_irr, h_grid_flag, h_irr_grid;
+  std::vector<double> h_kweight;
+  std::vector<int64_t> h_kmap;  // 3 per full point, as passed (for progress prints)
+  std::vector<int> h_full_of_grid;  // full-list index of each grid cell
+  DBuf<int> grid_irr, grid_flag, irr_grid;
+  DBuf<double> kweight;
+};
+
+// Builds the grid maps from the reference's kmap(3,Nkall) / invk(3,Nkall)
+// (1-based irreducible index, 0/1 flag) and validates them.
+void build_geom(Geom& g, const int64_t* kmap, const int64_t* invk, int64_t Nx, int64_t Ny,
+                int64_t Nz, int64_t Nk, int64_t Nw, int64_t Norb, int64_t Nchi);
+
+struct ChiPair {
+  int l, m, m2, l2;  // irreducible (m,l) and exchange partner (m2,l2), 0-based
+  int e13, e42;      // orbital elements a + Norb*b of G13 and G42
+  int self;          // partner is the pair itself
+  double2 J;         // tau=0 jump coefficient (tail reference only)
+};
+
+struct Term {  // one (m,l) term of a sigma / delta contraction
+  int m, l, ef;    // pair indices and the G/F element multiplied with it
+};
+
+struct Pairs {
+  int Norb = 1, Nchi = 1;
+  std::vector<int> o1, o2;                       // 0-based orbitals of chi index l
+  std::vector<ChiPair> chi;                      // irreducible pairs for chi0
+  std::vector<std::vector<Term>> sigma;          // per output element a + Norb*b
+  std::vector<std::vector<Term>> delta;          // per output element a + Norb*b (a >= b)
+};
+
+// chi_map / irr_chi from olist (fchi.f90:421-481) or taken from the caller
+// (get_chi0_conv_ passes them, 1-based, int32, Fortran layout).
+void build_pairs(Pairs& p, const int64_t* olist, int Norb, int Nchi, const int32_t* irr_chi = nullptr,
+                 const int32_t* chi_map = nullptr);
+
+// ------------------------------------------------------------------ stages
+// All pointers are device pointers; R is the bulk (FFT/contraction) type.
+
+// Gk = G0 (fself.f90:1-41) from eig (Norb,Nk) and uni (Norb,Norb,Nk)
+void green0(double2* G, const double* eig, const double2* uni, double mu, double temp, int Nk,
+            int Nw, int Norb);
+// Gk = (iw + mu - H - Sigma)^-1 (fself.f90:43-157); returns false if singular
+bool dyson(double2* G, const double2* sig, const double2* hamk, double mu, double temp, int Nk,
+           int Nw, int Norb);
+void green_inv_only(double2* G, const double2* sig, const double2* hamk, double mu, double temp,
+                    int Nk, int Nw, int Norb);
+bool invert_blocks(double2* G, long long nmat, int Norb, long long stride_mat, long long stride_el);
+
+struct TailRef {
+  const double* eig = nullptr;   // (Norb, Nk)
+  const double2* uni = nullptr;  // (Norb, Norb, Nk)
+  double mu = 0;
+};
+
+// chi0 by FFT convolution (fchi.f90:508-635), optionally tail-corrected
+// (fchi.f90:637-892).  chi (Nk,Nw,Nchi,Nchi) of type cx<R> is overwritten.
+template <typename R>
+void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const TailRef* tail,
+          cx<R>* chi);
+// Stoner factors: max Re eig(chi0(q,0) S) and of -chi0(q,0) C (fchi.f90:352-399)
+template <typename R>
+void stoner(const Geom& g, const cx<R>* chi, const double* S, const double* C, double* sdw,
+            double* cdw, int* q_sdw, int* q_cdw);
+// in-place vertex: mode 0 V_sigma (fUJ.f90:318-365), 1 singlet / 2 triplet
+// V_Delta (fUJ.f90:253-316), 3 chi_s, 4 chi_c with nu=0 slices only
+template <typename R>
+bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double* S, const double* C,
+            int mode);
+template <typename R> void scale_chi(cx<R>* chi, long long n, double s);
+// Sigma by FFT convolution (fself.f90:159-285), thresholded, FP64 output
+template <typename R>
+void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, const double* S,
+           const double* C, double temp, double2* sig);
+void hf_subtract(double2* sig, int Nk, int Nw, int Norb, int mode);
+
+// reductions (deterministic two-level)
+double dot_re(const double2* a, const double2* b, long long n);
+double2 inner_w(const double2* a, const double2* b, const double* kw, int Nk, long long n);
+double filling(const double2* eig_g, const double* eig, int Nk, int Nw, int Norb, double mu,
+               double temp);
+bool eig_gkinv(double2* eig_g, const double2* hamk, const double2* sig, int Nk, int Nw, int Norb);
+
+// Eliashberg
+void mkfk(double2* F, const double2* G, const double2* D, long long K, int Norb);
+// Transformed pairing vertex of every mkdelta term, kept across Arnoldi steps
+// when it fits in HBM (the reference re-transforms it on every application).
+template <typename R> struct DeltaKernelCache {
+  bool built = false;
+  DBuf<cx<R>> W;
+  std::vector<long long> offset;  // first term of each output element
+};
+template <typename R>
+void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, const double* S,
+             const double* C, const double* prt, bool singlet, double scale, double2* out,
+             DeltaKernelCache<R>* cache);
+void hermitize(double2* D, long long K, int Norb);
+void initial_delta(double2* D, const double* init, const double2* uni, int Nk, int Nw, int Norb,
+                   int gap_sym);
+void axpy(double2* y, double2 a, const double2* x, long long n);         // y += a x
+void scal(double2* y, double a, long long n);
+void lincomb(double2* y, const double2* const* xs, const double2* cs, int m, long long n);
+
+// small host helpers
+void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc);
+template <typename R> void widen(double2* out, const cx<R>* in, long long n);
+template <typename R> void narrow(cx<R>* out, const double2* in, long long n);
+
+}  // namespace pgb

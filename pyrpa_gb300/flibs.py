@@ -1,0 +1,478 @@
+"""Python host side of the GB300 FLEX/RPA engine.
+
+The functions mirror the pyrpa ctypes wrappers of the hot path
+(``libs/flibs/_hamiltonian.py``, ``_green.py``, ``_interaction.py``,
+``_susceptibility.py``, ``_selfenergy.py``, ``_eliashberg.py``): same names,
+argument order, array shapes and return values.  They bind the in-tree
+``libfmod.so`` built from ``csrc/`` (``pyrpa_gb300.build``).  There is no CPU
+implementation behind them: if the library is missing or no GPU is visible,
+the call raises.
+
+Where the reference library stops the process on a LAPACK failure, these
+functions raise ``RuntimeError`` with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, byref, c_bool, c_char, c_double, c_int64
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libfmod.so"
+
+_c128 = np.ctypeslib.ndpointer(dtype=np.complex128)
+_f64 = np.ctypeslib.ndpointer(dtype=np.float64)
+_i64 = np.ctypeslib.ndpointer(dtype=np.int64)
+_i32 = np.ctypeslib.ndpointer(dtype=np.int32)
+_pi = POINTER(c_int64)
+_pd = POINTER(c_double)
+_pb = POINTER(c_bool)
+
+# argument types of every bound symbol, in the order of the reference wrappers
+_SIGNATURES = {
+    "openmp_params": [_pi, _pb],
+    "generate_irr_kpoint_inv": [_f64, _i64, _i64, _pi, _pi, _pi, _pi],
+    "get_kweight": [_f64, _i64, _pi, _pi],
+    "gen_ham": [_c128, _f64, _c128, _f64, _pi, _pi, _pi],
+    "get_eig": [_f64, _c128, _c128, _pi, _pi],
+    "get_ffermi": [_f64, _f64, _pd, _pd, _pi, _pi],
+    "get_parity_prop": [_f64, _f64, _c128, _pi, _pi],
+    "get_scmat": [_f64, _f64, _i64, _i64, _pd, _pd, _pi],
+    "get_scmat_orb": [_f64, _f64, _i64, _i64, _f64, _f64, _pi, _pi],
+    "gen_green0_": [_c128, _f64, _c128, _pd, _pd, _pi, _pi, _pi],
+    "gen_green_inv_": [_c128, _c128, _c128, _pd, _pd, _pi, _pi, _pi],
+    "getinv_": [_c128, _pi, _pi, _pi],
+    "get_chi0_conv_": [_c128, _c128, _i64, _i64, _i32, _i32, _i64, _pd] + [_pi] * 8,
+    "get_chi0": [_c128, _f64, _f64, _c128, _i64, _i64, _i64, _pd] + [_pi] * 8 + [_pd],
+    "get_chi0_tail": [_c128, _f64, _f64, _c128, _f64, _c128, _i64, _i64, _i64, _pd, _pd] + [_pi] * 8 + [_pd],
+    "get_chis": [_c128, _c128, _f64, _pi, _pi],
+    "get_chis_chic": [_c128, _c128, _c128, _f64, _f64, _pi, _pi, _pi],
+    "get_eig_or_tr_chi": [_c128, _c128, _i64, _pi, _pi, _pi, _pb],
+    "get_vsigma_flex_nosoc_": [_c128, _f64, _f64, _pi, _pi, _pi],
+    "mkself": [_c128, _pd, _f64, _f64, _i64, _i64, _i64, _c128, _f64, _c128, _pd, _pd, _pd, _pi, _pd, _pd]
+    + [_pi] * 9 + [_pb, _pb, _pi, _pb, _pb, _pd],
+    "lin_eliash": [_c128, _c128, _c128, _c128, _f64, _f64, _f64, _i64, _f64, _i64, _i64, _pd, _pd]
+    + [_pi] * 11 + [_pd],
+    "mkfk_trs_nsoc_": [_c128, _c128, _c128, _pi, _pi, _pi],
+    "get_initial_delta_": [_c128, _f64, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi],
+    "remap_delta_": [_c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi],
+    "conv_delta_orb_to_band": [_c128, _c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi],
+    "pyrpa_gb_flex_eliash": [_c128, _pd, _c128, _pd, _pd, _f64, _f64, _f64, _i64, _i64, _i64, _c128, _f64, _c128,
+                             _f64, _f64, ctypes.c_void_p, _pd, _pd, _pd, _pd, _pd, _pi, _pd, _pd] + [_pi] * 10
+    + [_pb, _pb, _pi, _pi, _pi, _pd],
+    "pyrpa_gb_set_precision": [_pi],
+    "pyrpa_gb_get_precision": [_pi],
+    "pyrpa_gb_set_verbose": [_pi],
+    "pyrpa_gb_last_error": [POINTER(c_char), _pi, _pi],
+    "pyrpa_gb_clear_error": [],
+    "pyrpa_gb_kernel_launches": [_pi],
+    "pyrpa_gb_last_stats": [_f64],
+    "pyrpa_gb_device_info": [_pi, _pi],
+    "pyrpa_gb_fft_profile": [_pi],
+    "pyrpa_gb_fft_stats": [_f64],
+}
+
+_lib = None
+
+
+def load_library(path: str | Path | None = None):
+    """Load libfmod.so (once) and set the argument types of its symbols."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise ImportError(f"{p} is missing: build it with `python -m pyrpa_gb300.build` "
+                          "(needs nvcc); there is no CPU implementation of this path")
+    lib = ctypes.CDLL(str(p))
+    for name, args in _SIGNATURES.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = None
+    _lib = lib
+    return lib
+
+
+def i64(v):
+    return byref(c_int64(int(v)))
+
+
+def dbl(v):
+    return byref(c_double(float(v)))
+
+
+def _call(name, *args):
+    lib = load_library()
+    lib.pyrpa_gb_clear_error()
+    getattr(lib, name)(*args)
+    code = c_int64(0)
+    buf = ctypes.create_string_buffer(2048)
+    lib.pyrpa_gb_last_error(buf, i64(len(buf)), byref(code))
+    if code.value:
+        raise RuntimeError(buf.value.decode(errors="replace"))
+
+
+# ------------------------------------------------------------------ control
+def set_precision(bits: int) -> None:
+    """64: FP64 everywhere (the reference's arithmetic); 32: complex FP32 FFTs,
+    contractions and vertex solves, FP64 for G, Sigma, mu, DIIS and lambda."""
+    load_library().pyrpa_gb_set_precision(i64(bits))
+
+
+def get_precision() -> int:
+    v = c_int64(0)
+    load_library().pyrpa_gb_get_precision(byref(v))
+    return v.value
+
+
+def set_verbose(level: int) -> None:
+    load_library().pyrpa_gb_set_verbose(i64(level))
+
+
+def kernel_launches() -> int:
+    v = c_int64(0)
+    load_library().pyrpa_gb_kernel_launches(byref(v))
+    return v.value
+
+
+def last_stats() -> dict:
+    out = np.zeros(14)
+    load_library().pyrpa_gb_last_stats(out)
+    keys = ["iterations", "esterr", "stoner", "mu", "lambda", "applies", "t_chi0_ms", "t_vertex_ms",
+            "t_sigma_ms", "t_diis_ms", "t_mu_ms", "t_dyson_ms", "t_apply_ms"]
+    return dict(zip(keys, out[: len(keys)].tolist()))
+
+
+def fft_profile(on: bool) -> None:
+    """Bracket every FFT pass launch with CUDA events (see fft_stats)."""
+    load_library().pyrpa_gb_fft_profile(i64(1 if on else 0))
+
+
+def fft_stats() -> dict:
+    """Launches, summed device milliseconds and algorithmic bytes of the FFT
+    passes since the last call (requires fft_profile(True))."""
+    out = np.zeros(3)
+    load_library().pyrpa_gb_fft_stats(out)
+    return dict(launches=int(out[0]), ms=float(out[1]), bytes=float(out[2]))
+
+
+def omp_params():
+    n, c = c_int64(0), c_bool(False)
+    _call("openmp_params", byref(n), byref(c))
+    return n.value, c.value
+
+
+# -------------------------------------------------- k mesh and band structure
+def irr_k_count(Nx: int, Ny: int, Nz: int) -> int:
+    """Irreducible TRS k count (libs/flibs/_hamiltonian.py:367-378)."""
+    N = Nx * Ny * Nz
+    if N % 2 == 0:
+        if Nz % 2 == 0:
+            if Nx % 2 == 0 and Ny % 2 == 0:
+                return N // 2 + 4
+            return N // 2 + 2 if (Nx % 2 == 0 or Ny % 2 == 0) else N // 2 + 1
+        return N // 2 + 2 if (Nx % 2 == 0 and Ny % 2 == 0) else N // 2 + 1
+    return (N + 1) // 2
+
+
+def gen_irr_k_TRS(Nx: int, Ny: int, Nz: int):
+    """(klist[Nk,3], kmap[Nkall,3], invk[Nkall,3]) (libs/flibs/_hamiltonian.py:356-382)."""
+    Nk, Nkall = irr_k_count(Nx, Ny, Nz), Nx * Ny * Nz
+    klist = np.zeros((Nk, 3))
+    kmap = np.zeros((Nkall, 3), dtype=np.int64)
+    invk = np.zeros((Nkall, 3), dtype=np.int64)
+    _call("generate_irr_kpoint_inv", klist, kmap, invk, i64(Nk), i64(Nx), i64(Ny), i64(Nz))
+    return klist, kmap, invk
+
+
+def gen_kpoint_weight(invk, Nk: int):
+    w = np.zeros(Nk)
+    _call("get_kweight", w, invk, i64(Nk), i64(len(invk)))
+    return w
+
+
+def gen_ham(klist, ham_r, rvec):
+    """k-space Hamiltonian [Nk,Norb,Norb] (libs/flibs/_hamiltonian.py:75-99)."""
+    Nk, Nr, Norb = len(klist), len(rvec), ham_r.shape[1]
+    hamk = np.zeros((Nk, Norb, Norb), dtype=np.complex128)
+    _call("gen_ham", hamk, np.ascontiguousarray(klist, dtype=np.float64),
+          np.ascontiguousarray(ham_r, dtype=np.complex128), np.ascontiguousarray(rvec, dtype=np.float64),
+          i64(Nk), i64(Nr), i64(Norb))
+    return hamk
+
+
+def get_eig(hamk):
+    """(eig[Nk,Norb] ascending, uni[Nk,Norb,Norb]) (libs/flibs/_hamiltonian.py:101-125)."""
+    Nk, Norb = len(hamk), hamk.shape[1]
+    eig = np.zeros((Nk, Norb))
+    uni = np.zeros((Nk, Norb, Norb), dtype=np.complex128)
+    _call("get_eig", eig, uni, np.ascontiguousarray(hamk), i64(Nk), i64(Norb))
+    return eig, uni
+
+
+def get_ffermi(eig, mu: float, temp: float):
+    f = np.zeros_like(eig, dtype=np.float64)
+    _call("get_ffermi", f, np.ascontiguousarray(eig, dtype=np.float64), dbl(mu), dbl(temp),
+          i64(len(eig)), i64(eig.shape[1]))
+    return f
+
+
+def get_plist(rvec, ham_r):
+    """Orbital parities from H(R) vs H(-R) (libs/flibs/_hamiltonian.py:411-423)."""
+    Norb = ham_r.shape[1]
+    P = np.zeros((Norb, Norb))
+    _call("get_parity_prop", P, np.ascontiguousarray(rvec, dtype=np.float64),
+          np.ascontiguousarray(ham_r, dtype=np.complex128), i64(Norb), i64(len(rvec)))
+    return np.sign(P[0, :])
+
+
+# --------------------------------------------------------------- vertices
+def get_chi_orb_list(Norb: int, site_prof=(1,)):
+    """Orbital-pair list for one site, as plibs.get_chi_orb_list returns it: a
+    transposed view whose memory is Fortran olist(Nchi,2) (libs/plibs/_response.py:382-410)."""
+    if len(site_prof) != 1:
+        raise NotImplementedError("multi-site orbital-pair lists")
+    t = np.arange(Norb) + 1
+    o1, o2 = np.meshgrid(t, t)
+    return np.array([o1.flatten(), o2.flatten()]).T, np.ones(Norb * Norb, dtype=np.int64)
+
+
+def gen_SCmatrix(olist, site, U: float, J: float):
+    Nchi = len(olist)
+    S, C = np.zeros((Nchi, Nchi)), np.zeros((Nchi, Nchi))
+    _call("get_scmat", S, C, olist, np.asarray(site, dtype=np.int64), dbl(U), dbl(J), i64(Nchi))
+    return S, C
+
+
+def gen_SCmatrix_orb(olist, site, Umat, Jmat):
+    Nchi, Norb = len(olist), len(Umat)
+    S, C = np.zeros((Nchi, Nchi)), np.zeros((Nchi, Nchi))
+    _call("get_scmat_orb", S, C, olist, np.asarray(site, dtype=np.int64), np.ascontiguousarray(Umat, dtype=np.float64),
+          np.ascontiguousarray(Jmat, dtype=np.float64), i64(Nchi), i64(Norb))
+    return S, C
+
+
+# ----------------------------------------------------------------- Green
+def gen_Green0(eig, uni, mu: float, temp: float, Nw: int):
+    Nk, Norb = eig.shape
+    Gk = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("gen_green0_", Gk, np.ascontiguousarray(eig), np.ascontiguousarray(uni), dbl(mu), dbl(temp),
+          i64(Nk), i64(Nw), i64(Norb))
+    return Gk
+
+
+def gen_green(selfen, hamk, mu: float, temp: float):
+    Nk, Norb, Nw = len(hamk), hamk.shape[1], selfen.shape[2]
+    Gk = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("gen_green_inv_", Gk, np.ascontiguousarray(selfen), np.ascontiguousarray(hamk), dbl(mu), dbl(temp),
+          i64(Nk), i64(Nw), i64(Norb))
+    _call("getinv_", Gk, i64(Nk), i64(Nw), i64(Norb))
+    return Gk
+
+
+# ---------------------------------------------------------- susceptibility
+def chi_map_arrays(olist):
+    """(chi_map, irr_chi) int32, 1-based, memory = Fortran chi_map(Nchi,Nchi,2) and
+    irr_chi(Nchi(Nchi+1)/2,2); exchange symmetry chi_1234 = chi*_4321 (fchi.f90:421-481)."""
+    ol = np.asarray(olist, dtype=np.int64)
+    n = len(ol)
+    cmap = np.zeros((2, n, n), dtype=np.int32)
+    is_irr = np.zeros((n, n), dtype=bool)
+    for l1 in range(n):
+        for m1 in range(n):
+            want = (ol[l1, 0], ol[l1, 1], ol[m1, 0], ol[m1, 1])
+            hit = next(((l2, m2) for l2 in range(n) for m2 in range(n)
+                        if (ol[m2, 1], ol[m2, 0], ol[l2, 1], ol[l2, 0]) == want), None)
+            if hit is None:
+                continue
+            l2, m2 = hit
+            cmap[0, l1, m1], cmap[1, l1, m1] = m2 + 1, l2 + 1
+            if not is_irr[l2, m2]:
+                is_irr[l1, m1] = True
+    irr = np.zeros((2, n * (n + 1) // 2), dtype=np.int32)
+    for it, (l1, m1) in enumerate((l, m) for l in range(n) for m in range(n) if is_irr[l, m]):
+        irr[0, it], irr[1, it] = l1 + 1, m1 + 1
+    return cmap, irr
+
+
+def _dims(Gk):
+    Norb = len(Gk)
+    return Norb, Gk.shape[2], Gk.shape[3]
+
+
+def get_chi0_conv(Gk, kmap, invk, olist, temp: float, Nx: int, Ny: int, Nz: int):
+    Norb, Nw, Nk = _dims(Gk)
+    Nchi = len(olist)
+    chi = np.zeros((Nchi, Nchi, Nw, Nk), dtype=np.complex128)
+    cmap, irr = chi_map_arrays(olist)
+    _call("get_chi0_conv_", chi, np.ascontiguousarray(Gk), kmap, invk, irr, cmap, olist, dbl(temp), i64(Nx),
+          i64(Ny), i64(Nz), i64(Nw), i64(Nk), i64(len(kmap)), i64(Norb), i64(Nchi))
+    return chi
+
+
+def get_chi0(Smat, Cmat, Gk, olist, kmap, invk, temp: float, Nx: int, Ny: int, Nz: int):
+    """(chi0 [Nchi,Nchi,Nw,Nk], Stoner factor) (libs/flibs/_susceptibility.py:425-455)."""
+    Norb, Nw, Nk = _dims(Gk)
+    Nchi = len(olist)
+    chi = np.zeros((Nchi, Nchi, Nw, Nk), dtype=np.complex128)
+    st = c_double(0.0)
+    _call("get_chi0", chi, Smat, Cmat, np.ascontiguousarray(Gk), kmap, invk, olist, dbl(temp), i64(Nx), i64(Ny),
+          i64(Nz), i64(Nw), i64(Nk), i64(len(kmap)), i64(Norb), i64(Nchi), byref(st))
+    return chi, st.value
+
+
+def get_chi0_tail(Smat, Cmat, Gk, eig, uni, olist, kmap, invk, mu: float, temp: float, Nx: int, Ny: int, Nz: int):
+    """Tail-corrected chi0 (libs/flibs/_susceptibility.py:457-490)."""
+    Norb, Nw, Nk = _dims(Gk)
+    Nchi = len(olist)
+    chi = np.zeros((Nchi, Nchi, Nw, Nk), dtype=np.complex128)
+    st = c_double(0.0)
+    _call("get_chi0_tail", chi, Smat, Cmat, np.ascontiguousarray(Gk), np.ascontiguousarray(eig),
+          np.ascontiguousarray(uni), kmap, invk, olist, dbl(mu), dbl(temp), i64(Nx), i64(Ny), i64(Nz), i64(Nw),
+          i64(Nk), i64(len(kmap)), i64(Norb), i64(Nchi), byref(st))
+    return chi, st.value
+
+
+def get_chis(chi0, Smat):
+    Nchi, Nw = len(Smat), len(chi0)
+    chis = np.zeros((Nw, Nchi, Nchi), dtype=np.complex128)
+    _call("get_chis", chis, np.ascontiguousarray(chi0), Smat, i64(Nchi), i64(Nw))
+    return chis
+
+
+def get_chis_chic(chi, Smat, Cmat):
+    Nk, Nw, Nchi = chi.shape[3], chi.shape[2], len(Smat)
+    chis = np.zeros((Nchi, Nchi, Nk), dtype=np.complex128)
+    chic = np.zeros((Nchi, Nchi, Nk), dtype=np.complex128)
+    _call("get_chis_chic", chis, chic, np.ascontiguousarray(chi), Smat, Cmat, i64(Nk), i64(Nw), i64(Nchi))
+    return chis, chic
+
+
+def get_eig_or_tr_chi(chi, invk, sw_eig: bool):
+    Nkall, Nk, Nchi = len(invk), chi.shape[-1], chi.shape[0]
+    out = np.zeros(Nkall, dtype=np.complex128)
+    _call("get_eig_or_tr_chi", out, np.ascontiguousarray(chi), invk, i64(Nkall), i64(Nk), i64(Nchi),
+          byref(c_bool(bool(sw_eig))))
+    return out
+
+
+def get_Vsigma_nosoc_flex(chi, Smat, Cmat):
+    """V_sigma in place; like the reference wrapper it passes Nk=len(chi),
+    Nw=len(chi[0]) (libs/flibs/_selfenergy.py:60-73)."""
+    Nk, Nw, Nchi = len(chi), len(chi[0]), len(Smat)
+    _call("get_vsigma_flex_nosoc_", chi, Smat, Cmat, i64(Nk), i64(Nw), i64(Nchi))
+    return chi.copy()
+
+
+# --------------------------------------------------------------- FLEX loop
+def mkself(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, mu: float, fill: float, temp: float, Nw: int,
+           Nx: int, Ny: int, Nz: int, sw_out: bool, sw_in: bool, sub_sigma: int = 1, scf_loop: int = 300,
+           eps: float = 1.0e-4, pp: float = 0.3, m_diis: int = 5, sw_rescale: bool = False,
+           sw_tail: bool = False, sigma_scale: float = 1.0):
+    """FLEX self-consistency (libs/flibs/_selfenergy.py:76-127): (sigmak [Norb,Norb,Nw,Nk], mu)."""
+    Nkall, Nk, Nchi = len(kmap), len(hamk), len(Smat)
+    Norb = hamk.shape[1]
+    mu_self = c_double()
+    sigmak = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("mkself", sigmak, byref(mu_self), Smat, Cmat, kmap, invk, olist, np.ascontiguousarray(hamk),
+          np.ascontiguousarray(eig), np.ascontiguousarray(uni), dbl(mu), dbl(fill), dbl(temp), i64(scf_loop),
+          dbl(pp), dbl(eps), i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(Nchi), i64(Nx), i64(Ny), i64(Nz),
+          i64(sub_sigma), byref(c_bool(sw_out)), byref(c_bool(sw_in)), i64(m_diis), byref(c_bool(sw_rescale)),
+          byref(c_bool(sw_tail)), dbl(sigma_scale))
+    return sigmak, mu_self.value
+
+
+# -------------------------------------------------------------- Eliashberg
+def linearized_eliashberg(chi, Gk, uni, init_delta, Smat, Cmat, olist, plist, kmap, invk, Nx: int, Ny: int,
+                          Nz: int, temp: float, gap_sym: int, eps: float = 1.0e-5, itemax: int = 300,
+                          arnoldi_m: int = 10):
+    """Leading eigenvalue and gap (libs/flibs/_eliashberg.py:145-181); chi is
+    overwritten with the pairing vertex, as in the reference."""
+    Norb, Nchi = len(Gk), len(Smat)
+    Nkall, Nk, Nw = len(kmap), Gk.shape[3], Gk.shape[2]
+    delta = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    lam = c_double(0.0)
+    _call("lin_eliash", delta, chi, np.ascontiguousarray(Gk), np.ascontiguousarray(uni),
+          np.ascontiguousarray(init_delta, dtype=np.float64), Smat, Cmat, olist,
+          np.ascontiguousarray(plist, dtype=np.float64), kmap, invk, dbl(temp), dbl(eps), i64(Nkall), i64(Nk),
+          i64(Nw), i64(Nchi), i64(Norb), i64(Nx), i64(Ny), i64(Nz), i64(itemax), i64(gap_sym), i64(arnoldi_m),
+          byref(lam))
+    return delta, lam.value
+
+
+def gen_Fk(Gk, delta, invk):
+    """F = -G Delta G^dagger (libs/flibs/_eliashberg.py:343-355)."""
+    Nk, Nw, Norb = Gk.shape[3], delta.shape[2], len(delta)
+    Fk = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("mkfk_trs_nsoc_", Fk, np.ascontiguousarray(Gk), np.ascontiguousarray(delta), i64(Nk), i64(Nw), i64(Norb))
+    return Fk
+
+
+def get_initial_delta(init_delta, uni, kmap, invk, Nw: int, gap_sym: int):
+    Norb, Nk = init_delta.shape
+    delta = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("get_initial_delta_", delta, np.ascontiguousarray(init_delta, dtype=np.float64),
+          np.ascontiguousarray(uni), kmap, invk, i64(len(kmap)), i64(Nk), i64(Nw), i64(Norb), i64(gap_sym))
+    return delta
+
+
+def remap_gap(delta0, plist, invk, gap_sym: int):
+    Nkall, Nk, Norb = len(invk), delta0.shape[-1], len(plist)
+    Nw = delta0.shape[2]
+    delta = np.zeros((Norb, Norb, Nw, Nkall), dtype=np.complex128)
+    _call("remap_delta_", delta, np.ascontiguousarray(delta0), np.ascontiguousarray(plist, dtype=np.float64), invk,
+          i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(gap_sym))
+    return delta
+
+
+def conv_delta_orb_to_band(delta, uni, invk, plist, gap_sym: int):
+    Nkall, Nk, Nw, Norb = len(invk), len(uni), delta.shape[2], len(delta)
+    deltab = np.zeros((Norb, Norb, Nkall), dtype=np.complex128)
+    _call("conv_delta_orb_to_band", deltab, np.ascontiguousarray(delta), np.ascontiguousarray(uni),
+          np.ascontiguousarray(plist, dtype=np.float64), invk, i64(Norb), i64(Nkall), i64(Nk), i64(Nw), i64(gap_sym))
+    return deltab
+
+
+def get_initial_gap(klist, Norb: int, gap_sym: int):
+    """Band-basis initial gap [Norb, Nk] (libs/plibs/_response.py:413-462)."""
+    A = 2 * np.pi
+    kx, ky, kz = klist[:, 0], klist[:, 1], klist[:, 2]
+    rows = {0: np.ones(len(klist)), 1: np.cos(A * kx) - np.cos(A * ky), 2: 2 * np.cos(A * kx) * np.cos(A * ky),
+            3: 2 * np.sin(A * kx) * np.sin(A * ky), 4: 2 * np.sin(A * kx) * np.sin(A * kz),
+            5: 2 * np.sin(A * ky) * np.sin(A * kz), -1: 2 * np.sin(A * kx), -2: 2 * np.sin(A * ky)}
+    return np.tile(rows.get(gap_sym, np.zeros(len(klist))), (Norb, 1))
+
+
+# ------------------------------------------------ fused FLEX + Eliashberg
+def flex_eliash(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, init_delta, plist, mu: float, fill: float,
+                temp: float, Nw: int, Nx: int, Ny: int, Nz: int, gap_sym: int, sub_sigma: int = 1,
+                scf_loop: int = 300, eps: float = 1.0e-4, pp: float = 0.5, m_diis: int = 5,
+                sw_rescale: bool = True, sw_tail: bool = False, arnoldi_m: int = 10, itemax: int = 300,
+                eps_eliash: float = 1.0e-5, sigma_seed=None, seed_mu: float = 0.0, seed_mu_old: float = 0.0):
+    """mkself -> gen_green -> get_chi0(_tail) -> linearized_eliashberg in one
+    device-resident call (libs/plibs/_calc.py:370-405 with sw_self=True).
+
+    Returns a dict with sigmak [Norb,Norb,Nw,Nk], mu, gap, lambda, stoner and
+    the H2D / device / D2H milliseconds of the call.  ``sigma_seed`` (same
+    layout as sigmak) starts the loop from a given self-energy."""
+    Nkall, Nk, Nchi = len(kmap), len(hamk), len(Smat)
+    Norb = hamk.shape[1]
+    sigmak = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    gap = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    mu_o, lam, st = c_double(), c_double(), c_double()
+    times = np.zeros(3)
+    seed_ptr = None
+    if sigma_seed is not None:
+        sigma_seed = np.ascontiguousarray(sigma_seed, dtype=np.complex128)
+        assert sigma_seed.shape == sigmak.shape
+        seed_ptr = sigma_seed.ctypes.data_as(ctypes.c_void_p)
+    _call("pyrpa_gb_flex_eliash", sigmak, byref(mu_o), gap, byref(lam), byref(st), times, Smat, Cmat, kmap, invk,
+          olist, np.ascontiguousarray(hamk), np.ascontiguousarray(eig), np.ascontiguousarray(uni),
+          np.ascontiguousarray(init_delta, dtype=np.float64), np.ascontiguousarray(plist, dtype=np.float64),
+          seed_ptr, dbl(seed_mu), dbl(seed_mu_old), dbl(mu), dbl(fill), dbl(temp), i64(scf_loop), dbl(pp), dbl(eps),
+          i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(Nchi), i64(Nx), i64(Ny), i64(Nz), i64(sub_sigma),
+          i64(m_diis), byref(c_bool(sw_rescale)), byref(c_bool(sw_tail)), i64(gap_sym), i64(arnoldi_m),
+          i64(itemax), dbl(eps_eliash))
+    return dict(sigmak=sigmak, mu=mu_o.value, gap=gap, lam=lam.value, stoner=st.value,
+                h2d_ms=times[0], compute_ms=times[1], d2h_ms=times[2])
