@@ -13,14 +13,20 @@ namespace {
 
 // tab[t] = exp(-2 pi i t / L); sign < 0 uses it as is, sign > 0 its conjugate
 template <typename R>
-__device__ __forceinline__ cx<R> twid(const double2* tab, int t, int sign) {
-  double2 w = __ldg(tab + t);
-  return cmk<R>((R)w.x, (R)(sign < 0 ? w.y : -w.y));
+__device__ __forceinline__ cx<R> twid(const cx<R>* tab, int t, int sign) {
+  cx<R> w = __ldg(tab + t);
+  return cmk<R>(w.x, sign < 0 ? w.y : -w.y);
 }
+template <typename R> __device__ __forceinline__ const cx<R>* line_tab(const PassDesc& d);
+template <> __device__ __forceinline__ const double2* line_tab<double>(const PassDesc& d) { return d.tw_line; }
+template <> __device__ __forceinline__ const float2* line_tab<float>(const PassDesc& d) { return d.tw_line_f; }
+template <typename R> __device__ __forceinline__ const cx<R>* full_tab(const PassDesc& d);
+template <> __device__ __forceinline__ const double2* full_tab<double>(const PassDesc& d) { return d.tw_full; }
+template <> __device__ __forceinline__ const float2* full_tab<float>(const PassDesc& d) { return d.tw_full_f; }
 
 template <typename R, int RAD> struct Dft {
   // generic radix: direct O(RAD^2) evaluation with roots from the line table
-  __device__ static void run(cx<R>* v, int sign, const double2* tab, int L) {
+  __device__ static void run(cx<R>* v, int sign, const cx<R>* tab, int L) {
     cx<R> o[RAD];
     const int step = L / RAD;
 #pragma unroll
@@ -36,7 +42,7 @@ template <typename R, int RAD> struct Dft {
 };
 
 template <typename R> struct Dft<R, 2> {
-  __device__ static void run(cx<R>* v, int, const double2*, int) {
+  __device__ static void run(cx<R>* v, int, const cx<R>*, int) {
     cx<R> a = v[0] + v[1], b = v[0] - v[1];
     v[0] = a;
     v[1] = b;
@@ -44,7 +50,7 @@ template <typename R> struct Dft<R, 2> {
 };
 
 template <typename R> struct Dft<R, 4> {
-  __device__ static void run(cx<R>* v, int sign, const double2*, int) {
+  __device__ static void run(cx<R>* v, int sign, const cx<R>*, int) {
     cx<R> a0 = v[0] + v[2], a1 = v[0] - v[2], a2 = v[1] + v[3];
     cx<R> a3 = muli(v[1] - v[3], (R)sign);
     v[0] = a0 + a2;
@@ -55,7 +61,7 @@ template <typename R> struct Dft<R, 4> {
 };
 
 template <typename R> struct Dft<R, 3> {
-  __device__ static void run(cx<R>* v, int sign, const double2*, int) {
+  __device__ static void run(cx<R>* v, int sign, const cx<R>*, int) {
     const R h = (R)0.86602540378443864676372317075294;  // sqrt(3)/2
     cx<R> t1 = v[1] + v[2], t2 = v[1] - v[2];
     cx<R> m = v[0] - (R)0.5 * t1;
@@ -67,7 +73,7 @@ template <typename R> struct Dft<R, 3> {
 };
 
 template <typename R> struct Dft<R, 5> {
-  __device__ static void run(cx<R>* v, int sign, const double2*, int) {
+  __device__ static void run(cx<R>* v, int sign, const cx<R>*, int) {
     const R c1 = (R)0.30901699437494742410229341718282;   // cos(2 pi/5)
     const R c2 = (R)-0.80901699437494742410229341718282;  // cos(4 pi/5)
     const R s1 = (R)0.95105651629515357211643933337938;   // sin(2 pi/5)
@@ -84,7 +90,7 @@ template <typename R> struct Dft<R, 5> {
 };
 
 template <typename R> struct Dft<R, 8> {
-  __device__ static void run(cx<R>* v, int sign, const double2* t, int L) {
+  __device__ static void run(cx<R>* v, int sign, const cx<R>* t, int L) {
     const R h = (R)0.70710678118654752440084436210485;
     cx<R> e[4] = {v[0], v[2], v[4], v[6]};
     cx<R> o[4] = {v[1], v[3], v[5], v[7]};
@@ -108,7 +114,7 @@ template <typename R> struct Dft<R, 8> {
 // transforms on graphics processors", SC08, Fig. 2) over nl lines in smem.
 template <typename R, int RAD>
 __device__ void stage(const cx<R>* in, cx<R>* out, int L, int Ns, int nl, int sign,
-                      const double2* tab) {
+                      const cx<R>* tab) {
   const int nbf = L / RAD;
   const int total = nl * nbf;
   const int tstride = L / (Ns * RAD);
@@ -139,7 +145,7 @@ __device__ void four_step_twiddle(cx<R>* buf, const PassDesc& d, long long o, bo
     const int b = e / L, p = e - b * L;
     const long long k1 = ((contig ? o + b : o) % d.tw_L1);
     const int t = (int)(((long long)p * k1) % d.tw_Lfull);
-    if (t) buf[e] = buf[e] * twid<R>(d.tw_full, t, sign);
+    if (t) buf[e] = buf[e] * twid<R>(full_tab<R>(d), t, sign);
   }
 }
 
@@ -183,14 +189,14 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(cx<R>* data, long long P,
   for (int st = 0; st < d.nst; ++st) {
     const int rad = d.radix[st];
     switch (rad) {
-      case 2: stage<R, 2>(in, out, L, Ns, nl, sign, d.tw_line); break;
-      case 3: stage<R, 3>(in, out, L, Ns, nl, sign, d.tw_line); break;
-      case 4: stage<R, 4>(in, out, L, Ns, nl, sign, d.tw_line); break;
-      case 5: stage<R, 5>(in, out, L, Ns, nl, sign, d.tw_line); break;
-      case 7: stage<R, 7>(in, out, L, Ns, nl, sign, d.tw_line); break;
-      case 8: stage<R, 8>(in, out, L, Ns, nl, sign, d.tw_line); break;
-      case 11: stage<R, 11>(in, out, L, Ns, nl, sign, d.tw_line); break;
-      case 13: stage<R, 13>(in, out, L, Ns, nl, sign, d.tw_line); break;
+      case 2: stage<R, 2>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
+      case 3: stage<R, 3>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
+      case 4: stage<R, 4>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
+      case 5: stage<R, 5>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
+      case 7: stage<R, 7>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
+      case 8: stage<R, 8>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
+      case 11: stage<R, 11>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
+      case 13: stage<R, 13>(in, out, L, Ns, nl, sign, line_tab<R>(d)); break;
       default: break;
     }
     __syncthreads();
@@ -213,8 +219,122 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(cx<R>* data, long long P,
   }
 }
 
+
+// Two-level register FFT of lines L = A*B (see fft.cuh).  Input index
+// p = B*n1 + n2, output index q = k1 + A*k2:
+//   X[q] = sum_n2 w_B^(n2 k2) w_L^(n2 k1) sum_n1 w_A^(n1 k1) x[p].
+template <typename R, int A, int B>
+__global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, PassDesc d, int sign) {
+  constexpr int L = A * B;
+  constexpr int LDB = B + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);
+  cx<R>* arr = data + (long long)blockIdx.y * P;
+  const long long tile = blockIdx.x;
+  const bool contig = (d.S == 1);
+  const int nl = d.B;
+  long long o, base;
+  int nact;
+  if (contig) {
+    const long long line0 = tile * nl;
+    nact = (int)min((long long)nl, d.O - line0);
+    base = line0 * L;
+    o = line0;
+  } else {
+    const long long nsb = (d.S + nl - 1) / nl;
+    o = tile / nsb;
+    const long long s0 = (tile - o * nsb) * nl;
+    nact = (int)min((long long)nl, d.S - s0);
+    base = o * L * d.S + s0;
+  }
+  const bool tw4 = d.tw_L1 > 0;
+  // phase 1: load A elements per (line, n2), DFT over n1, inner twiddle
+  for (int it = threadIdx.x; it < nl * B; it += blockDim.x) {
+    int b, n2;
+    if (contig) { n2 = it % B; b = it / B; } else { b = it % nl; n2 = it / nl; }
+    if (b >= nact) continue;
+    cx<R> v[A];
+#pragma unroll
+    for (int n1 = 0; n1 < A; ++n1) {
+      const int p = B * n1 + n2;
+      const long long addr = contig ? base + (long long)b * L + p : base + (long long)p * d.S + b;
+      v[n1] = arr[addr];
+      if (tw4 && !d.tw_post) {
+        const long long k1o = (contig ? o + b : o) % d.tw_L1;
+        const int t = (int)(((long long)p * k1o) % d.tw_Lfull);
+        if (t) v[n1] = v[n1] * twid<R>(full_tab<R>(d), t, sign);
+      }
+    }
+    Dft<R, A>::run(v, sign, line_tab<R>(d), L);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) {
+      cx<R> w = v[k1];
+      if (k1 && n2) w = w * twid<R>(line_tab<R>(d), n2 * k1, sign);
+      sm[(b * A + k1) * LDB + n2] = w;
+    }
+  }
+  __syncthreads();
+  // phase 2: DFT over n2, write X[k1 + A k2]
+  for (int it = threadIdx.x; it < nl * A; it += blockDim.x) {
+    int b, k1;
+    if (contig) { k1 = it % A; b = it / A; } else { b = it % nl; k1 = it / nl; }
+    if (b >= nact) continue;
+    cx<R> u[B];
+#pragma unroll
+    for (int n2 = 0; n2 < B; ++n2) u[n2] = sm[(b * A + k1) * LDB + n2];
+    Dft<R, B>::run(u, sign, line_tab<R>(d), L);
+#pragma unroll
+    for (int k2 = 0; k2 < B; ++k2) {
+      const int q = k1 + A * k2;
+      cx<R> w = u[k2];
+      if (tw4 && d.tw_post) {
+        const long long k1o = (contig ? o + b : o) % d.tw_L1;
+        const int t = (int)(((long long)q * k1o) % d.tw_Lfull);
+        if (t) w = w * twid<R>(full_tab<R>(d), t, sign);
+      }
+      const long long addr = contig ? base + (long long)b * L + q : base + (long long)q * d.S + b;
+      arr[addr] = w;
+    }
+  }
+}
+
+// (A, B) pairs with a compiled two-level kernel
+constexpr int kFastPairs[][2] = {{8, 8}, {4, 8}, {8, 4}, {4, 4}, {2, 8}, {8, 2}, {2, 4}, {4, 2}, {2, 2},
+                                 {3, 8}, {8, 3}, {3, 4}, {4, 3}, {3, 3}, {2, 3}, {3, 2}, {5, 5}, {4, 5},
+                                 {5, 4}, {2, 5}, {5, 2}, {3, 5}, {5, 3}, {5, 8}, {8, 5}};
+
+bool fast_pair(int L, int* a, int* b) {
+  int best = -1;
+  for (int i = 0; i < (int)(sizeof(kFastPairs) / sizeof(kFastPairs[0])); ++i) {
+    const int x = kFastPairs[i][0], y = kFastPairs[i][1];
+    if (x * y != L) continue;
+    if (best < 0 || std::abs(x - y) < std::abs(kFastPairs[best][0] - kFastPairs[best][1])) best = i;
+  }
+  if (best < 0) return false;
+  *a = kFastPairs[best][0];
+  *b = kFastPairs[best][1];
+  return true;
+}
+
+template <typename R>
+void launch_fast(const PassDesc& d, dim3 grid, size_t smem, cudaStream_t s, cx<R>* data, long long P, int sign) {
+#define PGB_FAST(A_, B_)                                                                    \
+  if (d.fa == A_ && d.fb == B_) {                                                           \
+    fft2_kernel<R, A_, B_><<<grid, 256, smem, s>>>(data, P, d, sign);                       \
+    return;                                                                                 \
+  }
+  PGB_FAST(8, 8) PGB_FAST(4, 8) PGB_FAST(8, 4) PGB_FAST(4, 4) PGB_FAST(2, 8) PGB_FAST(8, 2)
+  PGB_FAST(2, 4) PGB_FAST(4, 2) PGB_FAST(2, 2) PGB_FAST(3, 8) PGB_FAST(8, 3) PGB_FAST(3, 4)
+  PGB_FAST(4, 3) PGB_FAST(3, 3) PGB_FAST(2, 3) PGB_FAST(3, 2) PGB_FAST(5, 5) PGB_FAST(4, 5)
+  PGB_FAST(5, 4) PGB_FAST(2, 5) PGB_FAST(5, 2) PGB_FAST(3, 5) PGB_FAST(5, 3) PGB_FAST(5, 8)
+  PGB_FAST(8, 5)
+#undef PGB_FAST
+  throw Error("no two-level FFT kernel for this line length");
+}
+
 std::mutex g_mu;
 std::map<int, double2*> g_tables;
+std::map<int, float2*> g_tables_f;
 
 struct PassEvent {
   cudaEvent_t a, b;
@@ -256,7 +376,19 @@ const double2* twiddle_table(int L) {
   PGB_CUDA(cudaMalloc(&d, sizeof(double2) * L));
   PGB_CUDA(cudaMemcpy(d, h.data(), sizeof(double2) * L, cudaMemcpyHostToDevice));
   g_tables[L] = d;
+  std::vector<float2> hf(L);
+  for (int t = 0; t < L; ++t) hf[t] = make_float2((float)h[t].x, (float)h[t].y);
+  float2* df = nullptr;
+  PGB_CUDA(cudaMalloc(&df, sizeof(float2) * L));
+  PGB_CUDA(cudaMemcpy(df, hf.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
+  g_tables_f[L] = df;
   return d;
+}
+
+const float2* twiddle_table_f(int L) {
+  twiddle_table(L);
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_tables_f[L];
 }
 
 bool factor_line(int L, int* radix, int* nst) {
@@ -278,6 +410,17 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
   d.L = L;
   d.S = S;
   d.O = O;
+  if (fast_pair(L, &d.fa, &d.fb)) {
+    long long nl = std::max(1, 2048 / L);
+    nl = std::min(nl, 64LL);
+    nl = (S == 1) ? std::min(nl, O) : std::min(nl, S);
+    d.B = (int)std::max(1LL, nl);
+    d.tw_line = twiddle_table(L);
+    d.tw_line_f = twiddle_table_f(L);
+    d.nst = 0;
+    return d;
+  }
+  d.fa = d.fb = 0;
   PGB_CHECK(factor_line(L, d.radix, &d.nst),
             "FFT length " + std::to_string(L) + " has a prime factor above 13 (unsupported)");
   long long B = std::max(1LL, 32768LL / ((long long)L * elem_bytes));
@@ -286,6 +429,7 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
   else B = std::min(B, S);
   d.B = (int)std::max(1LL, B);
   d.tw_line = twiddle_table(L);
+  d.tw_line_f = twiddle_table_f(L);
   return d;
 }
 
@@ -320,19 +464,33 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
     m.pos.resize(n);
     m.logical.resize(n);
     m.rev.resize(n);
-    if (n > 1 && n <= kMaxLine) {
+    int fa = 0, fb = 0, L1s = 0;
+    const bool direct_fast = fast_pair(n, &fa, &fb);
+    if (n > 64 && !direct_fast) {
+      // four-step split into two lengths that both have a two-level kernel
+      int best = -1;
+      for (int a1 = 2; a1 <= 64; ++a1) {
+        if (n % a1 || n / a1 > 64) continue;
+        int x, y, z, w;
+        if (!fast_pair(a1, &x, &y) || !fast_pair(n / a1, &z, &w)) continue;
+        if (best < 0 || std::abs(a1 - n / a1) < std::abs(best - n / best)) best = a1;
+      }
+      L1s = best > 0 ? best : 0;
+    }
+    if (n > 1 && L1s == 0 && n <= kMaxLine) {
       PassDesc p = make_pass(n, S, O, elem_bytes);
       fwd_.push_back(p);
       bwd_.push_back(p);
       if (a < 3) fwd_space_.push_back(p);
       for (int k = 0; k < n; ++k) m.pos[k] = k;
     } else if (n > 1) {
-      const int L1 = split_length(n), L2 = n / L1;
+      const int L1 = L1s ? L1s : split_length(n), L2 = n / L1;
       PassDesc pb = make_pass(L1, S * L2, O, elem_bytes);
       PassDesc pa = make_pass(L2, S, O * L1, elem_bytes);
       pa.tw_L1 = L1;
       pa.tw_Lfull = n;
       pa.tw_full = twiddle_table(n);
+      pa.tw_full_f = twiddle_table_f(n);
       PassDesc pa_inv = pa;
       pa_inv.tw_post = 1;
       fwd_.push_back(pb);
@@ -376,7 +534,8 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
   }
   for (const PassDesc& d : passes) {
     const long long tiles = (d.S == 1) ? (d.O + d.B - 1) / d.B : d.O * ((d.S + d.B - 1) / d.B);
-    const size_t smem = 2 * (size_t)d.B * d.L * sizeof(cx<R>);
+    const size_t smem = d.fa ? (size_t)d.B * d.fa * (d.fb + 1) * sizeof(cx<R>)
+                             : 2 * (size_t)d.B * d.L * sizeof(cx<R>);
     for (int b0 = 0; b0 < nb; b0 += 65535) {
       const int nbb = std::min(65535, nb - b0);
       dim3 grid((unsigned)tiles, (unsigned)nbb);
@@ -387,7 +546,8 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
         pe.bytes = 2.0 * (double)nbb * (double)P_ * sizeof(cx<R>);
         PGB_CUDA(cudaEventRecord(pe.a, s));
       }
-      fft_pass_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
+      if (d.fa) launch_fast<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
+      else fft_pass_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
       launch_check("fft_pass");
       if (g_prof) {
         PGB_CUDA(cudaEventRecord(pe.b, s));

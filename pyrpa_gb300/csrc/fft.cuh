@@ -6,7 +6,11 @@
 // tile of lines into shared memory (coalesced along the fastest index),
 // runs a mixed-radix Stockham FFT (radices 8,4,2,3,5,7 and a table-driven
 // generic radix for other primes <= 64) and writes the tile back in place.
-// Axes longer than kMaxLine are split four-step style into two passes
+// Lines of length L = A*B with A, B in {2,3,4,5,8} (L <= 64) use a two-level
+// register kernel: one coalesced read with a radix-A DFT in registers, one
+// shared-memory exchange, a radix-B DFT and one write.  Longer axes are
+// split four-step style into two such passes where possible; axes longer
+// than kMaxLine that cannot be split that way use two Stockham passes
 // (L = L1*L2) with the twiddle multiply fused into the second pass; the
 // frequency index of such an axis is then stored digit-transposed, which
 // all pointwise kernels handle through the per-axis position tables below.
@@ -33,6 +37,9 @@ struct PassDesc {
   int tw_post;         // 0: multiply before the line DFT, 1: after
   const double2* tw_line;  // exp(-2 pi i t / L), t < L
   const double2* tw_full;  // exp(-2 pi i t / Lfull), t < Lfull
+  const float2* tw_line_f; // the same tables rounded to FP32 for the FP32 kernels
+  const float2* tw_full_f; //   (FP64->FP32 conversions run on the FP64 pipe)
+  int fa, fb;              // L = fa * fb for the two-level register kernel (0: Stockham kernel)
 };
 
 // Position tables of one axis: pos[k] is where logical index k is stored,

@@ -402,19 +402,21 @@ __global__ void k_chi0_product(cx<R>* out, const cx<R>* F, const cx<R>* F0, cons
 
 template <typename R>
 __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs, const int* irr_grid,
-                               const double2* sawc, long long Nkall, int Nk, int Nw, int Nchi, long long P) {
+                               const cx<R>* sawc, long long Nkall, int Nk, int Nw, int Nchi, long long P) {
   const ChiDev pr = pairs[blockIdx.y];
   const cx<R>* t = tmp + (long long)blockIdx.y * P;
+  const cx<R> J = cmk<R>((R)pr.J.x, (R)pr.J.y);
   const long long K = (long long)Nk * Nw;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
        idx += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(idx % Nk), j = (int)(idx / Nk);
-    double2 v = ccast<double>(t[irr_grid[k] + Nkall * j]);
-    if (sawc) v += pr.J * sawc[j];
+    cx<R> v = t[irr_grid[k] + Nkall * j];
+    if (sawc) v += J * sawc[j];
     if (pr.self) v = conj(v);
-    v = thresh(v);
-    chi[fidx(k, j, pr.m, pr.l, Nk, Nw, Nchi)] = cmk<R>((R)v.x, (R)v.y);
-    if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = cmk<R>((R)v.x, (R)-v.y);
+    if (fabs(v.x) < (R)kThresh) v.x = 0;
+    if (fabs(v.y) < (R)kThresh) v.y = 0;
+    chi[fidx(k, j, pr.m, pr.l, Nk, Nw, Nchi)] = v;
+    if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = conj(v);
   }
 }
 
@@ -523,8 +525,7 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
   DBuf<cx<R>> F((size_t)No2 * g.P);
   pad_green_all<R>(g, G, F.p);
   fft.forward<R>(F.p, No2, st);
-  DBuf<cx<R>> F0, A, B;
-  DBuf<double2> sawc;
+  DBuf<cx<R>> F0, A, B, sawc;
   std::vector<ChiDev> hp(p.chi.size());
   for (size_t i = 0; i < p.chi.size(); ++i) {
     const ChiPair& c = p.chi[i];
@@ -563,9 +564,11 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
       if (a42 == b42) J = J - RB(a13, b13);
       c.J = J;
     }
-    sawc.alloc(g.Nw);
-    k_sawc<<<grid_1d(g.Nw, 128), 128, 0, st>>>(sawc.p, g.Nw, (int)g.M, temp);
+    DBuf<double2> sawc64(g.Nw);
+    k_sawc<<<grid_1d(g.Nw, 128), 128, 0, st>>>(sawc64.p, g.Nw, (int)g.M, temp);
     count_launch("sawc");
+    sawc.alloc(g.Nw);
+    narrow<R>(sawc.p, sawc64.p, g.Nw);
   }
   DBuf<ChiDev> dp(hp.size());
   dp.upload(hp.data(), hp.size());
@@ -726,6 +729,228 @@ __global__ void k_vertex(cx<R>* chi, long long nmat, long long mstride, long lon
   }
 }
 
+// Register-resident vertex for Nchi in {1,4,9,16,25}: lane i holds row i.
+// With Si = S^-1, Ci = C^-1 (computed once on the host):
+//   S (I - chi0 S)^-1 = (Si - chi0)^-1,   C (I + chi0 C)^-1 = (Ci + chi0)^-1,
+// so (fUJ.f90:253-365)
+//   V_sigma         = 1.5 (Si - X)^-1 - 0.5 (Ci + X)^-1 - 0.25 (S+C) X (S+C)
+//   V_Delta singlet = -S + 1.5 (Si - X)^-1 + 0.5 (Ci + X)^-1
+//   V_Delta triplet = S - C - 0.5 (Si - X)^-1 + 0.5 (Ci + X)^-1
+// Each inverse is an in-place Gauss-Jordan elimination with partial pivoting
+// (|Re|+|Im|, first maximum); row interchanges relabel lanes instead of
+// moving data, and the pivot row is broadcast with warp shuffles.
+template <typename R, int N>
+__device__ __forceinline__ cx<R> pick(const cx<R> (&a)[N], int k) {
+  cx<R> v = a[0];
+#pragma unroll
+  for (int j = 1; j < N; ++j)
+    if (j == k) v = a[j];
+  return v;
+}
+
+// The elimination step loop is kept rolled (register entries selected by
+// comparison, not by dynamic indexing): a fully unrolled 25x25 elimination
+// is tens of thousands of straight-line instructions per matrix and runs
+// from the instruction cache's backing store.
+template <typename R, int N>
+__device__ __forceinline__ bool warp_inverse(cx<R> (&a)[N], int* piv, int* map) {
+  const int lane = threadIdx.x & 31;
+  int label = lane;
+  bool ok = true;
+#pragma unroll 1
+  for (int k = 0; k < N; ++k) {
+    const cx<R> ak = pick<R, N>(a, k);
+    R v = (lane < N && label >= k) ? cabs1(ak) : (R)-1;
+    int key = (lane < N && label >= k) ? label : 1 << 20;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const R ov = __shfl_xor_sync(0xffffffffu, v, off);
+      const int ok2 = __shfl_xor_sync(0xffffffffu, key, off);
+      if (ov > v || (ov == v && ok2 < key)) { v = ov; key = ok2; }
+    }
+    const int plabel = key;
+    if (!(v > 0)) ok = false;
+    if (label == k) label = plabel;
+    else if (label == plabel) label = k;
+    if (lane == 0) piv[k] = plabel;
+    const unsigned m = __ballot_sync(0xffffffffu, label == k && lane < N);
+    const int src = __ffs(m) - 1;
+    const cx<R> pv = cmk<R>(__shfl_sync(0xffffffffu, ak.x, src), __shfl_sync(0xffffffffu, ak.y, src));
+    const cx<R> ip = ok ? cdiv(cmk<R>(1, 0), pv) : cmk<R>(0, 0);
+    const bool is_piv = (label == k);
+    const cx<R> kval = is_piv ? ip : -(ak * ip);
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      const cx<R> pj = cmk<R>(__shfl_sync(0xffffffffu, a[j].x, src), __shfl_sync(0xffffffffu, a[j].y, src)) * ip;
+      const cx<R> nv = is_piv ? pj : a[j] - ak * pj;
+      a[j] = (j == k) ? kval : nv;
+    }
+  }
+  __syncwarp();
+  // undo the interchanges: columns in reverse order
+#pragma unroll 1
+  for (int k = N - 1; k >= 0; --k) {
+    const int p = piv[k];
+    if (p != k) {
+      const cx<R> ak = pick<R, N>(a, k), ap = pick<R, N>(a, p);
+#pragma unroll
+      for (int j = 0; j < N; ++j) a[j] = (j == k) ? ap : ((j == p) ? ak : a[j]);
+    }
+  }
+  // bring logical row i back to lane i
+  if (lane < N) map[label] = lane;
+  __syncwarp();
+  const int from = (lane < N) ? map[lane] : lane;
+#pragma unroll
+  for (int j = 0; j < N; ++j) a[j] = cmk<R>(__shfl_sync(0xffffffffu, a[j].x, from), __shfl_sync(0xffffffffu, a[j].y, from));
+  __syncwarp();
+  return ok;
+}
+
+// Matrices of consecutive (q,iv) are staged through shared memory in tiles of
+// 2W: the loads and stores of the Fortran (Nk,Nw,Nchi,Nchi) layout are then
+// runs of 2W consecutive elements instead of one element per cache sector.
+template <typename R, int N, int W>
+__global__ void __launch_bounds__(32 * W) k_vertex_reg(cx<R>* chi, long long nmat, long long estride,
+                                                       const R* consts, int mode) {
+  constexpr int T = 2 * W;          // matrices per tile
+  constexpr int TP = T + 1;         // padded tile row
+  extern __shared__ __align__(16) unsigned char smraw[];
+  // constants in the compute precision: an FP64->FP32 conversion per use
+  // would run on the FP64 pipe
+  R* cs = reinterpret_cast<R*>(smraw);                                 // Si, Ci, S+C, S, C
+  constexpr size_t cs_bytes = (5 * N * N * sizeof(R) + 15) / 16 * 16;  // keep the tile 16-byte aligned
+  cx<R>* tile = reinterpret_cast<cx<R>*>(smraw + cs_bytes);            // [N*N][TP]
+  cx<R>* tb = tile + (size_t)N * N * TP;                               // [W][N*N]
+  int* pv = reinterpret_cast<int*>(tb + (size_t)W * N * N);            // [W][N+1]
+  int* mp = pv + W * (N + 1);                                          // [W][32]
+  for (int e = threadIdx.x; e < 5 * N * N; e += blockDim.x) cs[e] = consts[e];
+  const R* Si = cs;
+  const R* Ci = cs + N * N;
+  const R* SC = cs + 2 * N * N;
+  const R* Sm = cs + 3 * N * N;
+  const R* Cm = cs + 4 * N * N;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = lane < N ? lane : 0;
+  cx<R>* tbw = tb + (size_t)w * N * N;
+  const R c1 = mode == 2 ? (R)-0.5 : (R)1.5;
+  const R c2 = mode == 0 ? (R)-0.5 : (R)0.5;
+  for (long long m0 = (long long)blockIdx.x * T; m0 < nmat; m0 += (long long)gridDim.x * T) {
+    const int nt = (int)min((long long)T, nmat - m0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < N * N * T; idx += blockDim.x) {
+      const int t = idx % T, e = idx / T;
+      if (t < nt) tile[e * TP + t] = chi[m0 + t + estride * e];
+    }
+    __syncthreads();
+    for (int t = w; t < nt; t += W) {
+      // x(i, j) = tile[(i + N j) * TP + t]
+      cx<R> a[N], v[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) a[j] = cmk<R>((R)Si[i * N + j], (R)0) - tile[(i + N * j) * TP + t];
+      bool ok = warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        R base = 0;
+        if (mode == 1) base = (R)-Sm[i * N + j];
+        else if (mode == 2) base = (R)(Sm[i * N + j] - Cm[i * N + j]);
+        v[j] = cmk<R>(base, (R)0) + c1 * a[j];
+      }
+#pragma unroll
+      for (int j = 0; j < N; ++j) a[j] = cmk<R>((R)Ci[i * N + j], (R)0) + tile[(i + N * j) * TP + t];
+      ok &= warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+#pragma unroll
+      for (int j = 0; j < N; ++j) v[j] += c2 * a[j];
+      if (mode == 0) {
+        // -0.25 (S+C) X (S+C): t = X (S+C) row-local, then (S+C) t through smem
+#pragma unroll
+        for (int j = 0; j < N; ++j) a[j] = cmk<R>(0, 0);
+#pragma unroll 1
+        for (int k = 0; k < N; ++k) {
+          const cx<R> xk = tile[(i + N * k) * TP + t];
+#pragma unroll
+          for (int j = 0; j < N; ++j) a[j] += SC[k * N + j] * xk;
+        }
+        if (lane < N) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tbw[i * N + j] = a[j];
+        }
+        __syncwarp();
+#pragma unroll 1
+        for (int k = 0; k < N; ++k) {
+          const R sk = (R)-0.25 * SC[i * N + k];
+#pragma unroll
+          for (int j = 0; j < N; ++j) v[j] += sk * tbw[k * N + j];
+        }
+      }
+      if (!ok && lane == 0) atomicExch(&g_err_dev, 3);
+      __syncwarp();
+      if (lane < N) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) tile[(i + N * j) * TP + t] = v[j];
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < N * N * T; idx += blockDim.x) {
+      const int t = idx % T, e = idx / T;
+      if (t < nt) chi[m0 + t + estride * e] = tile[e * TP + t];
+    }
+  }
+}
+
+template <typename R, int N, int W> size_t vertex_reg_smem() {
+  return (sizeof(R) * 5 * N * N + 15) / 16 * 16 + sizeof(cx<R>) * ((size_t)N * N * (2 * W + 1) + (size_t)W * N * N) +
+         sizeof(int) * (W * (N + 1) + W * 32);
+}
+
+// host inverse of a small real matrix (row-major), false if (nearly) singular
+bool host_inverse(std::vector<double>& A, int n) {
+  std::vector<int> piv(n);
+  double amax = 0;
+  for (double v : A) amax = std::max(amax, std::fabs(v));
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int r = k + 1; r < n; ++r)
+      if (std::fabs(A[r * n + k]) > std::fabs(A[p * n + k])) p = r;
+    piv[k] = p;
+    if (std::fabs(A[p * n + k]) <= 1e-12 * std::max(amax, 1e-300)) return false;
+    if (p != k)
+      for (int j = 0; j < n; ++j) std::swap(A[k * n + j], A[p * n + j]);
+    const double d = 1.0 / A[k * n + k];
+    A[k * n + k] = 1.0;
+    for (int j = 0; j < n; ++j) A[k * n + j] *= d;
+    for (int r = 0; r < n; ++r) {
+      if (r == k) continue;
+      const double f = A[r * n + k];
+      A[r * n + k] = 0.0;
+      for (int j = 0; j < n; ++j) A[r * n + j] -= f * A[k * n + j];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k)
+    if (piv[k] != k)
+      for (int r = 0; r < n; ++r) std::swap(A[r * n + k], A[r * n + piv[k]]);
+  return true;
+}
+
+template <typename R, int N>
+bool vertex_reg_launch(cx<R>* chi, long long nmat, long long estride, const R* dconsts, int mode) {
+  constexpr int warps = (N >= 16) ? 4 : 8;
+  const size_t smem = vertex_reg_smem<R, N, warps>();
+  static bool attr = false;
+  if (!attr) {
+    PGB_CUDA(cudaFuncSetAttribute(k_vertex_reg<R, N, warps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    attr = true;
+  }
+  const long long tiles = (nmat + 2 * warps - 1) / (2 * warps);
+  const long long blocks = std::min<long long>(tiles, (long long)ctx().num_sms * 8);
+  k_vertex_reg<R, N, warps><<<(unsigned)std::max(1LL, blocks), 32 * warps, smem, ctx().stream>>>(
+      chi, nmat, estride, dconsts, mode);
+  count_launch("vertex_reg");
+  return true;
+}
+
 template <typename R>
 bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double* S, const double* C,
             int mode) {
@@ -734,6 +959,42 @@ bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double
   long long mstride = 1, estride = stride;
   if (stride < 0) { mstride = (long long)Nchi * Nchi; estride = 1; }
   const int n = Nchi;
+  const bool reg_size = (n == 1 || n == 4 || n == 9 || (sizeof(R) == 4 && (n == 16 || n == 25)));
+  if (mode <= 2 && reg_size && mstride == 1) {
+    std::vector<double> hS(n * n), hC(n * n);
+    PGB_CUDA(cudaMemcpyAsync(hS.data(), S, sizeof(double) * n * n, cudaMemcpyDeviceToHost, ctx().stream));
+    PGB_CUDA(cudaMemcpyAsync(hC.data(), C, sizeof(double) * n * n, cudaMemcpyDeviceToHost, ctx().stream));
+    sync();
+    // row-major copies: element (a,b) of a Fortran (n,n) matrix is at a + n*b
+    std::vector<double> Sr(n * n), Cr(n * n);
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) {
+        Sr[a * n + b] = hS[a + n * b];
+        Cr[a * n + b] = hC[a + n * b];
+      }
+    std::vector<double> Si(Sr), Ci(Cr);
+    if (host_inverse(Si, n) && host_inverse(Ci, n)) {
+      std::vector<R> consts(5 * n * n);
+      for (int e = 0; e < n * n; ++e) {
+        consts[e] = (R)Si[e];
+        consts[n * n + e] = (R)Ci[e];
+        consts[2 * n * n + e] = (R)(Sr[e] + Cr[e]);
+        consts[3 * n * n + e] = (R)Sr[e];
+        consts[4 * n * n + e] = (R)Cr[e];
+      }
+      DBuf<R> dc(consts.size());
+      dc.upload(consts.data(), consts.size());
+      reset_err();
+      switch (n) {
+        case 1: vertex_reg_launch<R, 1>(chi, nmat, estride, dc.p, mode); break;
+        case 4: vertex_reg_launch<R, 4>(chi, nmat, estride, dc.p, mode); break;
+        case 9: vertex_reg_launch<R, 9>(chi, nmat, estride, dc.p, mode); break;
+        case 16: vertex_reg_launch<R, (sizeof(R) == 4 ? 16 : 1)>(chi, nmat, estride, dc.p, mode); break;
+        case 25: vertex_reg_launch<R, (sizeof(R) == 4 ? 25 : 1)>(chi, nmat, estride, dc.p, mode); break;
+      }
+      return fetch_err() == 0;
+    }
+  }
   const size_t head = ((size_t)3 * n * n * sizeof(double) + 15) / 16 * 16;
   const size_t per_warp = (size_t)4 * n * n * sizeof(cx<R>);
   int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - head) / per_warp));

@@ -20,7 +20,7 @@ import numpy as np
 
 CONFIGS = {
     "c1": dict(Norb=1, Nx=32, Ny=32, Nz=1, Nw=1024, temp=0.02, fill=0.425, U=3.0, J=0.0, gap_sym=1),
-    "c2": dict(Norb=5, Nx=64, Ny=64, Nz=1, Nw=2048, temp=0.01, fill=3.0, U=1.2, J=0.2, gap_sym=0, seed=20261203,
+    "c2": dict(Norb=5, Nx=64, Ny=64, Nz=1, Nw=2048, temp=0.01, fill=3.0, U=1.2, J=0.2, gap_sym=0, seed=4,
                bandwidth=4.0),
     "c5": dict(Norb=3, Nx=24, Ny=24, Nz=24, Nw=1024, temp=0.008, fill=2.0, U=1.5, J=0.25, gap_sym=0, seed=5,
                bandwidth=3.0),
