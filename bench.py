@@ -48,7 +48,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
-    p.add_argument("--precision", type=int, default=32, choices=[32, 64])
+    p.add_argument("--precision", default="mixed", choices=["mixed", "32", "64"],
+                   help="mixed: FP32 bulk to the FP32 rounding floor, then FP64 bulk to eps")
     p.add_argument("--eps", type=float, default=1.0e-4)
     p.add_argument("--scf-loop", type=int, default=300)
     p.add_argument("--no-tail", action="store_true")
@@ -212,7 +213,7 @@ def main():
 
     F.load_library()
     F.set_verbose(0)
-    F.set_precision(a.precision)
+    F.set_precision({"mixed": F.MIXED, "32": 32, "64": 64}[a.precision])
     m = models.prepare(a.config)
     c = m["cfg"]
     call = dict(mu=m["mu"], fill=c["fill"], temp=c["temp"], Nw=c["Nw"], Nx=c["Nx"], Ny=c["Ny"], Nz=c["Nz"],
@@ -263,11 +264,14 @@ def main():
     rate, cores, npairs, cwall = cpu_pair_rate(c, a.cpu_pairs)
     cpu_v = cpu_seconds(c, tail, iters, applies, rate)
     config.update({"flex_iterations": iters, "eliashberg_applications": applies, "lambda": res["lam"],
-                   "stoner": res["stoner"], "mu": res["mu"], "precision": f"fp{a.precision} bulk"})
+                   "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
+                   "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, then FP64 bulk "
+                                          f"to eps; Eliashberg FP32 bulk with FP64 Arnoldi",
+                                 "32": "FP32 bulk", "64": "FP64"}[a.precision]})
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "c64" if a.precision == 32 else "c128", "data": "synthetic seeded tight-binding model",
+        "dtype": {"mixed": "c64+c128", "32": "c64", "64": "c128"}[a.precision], "data": "synthetic seeded tight-binding model",
         "config": config,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": int(launches),

@@ -141,8 +141,11 @@ void conv_delta_orb_to_band(double* deltab, const double* delta, const double* u
 
 /* ------------------------------------- additions without a reference counterpart --- */
 /* 64: FP64 everywhere (default, the reference's arithmetic); 32: complex FP32 FFTs,
- * contractions and vertex solves with G, Sigma, mu, DIIS and lambda kept in FP64.
- * The environment variable PYRPA_GB_PRECISION=fp32 sets 32 at first use. */
+ * contractions and vertex solves with G, Sigma, mu, DIIS and lambda kept in FP64;
+ * 3264 (mixed): as 32, except that the FLEX loop of mkself / pyrpa_gb_flex_eliash
+ * leaves FP32 once its residual reaches the FP32 rounding floor and finishes on
+ * FP64 bulk, so that convergence to eps is always judged on an FP64 iteration.
+ * PYRPA_GB_PRECISION=fp32 | mixed | fp64 in the environment sets it at first use. */
 void pyrpa_gb_set_precision(const int64_t* bits);
 void pyrpa_gb_get_precision(int64_t* bits);
 /* 0 silences the progress lines the reference prints to stdout */
@@ -154,7 +157,9 @@ void pyrpa_gb_clear_error(void);
 void pyrpa_gb_kernel_launches(int64_t* n);
 /* statistics of the last mkself / lin_eliash: iterations, esterr, Stoner, mu, lambda,
  * Eliashberg applications, then device milliseconds of chi0, vertex, Sigma, DIIS,
- * mu, Dyson, Eliashberg applications (14 doubles) */
+ * mu, Dyson, Eliashberg applications, then the FLEX iterations run on FP32 bulk,
+ * the FLEX iterations of a coarse-mesh warm start and its device milliseconds
+ * (16 doubles) */
 void pyrpa_gb_last_stats(double* out);
 void pyrpa_gb_device_info(int64_t* num_sms, int64_t* device);
 /* live timing of the FFT pass kernel: when on, every pass launch is bracketed
@@ -170,7 +175,14 @@ void pyrpa_gb_fft_stats(double* out);
  * G0 start by a given Sigma with chemical potentials seed_mu / seed_mu_old
  * (the sw_in path without a file).  times_ms[3] (may be NULL) receives the
  * host-to-device, device compute and device-to-host milliseconds measured
- * with CUDA events on the library stream.  No counterpart in the reference. */
+ * with CUDA events on the library stream.  coarse[2] (may be NULL) = {k
+ * divisor, frequency divisor}: unless both are 1 and when no sigma_seed is
+ * given, the FLEX loop starts from a warm start: the model solved first on the
+ * k mesh and Matsubara set divided by them (FP32 bulk, down to the FP32
+ * rounding floor), its Sigma Fourier-interpolated in k to the full mesh and
+ * extended in frequency with a c0 + c1/(i w) tail, its mu as the seed.  The
+ * coarse H, eigenvalues and eigenvectors are taken from the fine mesh at the
+ * same k.  No counterpart in the reference. */
 void pyrpa_gb_flex_eliash(double* sigmak, double* mu, double* delta, double* lambda_out, double* stoner,
                           double* times_ms, const double* Smat, const double* Cmat, const int64_t* kmap,
                           const int64_t* invk, const int64_t* olist, const double* hamk, const double* eig,
@@ -182,7 +194,7 @@ void pyrpa_gb_flex_eliash(double* sigmak, double* mu, double* delta, double* lam
                           const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* sub_sigma,
                           const int64_t* m_diis, const bool* sw_rescale, const bool* sw_tail,
                           const int64_t* gap_sym, const int64_t* arnoldi_m, const int64_t* itemax,
-                          const double* eps_eliash);
+                          const double* eps_eliash, const int64_t* coarse);
 
 /* Symbols outside the accelerated path (transport, impurity, SOC, Eilenberger,
  * real-frequency maps, Pade, nonlinear Eliashberg ...) are exported with no

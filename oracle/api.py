@@ -101,6 +101,8 @@ def get_Vsigma_nosoc_flex(chi, Smat, Cmat):
     Nk, Nw, Nchi = len(chi), len(chi[0]), len(Smat)
     flat = np.ascontiguousarray(chi).reshape(-1).copy()
     n = Nk * Nw * Nchi * Nchi
+    if n > flat.size:
+        raise ValueError("chi is smaller than the Nk*Nw*Nchi^2 elements the wrapper makes the library read")
     X = flat[:n].reshape((Nk, Nw, Nchi, Nchi), order="F")
     flat[:n] = O.vsigma_flex_nosoc(X, Smat.T, Cmat.T).reshape(-1, order="F")
     return flat.reshape(chi.shape)

@@ -48,6 +48,7 @@ void ensure_context() {
   if (const char* s = std::getenv("PYRPA_GB_PRECISION")) {
     std::string v(s);
     if (v == "32" || v == "fp32" || v == "FP32") c.precision = 32;
+    if (v == "3264" || v == "mixed" || v == "MIXED") c.precision = kPrecMixed;
   }
   if (const char* s = std::getenv("PYRPA_GB_VERBOSE")) c.verbose = std::atoi(s);
   c.ready = true;
@@ -78,7 +79,9 @@ template <typename T> void nan_fill(T* p, size_t n) {
   for (size_t i = 0; i < n * sizeof(T) / sizeof(double); ++i) d[i] = q;
 }
 
-bool fp32() { return ctx().precision == 32; }
+// FP32 bulk for every entry point except FP64 mode (the mixed schedule only
+// changes the FLEX loop)
+bool fp32() { return ctx().precision != 64; }
 
 // --------------------------------------------------------- setup kernels
 __global__ void k_gen_ham(double2* hk, const double* klist, const double2* hr, const double* rvec, int64_t Nk,
@@ -266,6 +269,55 @@ std::vector<std::array<int64_t, 3>> irr_grid(int64_t Nx, int64_t Ny, int64_t Nz,
 
 }  // namespace
 
+namespace {
+// klist (3,Nk), kmap (3,Nkall) and invk (3,Nkall) of generate_irr_kpoint_inv (finv.f90:1-290)
+void irr_mesh_fill(int64_t nx, int64_t ny, int64_t nz, int64_t nk, double* klist, int64_t* kmap, int64_t* invk) {
+  PGB_CHECK(nx > 0 && ny > 0 && nz > 0, "non-positive mesh");
+  PGB_CHECK(nk == irr_count(nx, ny, nz), "Nk differs from the irreducible count of this mesh");
+  auto irr = irr_grid(nx, ny, nz, nk);
+  std::unordered_map<int64_t, int64_t> direct, inverse;
+  auto key = [&](int64_t x, int64_t y, int64_t z) { return x + nx * (y + ny * z); };
+  for (int64_t j = 0; j < nk; ++j) {
+    const auto& c = irr[j];
+    if (klist) {
+      klist[3 * j] = (double)c[0] / (double)nx;
+      klist[3 * j + 1] = (double)c[1] / (double)ny;
+      klist[3 * j + 2] = (double)c[2] / (double)nz;
+    }
+    direct.emplace(key(c[0], c[1], c[2]), j);
+    inverse.emplace(key((nx - c[0]) % nx, (ny - c[1]) % ny, (nz - c[2]) % nz), j);
+  }
+  for (int64_t z = 0; z < nz; ++z)
+    for (int64_t y = 0; y < ny; ++y)
+      for (int64_t x = 0; x < nx; ++x) {
+        const int64_t i = key(x, y, z);
+        kmap[3 * i] = x;
+        kmap[3 * i + 1] = y;
+        kmap[3 * i + 2] = z;
+        auto d = direct.find(i), v = inverse.find(i);
+        PGB_CHECK(d != direct.end() || v != inverse.end(), "k point without irreducible partner");
+        if (d != direct.end() && (v == inverse.end() || d->second <= v->second)) {
+          invk[3 * i] = d->second + 1;
+          invk[3 * i + 1] = 0;
+        } else {
+          invk[3 * i] = v->second + 1;
+          invk[3 * i + 1] = 1;
+        }
+        invk[3 * i + 2] = key((nx - x) % nx, (ny - y) % ny, (nz - z) % nz) + 1;
+      }
+}
+}  // namespace
+
+namespace pgb {
+int64_t make_irr_mesh(int64_t nx, int64_t ny, int64_t nz, std::vector<int64_t>& kmap, std::vector<int64_t>& invk) {
+  const int64_t nk = irr_count(nx, ny, nz);
+  kmap.assign(3 * nx * ny * nz, 0);
+  invk.assign(3 * nx * ny * nz, 0);
+  irr_mesh_fill(nx, ny, nz, nk, nullptr, kmap.data(), invk.data());
+  return nk;
+}
+}  // namespace pgb
+
 // chi0 entry shared by get_chi0 / get_chi0_tail / get_chi0_conv_
 namespace {
 template <typename R>
@@ -331,7 +383,7 @@ extern "C" {
 
 // ============================================================== extras ==
 void pyrpa_gb_set_precision(const int64_t* bits) {
-  ctx().precision = (*bits == 32) ? 32 : 64;
+  ctx().precision = (*bits == 32) ? 32 : (*bits == kPrecMixed ? kPrecMixed : 64);
 }
 void pyrpa_gb_get_precision(int64_t* bits) {
   ABI_TRY ensure_context(); ABI_CATCH("pyrpa_gb_get_precision", (void)0)
@@ -355,8 +407,9 @@ void pyrpa_gb_clear_error() {
 void pyrpa_gb_kernel_launches(int64_t* n) { *n = ctx().kernel_launches; }
 void pyrpa_gb_last_stats(double* out) {
   const LastStats& s = last_stats();
-  const double v[14] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
-                        s.t_vertex, s.t_sigma, s.t_diis, s.t_mu, s.t_dyson, s.t_apply, 0.0};
+  const double v[16] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
+                        s.t_vertex, s.t_sigma, s.t_diis, s.t_mu, s.t_dyson, s.t_apply, (double)s.iterations32,
+                        (double)s.iterations_coarse, s.t_warm};
   memcpy(out, v, sizeof(v));
 }
 void pyrpa_gb_fft_profile(const int64_t* on) { fft_profile_enable(*on != 0); }
@@ -379,39 +432,7 @@ void openmp_params(int64_t* omp_num, bool* omp_check) {
 void generate_irr_kpoint_inv(double* klist, int64_t* kmap, int64_t* invk, const int64_t* Nk, const int64_t* Nx,
                              const int64_t* Ny, const int64_t* Nz) {
   ABI_TRY
-  const int64_t nx = *Nx, ny = *Ny, nz = *Nz, nk = *Nk, N = nx * ny * nz;
-  PGB_CHECK(nx > 0 && ny > 0 && nz > 0, "non-positive mesh");
-  PGB_CHECK(nk == irr_count(nx, ny, nz), "Nk differs from the irreducible count of this mesh");
-  auto irr = irr_grid(nx, ny, nz, nk);
-  std::unordered_map<int64_t, int64_t> direct, inverse;
-  auto key = [&](int64_t x, int64_t y, int64_t z) { return x + nx * (y + ny * z); };
-  for (int64_t j = 0; j < nk; ++j) {
-    const auto& c = irr[j];
-    klist[3 * j] = (double)c[0] / (double)nx;
-    klist[3 * j + 1] = (double)c[1] / (double)ny;
-    klist[3 * j + 2] = (double)c[2] / (double)nz;
-    direct.emplace(key(c[0], c[1], c[2]), j);
-    inverse.emplace(key((nx - c[0]) % nx, (ny - c[1]) % ny, (nz - c[2]) % nz), j);
-  }
-  for (int64_t z = 0; z < nz; ++z)
-    for (int64_t y = 0; y < ny; ++y)
-      for (int64_t x = 0; x < nx; ++x) {
-        const int64_t i = key(x, y, z);
-        kmap[3 * i] = x;
-        kmap[3 * i + 1] = y;
-        kmap[3 * i + 2] = z;
-        auto d = direct.find(i), v = inverse.find(i);
-        PGB_CHECK(d != direct.end() || v != inverse.end(), "k point without irreducible partner");
-        if (d != direct.end() && (v == inverse.end() || d->second <= v->second)) {
-          invk[3 * i] = d->second + 1;
-          invk[3 * i + 1] = 0;
-        } else {
-          invk[3 * i] = v->second + 1;
-          invk[3 * i + 1] = 1;
-        }
-        invk[3 * i + 2] = key((nx - x) % nx, (ny - y) % ny, (nz - z) % nz) + 1;
-      }
-  (void)N;
+  irr_mesh_fill(*Nx, *Ny, *Nz, *Nk, klist, kmap, invk);
   ABI_CATCH("generate_irr_kpoint_inv", (void)0)
 }
 
@@ -721,8 +742,7 @@ void mkself(double2* sigmak, double* mu, const double* Smat, const double* Cmat,
   MkselfArgs a{sigmak, mu, Smat, Cmat, kmap, invk, olist, hamk, eig, uni, *mu_init, *rfill, *temp, *scf_loop, *pp,
                *eps, *Nkall, *Nk, *Nw, *Norb, *Nchi, *Nx, *Ny, *Nz, *sub_sigma, *sw_out, *sw_in, *m_diis,
                *sw_rescale, *sw_tail, *sigma_scale};
-  if (fp32()) run_mkself<float>(a);
-  else run_mkself<double>(a);
+  run_mkself(a, ctx().precision);
   ABI_CATCH("mkself", (nan_fill(sigmak, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)), *mu = NAN))
 }
 
@@ -751,15 +771,19 @@ void pyrpa_gb_flex_eliash(double2* sigmak, double* mu, double2* delta, double* l
                           const int64_t* Norb, const int64_t* Nchi, const int64_t* Nx, const int64_t* Ny,
                           const int64_t* Nz, const int64_t* sub_sigma, const int64_t* m_diis, const bool* sw_rescale,
                           const bool* sw_tail, const int64_t* gap_sym, const int64_t* arnoldi_m,
-                          const int64_t* itemax, const double* eps_eliash) {
+                          const int64_t* itemax, const double* eps_eliash, const int64_t* coarse) {
   ABI_TRY
   ensure_context();
   PipelineArgs a{sigmak, mu, delta, lambda_out, stoner, times_ms, Smat, Cmat, kmap, invk, olist, hamk, eig, uni,
                  init_delta, prt, sigma_seed, seed_mu ? *seed_mu : 0.0, seed_mu_old ? *seed_mu_old : 0.0, *mu_init,
                  *rfill, *temp, *scf_loop, *pp, *eps, *Nkall, *Nk, *Nw, *Norb, *Nchi, *Nx, *Ny, *Nz, *sub_sigma,
                  *m_diis, *sw_rescale, *sw_tail, *gap_sym, *arnoldi_m, *itemax, *eps_eliash};
-  if (fp32()) run_pipeline<float>(a);
-  else run_pipeline<double>(a);
+  if (coarse) {
+    PGB_CHECK(coarse[0] >= 1 && coarse[1] >= 1, "coarse divisors must be >= 1");
+    a.coarse_kdiv = coarse[0];
+    a.coarse_wdiv = coarse[1];
+  }
+  run_pipeline(a, ctx().precision);
   ABI_CATCH("pyrpa_gb_flex_eliash", (nan_fill(sigmak, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)),
                                      nan_fill(delta, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)), *mu = NAN,
                                      *lambda_out = NAN))

@@ -110,7 +110,7 @@ struct Context {
   int device = 0;
   int num_sms = 0;
   bool ready = false;
-  int precision = 64;          // 64: FP64 bulk; 32: complex FP32 bulk with FP64 steps
+  int precision = 64;          // 64: FP64 bulk; 32: complex FP32 bulk with FP64 steps; 3264: mixed FLEX schedule
   int verbose = 1;             // progress prints like the reference's stdout
   long long kernel_launches = 0;
 };

@@ -6,7 +6,9 @@
 // the m x m Hessenberg eigenproblem of Arnoldi), all in FP64.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <fstream>
 #include <vector>
 
@@ -256,9 +258,83 @@ void upload_inputs(Inputs& in, const int64_t* kmap, const int64_t* invk, const i
 }
 
 // ================================================================ mkself ==
+// One bulk step of the FLEX loop: chi0 (plain or tail-corrected) -> Stoner
+// factor (and the sw_rescale clamp) -> V_sigma -> Sigma (FP64 out).  Each of
+// the three stages runs in FP32 or FP64 (bit 0 chi0, bit 1 vertex, bit 2
+// Sigma set = FP32); chi is converted between the stages where they differ.
 template <typename R>
+double stage_chi0(Inputs& in, const FlexParams& a, const double2* G, double mu, cx<R>* chi) {
+  const Geom& g = in.g;
+  Timer tm;
+  tm.start();
+  TailRef tail{in.eig.p, in.uni.p, mu};
+  chi0<R>(g, in.p, G, a.temp, a.sw_tail ? &tail : nullptr, chi);
+  g_stats.t_chi0 += tm.stop();
+  double sdw = 0, cdw = 0;
+  int qs = 0, qc = 0;
+  tm.start();
+  stoner<R>(g, chi, in.S.p, in.C.p, &sdw, &cdw, &qs, &qc);
+  ckchi_print(g, sdw, cdw, qs, qc);
+  if (a.sw_rescale && sdw >= 1.0) {
+    const double rt = 1.0 - 1.0e-4;
+    log("[FLEX] Stoner factor=%10.6f >= 1: rescaling chi0 to%7.4f\n", sdw, rt);
+    scale_chi<R>(chi, g.K * in.Nchi * in.Nchi, rt / sdw);
+  }
+  g_stats.t_vertex += tm.stop();
+  return sdw;
+}
+template <typename R>
+void stage_vertex(Inputs& in, cx<R>* chi) {
+  Timer tm;
+  tm.start();
+  PGB_CHECK(vertex<R>(chi, in.g.K, in.g.K, in.Nchi, in.S.p, in.C.p, 0), "zgesv failed in V_sigma");
+  g_stats.t_vertex += tm.stop();
+}
+template <typename R>
+void stage_sigma(Inputs& in, const FlexParams& a, const double2* G, const cx<R>* chi, double2* sig) {
+  Timer tm;
+  tm.start();
+  sigma<R>(in.g, in.p, G, chi, in.S.p, in.C.p, a.temp, sig);
+  g_stats.t_sigma += tm.stop();
+}
+
+double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, int fp32_mask, DBuf<float2>& chi32,
+                 DBuf<double2>& chi64, double2* sig) {
+  const long long KC = in.g.K * in.Nchi * in.Nchi;
+  const bool s0 = fp32_mask & 1, s1 = fp32_mask & 2, s2 = fp32_mask & 4;
+  if ((s0 || s1 || s2) && !chi32.p) chi32.alloc(KC);
+  if ((!s0 || !s1 || !s2) && !chi64.p) chi64.alloc(KC);
+  double sdw = s0 ? stage_chi0<float>(in, a, G, mu, chi32.p) : stage_chi0<double>(in, a, G, mu, chi64.p);
+  if (s0 != s1) {
+    if (s1) narrow<float>(chi32.p, chi64.p, KC);
+    else widen<float>(chi64.p, chi32.p, KC);
+  }
+  if (s1) stage_vertex<float>(in, chi32.p);
+  else stage_vertex<double>(in, chi64.p);
+  if (s1 != s2) {
+    if (s2) narrow<float>(chi32.p, chi64.p, KC);
+    else widen<float>(chi64.p, chi32.p, KC);
+  }
+  if (s2) stage_sigma<float>(in, a, G, chi32.p, sig);
+  else stage_sigma<double>(in, a, G, chi64.p, sig);
+  return sdw;
+}
+
+// Stages that the FP32 phase of the FLEX loop runs in FP32 (default all):
+// PYRPA_GB_FP32_STAGES is a comma list of chi0, vertex, sigma.
+int fp32_stage_mask() {
+  const char* s = std::getenv("PYRPA_GB_FP32_STAGES");
+  if (!s) return 7;
+  const std::string v(s);
+  return (v.find("chi0") != std::string::npos ? 1 : 0) | (v.find("vertex") != std::string::npos ? 2 : 0) |
+         (v.find("sigma") != std::string::npos ? 4 : 0);
+}
+
+// prec: 64 FP64 bulk, 32 FP32 bulk, kPrecMixed FP32 bulk until the residual
+// reaches the FP32 rounding floor, then FP64 bulk until eps (convergence is
+// only declared on an FP64 iteration).
 void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_out, const double2* seed,
-                 double seed_mu, double seed_mu_old) {
+                 double seed_mu, double seed_mu_old, int prec) {
   cudaStream_t st = ctx().stream;
   const Geom& g = in.g;
   const Pairs& p = in.p;
@@ -271,7 +347,10 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
   DBuf<double2>& H = in.H;
   DBuf<double2>& uni = in.uni;
   DBuf<double2> G(KE), sig(KE), sig0(KE), eg((size_t)K * Norb);
-  DBuf<cx<R>> chi((size_t)K * Nchi * Nchi);
+  DBuf<float2> chi32;
+  DBuf<double2> chi64;
+  bool use32 = (prec == 32 || prec == kPrecMixed);
+  const int mask32 = fp32_stage_mask();
   std::vector<DBuf<double2>> xout(a.m_diis), res(a.m_diis);
   for (int i = 0; i < a.m_diis; ++i) {
     xout[i].alloc(KE);
@@ -452,30 +531,15 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
   };
 
   Timer tm;
-  TailRef tail{eig.p, uni.p, mu};
   int it = 0;
+  // mixed schedule: leave FP32 once the residual is below kMixSwitch or, once
+  // it is below kMixStallFrom, has not reached a new minimum for kMixStall
+  // iterations
+  double best32 = 1e300;
+  int since_best = 0;
   for (it = 1; it <= a.scf_loop; ++it) {
     log("iter=%5d\n", it);
-    tm.start();
-    tail.mu = mu;
-    chi0<R>(g, p, G.p, a.temp, a.sw_tail ? &tail : nullptr, chi.p);
-    g_stats.t_chi0 += tm.stop();
-    double sdw = 0, cdw = 0;
-    int qs = 0, qc = 0;
-    tm.start();
-    stoner<R>(g, chi.p, S.p, C.p, &sdw, &cdw, &qs, &qc);
-    ckchi_print(g, sdw, cdw, qs, qc);
-    maxchi0s = sdw;
-    if (a.sw_rescale && maxchi0s >= 1.0) {
-      const double rt = 1.0 - 1.0e-4;
-      log("[FLEX] Stoner factor=%10.6f >= 1: rescaling chi0 to%7.4f\n", maxchi0s, rt);
-      scale_chi<R>(chi.p, K * Nchi * Nchi, rt / maxchi0s);
-    }
-    PGB_CHECK(vertex<R>(chi.p, K, K, Nchi, S.p, C.p, 0), "zgesv failed in V_sigma");
-    g_stats.t_vertex += tm.stop();
-    tm.start();
-    sigma<R>(g, p, G.p, chi.p, S.p, C.p, a.temp, sig.p);
-    g_stats.t_sigma += tm.stop();
+    maxchi0s = flex_bulk(in, a, G.p, mu, use32 ? mask32 : 0, chi32, chi64, sig.p);
     tm.start();
     if (a.sub_sigma > 0) hf_subtract(sig.p, Nk, Nw, Norb, (int)a.sub_sigma);
     compare_sigma();
@@ -483,7 +547,25 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
     g_stats.esterr = esterr;
     g_stats.iterations = it;
     g_stats.stoner = maxchi0s;
-    if (esterr < a.eps) break;
+    if (use32) g_stats.iterations32 = it;
+    bool switch64 = false;
+    if (use32 && prec == kPrecMixed) {
+      // the stall count starts once the residual is out of the initial transient
+      if (esterr < best32 * 0.9) {
+        best32 = esterr;
+        since_best = 0;
+      } else if (best32 < kMixStallFrom) {
+        ++since_best;
+      }
+      switch64 = esterr < a.eps || esterr < kMixSwitch || since_best >= kMixStall;
+    }
+    if (esterr < a.eps && !switch64) break;
+    if (switch64 && a.stop_at_fp32_floor) break;
+    if (switch64) {
+      log("[FLEX] residual%9.2E on FP32 bulk: continuing with FP64 bulk\n", esterr);
+      use32 = false;
+      chi32.release();
+    }
     tm.start();
     renew_mu();
     g_stats.t_mu += tm.stop();
@@ -511,8 +593,7 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
   g_stats.mu = mu;
 }
 
-template <typename R>
-void run_mkself(const MkselfArgs& a) {
+void run_mkself(const MkselfArgs& a, int prec) {
   g_stats = LastStats{};
   Inputs in;
   upload_inputs(in, a.kmap, a.invk, a.olist, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Smat, a.Cmat,
@@ -521,7 +602,7 @@ void run_mkself(const MkselfArgs& a) {
                  a.sw_rescale, a.sw_tail, a.sigma_scale};
   const long long KE = in.g.K * a.Norb * a.Norb;
   DBuf<double2> sig(KE);
-  mkself_core<R>(in, prm, sig.p, a.mu_out, nullptr, 0.0, 0.0);
+  mkself_core(in, prm, sig.p, a.mu_out, nullptr, 0.0, 0.0, prec);
   sig.download(a.sigmak, KE);
   sync();
 }
@@ -763,8 +844,72 @@ void run_lin_eliash(const LinEliashArgs& a) {
 // FLEX self-energy -> G -> chi0 -> linearized Eliashberg, device resident
 // between the stages (the reference's calc_lin_eliashberg_eq with
 // sw_self=True, libs/plibs/_calc.py:370-405, as one call).
+// Coarse-mesh warm start: the same model on the k mesh divided by
+// coarse_kdiv (each axis that it divides) with Nw / coarse_wdiv frequencies,
+// solved on FP32 bulk down to the FP32 rounding floor; its Sigma is
+// interpolated to the fine mesh (sigma_interp) and its mu seeds the fine loop.
+// H, its eigenvalues and eigenvectors on the coarse mesh are those of the fine
+// mesh at the same k (transposed / conjugated at -k), so no hopping data is
+// needed.
+void coarse_seed(Inputs& in, const PipelineArgs& a, const FlexParams& prm, DBuf<double2>& seed, double* mu_seed) {
+  const Geom& g = in.g;
+  const int No = in.Norb;
+  auto div = [&](int n) { return (a.coarse_kdiv > 1 && n % a.coarse_kdiv == 0 && n / a.coarse_kdiv >= 2)
+                                     ? n / (int)a.coarse_kdiv : n; };
+  const int Nxc = div(g.Nx), Nyc = div(g.Ny), Nzc = g.Nz > 1 ? div(g.Nz) : 1;
+  const int Nwc = std::max(1, g.Nw / (int)std::max<int64_t>(1, a.coarse_wdiv));
+  std::vector<int64_t> kmap_c, invk_c;
+  const int64_t Nkc = make_irr_mesh(Nxc, Nyc, Nzc, kmap_c, invk_c);
+  Inputs ic;
+  ic.Norb = No;
+  ic.Nchi = in.Nchi;
+  ic.Nk = (int)Nkc;
+  ic.Nw = Nwc;
+  build_geom(ic.g, kmap_c.data(), invk_c.data(), Nxc, Nyc, Nzc, Nkc, Nwc, No, in.Nchi);
+  ic.p = in.p;
+  const int fx = g.Nx / Nxc, fy = g.Ny / Nyc, fz = g.Nz / Nzc;
+  std::vector<double2> hc((size_t)No * No * Nkc), uc((size_t)No * No * Nkc);
+  std::vector<double> ec((size_t)No * Nkc);
+  for (int64_t j = 0; j < Nkc; ++j) {
+    const long long gc = ic.g.h_irr_grid[j];
+    const long long x = gc % Nxc, y = (gc / Nxc) % Nyc, z = gc / ((long long)Nxc * Nyc);
+    const long long gf = fx * x + (long long)g.Nx * (fy * y + (long long)g.Ny * fz * z);
+    const int kf = g.h_grid_irr[gf], fl = g.h_grid_flag[gf];
+    for (int e = 0; e < No * No; ++e) {
+      const double2 h = a.hamk[e + (size_t)No * No * kf], u = a.uni[e + (size_t)No * No * kf];
+      hc[e + (size_t)No * No * j] = fl ? conj(h) : h;  // H(-k) = H(k)^* under time reversal
+      uc[e + (size_t)No * No * j] = fl ? conj(u) : u;
+    }
+    for (int n = 0; n < No; ++n) ec[n + (size_t)No * j] = a.eig[n + (size_t)No * kf];
+  }
+  ic.H.alloc(hc.size());
+  ic.H.upload(hc.data(), hc.size());
+  ic.uni.alloc(uc.size());
+  ic.uni.upload(uc.data(), uc.size());
+  ic.eig.alloc(ec.size());
+  ic.eig.upload(ec.data(), ec.size());
+  ic.S.alloc((size_t)in.Nchi * in.Nchi);
+  ic.C.alloc((size_t)in.Nchi * in.Nchi);
+  PGB_CUDA(cudaMemcpyAsync(ic.S.p, in.S.p, sizeof(double) * in.Nchi * in.Nchi, cudaMemcpyDeviceToDevice,
+                           ctx().stream));
+  PGB_CUDA(cudaMemcpyAsync(ic.C.p, in.C.p, sizeof(double) * in.Nchi * in.Nchi, cudaMemcpyDeviceToDevice,
+                           ctx().stream));
+  FlexParams pc = prm;
+  pc.eps = prm.eps;
+  pc.stop_at_fp32_floor = true;
+  DBuf<double2> sc((size_t)ic.g.K * No * No);
+  double mu_c = 0;
+  log("[FLEX] warm start on the %dx%dx%d mesh with %d frequencies\n", Nxc, Nyc, Nzc, Nwc);
+  mkself_core(ic, pc, sc.p, &mu_c, nullptr, 0.0, 0.0, kPrecMixed);
+  g_stats.iterations_coarse = g_stats.iterations;
+  g_stats.iterations = g_stats.iterations32 = 0;
+  seed.alloc((size_t)g.K * No * No);
+  sigma_interp(ic.g, g, sc.p, seed.p, No, a.temp);
+  *mu_seed = mu_c;
+}
+
 template <typename R>
-void run_pipeline(const PipelineArgs& a) {
+void run_pipeline_impl(const PipelineArgs& a, int prec) {
   g_stats = LastStats{};
   cudaStream_t st = ctx().stream;
   Timer t;
@@ -785,9 +930,18 @@ void run_pipeline(const PipelineArgs& a) {
   t.start();
   FlexParams prm{a.mu_init, a.fill, a.temp, a.scf_loop, a.pp, a.eps, a.sub_sigma, false, false, a.m_diis,
                  a.sw_rescale, a.sw_tail, 1.0};
+  double seed_mu = a.seed_mu, seed_mu_old = a.seed_mu_old;
+  const bool warm = !a.sigma_seed && (a.coarse_kdiv > 1 || a.coarse_wdiv > 1);
+  if (warm) {
+    Timer tw;
+    tw.start();
+    coarse_seed(in, a, prm, seed, &seed_mu);
+    seed_mu_old = seed_mu;
+    g_stats.t_warm = tw.stop();
+  }
   DBuf<double2> sig(KE), G(KE), D(KE);
   double mu = 0;
-  mkself_core<R>(in, prm, sig.p, &mu, a.sigma_seed ? seed.p : nullptr, a.seed_mu, a.seed_mu_old);
+  mkself_core(in, prm, sig.p, &mu, seed.p, seed_mu, seed_mu_old, prec);
   const int iters = g_stats.iterations;
   seed.release();
   PGB_CHECK(dyson(G.p, sig.p, in.H.p, mu, a.temp, in.Nk, in.Nw, in.Norb), "singular G^-1 in the Dyson step");
@@ -820,11 +974,12 @@ void run_pipeline(const PipelineArgs& a) {
   g_stats.mu = mu;
 }
 
-template void run_mkself<float>(const MkselfArgs&);
-template void run_mkself<double>(const MkselfArgs&);
 template void run_lin_eliash<float>(const LinEliashArgs&);
 template void run_lin_eliash<double>(const LinEliashArgs&);
-template void run_pipeline<float>(const PipelineArgs&);
-template void run_pipeline<double>(const PipelineArgs&);
+// The Eliashberg stage runs in FP64 for prec 64 and in FP32 bulk otherwise.
+void run_pipeline(const PipelineArgs& a, int prec) {
+  if (prec == 64) run_pipeline_impl<double>(a, prec);
+  else run_pipeline_impl<float>(a, prec);
+}
 
 }  // namespace pgb

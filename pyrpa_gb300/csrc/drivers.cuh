@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
 
 #include "flex.cuh"
 
@@ -64,6 +65,9 @@ struct PipelineArgs {
   bool sw_rescale, sw_tail;
   int64_t gap_sym, arnoldi_m, itemax;
   double eps_eliash;
+  // coarse-mesh warm start: k mesh and Matsubara count divided by these
+  // (1 = not coarsened; both 1 = no warm start)
+  int64_t coarse_kdiv = 1, coarse_wdiv = 1;
 };
 
 // uploaded model data shared by the solvers
@@ -84,6 +88,7 @@ struct FlexParams {
   int64_t m_diis;
   bool sw_rescale, sw_tail;
   double sigma_scale;
+  bool stop_at_fp32_floor = false;  // mixed schedule: stop where it would switch to FP64
 };
 
 struct EliashParams {
@@ -92,16 +97,28 @@ struct EliashParams {
 };
 
 struct LastStats {
-  int iterations = 0;
+  int iterations = 0, iterations32 = 0;  // FLEX iterations (of which on FP32 bulk)
+  int iterations_coarse = 0;             // FLEX iterations of the coarse-mesh warm start
+  double t_warm = 0;                     // device ms of the warm start (coarse solve + interpolation)
   double esterr = 0, stoner = 0, mu = 0, lambda = 0;
   int applies = 0;
   // milliseconds on the device (CUDA events on the library stream)
   double t_chi0 = 0, t_vertex = 0, t_sigma = 0, t_diis = 0, t_mu = 0, t_dyson = 0, t_apply = 0;
 };
 
-template <typename R> void run_mkself(const MkselfArgs& a);
+// precision schedule of the FLEX loop: 64, 32 or kPrecMixed
+constexpr int kPrecMixed = 3264;
+constexpr double kMixSwitch = 2.0e-3;  // residual at which the mixed schedule leaves FP32
+constexpr int kMixStall = 6;           // or after this many FP32 iterations without a new minimum
+constexpr double kMixStallFrom = 0.1;  //   counted once the residual has been below this
+
+// the reference's irreducible TRS mesh (generate_irr_kpoint_inv): kmap and
+// invk (3 per full point), returns Nk
+int64_t make_irr_mesh(int64_t nx, int64_t ny, int64_t nz, std::vector<int64_t>& kmap, std::vector<int64_t>& invk);
+
+void run_mkself(const MkselfArgs& a, int prec);
 template <typename R> void run_lin_eliash(const LinEliashArgs& a);
-template <typename R> void run_pipeline(const PipelineArgs& a);
+void run_pipeline(const PipelineArgs& a, int prec);
 const LastStats& last_stats();
 
 }  // namespace pgb

@@ -481,7 +481,10 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
       PassDesc p = make_pass(n, S, O, elem_bytes);
       fwd_.push_back(p);
       bwd_.push_back(p);
-      if (a < 3) fwd_space_.push_back(p);
+      if (a < 3) {
+        fwd_space_.push_back(p);
+        bwd_space_.push_back(p);
+      }
       for (int k = 0; k < n; ++k) m.pos[k] = k;
     } else if (n > 1) {
       const int L1 = L1s ? L1s : split_length(n), L2 = n / L1;
@@ -500,6 +503,8 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
       if (a < 3) {
         fwd_space_.push_back(pb);
         fwd_space_.push_back(pa);
+        bwd_space_.push_back(pa_inv);
+        bwd_space_.push_back(pb);
       }
       for (int k = 0; k < n; ++k) m.pos[k] = (k / L1) + L2 * (k % L1);
     } else {
@@ -567,6 +572,9 @@ template <typename R> void FFT4D::backward(cx<R>* data, int nb, cudaStream_t s) 
 template <typename R> void FFT4D::forward_space(cx<R>* data, int nb, cudaStream_t s) const {
   run<R>(fwd_space_, data, nb, -1, s);
 }
+template <typename R> void FFT4D::backward_space(cx<R>* data, int nb, cudaStream_t s) const {
+  run<R>(bwd_space_, data, nb, +1, s);
+}
 
 template void FFT4D::forward<float>(float2*, int, cudaStream_t) const;
 template void FFT4D::forward<double>(double2*, int, cudaStream_t) const;
@@ -574,6 +582,8 @@ template void FFT4D::backward<float>(float2*, int, cudaStream_t) const;
 template void FFT4D::backward<double>(double2*, int, cudaStream_t) const;
 template void FFT4D::forward_space<float>(float2*, int, cudaStream_t) const;
 template void FFT4D::forward_space<double>(double2*, int, cudaStream_t) const;
+template void FFT4D::backward_space<float>(float2*, int, cudaStream_t) const;
+template void FFT4D::backward_space<double>(double2*, int, cudaStream_t) const;
 
 void fft_profile_enable(bool on) { g_prof = on; }
 

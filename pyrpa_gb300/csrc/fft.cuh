@@ -60,6 +60,8 @@ class FFT4D {
   template <typename R> void backward(cx<R>* data, int nb, cudaStream_t s) const;
   // spatial-only (x,y,z) forward transform; the t axis is left untouched
   template <typename R> void forward_space(cx<R>* data, int nb, cudaStream_t s) const;
+  // its inverse (unnormalized): spatial axes from the forward_space layout back to natural order
+  template <typename R> void backward_space(cx<R>* data, int nb, cudaStream_t s) const;
   const AxisMap& axis(int a) const { return maps_[a]; }
   // device copies of the position tables (pos, rev, logical) of each axis
   const int* d_pos(int a) const { return d_tables_ + off_pos_[a]; }
@@ -69,7 +71,7 @@ class FFT4D {
  private:
   int dims_[4] = {1, 1, 1, 1};
   long long P_ = 1;
-  std::vector<PassDesc> fwd_, bwd_, fwd_space_;
+  std::vector<PassDesc> fwd_, bwd_, fwd_space_, bwd_space_;
   AxisMap maps_[4];
   int* d_tables_ = nullptr;
   int off_pos_[4] = {0, 0, 0, 0}, off_rev_[4] = {0, 0, 0, 0}, off_log_[4] = {0, 0, 0, 0};

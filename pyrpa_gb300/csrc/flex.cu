@@ -2,7 +2,9 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstring>
+#include <cstdlib>
 #include <map>
+#include <string>
 
 #include "flex.cuh"
 #include "linalg.cuh"
@@ -899,6 +901,108 @@ __global__ void __launch_bounds__(32 * W) k_vertex_reg(cx<R>* chi, long long nma
   }
 }
 
+// Register vertex with the output accumulated in shared memory: one row of
+// the working matrix (N complex values) is the only per-lane register array,
+// so N = 25 fits in FP64.  One matrix per warp per tile.  The tile slot of a
+// matrix holds X until both inversions are done, then X(S+C) as the scratch
+// of the sandwich term, then the result.
+template <typename R, int N, int W>
+__global__ void __launch_bounds__(32 * W) k_vertex_vs(cx<R>* chi, long long nmat, long long estride,
+                                                      const R* consts, int mode) {
+  constexpr int T = W;
+  constexpr int TP = T + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  R* cs = reinterpret_cast<R*>(smraw);
+  constexpr size_t cs_bytes = (5 * N * N * sizeof(R) + 15) / 16 * 16;
+  cx<R>* tile = reinterpret_cast<cx<R>*>(smraw + cs_bytes);  // [N*N][TP]
+  cx<R>* vb = tile + (size_t)N * N * TP;                      // [W][N][32]
+  int* pv = reinterpret_cast<int*>(vb + (size_t)W * N * 32);  // [W][N+1]
+  int* mp = pv + W * (N + 1);                                 // [W][32]
+  for (int e = threadIdx.x; e < 5 * N * N; e += blockDim.x) cs[e] = consts[e];
+  const R* Si = cs;
+  const R* Ci = cs + N * N;
+  const R* SC = cs + 2 * N * N;
+  const R* Sm = cs + 3 * N * N;
+  const R* Cm = cs + 4 * N * N;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = lane < N ? lane : 0;
+  cx<R>* vw = vb + (size_t)w * N * 32;
+  const R c1 = mode == 2 ? (R)-0.5 : (R)1.5;
+  const R c2 = mode == 0 ? (R)-0.5 : (R)0.5;
+  for (long long m0 = (long long)blockIdx.x * T; m0 < nmat; m0 += (long long)gridDim.x * T) {
+    const int nt = (int)min((long long)T, nmat - m0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < N * N * T; idx += blockDim.x) {
+      const int t = idx % T, e = idx / T;
+      if (t < nt) tile[e * TP + t] = chi[m0 + t + estride * e];
+    }
+    __syncthreads();
+    const int t = w;
+    if (t < nt) {
+      cx<R> a[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) a[j] = cmk<R>(Si[i * N + j], (R)0) - tile[(i + N * j) * TP + t];
+      bool ok = warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        R base = 0;
+        if (mode == 1) base = -Sm[i * N + j];
+        else if (mode == 2) base = Sm[i * N + j] - Cm[i * N + j];
+        vw[j * 32 + lane] = cmk<R>(base, (R)0) + c1 * a[j];
+      }
+#pragma unroll
+      for (int j = 0; j < N; ++j) a[j] = cmk<R>(Ci[i * N + j], (R)0) + tile[(i + N * j) * TP + t];
+      ok &= warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+#pragma unroll
+      for (int j = 0; j < N; ++j) vw[j * 32 + lane] += c2 * a[j];
+      if (mode == 0) {
+        // -0.25 (S+C) X (S+C): row i of X (S+C) into the tile slot, then (S+C) times it
+#pragma unroll
+        for (int j = 0; j < N; ++j) a[j] = cmk<R>(0, 0);
+#pragma unroll 1
+        for (int k = 0; k < N; ++k) {
+          const cx<R> xk = tile[(i + N * k) * TP + t];
+#pragma unroll
+          for (int j = 0; j < N; ++j) a[j] += SC[k * N + j] * xk;
+        }
+        __syncwarp();
+        if (lane < N) {
+#pragma unroll
+          for (int j = 0; j < N; ++j) tile[(i + N * j) * TP + t] = a[j];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < N; ++j) a[j] = cmk<R>(0, 0);
+#pragma unroll 1
+        for (int k = 0; k < N; ++k) {
+          const R sk = (R)-0.25 * SC[i * N + k];
+#pragma unroll
+          for (int j = 0; j < N; ++j) a[j] += sk * tile[(k + N * j) * TP + t];
+        }
+#pragma unroll
+        for (int j = 0; j < N; ++j) vw[j * 32 + lane] += a[j];
+      }
+      if (!ok && lane == 0) atomicExch(&g_err_dev, 3);
+      __syncwarp();
+      if (lane < N) {
+#pragma unroll
+        for (int j = 0; j < N; ++j) tile[(i + N * j) * TP + t] = vw[j * 32 + lane];
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < N * N * T; idx += blockDim.x) {
+      const int t2 = idx % T, e = idx / T;
+      if (t2 < nt) chi[m0 + t2 + estride * e] = tile[e * TP + t2];
+    }
+  }
+}
+
+template <typename R, int N, int W> size_t vertex_vs_smem() {
+  return (sizeof(R) * 5 * N * N + 15) / 16 * 16 + sizeof(cx<R>) * ((size_t)N * N * (W + 1) + (size_t)W * N * 32) +
+         sizeof(int) * (W * (N + 1) + W * 32);
+}
+
 template <typename R, int N, int W> size_t vertex_reg_smem() {
   return (sizeof(R) * 5 * N * N + 15) / 16 * 16 + sizeof(cx<R>) * ((size_t)N * N * (2 * W + 1) + (size_t)W * N * N) +
          sizeof(int) * (W * (N + 1) + W * 32);
@@ -951,6 +1055,30 @@ bool vertex_reg_launch(cx<R>* chi, long long nmat, long long estride, const R* d
   return true;
 }
 
+template <typename R, int N>
+bool vertex_vs_launch(cx<R>* chi, long long nmat, long long estride, const R* dconsts, int mode) {
+  constexpr int warps = 6;
+  const size_t smem = vertex_vs_smem<R, N, warps>();
+  static bool attr = false;
+  if (!attr) {
+    PGB_CUDA(cudaFuncSetAttribute(k_vertex_vs<R, N, warps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  const long long tiles = (nmat + warps - 1) / warps;
+  const long long blocks = std::min<long long>(tiles, (long long)ctx().num_sms * 8);
+  k_vertex_vs<R, N, warps><<<(unsigned)std::max(1LL, blocks), 32 * warps, smem, ctx().stream>>>(chi, nmat, estride,
+                                                                                                dconsts, mode);
+  count_launch("vertex_vs");
+  return true;
+}
+
+// FP32, N = 25: the shared-memory-accumulator kernel instead of the
+// all-register one (PYRPA_GB_VERTEX=vs), for timing both variants
+bool vertex_fp32_vs() {
+  const char* s = std::getenv("PYRPA_GB_VERTEX");
+  return s && std::string(s) == "vs";
+}
+
 template <typename R>
 bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double* S, const double* C,
             int mode) {
@@ -959,7 +1087,7 @@ bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double
   long long mstride = 1, estride = stride;
   if (stride < 0) { mstride = (long long)Nchi * Nchi; estride = 1; }
   const int n = Nchi;
-  const bool reg_size = (n == 1 || n == 4 || n == 9 || (sizeof(R) == 4 && (n == 16 || n == 25)));
+  const bool reg_size = (n == 1 || n == 4 || n == 9 || n == 16 || n == 25);
   if (mode <= 2 && reg_size && mstride == 1) {
     std::vector<double> hS(n * n), hC(n * n);
     PGB_CUDA(cudaMemcpyAsync(hS.data(), S, sizeof(double) * n * n, cudaMemcpyDeviceToHost, ctx().stream));
@@ -989,8 +1117,18 @@ bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double
         case 1: vertex_reg_launch<R, 1>(chi, nmat, estride, dc.p, mode); break;
         case 4: vertex_reg_launch<R, 4>(chi, nmat, estride, dc.p, mode); break;
         case 9: vertex_reg_launch<R, 9>(chi, nmat, estride, dc.p, mode); break;
-        case 16: vertex_reg_launch<R, (sizeof(R) == 4 ? 16 : 1)>(chi, nmat, estride, dc.p, mode); break;
-        case 25: vertex_reg_launch<R, (sizeof(R) == 4 ? 25 : 1)>(chi, nmat, estride, dc.p, mode); break;
+        case 16:
+          if constexpr (sizeof(R) == 4) vertex_reg_launch<R, 16>(chi, nmat, estride, dc.p, mode);
+          else vertex_vs_launch<R, 16>(chi, nmat, estride, dc.p, mode);
+          break;
+        case 25:
+          if constexpr (sizeof(R) == 4) {
+            if (vertex_fp32_vs()) vertex_vs_launch<R, 25>(chi, nmat, estride, dc.p, mode);
+            else vertex_reg_launch<R, 25>(chi, nmat, estride, dc.p, mode);
+          } else {
+            vertex_vs_launch<R, 25>(chi, nmat, estride, dc.p, mode);
+          }
+          break;
       }
       return fetch_err() == 0;
     }
@@ -1021,6 +1159,150 @@ template <typename R> void scale_chi(cx<R>* chi, long long n, double s) {
   count_launch("scale");
 }
 
+// ====================================================== coarse-mesh seed ==
+// Sigma of a coarse mesh on the full coarse grid, [e][n][grid cell], FP32
+__global__ void k_sig_to_grid(float2* out, const double2* sig, const int* grid_irr, const int* grid_flag,
+                              long long Nkall, int Nk, int Nw, int No) {
+  const int e = blockIdx.y, a = e % No, b = e / No;
+  const long long N = Nkall * Nw;
+  float2* o = out + (long long)e * N;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)(idx / Nkall);
+    const int k = grid_irr[gi];
+    // Sigma(-k) = Sigma(k)^T under time reversal
+    const double2 v = grid_flag[gi] ? sig[fidx(k, n, b, a, Nk, Nw, No)] : sig[fidx(k, n, a, b, Nk, Nw, No)];
+    o[idx] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+// coarse logical index and weight of fine logical index l along one axis;
+// false where the fine Fourier component has no coarse counterpart
+__device__ __forceinline__ bool pad_axis(int l, int nc, int nf, int* c, float* w) {
+  if (nc == nf) {
+    *c = l;
+    return true;
+  }
+  const int r = (l < (nf + 1) / 2) ? l : l - nf;
+  const int ar = r < 0 ? -r : r;
+  if (nc % 2 == 0) {
+    if (ar < nc / 2) {
+      *c = (r + nc) % nc;
+      return true;
+    }
+    if (ar == nc / 2) {  // Nyquist plane: half to +nc/2, half to -nc/2
+      *c = nc / 2;
+      *w *= 0.5f;
+      return true;
+    }
+    return false;
+  }
+  if (ar <= (nc - 1) / 2) {
+    *c = (r + nc) % nc;
+    return true;
+  }
+  return false;
+}
+
+struct PadTables {
+  int nc[3], nf[3];
+  const int* pos_c[3];  // coarse position of each coarse logical index (forward_space layout)
+  const int* log_f[3];  // fine logical index of each fine position (backward_space input layout)
+};
+
+__global__ void k_pad_space(float2* out, const float2* in, long long Nkc, long long Nkf, int Nw, PadTables t) {
+  const int e = blockIdx.y;
+  const long long N = Nkf * Nw;
+  const float2* src = in + (long long)e * Nkc * Nw;
+  float2* o = out + (long long)e * N;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long s = idx % Nkf, n = idx / Nkf;
+    const int p[3] = {(int)(s % t.nf[0]), (int)((s / t.nf[0]) % t.nf[1]), (int)(s / ((long long)t.nf[0] * t.nf[1]))};
+    float w = 1.0f;
+    int c[3];
+    bool in_range = true;
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) in_range = in_range && pad_axis(t.log_f[ax][p[ax]], t.nc[ax], t.nf[ax], &c[ax], &w);
+    float2 v = make_float2(0.f, 0.f);
+    if (in_range) {
+      const long long ci = t.pos_c[0][c[0]] + (long long)t.nc[0] * (t.pos_c[1][c[1]] + (long long)t.nc[1] * t.pos_c[2][c[2]]);
+      const float2 u = src[n * Nkc + ci];
+      v = make_float2(w * u.x, w * u.y);
+    }
+    o[idx] = v;
+  }
+}
+
+// fine irreducible Sigma from the interpolated grid; frequencies beyond the
+// coarse set from c0 + c1/(i w) through the coarse frequencies n1 < n2
+__global__ void k_grid_to_sig(double2* sig, const float2* F, const int* irr_grid, long long Nkall, int Nk, int Nw_c,
+                              int Nw_f, int No, double scale, double temp) {
+  const long long N = (long long)Nk * Nw_f * No * No;
+  const int n2 = Nw_c >= 4 ? Nw_c - 2 : Nw_c - 1;
+  const int n1 = Nw_c >= 4 ? (3 * Nw_c) / 4 : n2;
+  const double pi = kPi;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk);
+    const int n = (int)((idx / Nk) % Nw_f);
+    const int e = (int)(idx / ((long long)Nk * Nw_f));
+    const float2* base = F + (long long)e * Nkall * Nw_c + irr_grid[k];
+    double2 v;
+    if (n < Nw_c) {
+      const float2 u = base[(long long)n * Nkall];
+      v = make_double2(scale * u.x, scale * u.y);
+    } else {
+      const float2 u1 = base[(long long)n1 * Nkall], u2 = base[(long long)n2 * Nkall];
+      const double2 s1 = make_double2(scale * u1.x, scale * u1.y), s2 = make_double2(scale * u2.x, scale * u2.y);
+      if (n1 == n2) {
+        v = s2;
+      } else {
+        // z = 1/(i w) = -i/w
+        const double2 z1 = make_double2(0.0, -1.0 / ((2 * n1 + 1) * pi * temp));
+        const double2 z2 = make_double2(0.0, -1.0 / ((2 * n2 + 1) * pi * temp));
+        const double2 zn = make_double2(0.0, -1.0 / ((2 * n + 1) * pi * temp));
+        const double2 c1 = cdiv(s1 - s2, z1 - z2);
+        const double2 c0 = s1 - c1 * z1;
+        v = c0 + c1 * zn;
+      }
+    }
+    sig[idx] = v;
+  }
+}
+
+void sigma_interp(const Geom& gc, const Geom& gf, const double2* sig_c, double2* sig_f, int No, double temp) {
+  cudaStream_t st = ctx().stream;
+  PGB_CHECK(gf.Nx % gc.Nx == 0 && gf.Ny % gc.Ny == 0 && gf.Nz % gc.Nz == 0 && gf.Nw >= gc.Nw,
+            "coarse mesh does not divide the fine mesh");
+  const int No2 = No * No;
+  const FFT4D& pc = fft_plan(gc.Nx, gc.Ny, gc.Nz, gc.Nw, (int)sizeof(float2));
+  const FFT4D& pf = fft_plan(gf.Nx, gf.Ny, gf.Nz, gc.Nw, (int)sizeof(float2));
+  DBuf<float2> A((size_t)No2 * gc.Nkall * gc.Nw), B((size_t)No2 * gf.Nkall * gc.Nw);
+  k_sig_to_grid<<<dim3(grid_1d(gc.Nkall * gc.Nw, 256, 4096), No2), 256, 0, st>>>(
+      A.p, sig_c, gc.grid_irr.p, gc.grid_flag.p, gc.Nkall, gc.Nk, gc.Nw, No);
+  count_launch("sig_to_grid");
+  pc.forward_space<float>(A.p, No2, st);
+  PadTables t{};
+  const int nc[3] = {gc.Nx, gc.Ny, gc.Nz}, nf[3] = {gf.Nx, gf.Ny, gf.Nz};
+  for (int ax = 0; ax < 3; ++ax) {
+    t.nc[ax] = nc[ax];
+    t.nf[ax] = nf[ax];
+    t.pos_c[ax] = pc.d_pos(ax);
+    t.log_f[ax] = pf.d_logical(ax);
+  }
+  k_pad_space<<<dim3(grid_1d(gf.Nkall * gc.Nw, 256, 4096), No2), 256, 0, st>>>(B.p, A.p, gc.Nkall, gf.Nkall, gc.Nw,
+                                                                                t);
+  count_launch("pad_space");
+  pf.backward_space<float>(B.p, No2, st);
+  const long long N = (long long)gf.Nk * gf.Nw * No2;
+  k_grid_to_sig<<<grid_1d(N, 256, 65536), 256, 0, st>>>(sig_f, B.p, gf.irr_grid.p, gf.Nkall, gf.Nk, gc.Nw, gf.Nw, No,
+                                                         1.0 / (double)gc.Nkall, temp);
+  count_launch("grid_to_sig");
+  sync();
+}
+
 // ================================================================= sigma ==
 template <typename R>
 __global__ void k_contract(cx<R>* out, const cx<R>* W, const cx<R>* F, const int* ef, int nt, long long P) {
@@ -1046,51 +1328,139 @@ __global__ void k_scatter_out(double2* dst, const void* tmp, int is_double, cons
   }
 }
 
+// Mirror pairs.  The padded bosonic arrays satisfy B_lm(k,s) = conj B_ml(k,-s)
+// at every slot except s = 0 (where it needs V(q,0) Hermitian in the pair
+// index) and s = Nw (where it needs the static matrix symmetric).  Hence
+//   W_lm(r,t) = conj W_ml(-r,t) + D_lm(r) + (-1)^t Nkall [r=0] (stat_lm - stat_ml),
+// with D_lm the 3-D transform of d(k) = B_lm(k,0) - conj B_ml(k,0): exact for
+// any input, and only Nchi(Nchi+1)/2 forward transforms per stage instead of
+// Nchi^2.  One MirrorTerm is a transformed base pair (m,l) (output a+No*b,
+// G element ef) and, if mirror != 0, its partner (l,m) (output b+No*a, ef_t).
+struct MirrorTerm {
+  int m, l, ef, ef_t, mirror, out_t;  // out_t: partner goes to the second output
+  double dstat;                        // stat_lm - stat_ml
+};
+
+// d(k) of every mirrored term at slot 0 (natural grid order), nt arrays of Nkall
+template <typename R>
+__global__ void k_mirror_delta0(cx<R>* out, const cx<R>* V, const MirrorTerm* terms, const int* grid_irr,
+                                const int* grid_flag, long long Nkall, int Nk, int Nw, int Nchi) {
+  const MirrorTerm t = terms[blockIdx.y];
+  cx<R>* o = out + (long long)blockIdx.y * Nkall;
+  for (long long gi = blockIdx.x * (long long)blockDim.x + threadIdx.x; gi < Nkall;
+       gi += (long long)gridDim.x * blockDim.x) {
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    const cx<R> vlm = V[fidx(k, 0, t.l, t.m, Nk, Nw, Nchi)], vml = V[fidx(k, 0, t.m, t.l, Nk, Nw, Nchi)];
+    o[gi] = t.mirror ? (fl ? vml - conj(vlm) : vlm - conj(vml)) : cmk<R>(0, 0);
+  }
+}
+
+// T0 = sum_t W_t G_ef(t) (+ mirrored partners with out_t == 0),
+// T1 = sum of the mirrored partners with out_t == 1.
+template <typename R>
+__global__ void k_contract_mirror(cx<R>* T0, cx<R>* T1, const cx<R>* W, const cx<R>* F, const cx<R>* D,
+                                  const MirrorTerm* terms, int nt, long long P, long long Nkall, int Nx, int Ny,
+                                  const int* rev_x, const int* rev_y, const int* rev_z, const int* log_t) {
+  const R nk = (R)Nkall;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long s = idx % Nkall, pt = idx / Nkall;
+    const int px = (int)(s % Nx), py = (int)((s / Nx) % Ny), pz = (int)(s / ((long long)Nx * Ny));
+    const long long s_m = rev_x[px] + (long long)Nx * (rev_y[py] + (long long)Ny * rev_z[pz]);
+    const long long idx_m = s_m + Nkall * pt;
+    const R sgn = (log_t[pt] & 1) ? (R)-1 : (R)1;
+    cx<R> a0 = cmk<R>(0, 0), a1 = cmk<R>(0, 0);
+    for (int i = 0; i < nt; ++i) {
+      const MirrorTerm t = terms[i];
+      const cx<R>* Wt = W + (long long)i * P;
+      a0 += Wt[idx] * F[(long long)t.ef * P + idx];
+      if (t.mirror) {
+        cx<R> wm = conj(Wt[idx_m]) + D[(long long)i * Nkall + s];
+        if (s == 0) wm.x += sgn * nk * (R)t.dstat;
+        const cx<R> c = wm * F[(long long)t.ef_t * P + idx];
+        if (t.out_t) a1 += c;
+        else a0 += c;
+      }
+    }
+    T0[idx] = a0;
+    if (T1) T1[idx] = a1;
+  }
+}
+
 template <typename R>
 void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, const double* S, const double* C,
            double temp, double2* sig) {
   cudaStream_t st = ctx().stream;
   const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, (int)g.M, (int)sizeof(cx<R>));
-  const int No2 = g.Norb * g.Norb;
+  const FFT4D& fft3 = fft_plan(g.Nx, g.Ny, g.Nz, 1, (int)sizeof(cx<R>));
+  const int No = g.Norb, No2 = No * No, Nchi = g.Nchi;
   DBuf<cx<R>> F((size_t)No2 * g.P);
   pad_green_all<R>(g, G, F.p);
   fft.forward<R>(F.p, No2, st);
-  std::vector<double> hS(g.Nchi * g.Nchi), hC(g.Nchi * g.Nchi);
+  std::vector<double> hS(Nchi * Nchi), hC(Nchi * Nchi);
   PGB_CUDA(cudaMemcpyAsync(hS.data(), S, sizeof(double) * hS.size(), cudaMemcpyDeviceToHost, st));
   PGB_CUDA(cudaMemcpyAsync(hC.data(), C, sizeof(double) * hC.size(), cudaMemcpyDeviceToHost, st));
   sync();
-  size_t maxt = 0;
-  for (auto& v : p.sigma) maxt = std::max(maxt, v.size());
-  DBuf<cx<R>> W(std::max<size_t>(1, maxt) * g.P), T(g.P);
-  DBuf<BosonTerm> dterms(std::max<size_t>(1, maxt));
-  DBuf<int> def(std::max<size_t>(1, maxt));
+  auto stat = [&](int m, int l) { return 1.5 * hS[m + Nchi * l] - 0.5 * hC[m + Nchi * l]; };
+  // groups: output e = a + No*b with a <= b, together with its transpose
+  struct Group { int e, et; std::vector<MirrorTerm> terms; };
+  std::vector<Group> groups;
+  for (int b = 0; b < No; ++b)
+    for (int a = 0; a <= b; ++a) {
+      Group gr{a + No * b, b + No * a, {}};
+      for (const Term& t : p.sigma[gr.e]) {
+        if (a == b && t.m > t.l) continue;  // covered as the mirror of (l,m)
+        MirrorTerm mt{};
+        mt.m = t.m;
+        mt.l = t.l;
+        mt.ef = t.ef;
+        mt.mirror = (t.m != t.l);
+        mt.ef_t = p.o2[t.l] + No * p.o2[t.m];
+        mt.out_t = (a != b);
+        mt.dstat = mt.mirror ? stat(t.l, t.m) - stat(t.m, t.l) : 0.0;
+        gr.terms.push_back(mt);
+      }
+      if (a != b || !gr.terms.empty()) groups.push_back(std::move(gr));
+    }
+  size_t maxt = 1;
+  for (auto& gr : groups) maxt = std::max(maxt, gr.terms.size());
+  DBuf<cx<R>> W(maxt * g.P), T((size_t)2 * g.P), Dm(maxt * g.Nkall);
+  DBuf<BosonTerm> dterms(maxt);
+  DBuf<MirrorTerm> mterms(maxt);
   PGB_CUDA(cudaMemsetAsync(sig, 0, sizeof(double2) * (size_t)g.K * No2, st));
   const double scale = temp / (double)g.Nkall / (double)g.P;
-  for (int e = 0; e < No2; ++e) {
-    const auto& terms = p.sigma[e];
-    if (terms.empty()) continue;
-    const int nt = (int)terms.size();
+  for (const Group& gr : groups) {
+    const int nt = (int)gr.terms.size();
+    const bool two = gr.e != gr.et;
+    if (nt == 0) continue;
     std::vector<BosonTerm> ht(nt);
-    std::vector<int> hef(nt);
-    for (int t = 0; t < nt; ++t) {
-      const int m = terms[t].m, l = terms[t].l;
-      ht[t] = BosonTerm{m, l, 1.5 * hS[m + g.Nchi * l] - 0.5 * hC[m + g.Nchi * l]};
-      hef[t] = terms[t].ef;
-    }
+    for (int t = 0; t < nt; ++t) ht[t] = BosonTerm{gr.terms[t].m, gr.terms[t].l, stat(gr.terms[t].m, gr.terms[t].l)};
     dterms.upload(ht.data(), nt);
-    def.upload(hef.data(), nt);
-    dim3 gr(grid_1d(g.P, 256, 4096), nt);
-    k_pad_boson<R><<<gr, 256, 0, st>>>(W.p, V, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw,
-                                        g.Nchi, g.P);
+    mterms.upload(gr.terms.data(), nt);
+    dim3 grd(grid_1d(g.P, 256, 4096), nt);
+    k_pad_boson<R><<<grd, 256, 0, st>>>(W.p, V, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, Nchi,
+                                         g.P);
     count_launch("pad_boson");
     fft.forward<R>(W.p, nt, st);
-    k_contract<R><<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(T.p, W.p, F.p, def.p, nt, g.P);
-    count_launch("contract");
-    fft.backward<R>(T.p, 1, st);
-    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)e * g.K, T.p, sizeof(R) == 8,
+    dim3 grd0(grid_1d(g.Nkall, 256, 4096), nt);
+    k_mirror_delta0<R><<<grd0, 256, 0, st>>>(Dm.p, V, mterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw,
+                                              Nchi);
+    count_launch("mirror_delta0");
+    fft3.forward<R>(Dm.p, nt, st);
+    k_contract_mirror<R><<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(
+        T.p, two ? T.p + g.P : nullptr, W.p, F.p, Dm.p, mterms.p, nt, g.P, g.Nkall, g.Nx, g.Ny, fft.d_rev(0),
+        fft.d_rev(1), fft.d_rev(2), fft.d_logical(3));
+    count_launch("contract_mirror");
+    fft.backward<R>(T.p, two ? 2 : 1, st);
+    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.e * g.K, T.p, sizeof(R) == 8,
                                                              g.irr_grid.p, g.Nkall, g.Nk, g.Nw, scale, 1);
     count_launch("scatter_sigma");
-    sync();  // host term buffers are reused by the next element
+    if (two) {
+      k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.et * g.K, T.p + g.P, sizeof(R) == 8,
+                                                               g.irr_grid.p, g.Nkall, g.Nk, g.Nw, scale, 1);
+      count_launch("scatter_sigma");
+    }
+    sync();  // host term buffers are reused by the next group
   }
 }
 

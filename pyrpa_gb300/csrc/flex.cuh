@@ -125,6 +125,14 @@ void axpy(double2* y, double2 a, const double2* x, long long n);         // y +=
 void scal(double2* y, double a, long long n);
 void lincomb(double2* y, const double2* const* xs, const double2* cs, int m, long long n);
 
+// Seed for a fine-mesh FLEX solve from a coarse-mesh one: Sigma on the coarse
+// irreducible mesh gc (Nw_c frequencies) is Fourier-interpolated in k to the
+// fine mesh gf (zero padding of Sigma(R), the Nyquist planes split in half) and
+// extended from Nw_c to Nw_f frequencies with the tail c0 + c1/(i w) through
+// two interior frequencies.  Both meshes share T; coarse k points must lie on
+// the fine mesh (Nx_f a multiple of Nx_c, and so on).
+void sigma_interp(const Geom& gc, const Geom& gf, const double2* sig_c, double2* sig_f, int Norb, double temp);
+
 // small host helpers
 void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc);
 template <typename R> void widen(double2* out, const cx<R>* in, long long n);

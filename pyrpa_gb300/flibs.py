@@ -60,7 +60,7 @@ _SIGNATURES = {
     "conv_delta_orb_to_band": [_c128, _c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi],
     "pyrpa_gb_flex_eliash": [_c128, _pd, _c128, _pd, _pd, _f64, _f64, _f64, _i64, _i64, _i64, _c128, _f64, _c128,
                              _f64, _f64, ctypes.c_void_p, _pd, _pd, _pd, _pd, _pd, _pi, _pd, _pd] + [_pi] * 10
-    + [_pb, _pb, _pi, _pi, _pi, _pd],
+    + [_pb, _pb, _pi, _pi, _pi, _pd, _i64],
     "pyrpa_gb_set_precision": [_pi],
     "pyrpa_gb_get_precision": [_pi],
     "pyrpa_gb_set_verbose": [_pi],
@@ -102,21 +102,33 @@ def dbl(v):
     return byref(c_double(float(v)))
 
 
+def last_error() -> str:
+    """Message of the last failure recorded by the library ('' if none)."""
+    lib = load_library()
+    code = c_int64(0)
+    buf = ctypes.create_string_buffer(2048)
+    lib.pyrpa_gb_last_error(buf, i64(len(buf)), byref(code))
+    return buf.value.decode(errors="replace") if code.value else ""
+
+
 def _call(name, *args):
     lib = load_library()
     lib.pyrpa_gb_clear_error()
     getattr(lib, name)(*args)
-    code = c_int64(0)
-    buf = ctypes.create_string_buffer(2048)
-    lib.pyrpa_gb_last_error(buf, i64(len(buf)), byref(code))
-    if code.value:
-        raise RuntimeError(buf.value.decode(errors="replace"))
+    msg = last_error()
+    if msg:
+        raise RuntimeError(msg)
 
 
 # ------------------------------------------------------------------ control
+MIXED = 3264
+
+
 def set_precision(bits: int) -> None:
     """64: FP64 everywhere (the reference's arithmetic); 32: complex FP32 FFTs,
-    contractions and vertex solves, FP64 for G, Sigma, mu, DIIS and lambda."""
+    contractions and vertex solves, FP64 for G, Sigma, mu, DIIS and lambda;
+    3264 (MIXED): as 32, but the FLEX loop finishes on FP64 bulk once its
+    residual reaches the FP32 rounding floor."""
     load_library().pyrpa_gb_set_precision(i64(bits))
 
 
@@ -137,10 +149,11 @@ def kernel_launches() -> int:
 
 
 def last_stats() -> dict:
-    out = np.zeros(14)
+    out = np.zeros(16)
     load_library().pyrpa_gb_last_stats(out)
     keys = ["iterations", "esterr", "stoner", "mu", "lambda", "applies", "t_chi0_ms", "t_vertex_ms",
-            "t_sigma_ms", "t_diis_ms", "t_mu_ms", "t_dyson_ms", "t_apply_ms"]
+            "t_sigma_ms", "t_diis_ms", "t_mu_ms", "t_dyson_ms", "t_apply_ms", "iterations_fp32",
+            "iterations_coarse", "t_warm_ms"]
     return dict(zip(keys, out[: len(keys)].tolist()))
 
 
@@ -361,6 +374,10 @@ def get_Vsigma_nosoc_flex(chi, Smat, Cmat):
     """V_sigma in place; like the reference wrapper it passes Nk=len(chi),
     Nw=len(chi[0]) (libs/flibs/_selfenergy.py:60-73)."""
     Nk, Nw, Nchi = len(chi), len(chi[0]), len(Smat)
+    if Nk * Nw * Nchi * Nchi > np.asarray(chi).size:
+        # the reference library would read past the end of the buffer here
+        raise ValueError(f"chi holds {np.asarray(chi).size} elements, the call reads Nk*Nw*Nchi^2 = "
+                         f"{Nk * Nw * Nchi * Nchi} (Nk=len(chi), Nw=len(chi[0]) as in the reference wrapper)")
     _call("get_vsigma_flex_nosoc_", chi, Smat, Cmat, i64(Nk), i64(Nw), i64(Nchi))
     return chi.copy()
 
@@ -449,13 +466,17 @@ def flex_eliash(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, init_delta, plist
                 temp: float, Nw: int, Nx: int, Ny: int, Nz: int, gap_sym: int, sub_sigma: int = 1,
                 scf_loop: int = 300, eps: float = 1.0e-4, pp: float = 0.5, m_diis: int = 5,
                 sw_rescale: bool = True, sw_tail: bool = False, arnoldi_m: int = 10, itemax: int = 300,
-                eps_eliash: float = 1.0e-5, sigma_seed=None, seed_mu: float = 0.0, seed_mu_old: float = 0.0):
+                eps_eliash: float = 1.0e-5, sigma_seed=None, seed_mu: float = 0.0, seed_mu_old: float = 0.0,
+                coarse=(1, 1)):
     """mkself -> gen_green -> get_chi0(_tail) -> linearized_eliashberg in one
     device-resident call (libs/plibs/_calc.py:370-405 with sw_self=True).
 
     Returns a dict with sigmak [Norb,Norb,Nw,Nk], mu, gap, lambda, stoner and
     the H2D / device / D2H milliseconds of the call.  ``sigma_seed`` (same
-    layout as sigmak) starts the loop from a given self-energy."""
+    layout as sigmak) starts the loop from a given self-energy.  ``coarse`` =
+    (k divisor, frequency divisor) other than (1, 1) first solves the model on
+    the k mesh and Matsubara set divided by them (FP32 bulk, down to the FP32
+    rounding floor) and starts the fine loop from its interpolated Sigma."""
     Nkall, Nk, Nchi = len(kmap), len(hamk), len(Smat)
     Norb = hamk.shape[1]
     sigmak = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
@@ -473,6 +494,6 @@ def flex_eliash(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, init_delta, plist
           seed_ptr, dbl(seed_mu), dbl(seed_mu_old), dbl(mu), dbl(fill), dbl(temp), i64(scf_loop), dbl(pp), dbl(eps),
           i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(Nchi), i64(Nx), i64(Ny), i64(Nz), i64(sub_sigma),
           i64(m_diis), byref(c_bool(sw_rescale)), byref(c_bool(sw_tail)), i64(gap_sym), i64(arnoldi_m),
-          i64(itemax), dbl(eps_eliash))
+          i64(itemax), dbl(eps_eliash), np.asarray(coarse, dtype=np.int64))
     return dict(sigmak=sigmak, mu=mu_o.value, gap=gap, lam=lam.value, stoner=st.value,
                 h2d_ms=times[0], compute_ms=times[1], d2h_ms=times[2])

@@ -330,3 +330,63 @@ def test_fp32_bulk_path(F):
     sg64, mu64 = F.mkself(*args, eps=1e-6, pp=0.5, sw_tail=True, sw_rescale=True)
     close(sg32, sg64, 1e-4, 1e-7)
     assert abs(mu32 - mu64) < 1e-5
+
+
+# ---------------------------------------------- register vertex, 16 and 25 pairs
+@pytest.mark.parametrize("Norb", [4, 5])
+@pytest.mark.parametrize("mode", ["fp64", "fp32", "fp32-vs"])
+def test_vertex_large_orbital_counts(F, Norb, mode):
+    """V_sigma and V_Delta for Nchi = 16 and 25 (the register kernels with the
+    shared-memory accumulator in FP64) against the oracle."""
+    m = build_model(Norb, 2, 2, 1, 2, 0.2, 0.0, seed=11, U=1.0, J=0.15)
+    rng = np.random.default_rng(Norb)
+    Nchi, Nk = Norb * Norb, len(m["klist"])
+    # the wrapper reads len(chi) x len(chi[0]) matrices (its Nk and Nw), so the
+    # V_sigma input is (Nchi, Nchi, Nchi, Nchi): Nchi^2 matrices
+    cs = (Nchi, Nchi, Nchi, Nchi)
+    chis = 0.05 * (rng.standard_normal(cs) + 1j * rng.standard_normal(cs))
+    chi = 0.05 * (rng.standard_normal((Nchi, Nchi, 2, Nk)) + 1j * rng.standard_normal((Nchi, Nchi, 2, Nk)))
+    prec, tol = (64, (1e-11, 1e-14)) if mode == "fp64" else (32, (2e-5, 1e-8))
+    old = os.environ.get("PYRPA_GB_VERTEX")
+    F.set_precision(prec)
+    try:
+        if mode == "fp32-vs":
+            os.environ["PYRPA_GB_VERTEX"] = "vs"
+        v = F.get_Vsigma_nosoc_flex(chis.copy(), m["S"], m["C"])
+    finally:
+        F.set_precision(64)
+        if old is None:
+            os.environ.pop("PYRPA_GB_VERTEX", None)
+        else:
+            os.environ["PYRPA_GB_VERTEX"] = old
+    close(v, O.get_Vsigma_nosoc_flex(chis.copy(), m["S"], m["C"]), *tol)
+    if mode != "fp64":
+        return
+    from oracle import flex_oracle as FO
+    init = F.get_initial_gap(m["klist"], Norb, 0)
+    for gap_sym in (0, -1):
+        c1 = chi.copy()
+        F.linearized_eliashberg(c1, m["Gk"], m["uni"], init, m["S"], m["C"], m["olist"], np.ones(Norb), m["kmap"],
+                                m["invk"], 2, 2, 1, m["temp"], gap_sym, eps=1e-6, itemax=2, arnoldi_m=2)
+        vd = FO.vdelta_nsoc_flex(chi.T, m["S"].T, m["C"].T, gap_sym >= 0).T
+        close(c1, vd, 1e-11, 1e-14)
+
+
+# ------------------------------------------------------ mixed FP32/FP64 schedule
+def test_mixed_schedule_matches_fp64(F):
+    """FP32 bulk until the FP32 floor, then FP64 to eps: the converged Sigma and
+    mu equal the all-FP64 solve's to the convergence tolerance."""
+    m = build_model(2, 8, 8, 1, 32, 0.1, 0.0, U=0.8, J=0.1)
+    args = (m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"], 0.9,
+            m["temp"], m["Nw"], 8, 8, 1, False, False)
+    F.set_precision(F.MIXED)
+    try:
+        sgm, mum = F.mkself(*args, eps=1e-8, pp=0.5, sw_tail=True, sw_rescale=True)
+        st = F.last_stats()
+    finally:
+        F.set_precision(64)
+    assert 0 < st["iterations_fp32"] < st["iterations"], st
+    assert st["esterr"] < 1e-8
+    sg64, mu64 = F.mkself(*args, eps=1e-8, pp=0.5, sw_tail=True, sw_rescale=True)
+    close(sgm, sg64, 1e-6, 1e-9)
+    assert abs(mum - mu64) < 1e-8
