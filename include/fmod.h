@@ -201,6 +201,24 @@ void pyrpa_gb_flex_eliash(double* sigmak, double* mu, double* delta, double* lam
  * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"
  * so that `import libs.flibs` binds every name it expects. */
 
+/* Allocation-free variant of get_eig_or_tr_chi.  No counterpart in the reference.
+ * All pointers are DEVICE pointers in the layouts of get_eig_or_tr_chi: chi
+ * (Nk,Nchi,Nchi) complex128, invk (3,Nkall) int64, chiqout (Nkall) complex128.
+ * The work is enqueued on `stream` (a cudaStream_t; NULL = the default stream)
+ * and the call returns without waiting; chiqout is ready when the stream gets
+ * there.  It allocates no device memory: the per-q scratch is a fixed 1 MiB
+ * device array, so Nk is limited to 65,536 (larger Nk is rejected with an
+ * error).  Nothing in the scratch has to start at zero: each call writes the
+ * Nk values it reads.  An invk(1,i) outside [1,Nk] gives NaN at chiqout(i).
+ * The first call on a device does a one-time set-up (it
+ * looks up the scratch address and launches each kernel once, empty); make
+ * that first call before any stream capture.  Calls whose work overlaps on
+ * the device (different streams, or threads) share the one scratch array and
+ * race: order them on one stream.  Returns 0 on success, 1 on an error whose
+ * message pyrpa_gb_last_error returns. */
+int pyrpa_gb_eig_or_tr_chi_noalloc(void* chiqout, const void* chi, const int64_t* invk, int64_t Nkall,
+                                   int64_t Nk, int64_t Nchi, int32_t sw_eig, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

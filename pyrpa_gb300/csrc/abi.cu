@@ -371,6 +371,35 @@ double chi0_entry(double2* chi_out, const double* Smat, const double* Cmat, cons
 }
 }  // namespace
 
+// ============================================== allocation-free variant ==
+// pyrpa_gb_eig_or_tr_chi_noalloc computes what get_eig_or_tr_chi computes, on
+// buffers that are already in device memory, and takes no device memory of
+// its own while it runs.  It serves callers that cannot let a library
+// allocate: a host framework whose own caching allocator has reserved nearly
+// all of HBM (an allocation by this library could then fail for want of
+// memory), and loops that enqueue work on their own stream and must not wait
+// for an allocation or a host copy on every call.  Its only scratch, one value
+// per irreducible q point, is the fixed array below.
+namespace {
+// 65,536 irreducible q points at most: 1 MiB, reserved when the library loads
+constexpr int64_t kNoAllocMaxNk = 65536;
+__device__ __align__(256) double2 g_noalloc_vals[kNoAllocMaxNk];
+constexpr int kNoAllocMaxDevices = 64;
+double2* g_noalloc_ptr[kNoAllocMaxDevices] = {};  // address of the array on each device
+std::mutex g_noalloc_mu;
+
+// k_map_full with the irreducible index checked: an invk(1,i) outside [1,Nk]
+// gives NaN instead of a read outside the scratch
+__global__ void k_map_full_checked(double2* out, const double2* vals, const int64_t* invk, int64_t Nkall,
+                                   int64_t Nk) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nkall;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int64_t k = invk[3 * i];
+    out[i] = (k >= 1 && k <= Nk) ? vals[k - 1] : make_double2(nan(""), nan(""));
+  }
+}
+}  // namespace
+
 #define ABI_TRY try {
 #define ABI_CATCH(name, onerr)            \
   }                                       \
@@ -934,5 +963,48 @@ PGB_STUB(pade_with_trace)
 PGB_STUB(phiq_map)
 PGB_STUB(riccati_chords)
 PGB_STUB(solve_cpa_array)
+
+// ============================================== allocation-free variant ==
+int pyrpa_gb_eig_or_tr_chi_noalloc(void* chiqout_v, const void* chi_v, const int64_t* invk, int64_t Nkall,
+                                   int64_t Nk, int64_t Nchi, int32_t sw_eig, void* stream) {
+  double2* chiqout = static_cast<double2*>(chiqout_v);
+  const double2* chi = static_cast<const double2*>(chi_v);
+  try {
+    if (Nk < 1 || Nk > kNoAllocMaxNk)
+      throw Error("Nk = " + std::to_string(Nk) + " is outside [1, 65536], the size of the fixed scratch");
+    if (Nchi < 1 || Nchi > kMaxChi) throw Error("Nchi above the engine limit of 32 orbital pairs");
+    if (Nkall < 1) throw Error("Nkall must be positive");
+    if (!chiqout || !chi || !invk) throw Error("null device pointer");
+    int dev = -1;
+    PGB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) throw Error("device ordinal above 63");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    double2* vals = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(g_noalloc_mu);
+      if (!g_noalloc_ptr[dev]) {
+        // set-up, once per device: the address of the scratch on this device,
+        // and one empty launch of each kernel, so that whatever the driver
+        // reserves for them (local memory of the eigenvalue kernel) is
+        // reserved now rather than on a later call
+        void* p = nullptr;
+        PGB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_vals));
+        k_eig_or_tr<<<1, 32, 0, st>>>(static_cast<double2*>(p), chi, 0, (int)Nchi, 1);
+        k_map_full_checked<<<1, 32, 0, st>>>(chiqout, static_cast<double2*>(p), invk, 0, Nk);
+        PGB_CUDA(cudaGetLastError());
+        g_noalloc_ptr[dev] = static_cast<double2*>(p);
+      }
+      vals = g_noalloc_ptr[dev];
+    }
+    k_eig_or_tr<<<g1(Nk, 32), 32, 0, st>>>(vals, chi, Nk, (int)Nchi, sw_eig ? 1 : 0);
+    k_map_full_checked<<<g1(Nkall, 256), 256, 0, st>>>(chiqout, vals, invk, Nkall, Nk);
+    PGB_CUDA(cudaGetLastError());
+    ctx().kernel_launches += 2;
+    return 0;
+  } catch (const std::exception& e) {
+    report("pyrpa_gb_eig_or_tr_chi_noalloc", e.what());
+    return 1;
+  }
+}
 
 }  // extern "C"

@@ -370,6 +370,22 @@ def get_eig_or_tr_chi(chi, invk, sw_eig: bool):
     return out
 
 
+def eig_or_tr_chi_noalloc(out_ptr: int, chi_ptr: int, invk_ptr: int, Nkall: int, Nk: int, Nchi: int,
+                          sw_eig: bool, stream: int = 0) -> None:
+    """get_eig_or_tr_chi on device buffers (integer device addresses), enqueued
+    on `stream` without allocating device memory; Nk <= 65536.  One call at a
+    time per device: overlapping calls share the entry's fixed scratch."""
+    lib = load_library()
+    f = lib.pyrpa_gb_eig_or_tr_chi_noalloc
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_int64, c_int64, c_int64, ctypes.c_int32,
+                  ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    lib.pyrpa_gb_clear_error()
+    rc = f(out_ptr, chi_ptr, invk_ptr, Nkall, Nk, Nchi, 1 if sw_eig else 0, stream or None)
+    if rc != 0:
+        raise RuntimeError(last_error())
+
+
 def get_Vsigma_nosoc_flex(chi, Smat, Cmat):
     """V_sigma in place; like the reference wrapper it passes Nk=len(chi),
     Nw=len(chi[0]) (libs/flibs/_selfenergy.py:60-73)."""
