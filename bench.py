@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--eps", type=float, default=1.0e-4)
     p.add_argument("--scf-loop", type=int, default=300)
     p.add_argument("--no-tail", action="store_true")
+    p.add_argument("--coarse", default="2,2",
+                   help="warm start: k-mesh and frequency divisors of the coarse solve ('1,1' = cold start)")
     p.add_argument("--cpu-pairs", type=int, default=0, help="orbital pairs in the CPU sample (0: one per core)")
     p.add_argument("--flex-iters", type=int, default=0)
     p.add_argument("--applies", type=int, default=0)
@@ -184,7 +186,7 @@ def main():
                           f"{cfg['Nw']} Matsubara, FLEX+linearized Eliashberg",
               "Norb": cfg["Norb"], "k_mesh": [cfg["Nx"], cfg["Ny"], cfg["Nz"]], "Nw": cfg["Nw"],
               "U": cfg["U"], "J": cfg["J"], "T": cfg["temp"], "fill_per_spin": cfg["fill"], "eps": a.eps,
-              "chi0": "tail-corrected" if tail else "sharp cutoff", "warm_start": "none (cold G0 start)",
+              "chi0": "tail-corrected" if tail else "sharp cutoff",
               "parallelism": f"replicas x{a.gpus}" if a.gpus > 1 else "single GPU",
               "l2": "inputs larger than L2 (FFT arrays >= 134 MB); no flush"}
 
@@ -216,8 +218,12 @@ def main():
     F.set_precision({"mixed": F.MIXED, "32": 32, "64": 64}[a.precision])
     m = models.prepare(a.config)
     c = m["cfg"]
+    coarse = tuple(int(x) for x in a.coarse.split(","))
     call = dict(mu=m["mu"], fill=c["fill"], temp=c["temp"], Nw=c["Nw"], Nx=c["Nx"], Ny=c["Ny"], Nz=c["Nz"],
-                gap_sym=c["gap_sym"], eps=a.eps, scf_loop=a.scf_loop, sw_tail=tail, sw_rescale=True)
+                gap_sym=c["gap_sym"], eps=a.eps, scf_loop=a.scf_loop, sw_tail=tail, sw_rescale=True, coarse=coarse)
+    config["warm_start"] = ("none (cold G0 start)" if coarse == (1, 1) else
+                            f"coarse-mesh seed: {c['Nx'] // coarse[0]}x{c['Ny'] // coarse[0]} k mesh, "
+                            f"{c['Nw'] // coarse[1]} frequencies, FP32 bulk, interpolated to the full mesh")
 
     def solve():
         return F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
@@ -264,6 +270,8 @@ def main():
     rate, cores, npairs, cwall = cpu_pair_rate(c, a.cpu_pairs)
     cpu_v = cpu_seconds(c, tail, iters, applies, rate)
     config.update({"flex_iterations": iters, "eliashberg_applications": applies, "lambda": res["lam"],
+                   "warm_start_iterations": int(stats["iterations_coarse"]),
+                   "warm_start_ms": stats["t_warm_ms"],
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
                    "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, then FP64 bulk "
                                           f"to eps; Eliashberg FP32 bulk with FP64 Arnoldi",

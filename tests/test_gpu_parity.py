@@ -390,3 +390,25 @@ def test_mixed_schedule_matches_fp64(F):
     sg64, mu64 = F.mkself(*args, eps=1e-8, pp=0.5, sw_tail=True, sw_rescale=True)
     close(sgm, sg64, 1e-6, 1e-9)
     assert abs(mum - mu64) < 1e-8
+
+
+# ------------------------------------------------------ coarse-mesh warm start
+@pytest.mark.parametrize("dims,Nw", [((8, 8, 1), 32), ((4, 4, 4), 8)])
+def test_warm_start_reaches_the_cold_fixed_point(F, dims, Nw):
+    """The fused solve from a coarse-mesh seed converges to the same Sigma,
+    mu and lambda as the cold start (FP64 bulk, eps 1e-8)."""
+    Nx, Ny, Nz = dims
+    m = build_model(2, Nx, Ny, Nz, Nw, 0.1, 0.0, seed=21 if Nz > 1 else 0, U=0.8, J=0.1)
+    init = F.get_initial_gap(m["klist"], 2, 0)
+    kw = dict(eps=1e-8, scf_loop=200, sw_tail=True, sw_rescale=True, arnoldi_m=20)
+    args = (m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], init, np.ones(2),
+            m["mu"], 0.9, m["temp"], Nw, Nx, Ny, Nz, 0)
+    cold = F.flex_eliash(*args, **kw)
+    st_cold = F.last_stats()
+    warm = F.flex_eliash(*args, coarse=(2, 2), **kw)
+    st_warm = F.last_stats()
+    assert st_warm["iterations_coarse"] > 0 and st_cold["iterations_coarse"] == 0
+    assert st_warm["iterations"] <= st_cold["iterations"], (st_warm, st_cold)
+    close(warm["sigmak"], cold["sigmak"], 1e-6, 1e-9)
+    assert abs(warm["mu"] - cold["mu"]) < 1e-8
+    assert abs(warm["lam"] - cold["lam"]) <= 1e-6 * max(1.0, abs(cold["lam"]))
