@@ -158,8 +158,8 @@ void pyrpa_gb_kernel_launches(int64_t* n);
 /* statistics of the last mkself / lin_eliash: iterations, esterr, Stoner, mu, lambda,
  * Eliashberg applications, then device milliseconds of chi0, vertex, Sigma, DIIS,
  * mu, Dyson, Eliashberg applications, then the FLEX iterations run on FP32 bulk,
- * the FLEX iterations of a coarse-mesh warm start and its device milliseconds
- * (16 doubles) */
+ * the FLEX iterations of a coarse-mesh warm start and its device milliseconds,
+ * and the device milliseconds of the Stoner factors in the FLEX loop (17 doubles) */
 void pyrpa_gb_last_stats(double* out);
 void pyrpa_gb_device_info(int64_t* num_sms, int64_t* device);
 /* live timing of the FFT pass kernel: when on, every pass launch is bracketed

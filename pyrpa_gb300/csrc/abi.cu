@@ -436,9 +436,9 @@ void pyrpa_gb_clear_error() {
 void pyrpa_gb_kernel_launches(int64_t* n) { *n = ctx().kernel_launches; }
 void pyrpa_gb_last_stats(double* out) {
   const LastStats& s = last_stats();
-  const double v[16] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
+  const double v[17] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
                         s.t_vertex, s.t_sigma, s.t_diis, s.t_mu, s.t_dyson, s.t_apply, (double)s.iterations32,
-                        (double)s.iterations_coarse, s.t_warm};
+                        (double)s.iterations_coarse, s.t_warm, s.t_stoner};
   memcpy(out, v, sizeof(v));
 }
 void pyrpa_gb_fft_profile(const int64_t* on) { fft_profile_enable(*on != 0); }

@@ -280,7 +280,7 @@ double stage_chi0(Inputs& in, const FlexParams& a, const double2* G, double mu, 
     log("[FLEX] Stoner factor=%10.6f >= 1: rescaling chi0 to%7.4f\n", sdw, rt);
     scale_chi<R>(chi, g.K * in.Nchi * in.Nchi, rt / sdw);
   }
-  g_stats.t_vertex += tm.stop();
+  g_stats.t_stoner += tm.stop();
   return sdw;
 }
 template <typename R>
@@ -318,6 +318,13 @@ double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, i
   if (s2) stage_sigma<float>(in, a, G, chi32.p, sig);
   else stage_sigma<double>(in, a, G, chi64.p, sig);
   return sdw;
+}
+
+// PYRPA_GB_MIX_DIIS=keep keeps the FP32-phase DIIS history across the switch
+// to FP64 bulk (default: a fresh history)
+bool mix_diis_reset() {
+  const char* s = std::getenv("PYRPA_GB_MIX_DIIS");
+  return !(s && std::string(s) == "keep");
 }
 
 // Stages that the FP32 phase of the FLEX loop runs in FP32 (default all):
@@ -565,6 +572,12 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
       log("[FLEX] residual%9.2E on FP32 bulk: continuing with FP64 bulk\n", esterr);
       use32 = false;
       chi32.release();
+      if (mix_diis_reset()) {
+        // the FP32 entries carry the FP32 rounding floor in their residuals;
+        // the FP64 phase starts a fresh history from the current Sigma
+        n_hist = 0;
+        i_hist = 0;
+      }
     }
     tm.start();
     renew_mu();

@@ -104,6 +104,7 @@ struct LastStats {
   int applies = 0;
   // milliseconds on the device (CUDA events on the library stream)
   double t_chi0 = 0, t_vertex = 0, t_sigma = 0, t_diis = 0, t_mu = 0, t_dyson = 0, t_apply = 0;
+  double t_stoner = 0;  // Stoner factor (and the sw_rescale clamp) of the FLEX loop
 };
 
 // precision schedule of the FLEX loop: 64, 32 or kPrecMixed

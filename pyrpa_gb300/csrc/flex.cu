@@ -362,9 +362,17 @@ void pad_green_all(const Geom& g, const double2* G, cx<R>* out) {
 }
 
 // ================================================================== chi0 ==
+// One backward transform of chi0: pair (l,m) written at element (m,l) and its
+// exchange partner (m2,l2).  If has_d, the same transform also yields the
+// swapped pair (m,l): chi_ml(q,nu) = conj chi_lm(q,-nu) holds term by term
+// (padding, product, analytic tau reference; the sawtooth coefficient is its
+// own dJ), so the swapped pair is read from the negative frequencies and
+// written at (dm,dl) and its partner (dm2,dl2).
 struct ChiDev {
-  int m, l, m2, l2, e13, e42, self, pad;
+  int m, l, m2, l2, e13, e42, self, has_d;
   double2 J;
+  int dm, dl, dm2, dl2;
+  double2 dJ;
 };
 
 template <typename R>
@@ -419,6 +427,15 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
     if (fabs(v.y) < (R)kThresh) v.y = 0;
     chi[fidx(k, j, pr.m, pr.l, Nk, Nw, Nchi)] = v;
     if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = conj(v);
+    if (pr.has_d) {
+      const long long M = 2LL * Nw;
+      cx<R> d = conj(t[irr_grid[k] + Nkall * ((M - j) % M)]);
+      if (sawc) d += cmk<R>((R)pr.dJ.x, (R)pr.dJ.y) * sawc[j];
+      if (fabs(d.x) < (R)kThresh) d.x = 0;
+      if (fabs(d.y) < (R)kThresh) d.y = 0;
+      chi[fidx(k, j, pr.dm, pr.dl, Nk, Nw, Nchi)] = d;
+      chi[fidx(k, j, pr.dm2, pr.dl2, Nk, Nw, Nchi)] = conj(d);
+    }
   }
 }
 
@@ -519,6 +536,12 @@ __global__ void k_sawc(double2* sawc, int Nw, int M, double temp) {
   sawc[j] = v;
 }
 
+// PYRPA_GB_CHI0_SWAP=0 computes every exchange class with its own transform
+bool chi0_swap_enabled() {
+  const char* s = std::getenv("PYRPA_GB_CHI0_SWAP");
+  return !(s && std::string(s) == "0");
+}
+
 template <typename R>
 void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const TailRef* tail, cx<R>* chi) {
   cudaStream_t st = ctx().stream;
@@ -531,7 +554,33 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
   std::vector<ChiDev> hp(p.chi.size());
   for (size_t i = 0; i < p.chi.size(); ++i) {
     const ChiPair& c = p.chi[i];
-    hp[i] = ChiDev{c.m, c.l, c.m2, c.l2, c.e13, c.e42, c.self, 0, make_double2(0, 0)};
+    hp[i] = ChiDev{c.m, c.l, c.m2, c.l2, c.e13, c.e42, c.self, 0, make_double2(0, 0), 0, 0, 0, 0,
+                   make_double2(0, 0)};
+  }
+  // swapped partners: for a pair p = (l,m) that is not its own exchange
+  // partner, W p = (m,l) belongs to another exchange class unless l == m or
+  // W p = E p; that class is then read off p's transform (derived[] = source)
+  const int Nchi = g.Nchi;
+  std::vector<int> cls((size_t)Nchi * Nchi, -1);  // element (m,l) -> index in hp
+  for (size_t i = 0; i < hp.size(); ++i) {
+    cls[hp[i].m + (size_t)Nchi * hp[i].l] = (int)i;
+    cls[hp[i].m2 + (size_t)Nchi * hp[i].l2] = (int)i;
+  }
+  std::vector<int> derived(hp.size(), -1);  // source transform of a derived class
+  if (chi0_swap_enabled()) {
+    for (size_t i = 0; i < hp.size(); ++i) {
+      const ChiDev& c = hp[i];
+      if (c.self || derived[i] >= 0 || c.has_d || c.l == c.m) continue;
+      const int j = cls[c.l + (size_t)Nchi * c.m];  // class of W p (element (l,m))
+      if (j < 0 || j == (int)i || hp[j].self || derived[j] >= 0 || hp[j].has_d) continue;
+      derived[j] = (int)i;
+      ChiDev& s = hp[i];
+      s.has_d = 1;
+      s.dm = c.l;  // W p = (l' = m, m' = l) is written at element (m', l') = (l, m)
+      s.dl = c.m;
+      s.dm2 = (hp[j].m == s.dm && hp[j].l == s.dl) ? hp[j].m2 : hp[j].m;
+      s.dl2 = (hp[j].m == s.dm && hp[j].l == s.dl) ? hp[j].l2 : hp[j].l;
+    }
   }
   if (tail) {
     DBuf<double2> G0((size_t)g.K * No2);
@@ -559,18 +608,28 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
     rb.download(hrb.data(), No2);
     sync();
     auto RB = [&](int m, int l) { return hrb[m + g.Norb * l]; };
-    for (auto& c : hp) {
-      const int a13 = p.o1[c.l], b13 = p.o1[c.m], a42 = p.o2[c.m], b42 = p.o2[c.l];
+    auto Jof = [&](int l, int m) {  // tau = 0 jump coefficient of pair (l,m) (fchi.f90:836-844)
+      const int a13 = p.o1[l], b13 = p.o1[m], a42 = p.o2[m], b42 = p.o2[l];
       double2 J = make_double2(0, 0);
       if (a13 == b13) J = J + RB(a42, b42);
       if (a42 == b42) J = J - RB(a13, b13);
-      c.J = J;
+      return J;
+    };
+    for (auto& c : hp) {
+      c.J = Jof(c.l, c.m);
+      if (c.has_d) c.dJ = Jof(c.dl, c.dm);
     }
     DBuf<double2> sawc64(g.Nw);
     k_sawc<<<grid_1d(g.Nw, 128), 128, 0, st>>>(sawc64.p, g.Nw, (int)g.M, temp);
     count_launch("sawc");
     sawc.alloc(g.Nw);
     narrow<R>(sawc.p, sawc64.p, g.Nw);
+  }
+  {  // keep only the transforms that are computed
+    std::vector<ChiDev> kept;
+    for (size_t i = 0; i < hp.size(); ++i)
+      if (derived[i] < 0) kept.push_back(hp[i]);
+    hp.swap(kept);
   }
   DBuf<ChiDev> dp(hp.size());
   dp.upload(hp.data(), hp.size());
