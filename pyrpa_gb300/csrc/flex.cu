@@ -557,9 +557,11 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
     hp[i] = ChiDev{c.m, c.l, c.m2, c.l2, c.e13, c.e42, c.self, 0, make_double2(0, 0), 0, 0, 0, 0,
                    make_double2(0, 0)};
   }
-  // swapped partners: for a pair p = (l,m) that is not its own exchange
-  // partner, W p = (m,l) belongs to another exchange class unless l == m or
-  // W p = E p; that class is then read off p's transform (derived[] = source)
+  // swapped partners: the relation chi_ml(q,nu) = conj chi_lm(q,-nu) is exact
+  // for any G, while the exchange relation is imposed (the partner is written
+  // as the conjugate of the class representative).  A class is therefore read
+  // off p's transform only when its own representative is exactly W p = (m,l)
+  // (derived[] = source); the other classes keep their transform.
   const int Nchi = g.Nchi;
   std::vector<int> cls((size_t)Nchi * Nchi, -1);  // element (m,l) -> index in hp
   for (size_t i = 0; i < hp.size(); ++i) {
@@ -573,13 +575,14 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
       if (c.self || derived[i] >= 0 || c.has_d || c.l == c.m) continue;
       const int j = cls[c.l + (size_t)Nchi * c.m];  // class of W p (element (l,m))
       if (j < 0 || j == (int)i || hp[j].self || derived[j] >= 0 || hp[j].has_d) continue;
+      if (hp[j].l != c.m || hp[j].m != c.l) continue;  // representative is E W p, not W p
       derived[j] = (int)i;
       ChiDev& s = hp[i];
       s.has_d = 1;
-      s.dm = c.l;  // W p = (l' = m, m' = l) is written at element (m', l') = (l, m)
-      s.dl = c.m;
-      s.dm2 = (hp[j].m == s.dm && hp[j].l == s.dl) ? hp[j].m2 : hp[j].m;
-      s.dl2 = (hp[j].m == s.dm && hp[j].l == s.dl) ? hp[j].l2 : hp[j].l;
+      s.dm = hp[j].m;  // W p = (l' = m, m' = l) is written at element (m', l') = (l, m)
+      s.dl = hp[j].l;
+      s.dm2 = hp[j].m2;
+      s.dl2 = hp[j].l2;
     }
   }
   if (tail) {
@@ -839,12 +842,15 @@ __device__ __forceinline__ bool warp_inverse(cx<R> (&a)[N], int* piv, int* map) 
     const cx<R> pv = cmk<R>(__shfl_sync(0xffffffffu, ak.x, src), __shfl_sync(0xffffffffu, ak.y, src));
     const cx<R> ip = ok ? cdiv(cmk<R>(1, 0), pv) : cmk<R>(0, 0);
     const bool is_piv = (label == k);
-    const cx<R> kval = is_piv ? ip : -(ak * ip);
+    // new row = base + f * (pivot row): the pivot lane scales (base 0, f = 1/p),
+    // the others eliminate (base = own row, f = -a_k/p); column k becomes f
+    const cx<R> f = is_piv ? ip : -(ak * ip);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const cx<R> pj = cmk<R>(__shfl_sync(0xffffffffu, a[j].x, src), __shfl_sync(0xffffffffu, a[j].y, src)) * ip;
-      const cx<R> nv = is_piv ? pj : a[j] - ak * pj;
-      a[j] = (j == k) ? kval : nv;
+      const R sx = __shfl_sync(0xffffffffu, a[j].x, src), sy = __shfl_sync(0xffffffffu, a[j].y, src);
+      const R bx = is_piv ? (R)0 : a[j].x, by = is_piv ? (R)0 : a[j].y;
+      const cx<R> nv = cmk<R>(fma(f.x, sx, fma(-f.y, sy, bx)), fma(f.x, sy, fma(f.y, sx, by)));
+      a[j] = (j == k) ? f : nv;
     }
   }
   __syncwarp();
