@@ -273,8 +273,9 @@ def main():
                    "warm_start_iterations": int(stats["iterations_coarse"]),
                    "warm_start_ms": stats["t_warm_ms"],
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
-                   "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, then FP64 bulk "
-                                          f"to eps; Eliashberg FP32 bulk with FP64 Arnoldi",
+                   "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, FP64 chi0 and "
+                                          f"Sigma with FP32 vertex for {int(stats['iterations_fp64_fp32vertex'])}, "
+                                          f"then FP64 bulk to eps; Eliashberg FP32 bulk with FP64 Arnoldi",
                                  "32": "FP32 bulk", "64": "FP64"}[a.precision]})
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,

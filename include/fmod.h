@@ -143,8 +143,9 @@ void conv_delta_orb_to_band(double* deltab, const double* delta, const double* u
 /* 64: FP64 everywhere (default, the reference's arithmetic); 32: complex FP32 FFTs,
  * contractions and vertex solves with G, Sigma, mu, DIIS and lambda kept in FP64;
  * 3264 (mixed): as 32, except that the FLEX loop of mkself / pyrpa_gb_flex_eliash
- * leaves FP32 once its residual reaches the FP32 rounding floor and finishes on
- * FP64 bulk, so that convergence to eps is always judged on an FP64 iteration.
+ * leaves FP32 once its residual reaches the FP32 rounding floor, continues with
+ * chi0 and Sigma on FP64 bulk and the vertex on FP32, and finishes on FP64 bulk,
+ * so that convergence to eps is always judged on an FP64 iteration.
  * PYRPA_GB_PRECISION=fp32 | mixed | fp64 in the environment sets it at first use. */
 void pyrpa_gb_set_precision(const int64_t* bits);
 void pyrpa_gb_get_precision(int64_t* bits);
@@ -159,7 +160,9 @@ void pyrpa_gb_kernel_launches(int64_t* n);
  * Eliashberg applications, then device milliseconds of chi0, vertex, Sigma, DIIS,
  * mu, Dyson, Eliashberg applications, then the FLEX iterations run on FP32 bulk,
  * the FLEX iterations of a coarse-mesh warm start and its device milliseconds,
- * and the device milliseconds of the Stoner factors in the FLEX loop (17 doubles) */
+ * the device milliseconds of the Stoner factors in the FLEX loop, and the
+ * iterations of the mixed schedule's middle phase (FP64 chi0 and Sigma, FP32
+ * vertex) (18 doubles) */
 void pyrpa_gb_last_stats(double* out);
 void pyrpa_gb_device_info(int64_t* num_sms, int64_t* device);
 /* live timing of the FFT pass kernel: when on, every pass launch is bracketed

@@ -49,6 +49,7 @@ void ensure_context() {
     std::string v(s);
     if (v == "32" || v == "fp32" || v == "FP32") c.precision = 32;
     if (v == "3264" || v == "mixed" || v == "MIXED") c.precision = kPrecMixed;
+    if (v == "48" || v == "df" || v == "DF") c.precision = kPrecDF;
   }
   if (const char* s = std::getenv("PYRPA_GB_VERBOSE")) c.verbose = std::atoi(s);
   c.ready = true;
@@ -81,7 +82,7 @@ template <typename T> void nan_fill(T* p, size_t n) {
 
 // FP32 bulk for every entry point except FP64 mode (the mixed schedule only
 // changes the FLEX loop)
-bool fp32() { return ctx().precision != 64; }
+bool fp32() { return ctx().precision == 32 || ctx().precision == kPrecMixed; }
 
 // --------------------------------------------------------- setup kernels
 __global__ void k_gen_ham(double2* hk, const double* klist, const double2* hr, const double* rvec, int64_t Nk,
@@ -369,6 +370,10 @@ double chi0_entry(double2* chi_out, const double* Smat, const double* Cmat, cons
   sync();
   return sdw;
 }
+// chi0 entry of the current precision: double-float convolutions in mode 48
+auto chi0_fn() {
+  return ctx().precision == kPrecDF ? chi0_entry<dfl> : (fp32() ? chi0_entry<float> : chi0_entry<double>);
+}
 }  // namespace
 
 // ============================================== allocation-free variant ==
@@ -412,7 +417,7 @@ extern "C" {
 
 // ============================================================== extras ==
 void pyrpa_gb_set_precision(const int64_t* bits) {
-  ctx().precision = (*bits == 32) ? 32 : (*bits == kPrecMixed ? kPrecMixed : 64);
+  ctx().precision = (*bits == 32 || *bits == kPrecMixed || *bits == kPrecDF) ? (int)*bits : 64;
 }
 void pyrpa_gb_get_precision(int64_t* bits) {
   ABI_TRY ensure_context(); ABI_CATCH("pyrpa_gb_get_precision", (void)0)
@@ -436,9 +441,9 @@ void pyrpa_gb_clear_error() {
 void pyrpa_gb_kernel_launches(int64_t* n) { *n = ctx().kernel_launches; }
 void pyrpa_gb_last_stats(double* out) {
   const LastStats& s = last_stats();
-  const double v[17] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
+  const double v[18] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
                         s.t_vertex, s.t_sigma, s.t_diis, s.t_mu, s.t_dyson, s.t_apply, (double)s.iterations32,
-                        (double)s.iterations_coarse, s.t_warm, s.t_stoner};
+                        (double)s.iterations_coarse, s.t_warm, s.t_stoner, (double)s.iterations_finish32};
   memcpy(out, v, sizeof(v));
 }
 void pyrpa_gb_fft_profile(const int64_t* on) { fft_profile_enable(*on != 0); }
@@ -649,7 +654,7 @@ void get_chi0(double2* chi, const double* Smat, const double* Cmat, const double
               const int64_t* Nchi, double* maxchi0s_out) {
   ABI_TRY
   ensure_context();
-  auto f = fp32() ? chi0_entry<float> : chi0_entry<double>;
+  auto f = chi0_fn();
   *maxchi0s_out = f(chi, Smat, Cmat, Gk, kmap, invk, olist, *temp, *Nx, *Ny, *Nz, *Nw, *Nk, *Nkall, *Norb, *Nchi,
                     nullptr, nullptr, 0.0, false, true, nullptr, nullptr);
   ABI_CATCH("get_chi0", (nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)), *maxchi0s_out = NAN))
@@ -662,7 +667,7 @@ void get_chi0_tail(double2* chi, const double* Smat, const double* Cmat, const d
                    double* maxchi0s_out) {
   ABI_TRY
   ensure_context();
-  auto f = fp32() ? chi0_entry<float> : chi0_entry<double>;
+  auto f = chi0_fn();
   *maxchi0s_out = f(chi, Smat, Cmat, Gk, kmap, invk, olist, *temp, *Nx, *Ny, *Nz, *Nw, *Nk, *Nkall, *Norb, *Nchi,
                     eig, uni, *mu, true, true, nullptr, nullptr);
   ABI_CATCH("get_chi0_tail", (nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)), *maxchi0s_out = NAN))
@@ -674,7 +679,7 @@ void get_chi0_conv_(double2* chi, const double2* Gk, const int64_t* kmap, const 
                     const int64_t* Norb, const int64_t* Nchi) {
   ABI_TRY
   ensure_context();
-  auto f = fp32() ? chi0_entry<float> : chi0_entry<double>;
+  auto f = chi0_fn();
   f(chi, nullptr, nullptr, Gk, kmap, invk, olist, *temp, *Nx, *Ny, *Nz, *Nw, *Nk, *Nkall, *Norb, *Nchi, nullptr,
     nullptr, 0.0, false, false, irr_chi, chi_map);
   ABI_CATCH("get_chi0_conv_", nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)))

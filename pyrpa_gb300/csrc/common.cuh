@@ -73,6 +73,79 @@ template <typename D, typename S> __host__ __device__ __forceinline__ cx<D> ccas
   return cmk<D>((D)a.x, (D)a.y);
 }
 
+// ------------------------------------------------------------ double-float --
+// A real carried as the unevaluated sum hi + lo of two floats (|lo| at most
+// half an ulp of hi): about 48 significant bits, with all arithmetic on the
+// FP32 pipe, which on GB300 has 64 times the FP64 rate.  The add and multiply
+// are the double-word algorithms built from Knuth's two-sum and the FMA
+// two-product (Hida, Li and Bailey, "Algorithms for quad-double precision
+// floating point arithmetic", ARITH 2001).  The FFT convolutions of the FLEX
+// loop use it where FP32 rounding would set the residual's floor.
+struct dfl {
+  float hi, lo;
+  __host__ __device__ constexpr dfl() : hi(0.f), lo(0.f) {}
+  __host__ __device__ constexpr dfl(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr dfl(float f) : hi(f), lo(0.f) {}
+  __host__ __device__ constexpr dfl(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+  __host__ __device__ constexpr dfl(int i) : dfl((double)i) {}
+  __host__ __device__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+struct __align__(16) cdf {
+  dfl x, y;
+};
+template <> struct cvec<dfl> { using type = cdf; };
+
+__host__ __device__ __forceinline__ dfl two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return dfl(s, (a - (s - bb)) + (b - bb));
+}
+__host__ __device__ __forceinline__ dfl fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return dfl(s, b - (s - a));
+}
+__host__ __device__ __forceinline__ dfl operator+(dfl a, dfl b) {
+  const dfl s = two_sum(a.hi, b.hi), t = two_sum(a.lo, b.lo);
+  const dfl u = fast_two_sum(s.hi, s.lo + t.hi);
+  return fast_two_sum(u.hi, u.lo + t.lo);
+}
+__host__ __device__ __forceinline__ dfl operator-(dfl a) { return dfl(-a.hi, -a.lo); }
+__host__ __device__ __forceinline__ dfl operator-(dfl a, dfl b) { return a + (-b); }
+__host__ __device__ __forceinline__ dfl operator*(dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return fast_two_sum(p, e);
+}
+__host__ __device__ __forceinline__ dfl& operator+=(dfl& a, dfl b) { a = a + b; return a; }
+__host__ __device__ __forceinline__ dfl& operator-=(dfl& a, dfl b) { a = a - b; return a; }
+__host__ __device__ __forceinline__ dfl dabs(dfl a) { return a.hi < 0.f ? -a : a; }
+__host__ __device__ __forceinline__ bool operator<(dfl a, dfl b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+// |x| < t for each bulk type (the reference's small-part zeroing)
+__host__ __device__ __forceinline__ bool abs_below(float x, double t) { return fabsf(x) < (float)t; }
+__host__ __device__ __forceinline__ bool abs_below(double x, double t) { return fabs(x) < t; }
+__host__ __device__ __forceinline__ bool abs_below(dfl x, double t) { return dabs(x) < dfl(t); }
+
+__host__ __device__ __forceinline__ cdf mkc(dfl a, dfl b) {
+  cdf r;
+  r.x = a;
+  r.y = b;
+  return r;
+}
+__host__ __device__ __forceinline__ cdf operator+(cdf a, cdf b) { return mkc(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ cdf operator-(cdf a, cdf b) { return mkc(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ cdf operator-(cdf a) { return mkc(-a.x, -a.y); }
+__host__ __device__ __forceinline__ cdf operator*(cdf a, cdf b) {
+  return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ cdf operator*(dfl s, cdf b) { return mkc(s * b.x, s * b.y); }
+__host__ __device__ __forceinline__ cdf operator*(cdf b, dfl s) { return mkc(s * b.x, s * b.y); }
+__host__ __device__ __forceinline__ cdf& operator+=(cdf& a, cdf b) { a = a + b; return a; }
+__host__ __device__ __forceinline__ cdf& operator-=(cdf& a, cdf b) { a = a - b; return a; }
+__host__ __device__ __forceinline__ cdf conj(cdf a) { return mkc(a.x, -a.y); }
+// a * (s i), s = +-1 (a sign change, no rounding)
+__host__ __device__ __forceinline__ cdf muli(cdf a, dfl s) { return s.hi > 0.f ? mkc(-a.y, a.x) : mkc(a.y, -a.x); }
+
 // ---------------------------------------------------------------- errors --
 struct Error : std::runtime_error {
   explicit Error(const std::string& s) : std::runtime_error(s) {}

@@ -298,26 +298,72 @@ void stage_sigma(Inputs& in, const FlexParams& a, const double2* G, const cx<R>*
   g_stats.t_sigma += tm.stop();
 }
 
-double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, int fp32_mask, DBuf<float2>& chi32,
-                 DBuf<double2>& chi64, double2* sig) {
+// the chi buffer of each bulk type, allocated on first use
+struct ChiBufs {
+  DBuf<float2> f32;
+  DBuf<double2> f64;
+  DBuf<cdf> fdf;
+  void* get(int prec, long long n) {
+    if (prec == 32) { if (!f32.p) f32.alloc(n); return f32.p; }
+    if (prec == 64) { if (!f64.p) f64.alloc(n); return f64.p; }
+    if (!fdf.p) fdf.alloc(n);
+    return fdf.p;
+  }
+  void keep_only(const StagePrec& sp) {
+    auto used = [&](int p) { return sp.chi0 == p || sp.vertex == p || sp.sigma == p; };
+    if (!used(32)) f32.release();
+    if (!used(64)) f64.release();
+    if (!used(48)) fdf.release();
+  }
+};
+
+void convert_chi(void* out, int to, const void* in, int from, long long n) {
+  if (to == from) return;
+  if (to == 32 && from == 64) convert<float, double>((float2*)out, (const double2*)in, n);
+  else if (to == 64 && from == 32) convert<double, float>((double2*)out, (const float2*)in, n);
+  else if (to == 32 && from == 48) convert<float, dfl>((float2*)out, (const cdf*)in, n);
+  else if (to == 48 && from == 32) convert<dfl, float>((cdf*)out, (const float2*)in, n);
+  else if (to == 64 && from == 48) convert<double, dfl>((double2*)out, (const cdf*)in, n);
+  else convert<dfl, double>((cdf*)out, (const double2*)in, n);
+}
+
+double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, const StagePrec& sp, ChiBufs& b,
+                 double2* sig) {
   const long long KC = in.g.K * in.Nchi * in.Nchi;
-  const bool s0 = fp32_mask & 1, s1 = fp32_mask & 2, s2 = fp32_mask & 4;
-  if ((s0 || s1 || s2) && !chi32.p) chi32.alloc(KC);
-  if ((!s0 || !s1 || !s2) && !chi64.p) chi64.alloc(KC);
-  double sdw = s0 ? stage_chi0<float>(in, a, G, mu, chi32.p) : stage_chi0<double>(in, a, G, mu, chi64.p);
-  if (s0 != s1) {
-    if (s1) narrow<float>(chi32.p, chi64.p, KC);
-    else widen<float>(chi64.p, chi32.p, KC);
-  }
-  if (s1) stage_vertex<float>(in, chi32.p);
-  else stage_vertex<double>(in, chi64.p);
-  if (s1 != s2) {
-    if (s2) narrow<float>(chi32.p, chi64.p, KC);
-    else widen<float>(chi64.p, chi32.p, KC);
-  }
-  if (s2) stage_sigma<float>(in, a, G, chi32.p, sig);
-  else stage_sigma<double>(in, a, G, chi64.p, sig);
+  PGB_CHECK(sp.vertex == 32 || sp.vertex == 64, "the vertex stage runs in FP32 or FP64");
+  void* c0 = b.get(sp.chi0, KC);
+  double sdw = 0;
+  if (sp.chi0 == 32) sdw = stage_chi0<float>(in, a, G, mu, (float2*)c0);
+  else if (sp.chi0 == 64) sdw = stage_chi0<double>(in, a, G, mu, (double2*)c0);
+  else sdw = stage_chi0<dfl>(in, a, G, mu, (cdf*)c0);
+  void* cv = b.get(sp.vertex, KC);
+  convert_chi(cv, sp.vertex, c0, sp.chi0, KC);
+  if (sp.vertex == 32) stage_vertex<float>(in, (float2*)cv);
+  else stage_vertex<double>(in, (double2*)cv);
+  void* cs = b.get(sp.sigma, KC);
+  convert_chi(cs, sp.sigma, cv, sp.vertex, KC);
+  if (sp.sigma == 32) stage_sigma<float>(in, a, G, (const float2*)cs, sig);
+  else if (sp.sigma == 64) stage_sigma<double>(in, a, G, (const double2*)cs, sig);
+  else stage_sigma<dfl>(in, a, G, (const cdf*)cs, sig);
   return sdw;
+}
+
+// Stages that the middle phase of the mixed schedule keeps on FP32 bulk:
+// PYRPA_GB_FINISH_FP32_STAGES, a comma list of chi0, vertex, sigma or
+// "none" (default "vertex").
+int mix_finish_mask() {
+  const char* s = std::getenv("PYRPA_GB_FINISH_FP32_STAGES");
+  if (!s) return 2;
+  const std::string v(s);
+  return (v.find("chi0") != std::string::npos ? 1 : 0) | (v.find("vertex") != std::string::npos ? 2 : 0) |
+         (v.find("sigma") != std::string::npos ? 4 : 0);
+}
+
+// Bulk type of the middle phase's other stages: double-float (default) or,
+// with PYRPA_GB_FINISH_BULK=fp64, FP64.
+int mix_finish_bulk() {
+  const char* s = std::getenv("PYRPA_GB_FINISH_BULK");
+  return (s && std::string(s) == "fp64") ? 64 : 48;
 }
 
 // PYRPA_GB_MIX_DIIS=keep keeps the FP32-phase DIIS history across the switch
@@ -354,9 +400,6 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
   DBuf<double2>& H = in.H;
   DBuf<double2>& uni = in.uni;
   DBuf<double2> G(KE), sig(KE), sig0(KE), eg((size_t)K * Norb);
-  DBuf<float2> chi32;
-  DBuf<double2> chi64;
-  bool use32 = (prec == 32 || prec == kPrecMixed);
   const int mask32 = fp32_stage_mask();
   std::vector<DBuf<double2>> xout(a.m_diis), res(a.m_diis);
   for (int i = 0; i < a.m_diis; ++i) {
@@ -539,14 +582,31 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
 
   Timer tm;
   int it = 0;
-  // mixed schedule: leave FP32 once the residual is below kMixSwitch or, once
-  // it is below kMixStallFrom, has not reached a new minimum for kMixStall
-  // iterations
-  double best32 = 1e300;
+  // Mixed schedule, three phases:
+  //   0  the stages in mask32 on FP32 bulk (default all);
+  //   1  chi0 and Sigma on FP64 bulk, the stages in finish_mask (default the
+  //      vertex) still on FP32: the FP32 rounding floor of the residual comes
+  //      from the chi0 and Sigma convolutions, not from the vertex solve;
+  //   2  everything on FP64.
+  // A phase ends when the residual is below eps, below kMixSwitch (phase 0
+  // only) or, once it is below kMixStallFrom, has not reached a new minimum
+  // for kMixStall iterations.  Convergence is declared only in phase 2.
+  const int finish_mask = mix_finish_mask();
+  const int finish_bulk = mix_finish_bulk();
+  int phase = (prec == kPrecMixed || prec == 32) ? 0 : 2;
+  auto prec_of = [&](int ph) {
+    if (prec == kPrecDF) return StagePrec{48, 64, 48};
+    auto pick = [&](int bit, int other) { return (ph == 0 ? mask32 : finish_mask) & bit ? 32 : other; };
+    if (ph == 2) return StagePrec{64, 64, 64};
+    const int other = ph == 0 ? 64 : finish_bulk;
+    return StagePrec{pick(1, other), pick(2, 64), pick(4, other)};
+  };
+  ChiBufs bufs;
+  double best = 1e300;
   int since_best = 0;
   for (it = 1; it <= a.scf_loop; ++it) {
     log("iter=%5d\n", it);
-    maxchi0s = flex_bulk(in, a, G.p, mu, use32 ? mask32 : 0, chi32, chi64, sig.p);
+    maxchi0s = flex_bulk(in, a, G.p, mu, prec_of(phase), bufs, sig.p);
     tm.start();
     if (a.sub_sigma > 0) hf_subtract(sig.p, Nk, Nw, Norb, (int)a.sub_sigma);
     compare_sigma();
@@ -554,29 +614,34 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
     g_stats.esterr = esterr;
     g_stats.iterations = it;
     g_stats.stoner = maxchi0s;
-    if (use32) g_stats.iterations32 = it;
-    bool switch64 = false;
-    if (use32 && prec == kPrecMixed) {
+    if (phase == 0) g_stats.iterations32 = it;
+    if (phase == 1) ++g_stats.iterations_finish32;
+    if (prec != kPrecMixed || phase == 2) {
+      if (esterr < a.eps) break;
+    } else {
       // the stall count starts once the residual is out of the initial transient
-      if (esterr < best32 * 0.9) {
-        best32 = esterr;
+      if (esterr < best * 0.9) {
+        best = esterr;
         since_best = 0;
-      } else if (best32 < kMixStallFrom) {
+      } else if (best < kMixStallFrom) {
         ++since_best;
       }
-      switch64 = esterr < a.eps || esterr < kMixSwitch || since_best >= kMixStall;
-    }
-    if (esterr < a.eps && !switch64) break;
-    if (switch64 && a.stop_at_fp32_floor) break;
-    if (switch64) {
-      log("[FLEX] residual%9.2E on FP32 bulk: continuing with FP64 bulk\n", esterr);
-      use32 = false;
-      chi32.release();
-      if (mix_diis_reset()) {
-        // the FP32 entries carry the FP32 rounding floor in their residuals;
-        // the FP64 phase starts a fresh history from the current Sigma
-        n_hist = 0;
-        i_hist = 0;
+      const bool next = esterr < a.eps || (phase == 0 && esterr < kMixSwitch) || since_best >= kMixStall;
+      if (next && phase == 0 && a.stop_at_fp32_floor) break;
+      if (next) {
+        const int from = phase;
+        phase = (phase == 0 && finish_mask != 0) ? 1 : 2;
+        log("[FLEX] residual%9.2E: continuing with %s\n", esterr,
+            phase == 1 ? "chi0 and Sigma on FP64 bulk" : "FP64 bulk");
+        if (from == 0 && mix_diis_reset()) {
+          // the FP32 entries carry the FP32 rounding floor in their residuals;
+          // the FP64 phases start a fresh history from the current Sigma
+          n_hist = 0;
+          i_hist = 0;
+        }
+        best = 1e300;
+        since_best = 0;
+        bufs.keep_only(prec_of(phase));
       }
     }
     tm.start();
@@ -991,7 +1056,7 @@ template void run_lin_eliash<float>(const LinEliashArgs&);
 template void run_lin_eliash<double>(const LinEliashArgs&);
 // The Eliashberg stage runs in FP64 for prec 64 and in FP32 bulk otherwise.
 void run_pipeline(const PipelineArgs& a, int prec) {
-  if (prec == 64) run_pipeline_impl<double>(a, prec);
+  if (prec == 64 || prec == kPrecDF) run_pipeline_impl<double>(a, prec);
   else run_pipeline_impl<float>(a, prec);
 }
 

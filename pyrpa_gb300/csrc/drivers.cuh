@@ -98,6 +98,7 @@ struct EliashParams {
 
 struct LastStats {
   int iterations = 0, iterations32 = 0;  // FLEX iterations (of which on FP32 bulk)
+  int iterations_finish32 = 0;           // mixed schedule: FP64 chi0/Sigma with FP32 vertex
   int iterations_coarse = 0;             // FLEX iterations of the coarse-mesh warm start
   double t_warm = 0;                     // device ms of the warm start (coarse solve + interpolation)
   double esterr = 0, stoner = 0, mu = 0, lambda = 0;
@@ -107,8 +108,14 @@ struct LastStats {
   double t_stoner = 0;  // Stoner factor (and the sw_rescale clamp) of the FLEX loop
 };
 
+// bulk type of each stage of a FLEX iteration: 32 FP32, 64 FP64, 48 double-float
+struct StagePrec {
+  int chi0, vertex, sigma;
+};
+
 // precision schedule of the FLEX loop: 64, 32 or kPrecMixed
 constexpr int kPrecMixed = 3264;
+constexpr int kPrecDF = 48;  // double-float chi0 and Sigma convolutions, FP64 elsewhere
 constexpr double kMixSwitch = 2.0e-3;  // residual at which the mixed schedule leaves FP32
 constexpr int kMixStall = 6;           // or after this many FP32 iterations without a new minimum
 constexpr double kMixStallFrom = 0.1;  //   counted once the residual has been below this

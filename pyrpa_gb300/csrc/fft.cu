@@ -23,6 +23,13 @@ template <> __device__ __forceinline__ const float2* line_tab<float>(const PassD
 template <typename R> __device__ __forceinline__ const cx<R>* full_tab(const PassDesc& d);
 template <> __device__ __forceinline__ const double2* full_tab<double>(const PassDesc& d) { return d.tw_full; }
 template <> __device__ __forceinline__ const float2* full_tab<float>(const PassDesc& d) { return d.tw_full_f; }
+template <> __device__ __forceinline__ const cdf* line_tab<dfl>(const PassDesc& d) { return d.tw_line_d; }
+template <> __device__ __forceinline__ const cdf* full_tab<dfl>(const PassDesc& d) { return d.tw_full_d; }
+// double-float roots: one 16-byte read-only load {re.hi, re.lo, im.hi, im.lo}
+template <> __device__ __forceinline__ cdf twid<dfl>(const cdf* tab, int t, int sign) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(tab + t));
+  return mkc(dfl(v.x, v.y), sign < 0 ? dfl(v.z, v.w) : dfl(-v.z, -v.w));
+}
 
 template <typename R, int RAD> struct Dft {
   // generic radix: direct O(RAD^2) evaluation with roots from the line table
@@ -335,6 +342,7 @@ void launch_fast(const PassDesc& d, dim3 grid, size_t smem, cudaStream_t s, cx<R
 std::mutex g_mu;
 std::map<int, double2*> g_tables;
 std::map<int, float2*> g_tables_f;
+std::map<int, cdf*> g_tables_d;
 
 struct PassEvent {
   cudaEvent_t a, b;
@@ -382,6 +390,24 @@ const double2* twiddle_table(int L) {
   PGB_CUDA(cudaMalloc(&df, sizeof(float2) * L));
   PGB_CUDA(cudaMemcpy(df, hf.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
   g_tables_f[L] = df;
+  // double-float copy: hi = float(root), lo = float(root - hi) from the
+  // extended-precision value
+  std::vector<cdf> hd(L);
+  for (int t = 0; t < L; ++t) {
+    long double c = h[t].x, s = h[t].y;
+    long long q = (long long)t * 4;
+    if (q % L != 0) {
+      const long double a = twopi * (long double)t / (long double)L;
+      c = cosl(a);
+      s = -sinl(a);
+    }
+    const float ch = (float)c, sh = (float)s;
+    hd[t] = mkc(dfl(ch, (float)(c - (long double)ch)), dfl(sh, (float)(s - (long double)sh)));
+  }
+  cdf* dd = nullptr;
+  PGB_CUDA(cudaMalloc(&dd, sizeof(cdf) * L));
+  PGB_CUDA(cudaMemcpy(dd, hd.data(), sizeof(cdf) * L, cudaMemcpyHostToDevice));
+  g_tables_d[L] = dd;
   return d;
 }
 
@@ -389,6 +415,12 @@ const float2* twiddle_table_f(int L) {
   twiddle_table(L);
   std::lock_guard<std::mutex> lk(g_mu);
   return g_tables_f[L];
+}
+
+const cdf* twiddle_table_d(int L) {
+  twiddle_table(L);
+  std::lock_guard<std::mutex> lk(g_mu);
+  return g_tables_d[L];
 }
 
 bool factor_line(int L, int* radix, int* nst) {
@@ -417,6 +449,7 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
     d.B = (int)std::max(1LL, nl);
     d.tw_line = twiddle_table(L);
     d.tw_line_f = twiddle_table_f(L);
+    d.tw_line_d = twiddle_table_d(L);
     d.nst = 0;
     return d;
   }
@@ -430,6 +463,7 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
   d.B = (int)std::max(1LL, B);
   d.tw_line = twiddle_table(L);
   d.tw_line_f = twiddle_table_f(L);
+  d.tw_line_d = twiddle_table_d(L);
   return d;
 }
 
@@ -494,6 +528,7 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
       pa.tw_Lfull = n;
       pa.tw_full = twiddle_table(n);
       pa.tw_full_f = twiddle_table_f(n);
+      pa.tw_full_d = twiddle_table_d(n);
       PassDesc pa_inv = pa;
       pa_inv.tw_post = 1;
       fwd_.push_back(pb);
@@ -584,6 +619,10 @@ template void FFT4D::forward_space<float>(float2*, int, cudaStream_t) const;
 template void FFT4D::forward_space<double>(double2*, int, cudaStream_t) const;
 template void FFT4D::backward_space<float>(float2*, int, cudaStream_t) const;
 template void FFT4D::backward_space<double>(double2*, int, cudaStream_t) const;
+template void FFT4D::forward<dfl>(cdf*, int, cudaStream_t) const;
+template void FFT4D::backward<dfl>(cdf*, int, cudaStream_t) const;
+template void FFT4D::forward_space<dfl>(cdf*, int, cudaStream_t) const;
+template void FFT4D::backward_space<dfl>(cdf*, int, cudaStream_t) const;
 
 void fft_profile_enable(bool on) { g_prof = on; }
 

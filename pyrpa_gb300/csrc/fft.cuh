@@ -39,6 +39,8 @@ struct PassDesc {
   const double2* tw_full;  // exp(-2 pi i t / Lfull), t < Lfull
   const float2* tw_line_f; // the same tables rounded to FP32 for the FP32 kernels
   const float2* tw_full_f; //   (FP64->FP32 conversions run on the FP64 pipe)
+  const cdf* tw_line_d;    // and as double-float pairs for the double-float kernels
+  const cdf* tw_full_d;
   int fa, fb;              // L = fa * fb for the two-level register kernel (0: Stockham kernel)
 };
 

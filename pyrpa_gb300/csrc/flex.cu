@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <map>
 #include <string>
+#include <type_traits>
 
 #include "flex.cuh"
 #include "linalg.cuh"
@@ -423,16 +424,16 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
     cx<R> v = t[irr_grid[k] + Nkall * j];
     if (sawc) v += J * sawc[j];
     if (pr.self) v = conj(v);
-    if (fabs(v.x) < (R)kThresh) v.x = 0;
-    if (fabs(v.y) < (R)kThresh) v.y = 0;
+    if (abs_below(v.x, kThresh)) v.x = 0;
+    if (abs_below(v.y, kThresh)) v.y = 0;
     chi[fidx(k, j, pr.m, pr.l, Nk, Nw, Nchi)] = v;
     if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = conj(v);
     if (pr.has_d) {
       const long long M = 2LL * Nw;
       cx<R> d = conj(t[irr_grid[k] + Nkall * ((M - j) % M)]);
       if (sawc) d += cmk<R>((R)pr.dJ.x, (R)pr.dJ.y) * sawc[j];
-      if (fabs(d.x) < (R)kThresh) d.x = 0;
-      if (fabs(d.y) < (R)kThresh) d.y = 0;
+      if (abs_below(d.x, kThresh)) d.x = 0;
+      if (abs_below(d.y, kThresh)) d.y = 0;
       chi[fidx(k, j, pr.dm, pr.dl, Nk, Nw, Nchi)] = d;
       chi[fidx(k, j, pr.dm2, pr.dl2, Nk, Nw, Nchi)] = conj(d);
     }
@@ -1379,14 +1380,18 @@ __global__ void k_contract(cx<R>* out, const cx<R>* W, const cx<R>* F, const int
   }
 }
 
-__global__ void k_scatter_out(double2* dst, const void* tmp, int is_double, const int* irr_grid, long long Nkall,
+// element type of an untyped work array: 0 float2, 1 double2, 2 double-float
+template <typename R> constexpr int elem_kind() { return sizeof(cx<R>) == 8 ? 0 : (sizeof(R) == 8 && sizeof(cx<R>) == 16 && !std::is_same<R, dfl>::value ? 1 : 2); }
+
+__global__ void k_scatter_out(double2* dst, const void* tmp, int kind, const int* irr_grid, long long Nkall,
                               int Nk, int Nw, double scale, int do_thresh) {
   const long long K = (long long)Nk * Nw;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
        idx += (long long)gridDim.x * blockDim.x) {
     const int k = (int)(idx % Nk), j = (int)(idx / Nk);
     const long long src = irr_grid[k] + Nkall * j;
-    double2 v = is_double ? ((const double2*)tmp)[src] : ccast<double>(((const float2*)tmp)[src]);
+    double2 v = kind == 1 ? ((const double2*)tmp)[src]
+                          : (kind == 0 ? ccast<double>(((const float2*)tmp)[src]) : ccast<double>(((const cdf*)tmp)[src]));
     v = scale * v;
     if (do_thresh) v = thresh(v);
     dst[idx] = v;
@@ -1426,7 +1431,7 @@ template <typename R>
 __global__ void k_contract_mirror(cx<R>* T0, cx<R>* T1, const cx<R>* W, const cx<R>* F, const cx<R>* D,
                                   const MirrorTerm* terms, int nt, long long P, long long Nkall, int Nx, int Ny,
                                   const int* rev_x, const int* rev_y, const int* rev_z, const int* log_t) {
-  const R nk = (R)Nkall;
+  const R nk = (R)(double)Nkall;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
        idx += (long long)gridDim.x * blockDim.x) {
     const long long s = idx % Nkall, pt = idx / Nkall;
@@ -1517,11 +1522,11 @@ void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, cons
         fft.d_rev(1), fft.d_rev(2), fft.d_logical(3));
     count_launch("contract_mirror");
     fft.backward<R>(T.p, two ? 2 : 1, st);
-    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.e * g.K, T.p, sizeof(R) == 8,
+    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.e * g.K, T.p, elem_kind<R>(),
                                                              g.irr_grid.p, g.Nkall, g.Nk, g.Nw, scale, 1);
     count_launch("scatter_sigma");
     if (two) {
-      k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.et * g.K, T.p + g.P, sizeof(R) == 8,
+      k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.et * g.K, T.p + g.P, elem_kind<R>(),
                                                                g.irr_grid.p, g.Nkall, g.Nk, g.Nw, scale, 1);
       count_launch("scatter_sigma");
     }
@@ -1824,7 +1829,7 @@ void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, c
     k_contract<R><<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(T.p, Wp, FF.p, def.p, nt, g.P);
     count_launch("contract");
     fft.backward<R>(T.p, 1, st);
-    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(out + (size_t)e * g.K, T.p, sizeof(R) == 8, g.irr_grid.p,
+    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(out + (size_t)e * g.K, T.p, elem_kind<R>(), g.irr_grid.p,
                                                              g.Nkall, g.Nk, g.Nw, scale, 0);
     count_launch("scatter_delta");
     sync();
@@ -1913,6 +1918,32 @@ template <typename R> void narrow(cx<R>* out, const double2* in, long long n) {
   count_launch("narrow");
 }
 
+// conversions between bulk types (double-float <-> float without the FP64 pipe)
+__device__ __forceinline__ void cvt(float2& o, float2 v) { o = v; }
+__device__ __forceinline__ void cvt(double2& o, double2 v) { o = v; }
+__device__ __forceinline__ void cvt(cdf& o, cdf v) { o = v; }
+__device__ __forceinline__ void cvt(float2& o, double2 v) { o = make_float2((float)v.x, (float)v.y); }
+__device__ __forceinline__ void cvt(double2& o, float2 v) { o = make_double2(v.x, v.y); }
+__device__ __forceinline__ void cvt(cdf& o, float2 v) { o = mkc(dfl(v.x), dfl(v.y)); }
+__device__ __forceinline__ void cvt(float2& o, cdf v) { o = make_float2(v.x.hi + v.x.lo, v.y.hi + v.y.lo); }
+__device__ __forceinline__ void cvt(cdf& o, double2 v) { o = mkc(dfl(v.x), dfl(v.y)); }
+__device__ __forceinline__ void cvt(double2& o, cdf v) { o = make_double2((double)v.x, (double)v.y); }
+template <typename To, typename From>
+__global__ void k_convert(cx<To>* out, const cx<From>* in, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    cvt(out[i], in[i]);
+}
+template <typename To, typename From> void convert(cx<To>* out, const cx<From>* in, long long n) {
+  k_convert<To, From><<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(out, in, n);
+  count_launch("convert");
+}
+template void convert<float, dfl>(float2*, const cdf*, long long);
+template void convert<dfl, float>(cdf*, const float2*, long long);
+template void convert<double, dfl>(double2*, const cdf*, long long);
+template void convert<dfl, double>(cdf*, const double2*, long long);
+template void convert<float, double>(float2*, const double2*, long long);
+template void convert<double, float>(double2*, const float2*, long long);
+
 // ======================================================== instantiations ==
 #define PGB_INST(R)                                                                                        \
   template void chi0<R>(const Geom&, const Pairs&, const double2*, double, const TailRef*, cx<R>*);        \
@@ -1928,5 +1959,13 @@ template <typename R> void narrow(cx<R>* out, const double2* in, long long n) {
   template void narrow<R>(cx<R>*, const double2*, long long);
 PGB_INST(float)
 PGB_INST(double)
+// double-float bulk: the FFT convolution stages and the conversions around them
+template void chi0<dfl>(const Geom&, const Pairs&, const double2*, double, const TailRef*, cx<dfl>*);
+template void stoner<dfl>(const Geom&, const cx<dfl>*, const double*, const double*, double*, double*, int*, int*);
+template void scale_chi<dfl>(cx<dfl>*, long long, double);
+template void sigma<dfl>(const Geom&, const Pairs&, const double2*, const cx<dfl>*, const double*, const double*,
+                         double, double2*);
+template void widen<dfl>(double2*, const cx<dfl>*, long long);
+template void narrow<dfl>(cx<dfl>*, const double2*, long long);
 
 }  // namespace pgb

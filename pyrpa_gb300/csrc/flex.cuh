@@ -136,6 +136,8 @@ void sigma_interp(const Geom& gc, const Geom& gf, const double2* sig_c, double2*
 // small host helpers
 void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc);
 template <typename R> void widen(double2* out, const cx<R>* in, long long n);
+// out = in between any two bulk types (float, double, double-float)
+template <typename To, typename From> void convert(cx<To>* out, const cx<From>* in, long long n);
 template <typename R> void narrow(cx<R>* out, const double2* in, long long n);
 
 }  // namespace pgb

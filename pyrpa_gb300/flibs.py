@@ -149,11 +149,11 @@ def kernel_launches() -> int:
 
 
 def last_stats() -> dict:
-    out = np.zeros(17)
+    out = np.zeros(18)
     load_library().pyrpa_gb_last_stats(out)
     keys = ["iterations", "esterr", "stoner", "mu", "lambda", "applies", "t_chi0_ms", "t_vertex_ms",
             "t_sigma_ms", "t_diis_ms", "t_mu_ms", "t_dyson_ms", "t_apply_ms", "iterations_fp32",
-            "iterations_coarse", "t_warm_ms", "t_stoner_ms"]
+            "iterations_coarse", "t_warm_ms", "t_stoner_ms", "iterations_fp64_fp32vertex"]
     return dict(zip(keys, out[: len(keys)].tolist()))
 
 

@@ -412,3 +412,47 @@ def test_warm_start_reaches_the_cold_fixed_point(F, dims, Nw):
     close(warm["sigmak"], cold["sigmak"], 1e-6, 1e-9)
     assert abs(warm["mu"] - cold["mu"]) < 1e-8
     assert abs(warm["lam"] - cold["lam"]) <= 1e-6 * max(1.0, abs(cold["lam"]))
+
+
+# ------------------------------------------------ double-float convolutions
+def test_double_float_chi0_matches_oracle(F, model):
+    """Precision 48: the chi0 FFT convolutions in double-float arithmetic on
+    the FP32 pipe meet the FP64 tolerances against the oracle (random
+    self-energy, conv and tail)."""
+    m = model
+    rng = np.random.default_rng(3)
+    sig = 0.05 * (rng.standard_normal(m["Gk"].shape) - 1j * np.abs(rng.standard_normal(m["Gk"].shape)))
+    G = O.gen_green(sig, m["hamk"], m["mu"], m["temp"])
+    a = (m["S"], m["C"], G, m["olist"], m["kmap"], m["invk"], m["temp"], m["Nx"], m["Ny"], m["Nz"])
+    t = (m["S"], m["C"], G, m["eig"], m["uni"], m["olist"], m["kmap"], m["invk"], m["mu"], m["temp"], m["Nx"],
+         m["Ny"], m["Nz"])
+    F.set_precision(48)
+    try:
+        conv, st = F.get_chi0(*a)
+        tail, st_t = F.get_chi0_tail(*t)
+    finally:
+        F.set_precision(64)
+    conv_o, st_o = O.get_chi0(*a)
+    close(conv, conv_o)
+    assert abs(st - st_o) <= 1e-9 * max(1.0, abs(st_o))
+    close(tail, O.get_chi0_tail(*t)[0])
+
+
+@pytest.mark.parametrize("tail", [False, True])
+def test_double_float_mkself_matches_oracle(F, tail):
+    """Precision 48 FLEX loop (double-float chi0 and Sigma, FP64 vertex) against
+    the oracle's FP64 loop, same iteration count."""
+    m = build_model(2, 4, 4, 1, 16, 0.1, 0.0, U=0.8, J=0.1)
+    args = (m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"], 0.9,
+            m["temp"], m["Nw"], m["Nx"], m["Ny"], m["Nz"], False, False)
+    kw = dict(eps=1e-8, pp=0.5, sw_rescale=True, sw_tail=tail)
+    F.set_precision(48)
+    try:
+        sg, mu = F.mkself(*args, **kw)
+        st = F.last_stats()
+    finally:
+        F.set_precision(64)
+    sgo, muo, r = O.mkself(*args, **kw, full=True)
+    assert st["iterations"] == r.iterations
+    assert abs(mu - muo) < 1e-8
+    close(sg, sgo, 1e-7, 1e-9)
