@@ -15,6 +15,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <unordered_map>
 #include <vector>
 
@@ -360,7 +361,7 @@ double chi0_entry(double2* chi_out, const double* Smat, const double* Cmat, cons
     stoner<R>(g, chi.p, S.p, C.p, &sdw, &cdw, &qs, &qc);
     ckchi_print(g, sdw, cdw, qs, qc);
   }
-  if (sizeof(R) == 8) {
+  if (std::is_same<R, double>::value) {
     chi.download(chi_out, KC);
   } else {
     DBuf<double2> w(KC);

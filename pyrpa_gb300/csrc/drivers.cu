@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <fstream>
 #include <vector>
 
@@ -708,7 +709,8 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
     g_stats.t_vertex += tv.stop();
     if (chi_host) {
       DBuf<double2> tmp(KC);
-      if (sizeof(R) == 8) PGB_CUDA(cudaMemcpyAsync(tmp.p, chi, KC * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      if (std::is_same<R, double>::value)
+        PGB_CUDA(cudaMemcpyAsync(tmp.p, chi, KC * sizeof(double2), cudaMemcpyDeviceToDevice, st));
       else widen<R>(tmp.p, chi, KC);
       tmp.download(chi_host, KC);
       sync();
@@ -909,7 +911,8 @@ void run_lin_eliash(const LinEliashArgs& a) {
   {
     DBuf<double2> tmp(KC);
     tmp.upload(a.chi, KC);
-    if (sizeof(R) == 8) PGB_CUDA(cudaMemcpyAsync(chi.p, tmp.p, KC * sizeof(double2), cudaMemcpyDeviceToDevice, ctx().stream));
+    if (std::is_same<R, double>::value)
+      PGB_CUDA(cudaMemcpyAsync(chi.p, tmp.p, KC * sizeof(double2), cudaMemcpyDeviceToDevice, ctx().stream));
     else narrow<R>(chi.p, tmp.p, KC);
   }
   EliashParams prm{a.temp, a.eps, a.itemax, a.gap_sym, a.arnoldi_m};

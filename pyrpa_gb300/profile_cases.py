@@ -4,10 +4,12 @@ Each case runs one ABI call on a synthetic input that is larger than L2
 (129 MB) but a few hundred MB at most, so that a profiler capture of one
 launch replays quickly:
 
-  vertex   get_vsigma_flex_nosoc_ on a 5-orbital chi0 (Nchi = 25),
-           130 irreducible q x 512 frequencies = 66,560 matrices (333 MB c64)
+  vertex   get_vsigma_flex_nosoc_ (FP64, as in the reference) on a 5-orbital
+           chi0 (Nchi = 25), 130 irreducible q x 512 frequencies = 66,560
+           matrices (666 MB c128)
   chi0     get_chi0_tail on a 5-orbital 16x16 mesh with 512 frequencies
-  sigma    mkself, one FLEX iteration, same model
+  flex     mkself, one FLEX iteration, same model (the FP32 vertex, chi0 and
+           Sigma kernels at --precision 32)
 
 Run as  python -m pyrpa_gb300.profile_cases <case> [--precision 32|64] [--repeat n]
 """
@@ -56,7 +58,7 @@ def case_chi0(F, repeat):
                         m["temp"], m["N"], m["N"], 1)
 
 
-def case_sigma(F, repeat):
+def case_flex(F, repeat):
     m = _model()
     for _ in range(repeat):
         F.mkself(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"],
@@ -66,7 +68,7 @@ def case_sigma(F, repeat):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("case", choices=["vertex", "chi0", "sigma"])
+    p.add_argument("case", choices=["vertex", "chi0", "flex"])
     p.add_argument("--precision", type=int, default=32, choices=[32, 64])
     p.add_argument("--repeat", type=int, default=1)
     a = p.parse_args(argv)
@@ -75,7 +77,7 @@ def main(argv=None):
     F.set_verbose(0)
     F.set_precision(a.precision)
     t0 = time.perf_counter()
-    {"vertex": case_vertex, "chi0": case_chi0, "sigma": case_sigma}[a.case](F, a.repeat)
+    {"vertex": case_vertex, "chi0": case_chi0, "flex": case_flex}[a.case](F, a.repeat)
     print(f"{a.case}: {a.repeat} call(s) in {time.perf_counter() - t0:.3f} s", flush=True)
     return 0
 
