@@ -4,6 +4,7 @@
 #include <cstring>
 #include <cstdlib>
 #include <map>
+#include <mutex>
 #include <string>
 #include <type_traits>
 
@@ -623,11 +624,22 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
       c.J = Jof(c.l, c.m);
       if (c.has_d) c.dJ = Jof(c.dl, c.dm);
     }
-    DBuf<double2> sawc64(g.Nw);
-    k_sawc<<<grid_1d(g.Nw, 128), 128, 0, st>>>(sawc64.p, g.Nw, (int)g.M, temp);
-    count_launch("sawc");
+    // the sawtooth transform depends on (Nw, T) only: computed once per pair
+    static std::map<std::pair<int, double>, DBuf<double2>*> sawc_cache;
+    static std::mutex sawc_mu;
+    const double2* sawc64 = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(sawc_mu);
+      DBuf<double2>*& e = sawc_cache[std::make_pair(g.Nw, temp)];
+      if (!e) {
+        e = new DBuf<double2>(g.Nw);
+        k_sawc<<<grid_1d(g.Nw, 128), 128, 0, st>>>(e->p, g.Nw, (int)g.M, temp);
+        count_launch("sawc");
+      }
+      sawc64 = e->p;
+    }
     sawc.alloc(g.Nw);
-    narrow<R>(sawc.p, sawc64.p, g.Nw);
+    narrow<R>(sawc.p, sawc64, g.Nw);
   }
   {  // keep only the transforms that are computed
     std::vector<ChiDev> kept;
@@ -664,27 +676,147 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
 }
 
 // ================================================================ stoner ==
+// Largest real part of the eigenvalues of M = sg chi0(q,0) V (fchi.f90:352-399,
+// zgeev there), one warp per matrix: the Householder reduction to Hessenberg
+// form and the Wilkinson-shifted QR iteration of eigvals_general, with lane j
+// owning column j in the left updates and row i in the right updates.  The
+// matrix sits in shared memory with a padded row; every lane evaluates the
+// scalar control flow (deflation, shifts, rotations) from shared memory, so
+// it is warp-uniform.
+constexpr int kStonerWarps = 4;
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
 template <typename R>
-__global__ void k_stoner(double* out, const cx<R>* chi, const double* S, const double* C, int Nk, int Nw,
-                         int n) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2 * Nk) return;
-  const int k = t % Nk, which = t / Nk;
+__global__ void __launch_bounds__(32 * kStonerWarps) k_stoner(double* out, const cx<R>* chi, const double* S,
+                                                              const double* C, int Nk, int Nw, int n) {
+  extern __shared__ __align__(16) unsigned char sm_st[];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ld = n + 1;
+  double2* A = reinterpret_cast<double2*>(sm_st) + (size_t)w * (n * ld + 64);
+  double2* v = A + n * ld;   // Householder vector / rotation sines
+  double* cs = reinterpret_cast<double*>(v + 32);
+  const int t = blockIdx.x * kStonerWarps + w;
+  if (t >= 2 * Nk) return;  // warp-uniform
+  const int k0 = t % Nk, which = t / Nk;
   const double* V = which ? C : S;
   const double sg = which ? -1.0 : 1.0;
-  double2 Mx[kMaxChi * kMaxChi];
-  double2 w[kMaxChi];
-  for (int a = 0; a < n; ++a)
+  if (lane < n) {
     for (int b = 0; b < n; ++b) {
       double2 acc = mkc(0.0, 0.0);
-      for (int c = 0; c < n; ++c) acc += V[c + n * b] * ccast<double>(chi[fidx(k, 0, a, c, Nk, Nw, n)]);
-      Mx[a * n + b] = sg * acc;
+      for (int c = 0; c < n; ++c) acc += V[c + n * b] * ccast<double>(chi[fidx(k0, 0, lane, c, Nk, Nw, n)]);
+      A[lane * ld + b] = sg * acc;
     }
-  const int rc = eigvals_general(Mx, n, w);
-  if (rc < 0) atomicExch(&g_err_dev, 2);
+  }
+  __syncwarp();
+  // Householder reduction to upper Hessenberg form
+  for (int k = 0; k + 2 < n; ++k) {
+    const double xn = sqrt(warp_sum((lane > k && lane < n) ? abs2(A[lane * ld + k]) : 0.0));
+    if (xn == 0) continue;
+    const double2 x0 = A[(k + 1) * ld + k];
+    const double a0 = hypot(x0.x, x0.y);
+    const double2 ph = a0 > 0 ? mkc(x0.x / a0, x0.y / a0) : mkc(1.0, 0.0);
+    const double2 alpha = mkc(-ph.x * xn, -ph.y * xn);
+    double2 vl = mkc(0.0, 0.0);
+    if (lane > k && lane < n) vl = A[lane * ld + k] - ((lane == k + 1) ? alpha : mkc(0.0, 0.0));
+    const double vn = warp_sum(abs2(vl));
+    if (lane < 32) v[lane] = vl;
+    __syncwarp();
+    if (vn == 0) continue;
+    const double sc = 2.0 / vn;
+    if (lane >= k && lane < n) {  // A = (I - sc v v^H) A, column j = lane
+      double2 s = mkc(0.0, 0.0);
+      for (int i = k + 1; i < n; ++i) s += conj(v[i]) * A[i * ld + lane];
+      s = sc * s;
+      for (int i = k + 1; i < n; ++i) A[i * ld + lane] -= v[i] * s;
+    }
+    __syncwarp();
+    if (lane < n) {  // A = A (I - sc v v^H), row i = lane
+      double2 s = mkc(0.0, 0.0);
+      for (int j = k + 1; j < n; ++j) s += A[lane * ld + j] * v[j];
+      s = sc * s;
+      for (int j = k + 1; j < n; ++j) A[lane * ld + j] -= s * conj(v[j]);
+      if (lane >= k + 2) A[lane * ld + k] = mkc(0.0, 0.0);
+    }
+    __syncwarp();
+  }
+  // shifted QR on the active block [l, hi]
   double best = -1e300;
-  for (int i = 0; i < n; ++i) best = fmax(best, w[i].x);
-  out[t] = best;
+  int hi = n - 1, iter = 0, total = 0;
+  bool failed = false;
+  const double eps = 2.220446049250313e-16;
+  while (hi >= 0) {
+    if (hi == 0) { best = fmax(best, A[0].x); break; }
+    int l = hi;
+    while (l > 0) {
+      double s = cabs1(A[(l - 1) * ld + l - 1]) + cabs1(A[l * ld + l]);
+      if (s == 0) s = 1.0;
+      if (cabs1(A[l * ld + l - 1]) <= eps * s) break;
+      --l;
+    }
+    if (l == hi) {
+      best = fmax(best, A[hi * ld + hi].x);
+      --hi;
+      iter = 0;
+      continue;
+    }
+    __syncwarp();
+    if (l > 0 && lane == 0) A[l * ld + l - 1] = mkc(0.0, 0.0);
+    __syncwarp();  // the exceptional shift may read the element just zeroed
+    if (++iter > 60 || ++total > 60 * n) { failed = true; break; }
+    double2 mu;
+    if (iter % 11 == 10) {  // exceptional shift
+      const double e = cabs1(A[hi * ld + hi - 1]) + (hi >= 2 ? cabs1(A[(hi - 1) * ld + hi - 2]) : 0.0);
+      mu = A[hi * ld + hi] + mkc(0.75 * e, 0.0);
+    } else {
+      const double2 a = A[(hi - 1) * ld + hi - 1], b = A[(hi - 1) * ld + hi];
+      const double2 c = A[hi * ld + hi - 1], d = A[hi * ld + hi];
+      const double2 hd = 0.5 * (a - d);
+      const double2 disc = csqrt_(hd * hd + b * c);
+      const double2 m1 = 0.5 * (a + d) + disc, m2 = 0.5 * (a + d) - disc;
+      mu = (abs2(m1 - d) < abs2(m2 - d)) ? m1 : m2;
+    }
+    __syncwarp();
+    if (lane >= l && lane <= hi) A[lane * ld + lane] -= mu;
+    __syncwarp();
+    for (int k = l; k < hi; ++k) {
+      const double2 a = A[k * ld + k], b = A[(k + 1) * ld + k];
+      const double aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
+      const double r = hypot(aa, bb);
+      double c;
+      double2 s;
+      if (r == 0) { c = 1.0; s = mkc(0.0, 0.0); }
+      else if (aa == 0) { c = 0.0; s = conj(b) * (1.0 / bb); }
+      else { c = aa / r; s = mkc(a.x / aa, a.y / aa) * conj(b) * (1.0 / r); }
+      if (lane == 0) { cs[k] = c; v[k] = s; }
+      __syncwarp();
+      if (lane >= k && lane <= hi) {
+        const double2 x = A[k * ld + lane], y = A[(k + 1) * ld + lane];
+        A[k * ld + lane] = c * x + s * y;
+        A[(k + 1) * ld + lane] = c * y - conj(s) * x;
+      }
+      __syncwarp();
+    }
+    for (int k = l; k < hi; ++k) {
+      const double c = cs[k];
+      const double2 s = v[k];
+      const int imax = (k + 2 < hi) ? k + 2 : hi;
+      if (lane >= l && lane <= imax) {
+        const double2 x = A[lane * ld + k], y = A[lane * ld + k + 1];
+        A[lane * ld + k] = c * x + y * conj(s);
+        A[lane * ld + k + 1] = c * y - x * s;
+      }
+      __syncwarp();
+    }
+    if (lane >= l && lane <= hi) A[lane * ld + lane] += mu;
+    __syncwarp();
+  }
+  if (lane == 0) {
+    if (failed) atomicExch(&g_err_dev, 2);
+    out[t] = best;
+  }
 }
 
 template <typename R>
@@ -692,7 +824,14 @@ void stoner(const Geom& g, const cx<R>* chi, const double* S, const double* C, d
             int* q_sdw, int* q_cdw) {
   reset_err();
   DBuf<double> out(2 * (size_t)g.Nk);
-  k_stoner<R><<<grid_1d(2LL * g.Nk, 32), 32, 0, ctx().stream>>>(out.p, chi, S, C, g.Nk, g.Nw, g.Nchi);
+  const size_t smem = (size_t)kStonerWarps * ((size_t)g.Nchi * (g.Nchi + 1) + 64) * sizeof(double2);
+  static bool attr = false;
+  if (!attr) {
+    PGB_CUDA(cudaFuncSetAttribute(k_stoner<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(96 * 1024)));
+    attr = true;
+  }
+  const unsigned blocks = (unsigned)((2LL * g.Nk + kStonerWarps - 1) / kStonerWarps);
+  k_stoner<R><<<blocks, 32 * kStonerWarps, smem, ctx().stream>>>(out.p, chi, S, C, g.Nk, g.Nw, g.Nchi);
   count_launch("stoner");
   std::vector<double> h(2 * (size_t)g.Nk);
   out.download(h.data(), h.size());

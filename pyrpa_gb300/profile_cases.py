@@ -10,6 +10,9 @@ launch replays quickly:
   chi0     get_chi0_tail on a 5-orbital 16x16 mesh with 512 frequencies
   flex     mkself, one FLEX iteration, same model (the FP32 vertex, chi0 and
            Sigma kernels at --precision 32)
+  fft      get_chi0 of a 1-orbital model on the 64x64 mesh with 2048
+           frequencies: FFT passes over 64x64x4096 arrays (134 MB in FP32,
+           larger than L2) as in the 5-orbital benchmark
 
 Run as  python -m pyrpa_gb300.profile_cases <case> [--precision 32|64] [--repeat n]
 """
@@ -58,6 +61,13 @@ def case_chi0(F, repeat):
                         m["temp"], m["N"], m["N"], 1)
 
 
+def case_fft(F, repeat):
+    m = _model(Norb=1, N=64, Nw=2048, temp=0.01)
+    Gk = F.gen_Green0(m["eig"], m["uni"], m["mu"], m["temp"], m["Nw"])
+    for _ in range(repeat):
+        F.get_chi0(m["S"], m["C"], Gk, m["olist"], m["kmap"], m["invk"], m["temp"], m["N"], m["N"], 1)
+
+
 def case_flex(F, repeat):
     m = _model()
     for _ in range(repeat):
@@ -68,7 +78,7 @@ def case_flex(F, repeat):
 
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("case", choices=["vertex", "chi0", "flex"])
+    p.add_argument("case", choices=["vertex", "chi0", "flex", "fft"])
     p.add_argument("--precision", type=int, default=32, choices=[32, 64])
     p.add_argument("--repeat", type=int, default=1)
     a = p.parse_args(argv)
@@ -77,7 +87,7 @@ def main(argv=None):
     F.set_verbose(0)
     F.set_precision(a.precision)
     t0 = time.perf_counter()
-    {"vertex": case_vertex, "chi0": case_chi0, "flex": case_flex}[a.case](F, a.repeat)
+    {"vertex": case_vertex, "chi0": case_chi0, "flex": case_flex, "fft": case_fft}[a.case](F, a.repeat)
     print(f"{a.case}: {a.repeat} call(s) in {time.perf_counter() - t0:.3f} s", flush=True)
     return 0
 
