@@ -273,8 +273,8 @@ def main():
                    "warm_start_iterations": int(stats["iterations_coarse"]),
                    "warm_start_ms": stats["t_warm_ms"],
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
-                   "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, FP64 chi0 and "
-                                          f"Sigma with FP32 vertex for {int(stats['iterations_fp64_fp32vertex'])}, "
+                   "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, double-float chi0 "
+                                          f"and Sigma with FP32 vertex for {int(stats['iterations_fp64_fp32vertex'])}, "
                                           f"then FP64 bulk to eps; Eliashberg FP32 bulk with FP64 Arnoldi",
                                  "32": "FP32 bulk", "64": "FP64"}[a.precision]})
     line = {

@@ -261,14 +261,15 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
     if (contig) { n2 = it % B; b = it / B; } else { b = it % nl; n2 = it / nl; }
     if (b >= nact) continue;
     cx<R> v[A];
+    // four-step twiddle exponent p * k1 mod Lfull in 32 bits (p < 64, k1 < L1 <= Lfull)
+    const int k1o = tw4 ? (int)((contig ? o + b : o) % d.tw_L1) : 0;
 #pragma unroll
     for (int n1 = 0; n1 < A; ++n1) {
       const int p = B * n1 + n2;
       const long long addr = contig ? base + (long long)b * L + p : base + (long long)p * d.S + b;
       v[n1] = arr[addr];
       if (tw4 && !d.tw_post) {
-        const long long k1o = (contig ? o + b : o) % d.tw_L1;
-        const int t = (int)(((long long)p * k1o) % d.tw_Lfull);
+        const int t = (p * k1o) % d.tw_Lfull;
         if (t) v[n1] = v[n1] * twid<R>(full_tab<R>(d), t, sign);
       }
     }
@@ -290,13 +291,13 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
 #pragma unroll
     for (int n2 = 0; n2 < B; ++n2) u[n2] = sm[(b * A + k1) * LDB + n2];
     Dft<R, B>::run(u, sign, line_tab<R>(d), L);
+    const int k1o = tw4 ? (int)((contig ? o + b : o) % d.tw_L1) : 0;
 #pragma unroll
     for (int k2 = 0; k2 < B; ++k2) {
       const int q = k1 + A * k2;
       cx<R> w = u[k2];
       if (tw4 && d.tw_post) {
-        const long long k1o = (contig ? o + b : o) % d.tw_L1;
-        const int t = (int)(((long long)q * k1o) % d.tw_Lfull);
+        const int t = (q * k1o) % d.tw_Lfull;
         if (t) w = w * twid<R>(full_tab<R>(d), t, sign);
       }
       const long long addr = contig ? base + (long long)b * L + q : base + (long long)q * d.S + b;
