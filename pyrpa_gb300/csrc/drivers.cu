@@ -1057,9 +1057,12 @@ void run_pipeline_impl(const PipelineArgs& a, int prec) {
 
 template void run_lin_eliash<float>(const LinEliashArgs&);
 template void run_lin_eliash<double>(const LinEliashArgs&);
-// The Eliashberg stage runs in FP64 for prec 64 and in FP32 bulk otherwise.
+// The Eliashberg stage runs in FP64 for prec 64 and 48 and in FP32 bulk
+// otherwise (PYRPA_GB_ELIASH=fp64 forces FP64).
 void run_pipeline(const PipelineArgs& a, int prec) {
-  if (prec == 64 || prec == kPrecDF) run_pipeline_impl<double>(a, prec);
+  const char* e = std::getenv("PYRPA_GB_ELIASH");
+  const bool eliash64 = e && std::string(e) == "fp64";
+  if (prec == 64 || prec == kPrecDF || eliash64) run_pipeline_impl<double>(a, prec);
   else run_pipeline_impl<float>(a, prec);
 }
 

@@ -1277,11 +1277,12 @@ bool vertex_vs_launch(cx<R>* chi, long long nmat, long long estride, const R* dc
   return true;
 }
 
-// FP32, N = 25: the shared-memory-accumulator kernel instead of the
-// all-register one (PYRPA_GB_VERTEX=vs), for timing both variants
+// FP32, N = 25: the shared-memory-accumulator kernel (default; 3.66 ms
+// against 4.21 ms for 66,560 matrices, from 12 instead of 8 resident warps)
+// or, with PYRPA_GB_VERTEX=reg, the all-register one
 bool vertex_fp32_vs() {
   const char* s = std::getenv("PYRPA_GB_VERTEX");
-  return s && std::string(s) == "vs";
+  return !(s && std::string(s) == "reg");
 }
 
 template <typename R>

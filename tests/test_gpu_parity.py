@@ -334,7 +334,7 @@ def test_fp32_bulk_path(F):
 
 # ---------------------------------------------- register vertex, 16 and 25 pairs
 @pytest.mark.parametrize("Norb", [4, 5])
-@pytest.mark.parametrize("mode", ["fp64", "fp32", "fp32-vs"])
+@pytest.mark.parametrize("mode", ["fp64", "fp32", "fp32-reg"])
 def test_vertex_large_orbital_counts(F, Norb, mode):
     """V_sigma and V_Delta for Nchi = 16 and 25 (the register kernels with the
     shared-memory accumulator in FP64) against the oracle."""
@@ -350,8 +350,8 @@ def test_vertex_large_orbital_counts(F, Norb, mode):
     old = os.environ.get("PYRPA_GB_VERTEX")
     F.set_precision(prec)
     try:
-        if mode == "fp32-vs":
-            os.environ["PYRPA_GB_VERTEX"] = "vs"
+        if mode == "fp32-reg":
+            os.environ["PYRPA_GB_VERTEX"] = "reg"
         v = F.get_Vsigma_nosoc_flex(chis.copy(), m["S"], m["C"])
     finally:
         F.set_precision(64)
