@@ -275,7 +275,7 @@ def main():
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
                    "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, double-float chi0 "
                                           f"and Sigma with FP32 vertex for {int(stats['iterations_fp64_fp32vertex'])}, "
-                                          f"then FP64 bulk to eps; Eliashberg FP32 bulk with FP64 Arnoldi",
+                                          f"then FP64 bulk to eps; Eliashberg stage FP64",
                                  "32": "FP32 bulk", "64": "FP64"}[a.precision]})
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,

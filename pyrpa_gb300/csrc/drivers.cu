@@ -483,10 +483,10 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
     log("esterr=%9.2E\n", esterr);
   };
 
-  auto get_rn = [&](double rmu) { return filling(eg.p, eig.p, Nk, Nw, Norb, rmu, a.temp); };
+  auto get_rn = [&](double rmu) { return filling_cp(eg.p, eig.p, Nk, Nw, Norb, rmu, a.temp); };
 
   auto renew_mu = [&]() {
-    PGB_CHECK(eig_gkinv(eg.p, H.p, sig.p, Nk, Nw, Norb), "eigenvalues of H+Sigma did not converge");
+    charpoly_gk(eg.p, H.p, sig.p, Nk, Nw, Norb);
     const double eps = (esterr > 1.0e-2) ? 1.0e-8 : esterr * 1.0e-1;
     double dmu = std::fabs(mu - mu_old) * 2.0;
     if (dmu < eps * 4.0) dmu = eps * 4.0;
@@ -1057,12 +1057,13 @@ void run_pipeline_impl(const PipelineArgs& a, int prec) {
 
 template void run_lin_eliash<float>(const LinEliashArgs&);
 template void run_lin_eliash<double>(const LinEliashArgs&);
-// The Eliashberg stage runs in FP64 for prec 64 and 48 and in FP32 bulk
-// otherwise (PYRPA_GB_ELIASH=fp64 forces FP64).
+// The Eliashberg stage (final G, chi0, V_Delta, Arnoldi) runs in FP64 except
+// in the pure FP32 mode or with PYRPA_GB_ELIASH=fp32: with FP32 bulk there,
+// lambda of the 5-orbital 64x64x2048 model moved by 3.6e-6 relative.
 void run_pipeline(const PipelineArgs& a, int prec) {
   const char* e = std::getenv("PYRPA_GB_ELIASH");
-  const bool eliash64 = e && std::string(e) == "fp64";
-  if (prec == 64 || prec == kPrecDF || eliash64) run_pipeline_impl<double>(a, prec);
+  const bool eliash32 = (prec == 32) || (e && std::string(e) == "fp32");
+  if (!eliash32) run_pipeline_impl<double>(a, prec);
   else run_pipeline_impl<float>(a, prec);
 }
 

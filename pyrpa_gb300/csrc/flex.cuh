@@ -104,6 +104,9 @@ double2 inner_w(const double2* a, const double2* b, const double* kw, int Nk, lo
 double filling(const double2* eig_g, const double* eig, int Nk, int Nw, int Norb, double mu,
                double temp);
 bool eig_gkinv(double2* eig_g, const double2* hamk, const double2* sig, int Nk, int Nw, int Norb);
+// coefficients of det(z - H - Sigma) per (k, iw) and the filling from them
+void charpoly_gk(double2* cp, const double2* hamk, const double2* sig, int Nk, int Nw, int Norb);
+double filling_cp(const double2* cp, const double* eig, int Nk, int Nw, int Norb, double mu, double temp);
 
 // Eliashberg
 void mkfk(double2* F, const double2* G, const double2* D, long long K, int Norb);
