@@ -165,6 +165,23 @@ struct Error : std::runtime_error {
     if (!(cond)) throw ::pgb::Error(msg);        \
   } while (0)
 
+// Device bytes this process can still allocate: what the driver reports free
+// plus what the default memory pool holds but no longer uses (blocks freed with
+// cudaFreeAsync stay in the pool, whose release threshold is kept at maximum).
+inline size_t device_bytes_available() {
+  size_t freeb = 0, totb = 0;
+  if (cudaMemGetInfo(&freeb, &totb) != cudaSuccess) return 0;
+  int dev = 0;
+  cudaMemPool_t pool;
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    unsigned long long reserved = 0, used = 0;
+    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) == cudaSuccess &&
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) == cudaSuccess && reserved > used)
+      freeb += (size_t)(reserved - used);
+  }
+  return freeb;
+}
+
 inline void launch_check(const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw Error(std::string("launch ") + what + ": " + cudaGetErrorString(e));

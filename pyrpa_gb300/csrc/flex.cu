@@ -651,8 +651,8 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
   dp.upload(hp.data(), hp.size());
   PGB_CUDA(cudaMemsetAsync(chi, 0, sizeof(cx<R>) * (size_t)g.K * g.Nchi * g.Nchi, st));
   // chunk of pairs per backward batch: bounded by free memory
-  size_t freeb = 0, totb = 0;
-  PGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+  sync();
+  const size_t freeb = device_bytes_available();
   long long ch = (long long)((freeb / 3) / (sizeof(cx<R>) * (size_t)g.P));
   ch = std::max(1LL, std::min<long long>(ch, (long long)hp.size()));
   ch = std::min(ch, 64LL);
@@ -2072,8 +2072,8 @@ void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, c
   DBuf<int> def(std::max<size_t>(1, maxt));
   // cache the transformed pairing vertex across Arnoldi steps when it fits
   if (cache && !cache->built) {
-    size_t freeb = 0, totb = 0;
-    PGB_CUDA(cudaMemGetInfo(&freeb, &totb));
+    sync();
+    const size_t freeb = device_bytes_available();
     const size_t need = total * (size_t)g.P * sizeof(cx<R>);
     cache->built = true;
     if (need < freeb * 0.7) {
