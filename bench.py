@@ -263,6 +263,11 @@ def main():
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = (fft["bytes"] / (fft["ms"] / 1e3) / 1e9) if fft["ms"] > 0 else None
     per_launch_bytes = fft["bytes"] / max(1, fft["launches"])
+    # DRAM bytes per algorithmic byte of an FFT pass, from an ncu capture of
+    # fft2_kernel<float,8,8> on one 64x64x4096 array (dram__bytes_read.sum +
+    # dram__bytes_write.sum = 208.7 MB over 268.4 MB algorithmic, mean of 3
+    # launches; the write total misses what is still in L2 at kernel end)
+    traffic_per_byte = 208.7 / 268.4
     in_bytes = sum(x.nbytes for x in (m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"],
                                         m["uni"], m["init"], m["plist"]))
     out_bytes = res["sigmak"].nbytes + res["gap"].nbytes
@@ -288,7 +293,9 @@ def main():
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
                      "bytes_per_launch": per_launch_bytes, "launches": fft["launches"],
-                     "avg_launch_ms": fft["ms"] / max(1, fft["launches"]), "traffic": None},
+                     "avg_launch_ms": fft["ms"] / max(1, fft["launches"]),
+                     "traffic": per_launch_bytes * traffic_per_byte,
+                     "traffic_source": "ncu capture of one 64x64x4096 FP32 pass, scaled by bytes per launch"},
         "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": cores, "kind": "port",
                          "sample": f"{npairs} full-size orbital-pair FFT convolutions (oracle, numpy) in {cwall:.1f} s "
                                    f"on {cores} spawned workers, extrapolated with this run's {iters} FLEX iterations "
