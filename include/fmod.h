@@ -204,6 +204,16 @@ void pyrpa_gb_flex_eliash(double* sigmak, double* mu, double* delta, double* lam
  * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"
  * so that `import libs.flibs` binds every name it expects. */
 
+/* plibs.regrid_sigma_bin (libs/plibs/_calc.py:52-182) without the file I/O:
+ * sigma (Nk,Nw_old,Norb,Norb) of the Matsubara mesh at temp_old onto Nw_new
+ * frequencies at temp_new (evaluated at w_scale * w_n(temp_new)): cubic
+ * spline over the conjugate-extended axis, c0 + c1/(iw) tail beyond the kept
+ * cutoff, diagonal clipped to Im <= 0.  The reference does this in Python;
+ * pyrpa_gb300.seed.regrid_sigma_bin wraps it with the sigma.bin I/O. */
+void pyrpa_gb_regrid_sigma(double* out, const double* sigma, const int64_t* Nk, const int64_t* Nw_old,
+                           const int64_t* Nw_new, const int64_t* Norb, const double* temp_old,
+                           const double* temp_new, const double* w_scale);
+
 /* Allocation-free variant of get_eig_or_tr_chi.  No counterpart in the reference.
  * All pointers are DEVICE pointers in the layouts of get_eig_or_tr_chi: chi
  * (Nk,Nchi,Nchi) complex128, invk (3,Nkall) int64, chiqout (Nkall) complex128.

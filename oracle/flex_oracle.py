@@ -990,3 +990,88 @@ def remap_delta_F(delta0, prt, invk, gap_sym):
     inv = invk[:, 1] == 1
     out[inv] *= dprt * prt[None, None, :, None] * prt[None, None, None, :]
     return out
+
+
+# --------------------------------------------------------------------------- #
+#  Sigma seed regrid along the Matsubara axis (libs/plibs/_calc.py:52-182)
+# --------------------------------------------------------------------------- #
+def _spline_uniform_notaknot(y, h):
+    """Second derivatives M of the not-a-knot cubic spline through y on a
+    uniform grid of spacing h, along axis 1 (scipy's CubicSpline default
+    boundary condition, restated on the uniform grid: the not-a-knot rows make
+    M_1 and M_{n-2} explicit, the interior is tridiagonal)."""
+    n = y.shape[1]
+    r = np.zeros_like(y)
+    r[:, 1:-1] = 6.0 * (y[:, 2:] - 2.0 * y[:, 1:-1] + y[:, :-2]) / (h * h)
+    M = np.zeros_like(y)
+    if n < 4:
+        return M if n < 3 else np.repeat(r[:, 1:2] / 6.0, 3, axis=1)
+    M[:, 1] = r[:, 1] / 6.0
+    M[:, n - 2] = r[:, n - 2] / 6.0
+    m = n - 4  # unknowns M_2 .. M_{n-3}
+    if m > 0:
+        d = r[:, 2:n - 2].copy()
+        d[:, 0] -= M[:, 1]
+        d[:, -1] -= M[:, n - 2]
+        # Thomas algorithm for tridiag(1, 4, 1)
+        c = np.zeros(m)
+        c[0] = 1.0 / 4.0
+        d[:, 0] /= 4.0
+        for i in range(1, m):
+            den = 4.0 - c[i - 1]
+            c[i] = 1.0 / den
+            d[:, i] = (d[:, i] - d[:, i - 1]) / den
+        for i in range(m - 2, -1, -1):
+            d[:, i] -= c[i] * d[:, i + 1]
+        M[:, 2:n - 2] = d
+    M[:, 0] = 2.0 * M[:, 1] - M[:, 2]
+    M[:, n - 1] = 2.0 * M[:, n - 2] - M[:, n - 3]
+    return M
+
+
+def regrid_sigma(sig, temp_old, temp_new, Nw_new, w_scale=1.0):
+    """Sigma(k, iw_n) of the Matsubara mesh at temp_old (Fortran view
+    (Nk, Nw_old, Norb, Norb)) onto Nw_new frequencies at temp_new, as
+    plibs.regrid_sigma_bin computes it (libs/plibs/_calc.py:127-171): the
+    outermost stored frequency is dropped, the data are extended to negative
+    frequencies with Sigma_lm(-iw) = conj Sigma_ml(iw), interpolated by a
+    not-a-knot cubic spline in w, extended beyond the kept cutoff by
+    c0 + c1/(iw) fitted by least squares over the stored points
+    [0.55 n, max(0.85 n, 0.55 n + 4)), and the diagonal clipped to
+    Im Sigma_ll <= 0."""
+    Nk, Nw_old, No, _ = sig.shape
+    s = sig[:, :Nw_old - 1]
+    nk = Nw_old - 1
+    w_old = (2.0 * np.arange(nk) + 1.0) * PI * temp_old
+    w_new = w_scale * (2.0 * np.arange(Nw_new) + 1.0) * PI * temp_new
+    mirror = np.conj(np.swapaxes(s, 2, 3))[:, ::-1]
+    ext = np.concatenate([mirror, s], axis=1)                  # (Nk, 2nk, No, No)
+    wext = np.concatenate([-w_old[::-1], w_old])
+    h = 2.0 * PI * temp_old
+    y = np.moveaxis(ext, 1, -1).reshape(-1, 2 * nk)            # series along the last axis
+    yy = np.concatenate([y.real, y.imag], axis=0)
+    M = _spline_uniform_notaknot(yy, h)
+    out = np.full((yy.shape[0], Nw_new), np.nan)
+    inside = (w_new >= wext[0]) & (w_new <= wext[-1])
+    for q in np.where(inside)[0]:
+        x = w_new[q]
+        i = min(int(np.floor((x - wext[0]) / h)), 2 * nk - 2)
+        a, b = wext[i + 1] - x, x - wext[i]
+        out[:, q] = (M[:, i] * a ** 3 + M[:, i + 1] * b ** 3) / (6.0 * h) + \
+            (yy[:, i] / h - M[:, i] * h / 6.0) * a + (yy[:, i + 1] / h - M[:, i + 1] * h / 6.0) * b
+    half = y.shape[0]
+    res = (out[:half] + 1j * out[half:]).reshape(Nk, No, No, Nw_new)
+    res = np.moveaxis(res, -1, 1).copy()
+    beyond = w_new > w_old[-1]
+    if beyond.any():
+        i0, i1 = int(0.55 * nk), max(int(0.85 * nk), int(0.55 * nk) + 4)
+        basis = np.stack([np.ones(i1 - i0), 1.0 / (1j * w_old[i0:i1])], axis=1)
+        rhs = s[:, i0:i1].reshape(Nk, i1 - i0, No * No).transpose(1, 0, 2).reshape(i1 - i0, -1)
+        coef = np.linalg.lstsq(basis, rhs, rcond=None)[0]
+        c0 = coef[0].reshape(Nk, No, No)
+        c1 = coef[1].reshape(Nk, No, No)
+        res[:, beyond] = c0[:, None] + c1[:, None] / (1j * w_new[beyond])[None, :, None, None]
+    di = np.arange(No)
+    d = res[:, :, di, di]
+    res[:, :, di, di] = d.real + 1j * np.minimum(d.imag, 0.0)
+    return res

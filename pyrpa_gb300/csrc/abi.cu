@@ -824,6 +824,20 @@ void pyrpa_gb_flex_eliash(double2* sigmak, double* mu, double2* delta, double* l
                                      *lambda_out = NAN))
 }
 
+void pyrpa_gb_regrid_sigma(double2* out, const double2* sig, const int64_t* Nk, const int64_t* Nw_old,
+                           const int64_t* Nw_new, const int64_t* Norb, const double* temp_old, const double* temp_new,
+                           const double* w_scale) {
+  ABI_TRY
+  ensure_context();
+  const long long n_old = (*Nk) * (*Nw_old) * (*Norb) * (*Norb), n_new = (*Nk) * (*Nw_new) * (*Norb) * (*Norb);
+  DBuf<double2> s(n_old), o(n_new);
+  s.upload(sig, n_old);
+  regrid_sigma(o.p, s.p, (int)*Nk, (int)*Nw_old, (int)*Nw_new, (int)*Norb, *temp_old, *temp_new, *w_scale);
+  o.download(out, n_new);
+  sync();
+  ABI_CATCH("pyrpa_gb_regrid_sigma", nan_fill(out, (size_t)(*Nk) * (*Nw_new) * (*Norb) * (*Norb)))
+}
+
 void mkfk_trs_nsoc_(double2* fk, const double2* Gk, const double2* delta, const int64_t* Nk, const int64_t* Nw,
                     const int64_t* Norb) {
   ABI_TRY

@@ -1365,6 +1365,123 @@ template <typename R> void scale_chi(cx<R>* chi, long long n, double s) {
   count_launch("scale");
 }
 
+// ============================================== Matsubara regrid of Sigma ==
+// plibs.regrid_sigma_bin (libs/plibs/_calc.py:52-182) on the GPU, one thread
+// per series (k, a, b): the outermost stored frequency is dropped, the series
+// is extended to negative frequencies by Sigma_lm(-iw) = conj Sigma_ml(iw),
+// a not-a-knot cubic spline through the n = 2(Nw_old - 1) points of that
+// uniform grid (spacing 2 pi T_old) is evaluated at the new frequencies, the
+// points beyond the kept cutoff take c0 + c1/(iw) fitted by least squares
+// over the stored window [i0, i1) (2x2 normal equations; the Gram matrix is
+// the same for every series), and the diagonal is clipped to Im <= 0.  On a
+// uniform grid the not-a-knot rows fix M_1 and M_{n-2}; M_2..M_{n-3} solve
+// tridiag(1, 4, 1) by the Thomas algorithm with the shared factors cth[].
+struct RegridArgs {
+  int Nk, Nw_old, Nw_new, No, i0, i1;
+  double temp_old, temp_new, w_scale, sw, sw2;  // sum over the window of 1/w and 1/w^2
+};
+
+__device__ __forceinline__ double2 regrid_y(const double2* sig, int i, int k, int a, int b, const RegridArgs& r) {
+  const int nk = r.Nw_old - 1;
+  return i < nk ? conj(sig[fidx(k, nk - 1 - i, b, a, r.Nk, r.Nw_old, r.No)])
+                : sig[fidx(k, i - nk, a, b, r.Nk, r.Nw_old, r.No)];
+}
+
+__global__ void k_regrid_sigma(double2* out, const double2* sig, double2* dsc, const double* cth, RegridArgs r) {
+  const long long NS = (long long)r.Nk * r.No * r.No;
+  const int nk = r.Nw_old - 1, n = 2 * nk, m = n - 4;
+  const double h = 2.0 * kPi * r.temp_old, h2 = h * h;
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < NS;
+       s += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(s % r.Nk), a = (int)((s / r.Nk) % r.No), b = (int)(s / ((long long)r.Nk * r.No));
+    auto rhs = [&](int i) {  // 6 (y_{i+1} - 2 y_i + y_{i-1}) / h^2
+      const double2 d = regrid_y(sig, i + 1, k, a, b, r) - 2.0 * regrid_y(sig, i, k, a, b, r) +
+                        regrid_y(sig, i - 1, k, a, b, r);
+      return (6.0 / h2) * d;
+    };
+    const double2 M1 = (1.0 / 6.0) * rhs(1), Mn2 = (1.0 / 6.0) * rhs(n - 2);
+    // forward sweep of tridiag(1, 4, 1) for M_2..M_{n-3}, stored [j][series]
+    double2 prev = mkc(0.0, 0.0);
+    for (int j = 0; j < m; ++j) {
+      double2 d = rhs(j + 2);
+      if (j == 0) d = d - M1;
+      if (j == m - 1) d = d - Mn2;
+      d = (j == 0) ? 0.25 * d : (d - prev) * (1.0 / (4.0 - cth[j - 1]));
+      dsc[(long long)j * NS + s] = d;
+      prev = d;
+    }
+    for (int j = m - 2; j >= 0; --j) {
+      const double2 d = dsc[(long long)j * NS + s] - cth[j] * dsc[(long long)(j + 1) * NS + s];
+      dsc[(long long)j * NS + s] = d;
+    }
+    auto Mat = [&](int i) -> double2 {
+      if (i == 1) return M1;
+      if (i == n - 2) return Mn2;
+      if (i == 0) return 2.0 * M1 - (m > 0 ? dsc[s] : Mn2);
+      if (i == n - 1) return 2.0 * Mn2 - (m > 0 ? dsc[(long long)(m - 1) * NS + s] : M1);
+      return dsc[(long long)(i - 2) * NS + s];
+    };
+    // tail c0 + c1/(iw): normal equations of the basis [1, -i/w] over the window
+    double2 b0 = mkc(0.0, 0.0), b1 = mkc(0.0, 0.0);
+    for (int t = r.i0; t < r.i1; ++t) {
+      const double w = (2.0 * t + 1.0) * kPi * r.temp_old;
+      const double2 y = sig[fidx(k, t, a, b, r.Nk, r.Nw_old, r.No)];
+      b0 += y;
+      b1 += mkc(-y.y / w, y.x / w);  // (i/w) y
+    }
+    const double mw = (double)(r.i1 - r.i0), det = mw * r.sw2 - r.sw * r.sw;
+    // G01 = -i sw, G10 = +i sw: c0 = (sw2 b0 + i sw b1)/det, c1 = (-i sw b0 + m b1)/det
+    const double2 c0 = (1.0 / det) * (r.sw2 * b0 + mkc(-r.sw * b1.y, r.sw * b1.x));
+    const double2 c1 = (1.0 / det) * (mkc(r.sw * b0.y, -r.sw * b0.x) + mw * b1);
+    const double x0 = -(2.0 * (nk - 1) + 1.0) * kPi * r.temp_old, xlast = -x0;
+    for (int q = 0; q < r.Nw_new; ++q) {
+      const double x = r.w_scale * (2.0 * q + 1.0) * kPi * r.temp_new;
+      double2 v;
+      if (x >= x0 && x <= xlast) {
+        int i = (int)floor((x - x0) / h);
+        if (i > n - 2) i = n - 2;
+        const double xa = x0 + (i + 1) * h - x, xb = x - (x0 + i * h);
+        const double2 Mi = Mat(i), Mj = Mat(i + 1);
+        const double2 yi = regrid_y(sig, i, k, a, b, r), yj = regrid_y(sig, i + 1, k, a, b, r);
+        v = (1.0 / (6.0 * h)) * (xa * xa * xa * Mi + xb * xb * xb * Mj) + xa * ((1.0 / h) * yi - (h / 6.0) * Mi) +
+            xb * ((1.0 / h) * yj - (h / 6.0) * Mj);
+      } else {
+        v = c0 + mkc(c1.y / x, -c1.x / x);  // c1 / (i x)
+      }
+      if (a == b && v.y > 0) v.y = 0.0;
+      out[fidx(k, q, a, b, r.Nk, r.Nw_new, r.No)] = v;
+    }
+  }
+}
+
+void regrid_sigma(double2* out, const double2* sig, int Nk, int Nw_old, int Nw_new, int Norb, double temp_old,
+                  double temp_new, double w_scale) {
+  PGB_CHECK(Nw_old >= 3, "regrid needs at least 3 stored frequencies");
+  PGB_CHECK(Nw_new >= 1 && Nk >= 1 && Norb >= 1, "non-positive regrid size");
+  PGB_CHECK(temp_old > 0 && temp_new > 0 && w_scale > 0, "non-positive temperature or frequency scale");
+  const int nk = Nw_old - 1, n = 2 * nk, m = n - 4;
+  RegridArgs r{Nk, Nw_old, Nw_new, Norb, (int)(0.55 * nk), 0, temp_old, temp_new, w_scale, 0.0, 0.0};
+  r.i1 = std::max((int)(0.85 * nk), (int)(0.55 * nk) + 4);
+  PGB_CHECK(r.i1 <= nk, "too few stored frequencies for the tail window");
+  for (int t = r.i0; t < r.i1; ++t) {
+    const double w = (2.0 * t + 1.0) * kPi * temp_old;
+    r.sw += 1.0 / w;
+    r.sw2 += 1.0 / (w * w);
+  }
+  std::vector<double> c(std::max(1, m), 0.0);
+  if (m > 0) {
+    c[0] = 0.25;
+    for (int j = 1; j < m; ++j) c[j] = 1.0 / (4.0 - c[j - 1]);
+  }
+  const long long NS = (long long)Nk * Norb * Norb;
+  DBuf<double> dc(c.size());
+  dc.upload(c.data(), c.size());
+  DBuf<double2> dsc((size_t)std::max(1, m) * NS);
+  k_regrid_sigma<<<grid_1d(NS, 128, 65536), 128, 0, ctx().stream>>>(out, sig, dsc.p, dc.p, r);
+  count_launch("regrid_sigma");
+  sync();
+}
+
 // ====================================================== coarse-mesh seed ==
 // Sigma of a coarse mesh on the full coarse grid, [e][n][grid cell], FP32
 __global__ void k_sig_to_grid(float2* out, const double2* sig, const int* grid_irr, const int* grid_flag,

@@ -136,6 +136,11 @@ void lincomb(double2* y, const double2* const* xs, const double2* cs, int m, lon
 // the fine mesh (Nx_f a multiple of Nx_c, and so on).
 void sigma_interp(const Geom& gc, const Geom& gf, const double2* sig_c, double2* sig_f, int Norb, double temp);
 
+// Sigma (Nk, Nw_old, Norb, Norb) of the mesh at temp_old onto Nw_new
+// frequencies at temp_new (plibs.regrid_sigma_bin, libs/plibs/_calc.py:52-182)
+void regrid_sigma(double2* out, const double2* sig, int Nk, int Nw_old, int Nw_new, int Norb, double temp_old,
+                  double temp_new, double w_scale);
+
 // small host helpers
 void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc);
 template <typename R> void widen(double2* out, const cx<R>* in, long long n);

@@ -61,6 +61,7 @@ _SIGNATURES = {
     "pyrpa_gb_flex_eliash": [_c128, _pd, _c128, _pd, _pd, _f64, _f64, _f64, _i64, _i64, _i64, _c128, _f64, _c128,
                              _f64, _f64, ctypes.c_void_p, _pd, _pd, _pd, _pd, _pd, _pi, _pd, _pd] + [_pi] * 10
     + [_pb, _pb, _pi, _pi, _pi, _pd, _i64],
+    "pyrpa_gb_regrid_sigma": [_c128, _c128, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
     "pyrpa_gb_set_precision": [_pi],
     "pyrpa_gb_get_precision": [_pi],
     "pyrpa_gb_set_verbose": [_pi],
@@ -384,6 +385,17 @@ def eig_or_tr_chi_noalloc(out_ptr: int, chi_ptr: int, invk_ptr: int, Nkall: int,
     rc = f(out_ptr, chi_ptr, invk_ptr, Nkall, Nk, Nchi, 1 if sw_eig else 0, stream or None)
     if rc != 0:
         raise RuntimeError(last_error())
+
+
+def regrid_sigma(sigmak, temp_old: float, temp_new: float, Nw_new: int, w_scale: float = 1.0):
+    """sigmak [Norb, Norb, Nw_old, Nk] (the wrappers' layout) onto Nw_new
+    frequencies at temp_new, as plibs.regrid_sigma_bin does to sigma.bin."""
+    sigmak = np.ascontiguousarray(sigmak, dtype=np.complex128)
+    Norb, _, Nw_old, Nk = sigmak.shape
+    out = np.zeros((Norb, Norb, Nw_new, Nk), dtype=np.complex128)
+    _call("pyrpa_gb_regrid_sigma", out, sigmak, i64(Nk), i64(Nw_old), i64(Nw_new), i64(Norb), dbl(temp_old),
+          dbl(temp_new), dbl(w_scale))
+    return out
 
 
 def get_Vsigma_nosoc_flex(chi, Smat, Cmat):

@@ -456,3 +456,46 @@ def test_double_float_mkself_matches_oracle(F, tail):
     assert st["iterations"] == r.iterations
     assert abs(mu - muo) < 1e-8
     close(sg, sgo, 1e-7, 1e-9)
+
+
+# ------------------------------------------------------ sigma.bin regrid seed
+def _regrid_golden():
+    from pathlib import Path
+    return np.load(Path(__file__).resolve().parent / "golden" / "regrid_sigma_golden.npz")
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_regrid_sigma_matches_reference_output(F, case):
+    """pyrpa_gb_regrid_sigma against the output of the reference's own
+    plibs.regrid_sigma_bin (golden vectors), 1e-12 of the maximum."""
+    g = _regrid_golden()
+    sig, ref, par = g[f"case{case}_in"], g[f"case{case}_out"], g[f"case{case}_par"]
+    T_old, T_new, Nw_new, ws = par
+    out = F.regrid_sigma(sig.T, T_old, T_new, int(Nw_new), ws).T
+    close(out, ref, 1e-12, 1e-15)
+
+
+def test_regrid_sigma_bin_file_round_trip(F, tmp_path):
+    """pyrpa_gb300.seed.regrid_sigma_bin reads and writes sigma.bin as the
+    reference does (records, footer of the new mesh)."""
+    from scipy.io import FortranFile
+    from pyrpa_gb300 import seed
+    g = _regrid_golden()
+    sig, ref, par = g["case0_in"], g["case0_out"], g["case0_par"]
+    Nk, Nw_old, No, _ = sig.shape
+    path = tmp_path / "sigma.bin"
+    with FortranFile(str(path), "w") as f:
+        f.write_record(np.array([0.1]))
+        f.write_record(np.array([0.12]))
+        f.write_record(np.ascontiguousarray(sig.ravel(order="F")))
+        f.write_record(np.array([par[0], float(Nw_old), float(No), float(Nk)]))
+    assert seed.regrid_sigma_bin(temp_new=par[1], Nw_new=int(par[2]), path=str(path)) == (Nk, int(par[2]))
+    with FortranFile(str(path), "r") as f:
+        mu, mu_old = f.read_record(np.float64), f.read_record(np.float64)
+        flat = f.read_record(np.complex128)
+        meta = f.read_record(np.float64)
+    assert mu[0] == 0.1 and mu_old[0] == 0.12
+    assert np.allclose(meta, [par[1], par[2], No, Nk])
+    close(flat.reshape((Nk, int(par[2]), No, No), order="F"), ref, 1e-12, 1e-15)
+    with pytest.raises(ValueError):
+        seed.regrid_sigma_bin(temp_old=0.5, temp_new=par[1], path=str(path))
