@@ -214,6 +214,16 @@ void pyrpa_gb_regrid_sigma(double* out, const double* sigma, const int64_t* Nk, 
                            const int64_t* Nw_new, const int64_t* Norb, const double* temp_old,
                            const double* temp_new, const double* w_scale);
 
+/* The k -> R step of plibs.output_self_wannier / output_gap_wannier
+ * (libs/plibs/_wannier_io.py:52-98): data in the wrappers' layout
+ * [Norb][Norb][Nw][Nk_data] (Nk_data = irreducible count, complex conjugate at
+ * -k; or Nkall, full grid) -> inverse FFT over the k mesh (1/Nkall) of the
+ * first min(Ncut, Nw) frequencies, out [Norb][Norb][Ncut][Nz][Ny][Nx].
+ * pyrpa_gb300.wannier does the zeroing, R selection and file output. */
+void pyrpa_gb_wannier_r(double* out, const double* data, const int64_t* kmap, const int64_t* invk,
+                        const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* Nk_data,
+                        const int64_t* Nw, const int64_t* Norb, const int64_t* Ncut);
+
 /* Allocation-free variant of get_eig_or_tr_chi.  No counterpart in the reference.
  * All pointers are DEVICE pointers in the layouts of get_eig_or_tr_chi: chi
  * (Nk,Nchi,Nchi) complex128, invk (3,Nkall) int64, chiqout (Nkall) complex128.

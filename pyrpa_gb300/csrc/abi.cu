@@ -838,6 +838,27 @@ void pyrpa_gb_regrid_sigma(double2* out, const double2* sig, const int64_t* Nk, 
   ABI_CATCH("pyrpa_gb_regrid_sigma", nan_fill(out, (size_t)(*Nk) * (*Nw_new) * (*Norb) * (*Norb)))
 }
 
+void pyrpa_gb_wannier_r(double2* out, const double2* data, const int64_t* kmap, const int64_t* invk,
+                        const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* Nk_data,
+                        const int64_t* Nw, const int64_t* Norb, const int64_t* Ncut) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nkall = (*Nx) * (*Ny) * (*Nz), no = *Norb, nw = *Nw, ncut = std::min(*Ncut, *Nw);
+  PGB_CHECK(*Ncut >= 1, "N_cut must be positive");
+  const bool full_bz = (*Nk_data == nkall) && (irr_count(*Nx, *Ny, *Nz) != nkall);
+  int64_t nk = *Nk_data;
+  if (full_bz) nk = irr_count(*Nx, *Ny, *Nz);
+  Geom g;
+  build_geom(g, kmap, invk, *Nx, *Ny, *Nz, nk, 1, no, no * no <= kMaxChi ? no * no : 1);
+  const long long n_in = (*Nk_data) * nw * no * no, n_out = nkall * ncut * no * no;
+  DBuf<double2> d(n_in), o(n_out);
+  d.upload(data, n_in);
+  wannier_r(o.p, d.p, g, (int)nw, (int)no, (int)ncut, full_bz);
+  o.download(out, n_out);
+  sync();
+  ABI_CATCH("pyrpa_gb_wannier_r", nan_fill(out, (size_t)((*Nx) * (*Ny) * (*Nz) * std::min(*Ncut, *Nw) * (*Norb) * (*Norb))))
+}
+
 void mkfk_trs_nsoc_(double2* fk, const double2* Gk, const double2* delta, const int64_t* Nk, const int64_t* Nw,
                     const int64_t* Norb) {
   ABI_TRY

@@ -1482,6 +1482,55 @@ void regrid_sigma(double2* out, const double2* sig, int Nk, int Nw_old, int Nw_n
   sync();
 }
 
+// ======================================================= Wannier R space ==
+// plibs.output_self_wannier / output_gap_wannier (libs/plibs/_wannier_io.py:
+// 52-68, 70-98): data given on the irreducible k points (or on the full grid)
+// in the wrappers' layout [Norb][Norb][Nw][Nk] is put on the full grid for
+// the first N_cut frequencies, with plain complex conjugation at -k (the
+// writers' convention), and inverse-transformed over k with 1/Nkall.  The
+// full-grid values go to the positions the spatial backward transform reads
+// (FFT4D position tables), so its output is in natural R order.
+__global__ void k_wannier_expand(double2* out, const double2* data, const int* grid_irr, const int* grid_flag,
+                                 const int* pos_x, const int* pos_y, const int* pos_z, int Nx, int Ny, int Nz,
+                                 int Nk, int Nw, int No, int Ncut, int full_bz) {
+  const long long Nkall = (long long)Nx * Ny * Nz;
+  const long long N = Nkall * Ncut * No * No;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)((idx / Nkall) % Ncut);
+    const long long e = idx / (Nkall * Ncut);
+    const int x = (int)(gi % Nx), y = (int)((gi / Nx) % Ny), z = (int)(gi / ((long long)Nx * Ny));
+    const long long p = pos_x[x] + (long long)Nx * (pos_y[y] + (long long)Ny * pos_z[z]);
+    double2 v;
+    if (full_bz) {
+      v = data[(e * Nw + n) * Nkall + gi];
+    } else {
+      v = data[(e * Nw + n) * Nk + grid_irr[gi]];
+      if (grid_flag[gi]) v = conj(v);
+    }
+    out[(e * Ncut + n) * Nkall + p] = v;
+  }
+}
+__global__ void k_scale64(double2* a, long long n, double s) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a[i] = s * a[i];
+}
+
+void wannier_r(double2* out, const double2* data, const Geom& g, int Nw, int No, int Ncut, bool full_bz) {
+  cudaStream_t st = ctx().stream;
+  const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, Ncut, (int)sizeof(double2));
+  const long long N = g.Nkall * Ncut * No * No;
+  k_wannier_expand<<<grid_1d(N, 256, 65536), 256, 0, st>>>(out, data, g.grid_irr.p, g.grid_flag.p, fft.d_pos(0),
+                                                          fft.d_pos(1), fft.d_pos(2), g.Nx, g.Ny, g.Nz, g.Nk, Nw,
+                                                          No, Ncut, full_bz ? 1 : 0);
+  count_launch("wannier_expand");
+  fft.backward_space<double>(out, No * No, st);
+  k_scale64<<<grid_1d(N, 256, 65536), 256, 0, st>>>(out, N, 1.0 / (double)g.Nkall);
+  count_launch("scale");
+  sync();
+}
+
 // ====================================================== coarse-mesh seed ==
 // Sigma of a coarse mesh on the full coarse grid, [e][n][grid cell], FP32
 __global__ void k_sig_to_grid(float2* out, const double2* sig, const int* grid_irr, const int* grid_flag,

@@ -141,6 +141,10 @@ void sigma_interp(const Geom& gc, const Geom& gf, const double2* sig_c, double2*
 void regrid_sigma(double2* out, const double2* sig, int Nk, int Nw_old, int Nw_new, int Norb, double temp_old,
                   double temp_new, double w_scale);
 
+// Sigma or Delta on the irreducible k points (or the full grid) -> R space for
+// the first Ncut frequencies, [Norb][Norb][Ncut][z][y][x] (plibs Wannier writers)
+void wannier_r(double2* out, const double2* data, const Geom& g, int Nw, int No, int Ncut, bool full_bz);
+
 // small host helpers
 void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc);
 template <typename R> void widen(double2* out, const cx<R>* in, long long n);

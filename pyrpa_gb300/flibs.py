@@ -62,6 +62,7 @@ _SIGNATURES = {
                              _f64, _f64, ctypes.c_void_p, _pd, _pd, _pd, _pd, _pd, _pi, _pd, _pd] + [_pi] * 10
     + [_pb, _pb, _pi, _pi, _pi, _pd, _i64],
     "pyrpa_gb_regrid_sigma": [_c128, _c128, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
+    "pyrpa_gb_wannier_r": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _pi, _pi],
     "pyrpa_gb_set_precision": [_pi],
     "pyrpa_gb_get_precision": [_pi],
     "pyrpa_gb_set_verbose": [_pi],
@@ -396,6 +397,20 @@ def regrid_sigma(sigmak, temp_old: float, temp_new: float, Nw_new: int, w_scale:
     _call("pyrpa_gb_regrid_sigma", out, sigmak, i64(Nk), i64(Nw_old), i64(Nw_new), i64(Norb), dbl(temp_old),
           dbl(temp_new), dbl(w_scale))
     return out
+
+
+def wannier_r(data, kmap, invk, Nx: int, Ny: int, Nz: int, N_cut: int):
+    """data [Norb, Norb, Nw, Nk_irr or Nkall] -> inverse k-FFT for the first
+    N_cut frequencies, [Norb, Norb, N_cut, Nx, Ny, Nz] (conj at -k when data
+    are on the irreducible points)."""
+    data = np.ascontiguousarray(data, dtype=np.complex128)
+    Norb, _, Nw, Nkd = data.shape
+    ncut = min(N_cut, Nw)
+    out = np.zeros((Norb, Norb, ncut, Nz, Ny, Nx), dtype=np.complex128)
+    _call("pyrpa_gb_wannier_r", out, data, np.ascontiguousarray(kmap, dtype=np.int64),
+          np.ascontiguousarray(invk, dtype=np.int64), i64(Nx), i64(Ny), i64(Nz), i64(Nkd), i64(Nw), i64(Norb),
+          i64(N_cut))
+    return np.ascontiguousarray(out.transpose(0, 1, 2, 5, 4, 3))
 
 
 def get_Vsigma_nosoc_flex(chi, Smat, Cmat):

@@ -499,3 +499,34 @@ def test_regrid_sigma_bin_file_round_trip(F, tmp_path):
     close(flat.reshape((Nk, int(par[2]), No, No), order="F"), ref, 1e-12, 1e-15)
     with pytest.raises(ValueError):
         seed.regrid_sigma_bin(temp_old=0.5, temp_new=par[1], path=str(path))
+
+
+# ------------------------------------------------------ Wannier R-space output
+@pytest.mark.parametrize("case", range(3))
+def test_wannier_output_matches_reference_files(F, case, tmp_path):
+    """pyrpa_gb300.wannier against the files the reference's own
+    output_self_wannier / output_gap_wannier wrote (golden vectors)."""
+    from pathlib import Path
+    from pyrpa_gb300 import wannier
+    g = np.load(Path(__file__).resolve().parent / "golden" / "wannier_golden.npz")
+    Nx, Ny, Nz, Nw, Ncut, tol, is_self = g[f"case{case}_par"]
+    Nx, Ny, Nz, Nw, Ncut = int(Nx), int(Ny), int(Nz), int(Nw), int(Ncut)
+    data = g[f"case{case}_data"]
+    klist, kmap, invk = F.gen_irr_k_TRS(Nx, Ny, Nz)
+    fname = str(tmp_path / "w")
+    if is_self:
+        wannier.output_self_wannier(data, 0.25, kmap, invk, Nx, Ny, Nz, Nw, 0.02, N_cut=Ncut, zero_tol=tol, fname=fname)
+        key = "sigma"
+    else:
+        wannier.output_gap_wannier(data, kmap, invk, Nx, Ny, Nz, Nw, 0.02, N_cut=Ncut, zero_tol=tol, fname=fname)
+        key = "gap"
+    z = np.load(fname + ".npz")
+    assert np.array_equal(z["rvec"], g[f"case{case}_npz_rvec"])
+    close(z[key], g[f"case{case}_npz_{key}"], 1e-12, 1e-15)
+    assert np.allclose(z["iw"], g[f"case{case}_npz_iw"], rtol=1e-15, atol=0)
+    got = (tmp_path / "w.dat").read_text().splitlines()
+    ref = str(g[f"case{case}_dat"]).splitlines()
+    assert got[:2] == ref[:2] and len(got) == len(ref)
+    for a, b in zip(got[2:], ref[2:]):
+        assert a[:21] == b[:21]  # R, orbitals, frequency index
+        assert np.allclose([float(a[21:37]), float(a[37:])], [float(b[21:37]), float(b[37:])], rtol=2e-8, atol=1e-20)
