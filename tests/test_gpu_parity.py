@@ -528,5 +528,5 @@ def test_wannier_output_matches_reference_files(F, case, tmp_path):
     ref = str(g[f"case{case}_dat"]).splitlines()
     assert got[:2] == ref[:2] and len(got) == len(ref)
     for a, b in zip(got[2:], ref[2:]):
-        assert a[:21] == b[:21]  # R, orbitals, frequency index
-        assert np.allclose([float(a[21:37]), float(a[37:])], [float(b[21:37]), float(b[37:])], rtol=2e-8, atol=1e-20)
+        assert a[:23] == b[:23]  # Rx Ry Rz (%4d), io jo (%3d), iw (%5d)
+        assert np.allclose([float(a[23:39]), float(a[39:])], [float(b[23:39]), float(b[39:])], rtol=2e-8, atol=1e-20)
