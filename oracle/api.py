@@ -160,3 +160,19 @@ def conv_delta_orb_to_band(delta, uni, invk, plist, gap_sym):
 def get_plist(rvec, ham_r):
     P = O.get_parity_prop(rvec, ham_r)
     return np.sign(P.T[0, :])
+
+
+def nonlinear_eliashberg(delta_init, Gk, hamk, Smat, Cmat, olist, plist, kmap, invk, mu, temp, gap_sym, Nx, Ny, Nz,
+                         sw_sigma=False, sw_Vconst=False, eps=1.0e-4, itemax=100, m_diis=5, gap_min=1.0e-2,
+                         sw_amp_newton=True, full=False):
+    """libs/flibs/_eliashberg.py nonlinear_eliashberg; like the library, Gk is
+    overwritten with the final G."""
+    Nk = delta_init.shape[-1]
+    sig0 = np.zeros_like(delta_init)
+    r = O.nonlinear_eliashberg(np.asarray(delta_init).T, sig0.T, Gk.T, hamk.transpose(0, 2, 1), Smat.T, Cmat.T,
+                               np.asarray(olist), np.asarray(plist, dtype=np.float64), np.asarray(kmap),
+                               np.asarray(invk), mu, temp, eps, Nx, Ny, Nz, itemax, gap_sym, sw_sigma, sw_Vconst,
+                               m_diis, gap_min, sw_amp_newton)
+    Gk[...] = r.G.T
+    delta, sigma = np.ascontiguousarray(r.delta.T), np.ascontiguousarray(r.sigma.T)
+    return (delta, sigma, r) if full else (delta, sigma)

@@ -1075,3 +1075,203 @@ def regrid_sigma(sig, temp_old, temp_new, Nw_new, w_scale=1.0):
     d = res[:, :, di, di]
     res[:, :, di, di] = d.real + 1j * np.minimum(d.imag, 0.0)
     return res
+
+
+# --------------------------------------------------------------------------- #
+#  Nonlinear FLEX-Eliashberg (ffeliash.f90:1-612)
+# --------------------------------------------------------------------------- #
+def mkgreliah_F(G0, F, delta):
+    """G = G0 (I + Delta F^H) per (k, iw)  (ffeliash.f90:316-343)."""
+    No = G0.shape[-1]
+    M = delta @ np.conj(np.swapaxes(F, -1, -2)) + np.eye(No)
+    return G0 @ M
+
+
+def mkfkeliash_F(G0, G, delta):
+    """F = -G0 Delta G^H, diagonal real, upper = conj(lower)  (ffeliash.f90:345-377)."""
+    F = -(G0 @ (delta @ np.conj(np.swapaxes(G, -1, -2))))
+    return hermitize_lower(F)
+
+
+def mkV_flex_sc(XS0, XC0, S_F, C_F, singlet: bool):
+    """V_sigma and V_Delta from the spin- and charge-channel chi0 (ffeliash.f90:379-452).
+    The double-counting term uses chi0_S S + chi0_C C, as the reference assembles it."""
+    n = S_F.shape[0]
+    I = np.eye(n)
+    P = XS0 @ S_F
+    Q = XC0 @ C_F
+    X5 = P + Q
+    chis = np.linalg.solve(I - P, P)
+    chic = np.linalg.solve(I + Q, Q)
+    Vs = (1.5 * S_F - 0.5 * C_F) + 1.5 * (S_F @ chis) + 0.5 * (C_F @ chic) - 0.25 * ((S_F + C_F) @ X5)
+    if singlet:
+        Vd = 0.5 * (S_F + C_F) + 1.5 * (S_F @ chis) - 0.5 * (C_F @ chic)
+    else:
+        Vd = 0.5 * (S_F - C_F) - 0.5 * (S_F @ chis) - 0.5 * (C_F @ chic)
+    return Vs, Vd
+
+
+def get_chi0_conv_ff(F, grid: KGrid, olist, prt, temp, singlet: bool):
+    """chi^FF bubble by FFT convolution (ffeliash.f90:491-612).  At -k the
+    reference reads F(olist(m,1), olist(l,1)) for the +iw leg of F^+14 and
+    F(olist(l,2), olist(m,2)) for F23 (where +k reads olist(m,2) / olist(m,1));
+    that is restated as it is."""
+    Nk, Nw, No, _ = F.shape
+    Nchi = len(olist)
+    Nkall = len(grid.ki)
+    sgn = dprt = 1.0 if singlet else -1.0
+    weight = temp / Nkall
+    chi = np.zeros((Nk, Nw, Nchi, Nchi), dtype=np.complex128)
+    chi_map, irr = get_chi_map(olist)
+    o1, o2 = olist[:, 0] - 1, olist[:, 1] - 1
+    rev = 2 * Nw - 1 - np.arange(Nw)
+    d = grid.flag == 0
+    for (l, m) in irr:
+        A = grid.empty(2 * Nw)
+        B = grid.empty(2 * Nw)
+        pa = prt[o1[l]] * prt[o2[m]] * sgn * dprt
+        pb = prt[o1[m]] * prt[o2[l]] * sgn * dprt
+        for sel, inv in ((d, False), (~d, True)):
+            gx, gy, gz, ki = grid.gx[sel], grid.gy[sel], grid.gz[sel], grid.ki[sel]
+            ix = (gx[:, None], gy[:, None], gz[:, None], rev[None, :])
+            if not inv:
+                A[gx, gy, gz, :Nw] = np.conj(F[ki, :, o2[m], o1[l]])
+                B[gx, gy, gz, :Nw] = F[ki, :, o2[l], o1[m]]
+                A[ix] = pa * np.conj(F[ki, :, o1[l], o2[m]])
+                B[ix] = pb * F[ki, :, o1[m], o2[l]]
+            else:
+                A[gx, gy, gz, :Nw] = np.conj(F[ki, :, o1[m], o1[l]])
+                B[gx, gy, gz, :Nw] = F[ki, :, o2[l], o2[m]]
+                A[ix] = pa * np.conj(F[ki, :, o1[l], o2[m]])
+                B[ix] = pb * F[ki, :, o2[l], o1[m]]
+        tmp = np.fft.ifftn(-np.fft.fftn(A) * _reverse_all(np.fft.fftn(B)))
+        v = grid.gather_irr(tmp, Nw) * weight
+        v = np.where(np.abs(v.real) < 1e-9, 0.0, v.real) + 1j * np.where(np.abs(v.imag) < 1e-9, 0.0, v.imag)
+        chi[:, :, m, l] = v
+        m2, l2 = chi_map[m, l]
+        chi[:, :, m2, l2] = np.conj(chi[:, :, m, l])
+    return chi
+
+
+def get_chi0sc(G, F, grid, olist, prt, temp, singlet):
+    """(chi0_S, chi0_C) = chi^GG +- chi^FF  (ffeliash.f90:454-489)."""
+    gg = get_chi0_conv(G, grid, olist, temp)
+    ff = get_chi0_conv_ff(F, grid, olist, prt, temp, singlet)
+    return gg + ff, gg - ff
+
+
+class NonlinEliashResult:
+    def __init__(self, delta, sigma, G, iterations, history):
+        self.delta, self.sigma, self.G = delta, sigma, G
+        self.iterations, self.history = iterations, history
+
+
+def nonlinear_eliashberg(delta, sigma, G, H_F, S_F, C_F, olist, prt, kmap, invk, mu, temp, eps, Nx, Ny, Nz,
+                         itemax, gap_sym, sw_sigma, sw_Vconst, m_diis, gap_min, sw_amp_newton):
+    """Nonlinear FLEX-Eliashberg loop (ffeliash.f90:2-314), Fortran-view arrays."""
+    delta, sigma, G = delta.copy(), sigma.copy(), G.copy()
+    grid = KGrid(kmap, invk, Nx, Ny, Nz)
+    Nkall = len(grid.ki)
+    singlet = gap_sym >= 0
+    m_eff = max(int(m_diis), 1)
+    pp, eps_reg = 0.3, 1.0e-12
+    weight = temp / Nkall
+    xout = [None] * m_eff
+    res = [None] * m_eff
+    n_hist = i_hist = 0
+    amp_phase, npts, n_polish, n_anchor = 1, 0, 0, 0
+    a1 = a2 = g1 = g2 = 0.0
+    a_cur = float(np.sqrt(np.sum(np.conj(delta) * delta).real)) + 1.0e-300
+    v0 = delta / a_cur
+    if not sw_amp_newton:
+        amp_phase = 2
+    G0 = G.copy()
+    delta0_max = np.abs(delta).max() + 1.0e-30
+    if sw_Vconst:
+        XS, XC = get_chi0sc(G, np.zeros_like(G), grid, olist, prt, temp, singlet)
+        F = mkfk_F(G, delta)
+    else:
+        F = mkfk_F(G, delta)
+        XS, XC = get_chi0sc(G, F, grid, olist, prt, temp, singlet)
+    Vs, Vd = mkV_flex_sc(XS, XC, S_F, C_F, singlet)
+    if not sw_sigma:
+        sigma[...] = 0.0
+    history = []
+    it = 0
+    for it in range(1, itemax + 1):
+        newdelta = mkdelta_nsoc(F, Vd, S_F, C_F, grid, prt, olist, singlet) * weight
+        diff = np.abs(newdelta - delta).max()
+        norm = np.abs(delta).max() + 1.0e-30
+        new_max = np.abs(newdelta).max()
+        history.append(dict(rel=diff / norm, new_max=new_max))
+        if diff / norm < eps:
+            delta = newdelta
+            break
+        if gap_min > 0.0 and new_max < gap_min * delta0_max:
+            delta = newdelta
+            break
+        if sw_amp_newton and amp_phase == 2 and n_polish >= 10:
+            a_cur = float(np.sqrt(np.sum(np.conj(delta) * delta).real)) + 1.0e-300
+            v0 = delta / a_cur
+            npts, a1, a2, g1, g2 = 0, 0.0, 0.0, 0.0, 0.0
+            amp_phase = 1
+            n_anchor += 1
+        if amp_phase == 1:
+            proj = float(np.sum(np.conj(v0) * newdelta).real)
+            g_cur = proj / a_cur
+            a2, g2, a1, g1 = a1, g1, a_cur, g_cur
+            npts = min(npts + 1, 2)
+            if npts >= 2 and abs(a1 * a1 - a2 * a2) > 1.0e-30:
+                cfit = (g1 - g2) / (a2 * a2 - a1 * a1)
+                lam0 = g1 + cfit * a1 * a1
+                if cfit > 1.0e-12 and lam0 > 1.0:
+                    a_nxt = float(np.sqrt((lam0 - 1.0) / cfit))
+                    a_nxt = min(max(a_nxt, 0.3 * a_cur), 3.0 * a_cur)
+                else:
+                    a_nxt = 0.5 * a_cur
+            else:
+                a_nxt = 0.9 * a_cur if abs(g_cur - 1.0) < 0.2 else 0.6 * a_cur
+            if abs(g_cur - 1.0) < 2.0e-2:
+                amp_phase = 2
+                a_nxt = a_cur
+                n_polish = 0
+                n_hist = i_hist = 0
+            delta = a_nxt * v0
+            a_cur = a_nxt
+        else:
+            i_hist = i_hist % m_eff + 1
+            n_hist = min(n_hist + 1, m_eff)
+            n = n_hist
+            xout[i_hist - 1] = newdelta.copy()
+            res[i_hist - 1] = newdelta - delta
+            do_pulay = n >= 2 and m_eff >= 2
+            if do_pulay:
+                idx = [((i_hist - n + h - 1) % m_eff) for h in range(1, n + 1)]
+                B = np.zeros((n + 1, n + 1))
+                for a_, ia in enumerate(idx):
+                    for b_, ib in enumerate(idx):
+                        B[a_, b_] = np.sum(np.conj(res[ia]) * res[ib]).real
+                    B[a_, a_] += eps_reg
+                    B[a_, n] = B[n, a_] = 1.0
+                rhs = np.zeros(n + 1)
+                rhs[n] = 1.0
+                try:
+                    c = np.linalg.solve(B, rhs)
+                except np.linalg.LinAlgError:
+                    do_pulay = False
+            if do_pulay:
+                delta = np.zeros_like(delta)
+                for a_, ia in enumerate(idx):
+                    delta = delta + c[a_] * xout[ia]
+            else:
+                delta = pp * newdelta + (1.0 - pp) * delta
+            n_polish += 1
+        if sw_sigma:
+            sigma = calc_sigma(G, Vs, S_F, C_F, grid, olist, temp)
+            G0 = gen_green_F(sigma, H_F, mu, temp)
+        G = mkgreliah_F(G0, F, delta)
+        F = mkfkeliash_F(G0, G, delta)
+        if not sw_Vconst:
+            XS, XC = get_chi0sc(G, F, grid, olist, prt, temp, singlet)
+            Vs, Vd = mkV_flex_sc(XS, XC, S_F, C_F, singlet)
+    return NonlinEliashResult(delta, sigma, G, it, history)

@@ -226,3 +226,43 @@ def test_mkself_sw_tail_smoke():
     assert np.isfinite(sg2).all()
     smax = np.abs(sg1).max()
     assert smax > 0 and np.abs(sg1 - sg2).max() < 0.6 * smax
+
+
+def test_nonlinear_eliashberg_zero_seed_and_zero_interaction_stays_zero():
+    """test_rpa_flex.py:208-224: the nonlinear FLEX-Eliashberg loop keeps the
+    trivial zero-gap solution at S = C = 0."""
+    rvec, ham_r = M.square_hoppings(1.0, 0.5)
+    klist, kmap, invk = O.gen_irr_k_TRS(2, 2, 1)
+    hamk = O.gen_ham(klist, ham_r, rvec)
+    eig, uni = O.get_eig(hamk)
+    Nw, temp = 3, 0.1
+    Gk = O.gen_Green0(eig, uni, 0.0, temp, Nw)
+    olist, site = O.get_chi_orb_list(1)
+    S, C = O.gen_SCmatrix(np.asarray(olist), site, 0.0, 0.0)
+    delta0 = np.zeros((1, 1, Nw, len(klist)), dtype=np.complex128)
+    delta, sigmak = O.nonlinear_eliashberg(delta0, Gk.copy(), hamk, S, C, olist, np.ones(1), kmap, invk, 0.0, temp,
+                                           0, 2, 2, 1, sw_sigma=False, sw_Vconst=True, eps=1e-6, itemax=2, m_diis=1,
+                                           gap_min=0.0, sw_amp_newton=False)
+    assert delta.shape == delta0.shape and sigmak.shape == delta0.shape
+    assert np.allclose(delta, 0.0) and np.allclose(sigmak, 0.0)
+
+
+def test_nonlinear_eliashberg_oracle_runs_all_branches():
+    """Finite, Hermitian-structured output on a 2-orbital model for the
+    amplitude-secant and DIIS paths, with and without the FLEX self-energy."""
+    rvec, ham_r = M.two_orbital_hoppings()
+    klist, kmap, invk = O.gen_irr_k_TRS(4, 4, 1)
+    hamk = O.gen_ham(klist, ham_r, rvec)
+    eig, uni = O.get_eig(hamk)
+    Nw, temp = 8, 0.1
+    olist, site = O.get_chi_orb_list(2)
+    S, C = O.gen_SCmatrix(np.asarray(olist), site, 1.2, 0.2)
+    init = O.get_initial_gap(klist, 2, 0)
+    d0 = 0.05 * O.get_initial_delta(init, uni, invk, Nw, 0)
+    for kw in (dict(sw_amp_newton=True, sw_sigma=False), dict(sw_amp_newton=False, sw_sigma=True, m_diis=3)):
+        Gk = O.gen_Green0(eig, uni, 0.0, temp, Nw)
+        delta, sigmak, r = O.nonlinear_eliashberg(d0, Gk, hamk, S, C, olist, np.ones(2), kmap, invk, 0.0, temp, 0,
+                                                  4, 4, 1, eps=1e-12, itemax=4, gap_min=0.0, full=True, **kw)
+        assert np.isfinite(delta).all() and np.isfinite(sigmak).all() and np.isfinite(Gk).all()
+        assert r.iterations == 4
+        assert np.allclose(delta[0, 1], np.conj(delta[1, 0]))  # Hermitian in the orbital pair
