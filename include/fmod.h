@@ -199,8 +199,29 @@ void pyrpa_gb_flex_eliash(double* sigmak, double* mu, double* delta, double* lam
                           const int64_t* gap_sym, const int64_t* arnoldi_m, const int64_t* itemax,
                           const double* eps_eliash, const int64_t* coarse);
 
+/* Nonlinear FLEX-Eliashberg loop (libs/src/ffeliash.f90:2-314, bound by
+ * libs/flibs/_eliashberg.py:53-74 and called by nonlinear_eliashberg at
+ * :225-300).  delta (Nk,Nw,Norb,Norb) is the seed on entry and the gap on
+ * exit; Gk is the normal-state G on entry and the last self-consistent G on
+ * exit; sigmak is the FLEX Sigma of the last step (zero unless sw_sigma).
+ * Per iteration: Delta_new = -T/N sum V_Delta F (hermitized), convergence on
+ * max|Delta_new - Delta| / max|Delta| < eps, stop once max|Delta_new| falls
+ * below gap_min * max|Delta_seed|; amplitude secant on the seed shape
+ * (sw_amp_newton) then DIIS over m_diis steps (linear mixing 0.3 below two
+ * entries or on a singular system); optionally Sigma -> G0; then
+ * G = G0 (1 + Delta F^+), F = -G0 Delta G^+ and, unless sw_Vconst, the
+ * spin and charge bubbles chi_S/C = chi^GG +- chi^FF and the vertices
+ * V_sigma, V_Delta.  All of it runs in FP64 on the device. */
+void eliashberg(double* delta, double* sigmak, double* Gk, const double* hamk, const double* Smat,
+                const double* Cmat, const int64_t* olist, const double* prt, const int64_t* kmap,
+                const int64_t* invk, const double* mu, const double* temp, const double* eps,
+                const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw, const int64_t* Nchi,
+                const int64_t* Norb, const int64_t* Nx, const int64_t* Ny, const int64_t* Nz,
+                const int64_t* itemax, const int64_t* gap_sym, const bool* sw_sigma, const bool* sw_Vconst,
+                const int64_t* m_diis, const double* gap_min, const bool* sw_amp_newton);
+
 /* Symbols outside the accelerated path (transport, impurity, SOC, Eilenberger,
- * real-frequency maps, Pade, nonlinear Eliashberg ...) are exported with no
+ * real-frequency maps, Pade ...) are exported with no
  * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"
  * so that `import libs.flibs` binds every name it expects. */
 

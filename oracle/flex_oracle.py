@@ -1236,6 +1236,7 @@ def nonlinear_eliashberg(delta, sigma, G, H_F, S_F, C_F, olist, prt, kmap, invk,
                 a_nxt = a_cur
                 n_polish = 0
                 n_hist = i_hist = 0
+            history[-1].update(phase=1, a=a_cur, g=g_cur, a_next=a_nxt)
             delta = a_nxt * v0
             a_cur = a_nxt
         else:

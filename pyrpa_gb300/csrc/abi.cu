@@ -859,6 +859,22 @@ void pyrpa_gb_wannier_r(double2* out, const double2* data, const int64_t* kmap, 
   ABI_CATCH("pyrpa_gb_wannier_r", nan_fill(out, (size_t)((*Nx) * (*Ny) * (*Nz) * std::min(*Ncut, *Nw) * (*Norb) * (*Norb))))
 }
 
+void eliashberg(double2* delta, double2* sigmak, double2* Gk, const double2* hamk, const double* Smat,
+                const double* Cmat, const int64_t* olist, const double* prt, const int64_t* kmap, const int64_t* invk,
+                const double* mu, const double* temp, const double* eps, const int64_t* Nkall, const int64_t* Nk,
+                const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nx, const int64_t* Ny,
+                const int64_t* Nz, const int64_t* itemax, const int64_t* gap_sym, const bool* sw_sigma,
+                const bool* sw_Vconst, const int64_t* m_diis, const double* gap_min, const bool* sw_amp_newton) {
+  ABI_TRY
+  ensure_context();
+  NonlinArgs a{delta, sigmak, Gk, hamk, Smat, Cmat, olist, prt, kmap, invk, *mu, *temp, *eps, *Nkall, *Nk, *Nw,
+               *Nchi, *Norb, *Nx, *Ny, *Nz, *itemax, *gap_sym, *sw_sigma, *sw_Vconst, *m_diis, *gap_min,
+               *sw_amp_newton};
+  run_nonlin_eliash(a);
+  ABI_CATCH("eliashberg", (nan_fill(delta, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)),
+                           nan_fill(sigmak, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb))))
+}
+
 void mkfk_trs_nsoc_(double2* fk, const double2* Gk, const double2* delta, const int64_t* Nk, const int64_t* Nw,
                     const int64_t* Norb) {
   ABI_TRY
@@ -966,7 +982,6 @@ PGB_STUB(calc_tau_epa)
 PGB_STUB(calc_tdf)
 PGB_STUB(chiq_map)
 PGB_STUB(conv_delta_orb_to_band_soc)
-PGB_STUB(eliashberg)
 PGB_STUB(gen_dos)
 PGB_STUB(gen_green_inv_from_eig)
 PGB_STUB(gen_imp_ham)

@@ -1057,6 +1057,213 @@ void run_pipeline_impl(const PipelineArgs& a, int prec) {
 
 template void run_lin_eliash<float>(const LinEliashArgs&);
 template void run_lin_eliash<double>(const LinEliashArgs&);
+// ================================================ nonlinear Eliashberg ==
+namespace {
+// max |a - b| (b may be null: max |a|), two-level
+__global__ void k_maxabs(double* part, const double2* a, const double2* b, long long n) {
+  __shared__ double red[256];
+  double m = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = b ? a[i] - b[i] : a[i];
+    m = fmax(m, hypot(v.x, v.y));
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+double maxabs(const double2* a, const double2* b, long long n) {
+  DBuf<double> part(1024), out(1);
+  k_maxabs<<<1024, 256, 0, ctx().stream>>>(part.p, a, b, n);
+  launch_check("maxabs");
+  k_max_parts<<<1, 256, 0, ctx().stream>>>(out.p, part.p, 1024);
+  launch_check("max_parts");
+  ctx().kernel_launches += 2;
+  double h = 0;
+  out.download(&h, 1);
+  sync();
+  return h;
+}
+}  // namespace
+
+void run_nonlin_eliash(const NonlinArgs& a) {
+  g_stats = LastStats{};
+  cudaStream_t st = ctx().stream;
+  Inputs in;
+  upload_inputs(in, a.kmap, a.invk, a.olist, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Smat, a.Cmat,
+                a.hamk, nullptr, nullptr);
+  const Geom& g = in.g;
+  const int No = (int)a.Norb, Nchi = (int)a.Nchi, Nk = (int)a.Nk, Nw = (int)a.Nw;
+  const long long K = g.K, KE = K * No * No, KC = K * Nchi * Nchi;
+  const bool singlet = a.gap_sym >= 0;
+  const int m_eff = (int)std::max<int64_t>(a.m_diis, 1);
+  const double pp = 0.3, eps_reg = 1.0e-12, weight = a.temp / (double)g.Nkall, scale = weight / (double)g.P;
+  std::vector<double> hprt(a.prt, a.prt + No);
+  DBuf<double> prt(No);
+  prt.upload(a.prt, No);
+  DBuf<double2> D(KE), ND(KE), Sig(KE), G(KE), G0(KE), F(KE), v0(KE), XS(KC), XC(KC);
+  D.upload(a.delta, KE);
+  G.upload(a.Gk, KE);
+  std::vector<DBuf<double2>> xout(m_eff), res(m_eff);
+  for (int i = 0; i < m_eff; ++i) {
+    xout[i].alloc(KE);
+    res[i].alloc(KE);
+  }
+  log(singlet ? "singlet\n" : "triplet\n");
+  if (a.m_diis <= 1) log("DIIS disabled (m_diis=%lld); pure linear mixing pp=%4.2f.\n", (long long)a.m_diis, pp);
+  else log("DIIS enabled, m_diis=%d; linear-mixing fallback pp=%4.2f.\n", m_eff, pp);
+  auto norm2 = [&](const double2* x) { return dot_re(x, x, KE); };
+  auto set_scaled = [&](double2* y, double c, const double2* x) {  // y = c x
+    const double2* xs[1] = {x};
+    const double2 cs[1] = {make_double2(c, 0.0)};
+    lincomb(y, xs, cs, 1, KE);
+  };
+  auto chi_sc = [&]() {  // XS = chi0_S, XC = chi0_C (ffeliash.f90:454-489)
+    chi0<double>(g, in.p, G.p, a.temp, nullptr, XS.p);
+    chi0_ff<double>(g, in.p, F.p, hprt, a.temp, singlet, XC.p);
+    combine_sc(XS.p, XC.p, KC);
+    double sdw = 0, cdw = 0;
+    int qs = 0, qc = 0;
+    stoner<double>(g, XS.p, in.S.p, in.C.p, &sdw, &cdw, &qs, &qc);
+    ckchi_print(g, sdw, cdw, qs, qc);
+    PGB_CHECK(vertex_sc(XS.p, XC.p, K, Nchi, in.S.p, in.C.p, singlet), "zgesv failed in the SC vertex");
+  };
+  int n_hist = 0, i_hist = 0, amp_phase = 1, npts = 0, n_polish = 0, n_anchor = 0;
+  double a1 = 0, a2 = 0, g1 = 0, g2 = 0;
+  double a_cur = std::sqrt(norm2(D.p)) + 1.0e-300;
+  set_scaled(v0.p, 1.0 / a_cur, D.p);
+  if (!a.sw_amp_newton) amp_phase = 2;
+  PGB_CUDA(cudaMemcpyAsync(G0.p, G.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  const double delta0_max = maxabs(D.p, nullptr, KE) + 1.0e-30;
+  if (a.sw_Vconst) {
+    F.zero();
+    chi_sc();
+    mkfk(F.p, G.p, D.p, K, No);
+  } else {
+    mkfk(F.p, G.p, D.p, K, No);
+    chi_sc();
+  }
+  if (!a.sw_sigma) Sig.zero();
+  DeltaKernelCache<double> cache;  // the transformed V_Delta stays valid while V is constant
+  int it = 0;
+  for (it = 1; it <= a.itemax; ++it) {
+    log("iter=%5d\n", it);
+    mkdelta<double>(g, in.p, F.p, XC.p, in.S.p, in.C.p, prt.p, singlet, scale, ND.p,
+                    a.sw_Vconst ? &cache : nullptr);
+    const double diff = maxabs(ND.p, D.p, KE), dn = maxabs(D.p, nullptr, KE) + 1.0e-30,
+                 new_max = maxabs(ND.p, nullptr, KE);
+    log("  |D_new-D|max=%12.4E  rel=%12.4E  |D_new|max=%12.4E\n", diff, diff / dn, new_max);
+    g_stats.esterr = diff / dn;
+    if (diff / dn < a.eps) {
+      PGB_CUDA(cudaMemcpyAsync(D.p, ND.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      log("converged at iter=%5d\n", it);
+      break;
+    }
+    if (a.gap_min > 0.0 && new_max < a.gap_min * delta0_max) {
+      PGB_CUDA(cudaMemcpyAsync(D.p, ND.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      log("gap collapsed: |D_new|max=%12.4E < %12.4E (likely T >= Tc; no SC solution), stopping\n", new_max,
+          a.gap_min * delta0_max);
+      break;
+    }
+    if (a.sw_amp_newton && amp_phase == 2 && n_polish >= 10) {  // re-anchor the shape
+      a_cur = std::sqrt(norm2(D.p)) + 1.0e-300;
+      set_scaled(v0.p, 1.0 / a_cur, D.p);
+      npts = 0;
+      a1 = a2 = g1 = g2 = 0.0;
+      amp_phase = 1;
+      ++n_anchor;
+      log("  re-anchor #%d: v0 <- relaxed shape, re-solving amplitude\n", n_anchor);
+    }
+    if (amp_phase == 1) {
+      // v0-anchored amplitude: g(a) = <v0, M[a v0]>/a = lam0 - c a^2, root of g = 1
+      const double g_cur = dot_re(v0.p, ND.p, KE) / a_cur;
+      a2 = a1;
+      g2 = g1;
+      a1 = a_cur;
+      g1 = g_cur;
+      npts = std::min(npts + 1, 2);
+      double a_nxt;
+      if (npts >= 2 && std::fabs(a1 * a1 - a2 * a2) > 1.0e-30) {
+        const double cfit = (g1 - g2) / (a2 * a2 - a1 * a1), lam0 = g1 + cfit * a1 * a1;
+        if (cfit > 1.0e-12 && lam0 > 1.0) {
+          a_nxt = std::sqrt((lam0 - 1.0) / cfit);
+          a_nxt = std::min(std::max(a_nxt, 0.3 * a_cur), 3.0 * a_cur);
+        } else {
+          a_nxt = 0.5 * a_cur;
+        }
+      } else {
+        a_nxt = std::fabs(g_cur - 1.0) < 0.2 ? 0.9 * a_cur : 0.6 * a_cur;
+      }
+      if (std::fabs(g_cur - 1.0) < 2.0e-2) {
+        amp_phase = 2;
+        a_nxt = a_cur;
+        n_polish = 0;
+        n_hist = i_hist = 0;
+        log("  amplitude solved (g=%9.5f); DIIS shape polish\n", g_cur);
+      }
+      set_scaled(D.p, a_nxt, v0.p);
+      a_cur = a_nxt;
+    } else {
+      i_hist = i_hist % m_eff + 1;
+      n_hist = std::min(n_hist + 1, m_eff);
+      const int n = n_hist, slot = i_hist - 1;
+      PGB_CUDA(cudaMemcpyAsync(xout[slot].p, ND.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      {
+        const double2* xs[2] = {ND.p, D.p};
+        const double2 cs[2] = {make_double2(1.0, 0.0), make_double2(-1.0, 0.0)};
+        lincomb(res[slot].p, xs, cs, 2, KE);
+      }
+      bool do_pulay = n >= 2 && m_eff >= 2;
+      std::vector<int> idx(n);
+      std::vector<double> c(n + 1, 0.0);
+      if (do_pulay) {
+        for (int h = 1; h <= n; ++h) idx[h - 1] = ((i_hist - n + h - 1) % m_eff + m_eff) % m_eff;
+        const int nn = n + 1;
+        std::vector<double> B((size_t)nn * nn, 0.0);
+        for (int i = 0; i < n; ++i) {
+          for (int j = 0; j < n; ++j) B[i * nn + j] = dot_re(res[idx[i]].p, res[idx[j]].p, KE);
+          B[i * nn + i] += eps_reg;
+          B[i * nn + n] = B[n * nn + i] = 1.0;
+        }
+        c[n] = 1.0;
+        if (!solve_real(B, c, nn)) {
+          log("DIIS: dgesv failed, falling back to linear mixing pp=0.30.\n");
+          do_pulay = false;
+        }
+      }
+      if (do_pulay) {
+        std::vector<const double2*> xs(n);
+        std::vector<double2> cs(n);
+        for (int h = 0; h < n; ++h) {
+          xs[h] = xout[idx[h]].p;
+          cs[h] = make_double2(c[h], 0.0);
+        }
+        lincomb(D.p, xs.data(), cs.data(), n, KE);
+      } else {
+        const double2* xs[2] = {ND.p, D.p};
+        const double2 cs[2] = {make_double2(pp, 0.0), make_double2(1.0 - pp, 0.0)};
+        lincomb(D.p, xs, cs, 2, KE);
+      }
+      ++n_polish;
+    }
+    if (a.sw_sigma) {  // FLEX self-energy and the dressed G0 (no HF subtraction here)
+      sigma<double>(g, in.p, G.p, XS.p, in.S.p, in.C.p, a.temp, Sig.p);
+      PGB_CHECK(dyson(G0.p, Sig.p, in.H.p, a.mu, a.temp, Nk, Nw, No), "singular G^-1 in the Dyson step");
+    }
+    mkgreliah(G.p, G0.p, F.p, D.p, K, No);
+    mkfkeliash(F.p, G0.p, G.p, D.p, K, No);
+    if (!a.sw_Vconst) chi_sc();
+  }
+  g_stats.iterations = std::min<int>(it, (int)a.itemax);
+  D.download(a.delta, KE);
+  Sig.download(a.sigmak, KE);
+  G.download(a.Gk, KE);
+  sync();
+}
+
 // The Eliashberg stage (final G, chi0, V_Delta, Arnoldi) runs in FP64 except
 // in the pure FP32 mode or with PYRPA_GB_ELIASH=fp32: with FP32 bulk there,
 // lambda of the 5-orbital 64x64x2048 model moved by 3.6e-6 relative.

@@ -70,6 +70,24 @@ struct PipelineArgs {
   int64_t coarse_kdiv = 1, coarse_wdiv = 1;
 };
 
+// nonlinear FLEX-Eliashberg loop (ffeliash.f90:2-314), host pointers as the ABI receives them
+struct NonlinArgs {
+  double2* delta;                  // inout (Nk,Nw,Norb,Norb)
+  double2* sigmak;                 // out
+  double2* Gk;                     // inout: initial G, on exit the last SC G
+  const double2* hamk;             // (Norb,Norb,Nk)
+  const double *Smat, *Cmat;
+  const int64_t* olist;
+  const double* prt;
+  const int64_t *kmap, *invk;
+  double mu, temp, eps;
+  int64_t Nkall, Nk, Nw, Nchi, Norb, Nx, Ny, Nz, itemax, gap_sym;
+  bool sw_sigma, sw_Vconst;
+  int64_t m_diis;
+  double gap_min;
+  bool sw_amp_newton;
+};
+
 // uploaded model data shared by the solvers
 struct Inputs {
   Geom g;
@@ -127,6 +145,7 @@ int64_t make_irr_mesh(int64_t nx, int64_t ny, int64_t nz, std::vector<int64_t>& 
 void run_mkself(const MkselfArgs& a, int prec);
 template <typename R> void run_lin_eliash(const LinEliashArgs& a);
 void run_pipeline(const PipelineArgs& a, int prec);
+void run_nonlin_eliash(const NonlinArgs& a);
 const LastStats& last_stats();
 
 }  // namespace pgb

@@ -1531,6 +1531,264 @@ void wannier_r(double2* out, const double2* data, const Geom& g, int Nw, int No,
   sync();
 }
 
+// ============================================ nonlinear FLEX-Eliashberg ==
+// SC Dyson updates of ffeliash.f90:316-377, per (k, iw):
+//   G = G0 (I + Delta F^H),   F = -G0 Delta G^H (diagonal real, upper = conj lower)
+__global__ void k_mkgreliah(double2* G, const double2* G0, const double2* F, const double2* D, long long K, int No) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double2 m[kMaxOrb * kMaxOrb];
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 s = mkc(a == b ? 1.0 : 0.0, 0.0);
+        for (int c = 0; c < No; ++c) s += D[idx + K * (a + No * c)] * conj(F[idx + K * (b + No * c)]);
+        m[a * No + b] = s;
+      }
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 s = mkc(0.0, 0.0);
+        for (int c = 0; c < No; ++c) s += G0[idx + K * (a + No * c)] * m[c * No + b];
+        G[idx + K * (a + No * b)] = s;
+      }
+  }
+}
+__global__ void k_mkfkeliash(double2* F, const double2* G0, const double2* G, const double2* D, long long K, int No) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double2 m[kMaxOrb * kMaxOrb];
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 s = mkc(0.0, 0.0);
+        for (int c = 0; c < No; ++c) s += D[idx + K * (a + No * c)] * conj(G[idx + K * (b + No * c)]);
+        m[a * No + b] = s;
+      }
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b <= a; ++b) {
+        double2 s = mkc(0.0, 0.0);
+        for (int c = 0; c < No; ++c) s += G0[idx + K * (a + No * c)] * m[c * No + b];
+        s = -s;
+        if (a == b) s.y = 0.0;
+        F[idx + K * (a + No * b)] = s;
+        if (a != b) F[idx + K * (b + No * a)] = conj(s);
+      }
+  }
+}
+void mkgreliah(double2* G, const double2* G0, const double2* F, const double2* D, long long K, int Norb) {
+  k_mkgreliah<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, G0, F, D, K, Norb);
+  count_launch("mkgreliah");
+}
+void mkfkeliash(double2* F, const double2* G0, const double2* G, const double2* D, long long K, int Norb) {
+  k_mkfkeliash<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(F, G0, G, D, K, Norb);
+  count_launch("mkfkeliash");
+}
+
+// chi^FF padding of one irreducible pair (l, m) (ffeliash.f90:556-570):
+// array 2c is F^+14, array 2c+1 is F23; at -k the reference reads
+// F(o1[m], o1[l]) for the +iw leg of F^+14 and F(o2[l], o2[m]) for F23.
+struct FFPad {
+  int o1l, o2l, o1m, o2m;
+  double pa, pb;  // prt products times sgn * dprt
+};
+template <typename R>
+__global__ void k_pad_ff(cx<R>* out, const double2* F, const FFPad* pads, const int* grid_irr, const int* grid_flag,
+                         long long Nkall, int Nk, int Nw, int No, long long P) {
+  const int c = blockIdx.y >> 1, which = blockIdx.y & 1;
+  const FFPad t = pads[c];
+  cx<R>* o = out + (long long)blockIdx.y * P;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)(idx / Nkall);
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    double2 v;
+    if (n < Nw) {
+      if (which == 0) v = conj(fl ? F[fidx(k, n, t.o1m, t.o1l, Nk, Nw, No)] : F[fidx(k, n, t.o2m, t.o1l, Nk, Nw, No)]);
+      else v = fl ? F[fidx(k, n, t.o2l, t.o2m, Nk, Nw, No)] : F[fidx(k, n, t.o2l, t.o1m, Nk, Nw, No)];
+    } else {
+      const int j = 2 * Nw - 1 - n;
+      if (which == 0) v = t.pa * conj(F[fidx(k, j, t.o1l, t.o2m, Nk, Nw, No)]);
+      else v = t.pb * (fl ? F[fidx(k, j, t.o2l, t.o1m, Nk, Nw, No)] : F[fidx(k, j, t.o1m, t.o2l, Nk, Nw, No)]);
+    }
+    o[idx] = cmk<R>((R)v.x, (R)v.y);
+  }
+}
+
+// chi^FF(q, nu) = -sum F^+14(k+q) F23(k) by FFT convolution (ffeliash.f90:491-612)
+template <typename R>
+void chi0_ff(const Geom& g, const Pairs& p, const double2* F, const std::vector<double>& prt, double temp,
+             bool singlet, cx<R>* chi) {
+  cudaStream_t st = ctx().stream;
+  const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, (int)g.M, (int)sizeof(cx<R>));
+  const double sgnd = singlet ? 1.0 : 1.0;  // sgn * dprt: (+1)(+1) singlet, (-1)(-1) triplet
+  std::vector<FFPad> hp(p.chi.size());
+  std::vector<ChiDev> hc(p.chi.size());
+  for (size_t i = 0; i < p.chi.size(); ++i) {
+    const ChiPair& c = p.chi[i];
+    const int o1l = p.o1[c.l], o2l = p.o2[c.l], o1m = p.o1[c.m], o2m = p.o2[c.m];
+    hp[i] = FFPad{o1l, o2l, o1m, o2m, prt[o1l] * prt[o2m] * sgnd, prt[o1m] * prt[o2l] * sgnd};
+    hc[i] = ChiDev{c.m, c.l, c.m2, c.l2, 0, 0, c.self, 0, make_double2(0, 0), 0, 0, 0, 0, make_double2(0, 0)};
+  }
+  PGB_CUDA(cudaMemsetAsync(chi, 0, sizeof(cx<R>) * (size_t)g.K * g.Nchi * g.Nchi, st));
+  sync();
+  const size_t freeb = device_bytes_available();
+  long long ch = (long long)((freeb / 4) / (3 * sizeof(cx<R>) * (size_t)g.P));
+  ch = std::max(1LL, std::min<long long>(std::min<long long>(ch, 32), (long long)hp.size()));
+  DBuf<cx<R>> A((size_t)2 * ch * g.P), T((size_t)ch * g.P);
+  DBuf<FFPad> dp(ch);
+  DBuf<ChiDev> dc(ch);
+  const double sc = temp / (double)g.Nkall / (double)g.P;
+  for (long long c0 = 0; c0 < (long long)hp.size(); c0 += ch) {
+    const int nc = (int)std::min<long long>(ch, (long long)hp.size() - c0);
+    std::vector<ChiDev> cc(hc.begin() + c0, hc.begin() + c0 + nc);
+    for (int c = 0; c < nc; ++c) {
+      cc[c].e13 = 2 * c;
+      cc[c].e42 = 2 * c + 1;
+    }
+    dp.upload(hp.data() + c0, nc);
+    dc.upload(cc.data(), nc);
+    k_pad_ff<R><<<dim3(grid_1d(g.P, 256, 4096), 2 * nc), 256, 0, st>>>(A.p, F, dp.p, g.grid_irr.p, g.grid_flag.p,
+                                                                      g.Nkall, g.Nk, g.Nw, g.Norb, g.P);
+    count_launch("pad_ff");
+    fft.forward<R>(A.p, 2 * nc, st);
+    k_chi0_product<R><<<dim3(grid_1d(g.P, 256, 4096), nc), 256, 0, st>>>(
+        T.p, A.p, nullptr, nullptr, nullptr, dc.p, g.P, g.Nx, g.Ny, g.Nz, (int)g.M, fft.d_rev(0), fft.d_rev(1),
+        fft.d_rev(2), fft.d_rev(3), fft.d_logical(3), (R)sc, (R)0);
+    count_launch("chi0_product");
+    fft.backward<R>(T.p, nc, st);
+    k_chi0_scatter<R><<<dim3(grid_1d(g.K, 256, 4096), nc), 256, 0, st>>>(chi, T.p, dc.p, g.irr_grid.p, nullptr,
+                                                                        g.Nkall, g.Nk, g.Nw, g.Nchi, g.P);
+    count_launch("chi0_scatter");
+    sync();
+  }
+}
+
+// chi0_S = GG + FF (into gg), chi0_C = GG - FF (into ff)
+__global__ void k_combine_sc(double2* gg, double2* ff, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 a = gg[i], b = ff[i];
+    gg[i] = a + b;
+    ff[i] = a - b;
+  }
+}
+void combine_sc(double2* gg, double2* ff, long long n) {
+  k_combine_sc<<<grid_1d(n, 256, 65536), 256, 0, ctx().stream>>>(gg, ff, n);
+  count_launch("combine_sc");
+}
+
+// V_sigma and V_Delta from chi0_S (in XS) and chi0_C (in XC), in place
+// (ffeliash.f90:379-452), one warp per (q, iw), row i on lane i:
+//   P = chi0_S S, Q = chi0_C C, chi_s = (I-P)^-1 P, chi_c = (I+Q)^-1 Q,
+//   V_sigma = 3/2 S - 1/2 C + 3/2 S chi_s + 1/2 C chi_c - 1/4 (S+C)(P+Q),
+//   V_Delta = V0 + cs S chi_s + cc C chi_c  (singlet V0=(S+C)/2, cs=3/2, cc=-1/2;
+//             triplet V0=(S-C)/2, cs=cc=-1/2).
+// Per warp, shared memory holds P (then chi_s), Q (then chi_c), P+Q and one
+// accumulation row per lane.
+template <int N, int W>
+__global__ void __launch_bounds__(32 * W) k_vertex_sc(double2* XS, double2* XC, long long K, const double* S,
+                                                      const double* C, int singlet) {
+  extern __shared__ __align__(16) unsigned char smsc[];
+  double* sS = reinterpret_cast<double*>(smsc);  // row-major S, C
+  double* sC = sS + N * N;
+  double2* base = reinterpret_cast<double2*>(smsc + ((2 * N * N * sizeof(double) + 15) / 16) * 16);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double2* Pm = base + (size_t)w * (4 * N * N + 0);
+  double2* Qm = Pm + N * N;
+  double2* X5 = Qm + N * N;
+  double2* Rb = X5 + N * N;  // [j][lane]
+  int* ints = reinterpret_cast<int*>(base + (size_t)W * 4 * N * N);
+  int* pv = ints + w * (N + 1);
+  int* mp = ints + W * (N + 1) + w * 32;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+    sS[(e % N) * N + e / N] = S[e];  // Fortran (a,b) at a + N b -> row-major
+    sC[(e % N) * N + e / N] = C[e];
+  }
+  __syncthreads();
+  const int i = lane < N ? lane : 0;
+  const double cs = singlet ? 1.5 : -0.5, cc = -0.5;
+  const double v0c = singlet ? 1.0 : -1.0;
+  for (long long q = (long long)blockIdx.x * W + w; q < K; q += (long long)gridDim.x * W) {
+    double2 a[N];
+    // P row i = chi0_S(i,:) S ; Q row i = chi0_C(i,:) C
+#pragma unroll
+    for (int j = 0; j < N; ++j) a[j] = XS[q + K * (i + N * j)];
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < N; ++c) s += sS[c * N + j] * a[c];
+      if (lane < N) Pm[i * N + j] = s;
+    }
+#pragma unroll
+    for (int j = 0; j < N; ++j) a[j] = XC[q + K * (i + N * j)];
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < N; ++c) s += sC[c * N + j] * a[c];
+      if (lane < N) {
+        Qm[i * N + j] = s;
+        X5[i * N + j] = Pm[i * N + j] + s;
+      }
+    }
+    __syncwarp();
+    bool ok = true;
+    for (int pass = 0; pass < 2; ++pass) {
+      double2* Mm = pass == 0 ? Pm : Qm;
+      const double sg = pass == 0 ? -1.0 : 1.0;  // I - P, I + Q
+#pragma unroll
+      for (int j = 0; j < N; ++j) a[j] = mkc(i == j ? 1.0 : 0.0, 0.0) + sg * Mm[i * N + j];
+      ok &= warp_inverse<double, N>(a, pv, mp);
+      for (int j = 0; j < N; ++j) Rb[j * 32 + lane] = mkc(0.0, 0.0);
+      for (int c = 0; c < N; ++c) {
+        const double2 ac = pick<double, N>(a, c);
+        for (int j = 0; j < N; ++j) Rb[j * 32 + lane] += ac * Mm[c * N + j];
+      }
+      __syncwarp();
+      if (lane < N)
+        for (int j = 0; j < N; ++j) Mm[i * N + j] = Rb[j * 32 + lane];  // chi_s or chi_c
+      __syncwarp();
+    }
+    if (!ok && lane == 0) atomicExch(&g_err_dev, 5);
+    // V_sigma row i
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(1.5 * sS[i * N + j] - 0.5 * sC[i * N + j], 0.0);
+      for (int c = 0; c < N; ++c)
+        s += 1.5 * sS[i * N + c] * Pm[c * N + j] + 0.5 * sC[i * N + c] * Qm[c * N + j] -
+             0.25 * (sS[i * N + c] + sC[i * N + c]) * X5[c * N + j];
+      if (lane < N) XS[q + K * (i + N * j)] = s;
+    }
+    // V_Delta row i
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(0.5 * (sS[i * N + j] + v0c * sC[i * N + j]), 0.0);
+      for (int c = 0; c < N; ++c) s += cs * sS[i * N + c] * Pm[c * N + j] + cc * sC[i * N + c] * Qm[c * N + j];
+      if (lane < N) XC[q + K * (i + N * j)] = s;
+    }
+    __syncwarp();
+  }
+}
+
+bool vertex_sc(double2* XS, double2* XC, long long K, int Nchi, const double* S, const double* C, bool singlet) {
+  constexpr int W = 2;
+  auto launch = [&](auto kernel, int n) {
+    const size_t smem = ((2 * (size_t)n * n * sizeof(double) + 15) / 16) * 16 + (size_t)W * 4 * n * n * sizeof(double2) +
+                        sizeof(int) * (W * (n + 1) + W * 32);
+    PGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long blocks = std::min<long long>((K + W - 1) / W, (long long)ctx().num_sms * 16);
+    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(XS, XC, K, S, C, singlet ? 1 : 0);
+  };
+  reset_err();
+  switch (Nchi) {
+    case 1: launch(k_vertex_sc<1, W>, 1); break;
+    case 4: launch(k_vertex_sc<4, W>, 4); break;
+    case 9: launch(k_vertex_sc<9, W>, 9); break;
+    case 16: launch(k_vertex_sc<16, W>, 16); break;
+    case 25: launch(k_vertex_sc<25, W>, 25); break;
+    default: throw Error("the nonlinear Eliashberg vertex supports Nchi = Norb^2 with Norb <= 5");
+  }
+  count_launch("vertex_sc");
+  return fetch_err() == 0;
+}
+template void chi0_ff<double>(const Geom&, const Pairs&, const double2*, const std::vector<double>&, double, bool,
+                              double2*);
+
 // ====================================================== coarse-mesh seed ==
 // Sigma of a coarse mesh on the full coarse grid, [e][n][grid cell], FP32
 __global__ void k_sig_to_grid(float2* out, const double2* sig, const int* grid_irr, const int* grid_flag,

@@ -145,6 +145,16 @@ void regrid_sigma(double2* out, const double2* sig, int Nk, int Nw_old, int Nw_n
 // the first Ncut frequencies, [Norb][Norb][Ncut][z][y][x] (plibs Wannier writers)
 void wannier_r(double2* out, const double2* data, const Geom& g, int Nw, int No, int Ncut, bool full_bz);
 
+// nonlinear FLEX-Eliashberg (ffeliash.f90): SC Dyson updates, chi^FF bubble,
+// chi0_S/chi0_C, and the two-channel vertex (V_sigma into XS, V_Delta into XC)
+void mkgreliah(double2* G, const double2* G0, const double2* F, const double2* D, long long K, int Norb);
+void mkfkeliash(double2* F, const double2* G0, const double2* G, const double2* D, long long K, int Norb);
+template <typename R>
+void chi0_ff(const Geom& g, const Pairs& p, const double2* F, const std::vector<double>& prt, double temp,
+             bool singlet, cx<R>* chi);
+void combine_sc(double2* gg, double2* ff, long long n);
+bool vertex_sc(double2* XS, double2* XC, long long K, int Nchi, const double* S, const double* C, bool singlet);
+
 // small host helpers
 void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc);
 template <typename R> void widen(double2* out, const cx<R>* in, long long n);

@@ -54,6 +54,8 @@ _SIGNATURES = {
     + [_pi] * 9 + [_pb, _pb, _pi, _pb, _pb, _pd],
     "lin_eliash": [_c128, _c128, _c128, _c128, _f64, _f64, _f64, _i64, _f64, _i64, _i64, _pd, _pd]
     + [_pi] * 11 + [_pd],
+    "eliashberg": [_c128, _c128, _c128, _c128, _f64, _f64, _i64, _f64, _i64, _i64, _pd, _pd, _pd]
+    + [_pi] * 10 + [_pb, _pb, _pi, _pd, _pb],
     "mkfk_trs_nsoc_": [_c128, _c128, _c128, _pi, _pi, _pi],
     "get_initial_delta_": [_c128, _f64, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi],
     "remap_delta_": [_c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi],
@@ -459,6 +461,33 @@ def linearized_eliashberg(chi, Gk, uni, init_delta, Smat, Cmat, olist, plist, km
           i64(Nw), i64(Nchi), i64(Norb), i64(Nx), i64(Ny), i64(Nz), i64(itemax), i64(gap_sym), i64(arnoldi_m),
           byref(lam))
     return delta, lam.value
+
+
+def nonlinear_eliashberg(delta_init, Gk, hamk, Smat, Cmat, olist, plist, kmap, invk, mu: float, temp: float,
+                         gap_sym: int, Nx: int, Ny: int, Nz: int, sw_sigma: bool = False, sw_Vconst: bool = False,
+                         eps: float = 1.0e-4, itemax: int = 100, m_diis: int = 5, gap_min: float = 1.0e-2,
+                         sw_amp_newton: bool = True):
+    """Nonlinear FLEX-Eliashberg loop (libs/flibs/_eliashberg.py:225-300).
+    Like the reference, a C-contiguous complex128 delta_init is updated in
+    place and Gk is overwritten with the last self-consistent G; returns
+    (delta, sigmak), sigmak zero unless sw_sigma."""
+    if delta_init.dtype != np.complex128 or not delta_init.flags['C_CONTIGUOUS']:
+        delta = np.ascontiguousarray(delta_init, dtype=np.complex128)
+    else:
+        delta = delta_init
+    if Gk.dtype != np.complex128 or not Gk.flags['C_CONTIGUOUS']:
+        raise ValueError("Gk must be a C-contiguous complex128 array: it is overwritten with the final G")
+    Norb, _, Nw, Nk = delta.shape
+    Nkall, Nchi = len(kmap), len(Smat)
+    if Gk.shape != delta.shape or len(hamk) != Nk or Nkall != Nx * Ny * Nz:
+        raise ValueError("delta_init, Gk, hamk and the k-mesh sizes disagree")
+    sigmak = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("eliashberg", delta, sigmak, Gk, np.ascontiguousarray(hamk), Smat, Cmat, olist,
+          np.ascontiguousarray(plist, dtype=np.float64), kmap, invk, dbl(mu), dbl(temp), dbl(eps), i64(Nkall),
+          i64(Nk), i64(Nw), i64(Nchi), i64(Norb), i64(Nx), i64(Ny), i64(Nz), i64(itemax), i64(gap_sym),
+          byref(c_bool(bool(sw_sigma))), byref(c_bool(bool(sw_Vconst))), i64(m_diis), dbl(gap_min),
+          byref(c_bool(bool(sw_amp_newton))))
+    return delta, sigmak
 
 
 def gen_Fk(Gk, delta, invk):

@@ -1,0 +1,165 @@
+"""GPU parity of the nonlinear FLEX-Eliashberg loop (libs/src/ffeliash.f90:2-314)
+against the oracle's restatement, through the C ABI symbol ``eliashberg``.
+
+Each case runs a fixed number of iterations (eps far below reach, no
+gap-collapse stop) so that every branch taken by the oracle is also taken by
+the GPU loop, then compares the gap, the self-energy and the overwritten G.
+
+Tolerance: 1e-9 relative to the array maximum, as for the other FP64 paths,
+except where the loop itself amplifies rounding.  The amplitude secant
+divides differences of gains, and a DIIS step with nearly parallel residuals
+solves an ill-conditioned system; for those cases the oracle was run twice
+with seeds that differ by 1e-13 relative and the tolerance is about 100x the
+spread it showed (written beside each case).
+"""
+import numpy as np
+import pytest
+
+from oracle import api as O
+import _models as M
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def F():
+    from pyrpa_gb300 import build, flibs
+    if not build.LIB.exists():
+        build.build()
+    flibs.load_library()
+    flibs.set_verbose(0)
+    flibs.set_precision(64)
+    return flibs
+
+
+def close(a, b, rtol, atol=1e-300):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    scale = max(np.abs(b).max(), 1e-300)
+    err = np.abs(a - b).max()
+    assert err <= rtol * scale + atol, f"max |diff| {err:.3e} vs scale {scale:.3e}"
+
+
+def setup(Norb, dims, Nw, temp, mu, U, J, gap_sym, seed=0, complex_hop=False, gap_max=0.1, lin_seed=False):
+    """Model, bare G and a gap seed scaled to max |Delta| = gap_max: the
+    symmetry-adapted initial gap, or (lin_seed) the leading linearized
+    Eliashberg eigenvector, the seed the reference recommends."""
+    if Norb == 1 and seed == 0:
+        rvec, ham_r = M.square_hoppings(1.0, 1.0, -0.25)
+    elif Norb == 2 and seed == 0:
+        rvec, ham_r = M.two_orbital_hoppings()
+    else:
+        rvec, ham_r = M.random_hoppings(Norb, seed, complex_hop=complex_hop, dim=3 if dims[2] > 1 else 2,
+                                        bandwidth=4.0)
+    klist, kmap, invk = O.gen_irr_k_TRS(*dims)
+    hamk = O.gen_ham(klist, ham_r, rvec)
+    eig, uni = O.get_eig(hamk)
+    olist, site = O.get_chi_orb_list(Norb)
+    olist = np.asarray(olist)
+    S, C = O.gen_SCmatrix(olist, site, U, J)
+    G0 = O.gen_Green0(eig, uni, mu, temp, Nw)
+    init = O.get_initial_gap(klist, Norb, gap_sym)
+    if lin_seed:
+        chi, _ = O.get_chi0(S, C, G0, olist, kmap, invk, temp, *dims)
+        d0, _ = O.linearized_eliashberg(chi, G0, uni, init, S, C, olist, np.ones(Norb), kmap, invk, *dims, temp,
+                                        gap_sym, eps=1e-8, itemax=200, arnoldi_m=10)
+        i = np.argmax(np.abs(d0))
+        d0 = d0 * (abs(d0.flat[i]) / d0.flat[i])  # real gauge
+    else:
+        d0 = O.get_initial_delta(init, uni, invk, Nw, gap_sym)
+    d0 = gap_max * d0 / max(np.abs(d0).max(), 1e-300)
+    return dict(hamk=hamk, S=S, C=C, olist=olist, kmap=kmap, invk=invk, d0=d0, G0=G0, mu=mu, temp=temp,
+                gap_sym=gap_sym, dims=dims, plist=np.ones(Norb))
+
+
+def args_of(m):
+    return (m["hamk"], m["S"], m["C"], m["olist"], m["plist"], m["kmap"], m["invk"], m["mu"], m["temp"],
+            m["gap_sym"], *m["dims"])
+
+
+def run_both(F, m, **kw):
+    Gg, Go = m["G0"].copy(), m["G0"].copy()
+    dg, sg = F.nonlinear_eliashberg(m["d0"].copy(), Gg, *args_of(m), **kw)
+    st = F.last_stats()
+    do, so, r = O.nonlinear_eliashberg(m["d0"].copy(), Go, *args_of(m), full=True, **kw)
+    return (dg, sg, Gg, int(st["iterations"])), (do, so, Go, r)
+
+
+# 1 orbital, t = 1, t' = -0.25, mu = -0.3, T = 0.05, U = 2.5: Stoner factor 0.93
+# and a d-wave pairing eigenvalue of 1.53 on 8x8 k points and 32 frequencies, so
+# the loop has a gap solution (max |Delta| = 0.175) to move towards
+D1 = dict(Norb=1, dims=(8, 8, 1), Nw=32, temp=0.05, mu=-0.3, U=2.5, J=0.0, gap_sym=1, lin_seed=True)
+# (model, loop options, rtol)
+CASES = {
+    "1orb-d-amplitude": (D1, dict(sw_amp_newton=True, itemax=12), 1e-9),
+    "1orb-d-diis-sigma": (D1, dict(sw_amp_newton=False, sw_sigma=True, m_diis=4, itemax=10), 1e-9),
+    "1orb-d-vconst": (D1, dict(sw_amp_newton=True, sw_Vconst=True, itemax=12), 1e-9),
+    # oracle spread 4e-11 after six DIIS steps with nearly parallel residuals
+    "1orb-d-diis-only": (D1, dict(sw_amp_newton=False, m_diis=5, itemax=6), 1e-8),
+    "1orb-p-triplet-linear": (dict(D1, gap_sym=-1, U=2.0, lin_seed=False), dict(sw_amp_newton=False, m_diis=1,
+                                                                                   itemax=5), 1e-9),
+    "2orb-d-diis-sigma": (dict(Norb=2, dims=(4, 4, 1), Nw=16, temp=0.1, mu=0.0, U=1.0, J=0.1, gap_sym=1),
+                          dict(sw_amp_newton=False, sw_sigma=True, m_diis=3, itemax=4), 1e-9),
+    "3orb-cplx-sigma-amplitude": (dict(Norb=3, dims=(4, 6, 1), Nw=8, temp=0.1, mu=0.1, U=0.6, J=0.1, gap_sym=0,
+                                       seed=3, complex_hop=True),
+                                  dict(sw_amp_newton=True, sw_sigma=True, itemax=5), 1e-9),
+    "2orb-3d-diis": (dict(Norb=2, dims=(4, 4, 4), Nw=4, temp=0.2, mu=0.0, U=1.0, J=0.1, gap_sym=0, seed=5),
+                     dict(sw_amp_newton=False, m_diis=5, itemax=6), 1e-9),
+}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_nonlinear_eliashberg_matches_oracle(F, case):
+    mk, kw, rtol = CASES[case]
+    m = setup(**mk)
+    (dg, sg, Gg, ig), (do, so, Go, r) = run_both(F, m, eps=1e-14, gap_min=0.0, **kw)
+    assert ig == r.iterations == kw["itemax"]
+    close(dg, do, rtol)
+    close(Gg, Go, rtol)
+    if kw.get("sw_sigma"):
+        close(sg, so, rtol)
+    else:
+        assert not sg.any() and not so.any()
+
+
+def test_nonlinear_eliashberg_polish_and_reanchor(F):
+    """Amplitude solved within 2 %, ten DIIS polish steps, re-anchor, amplitude
+    again: seeded at 0.9x the converged gap.  The oracle's spread under a 1e-13
+    seed perturbation is 1.5e-8 here (the secant after the re-anchor divides
+    a small gain difference), hence rtol 1e-6."""
+    m = setup(**D1)
+    dc, _ = O.nonlinear_eliashberg(m["d0"].copy(), m["G0"].copy(), *args_of(m), eps=1e-6, gap_min=0.0,
+                                   sw_amp_newton=False, m_diis=5, itemax=100)
+    m["d0"] = 0.9 * dc
+    (dg, _, Gg, ig), (do, _, Go, r) = run_both(F, m, eps=1e-14, gap_min=0.0, sw_amp_newton=True, itemax=14)
+    phases = "".join(str(h.get("phase", 2)) for h in r.history)
+    assert phases.startswith("11" + "2" * 10 + "1"), phases
+    assert ig == r.iterations == 14
+    close(dg, do, 1e-6)
+    close(Gg, Go, 1e-6)
+
+
+def test_nonlinear_eliashberg_stops_where_the_oracle_stops(F):
+    """Convergence and gap-collapse exits end on the same iteration."""
+    m = setup(**D1)
+    (dg, _, Gg, ig), (do, _, Go, r) = run_both(F, m, eps=1e-4, gap_min=0.0, itemax=200, sw_amp_newton=False,
+                                               m_diis=1)
+    assert ig == r.iterations < 200 and r.history[-1]["rel"] < 1e-4
+    close(dg, do, 1e-8)
+    close(Gg, Go, 1e-8)
+    weak = setup(**dict(D1, U=2.0))  # pairing eigenvalue 0.38: the gap decays
+    (dg, _, _, ig), (do, _, _, r) = run_both(F, weak, eps=1e-14, gap_min=0.2, itemax=60, sw_amp_newton=False,
+                                             m_diis=1)
+    assert 1 < ig == r.iterations < 60 and r.history[-1]["new_max"] < 0.2 * np.abs(weak["d0"]).max()
+    close(dg, do, 1e-9)
+
+
+def test_nonlinear_eliashberg_zero_seed_stays_zero(F):
+    """test_rpa_flex.py:208-224 on the GPU path: S = C = 0 and a zero seed."""
+    m = setup(Norb=1, dims=(2, 2, 1), Nw=3, temp=0.1, mu=0.0, U=0.0, J=0.0, gap_sym=0, gap_max=0.0)
+    Gk = m["G0"].copy()
+    delta, sigmak = F.nonlinear_eliashberg(m["d0"].copy(), Gk, m["hamk"], m["S"], m["C"], m["olist"], m["plist"],
+                                           m["kmap"], m["invk"], 0.0, m["temp"], 0, 2, 2, 1, sw_sigma=False,
+                                           sw_Vconst=True, eps=1e-6, itemax=2, m_diis=1, gap_min=0.0,
+                                           sw_amp_newton=False)
+    assert np.allclose(delta, 0.0) and np.allclose(sigmak, 0.0)
