@@ -220,6 +220,23 @@ void eliashberg(double* delta, double* sigmak, double* Gk, const double* hamk, c
                 const int64_t* itemax, const int64_t* gap_sym, const bool* sw_sigma, const bool* sw_Vconst,
                 const int64_t* m_diis, const double* gap_min, const bool* sw_amp_newton);
 
+/* Building blocks of the nonlinear loop, each one call (no counterpart symbol
+ * in the reference, which keeps them internal to ffeliash.f90):
+ * pyrpa_gb_chi0sc: get_chi0sc (ffeliash.f90:454-489), chi0_S = chi^GG + chi^FF
+ * and chi0_C = chi^GG - chi^FF of Gk and fk (Nk,Nw,Norb,Norb) into xs, xc
+ * (Nk,Nw,Nchi,Nchi); with *vertex != 0 followed by mkV_flex_nosoc
+ * (ffeliash.f90:379-452): V_sigma into xs, V_Delta into xc.
+ * pyrpa_gb_sc_dyson: mkgreliah_trs_nsoc then mkfkeliash_trs_nsoc
+ * (ffeliash.f90:316-377): Gk = G0 (1 + delta fk^+), then fk = -G0 delta Gk^+
+ * (fk in: the previous F, out: the new one). */
+void pyrpa_gb_chi0sc(double* xs, double* xc, const double* Gk, const double* fk, const double* Smat,
+                     const double* Cmat, const int64_t* olist, const double* prt, const int64_t* kmap,
+                     const int64_t* invk, const double* temp, const int64_t* Nkall, const int64_t* Nk,
+                     const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nx,
+                     const int64_t* Ny, const int64_t* Nz, const int64_t* gap_sym, const int64_t* vertex);
+void pyrpa_gb_sc_dyson(double* Gk, double* fk, const double* G0, const double* delta, const int64_t* Nk,
+                       const int64_t* Nw, const int64_t* Norb);
+
 /* Symbols outside the accelerated path (transport, impurity, SOC, Eilenberger,
  * real-frequency maps, Pade ...) are exported with no
  * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"

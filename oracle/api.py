@@ -162,6 +162,23 @@ def get_plist(rvec, ham_r):
     return np.sign(P.T[0, :])
 
 
+def get_chi0sc(Gk, Fk, Smat, Cmat, olist, plist, kmap, invk, Nx, Ny, Nz, temp, gap_sym, vertex=False):
+    """chi0_S, chi0_C (ffeliash.f90:454-489) or V_sigma, V_Delta (379-452), wrapper layout."""
+    grid = _grid(kmap, invk, Nx, Ny, Nz)
+    singlet = gap_sym >= 0
+    xs, xc = O.get_chi0sc(Gk.T, Fk.T, grid, np.asarray(olist), np.asarray(plist, dtype=np.float64), temp, singlet)
+    if vertex:
+        xs, xc = O.mkV_flex_sc(xs, xc, Smat.T, Cmat.T, singlet)
+    return np.ascontiguousarray(xs.T), np.ascontiguousarray(xc.T)
+
+
+def sc_dyson(G0, Fk, delta):
+    """G = G0 (1 + delta Fk^+), F = -G0 delta G^+ (ffeliash.f90:316-377)."""
+    G = O.mkgreliah_F(G0.T, Fk.T, delta.T)
+    F = O.mkfkeliash_F(G0.T, G, delta.T)
+    return np.ascontiguousarray(G.T), np.ascontiguousarray(F.T)
+
+
 def nonlinear_eliashberg(delta_init, Gk, hamk, Smat, Cmat, olist, plist, kmap, invk, mu, temp, gap_sym, Nx, Ny, Nz,
                          sw_sigma=False, sw_Vconst=False, eps=1.0e-4, itemax=100, m_diis=5, gap_min=1.0e-2,
                          sw_amp_newton=True, full=False):

@@ -875,6 +875,39 @@ void eliashberg(double2* delta, double2* sigmak, double2* Gk, const double2* ham
                            nan_fill(sigmak, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb))))
 }
 
+void pyrpa_gb_chi0sc(double2* xs, double2* xc, const double2* Gk, const double2* Fk, const double* Smat,
+                     const double* Cmat, const int64_t* olist, const double* prt, const int64_t* kmap,
+                     const int64_t* invk, const double* temp, const int64_t* Nkall, const int64_t* Nk,
+                     const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nx, const int64_t* Ny,
+                     const int64_t* Nz, const int64_t* gap_sym, const int64_t* vertex) {
+  ABI_TRY
+  ensure_context();
+  nonlin_bubbles(xs, xc, Gk, Fk, Smat, Cmat, olist, prt, kmap, invk, *temp, *Nkall, *Nk, *Nw, *Nchi, *Norb, *Nx, *Ny,
+                 *Nz, *gap_sym >= 0, *vertex != 0);
+  ABI_CATCH("pyrpa_gb_chi0sc", (nan_fill(xs, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)),
+                                nan_fill(xc, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi))))
+}
+
+void pyrpa_gb_sc_dyson(double2* Gk, double2* fk, const double2* G0, const double2* delta, const int64_t* Nk,
+                       const int64_t* Nw, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  const long long K = (*Nk) * (*Nw), KE = K * no * no;
+  DBuf<double2> G(KE), F(KE), G0d(KE), D(KE);
+  G0d.upload(G0, KE);
+  F.upload(fk, KE);
+  D.upload(delta, KE);
+  mkgreliah(G.p, G0d.p, F.p, D.p, K, (int)no);
+  mkfkeliash(F.p, G0d.p, G.p, D.p, K, (int)no);
+  G.download(Gk, KE);
+  F.download(fk, KE);
+  sync();
+  ABI_CATCH("pyrpa_gb_sc_dyson", (nan_fill(Gk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)),
+                                  nan_fill(fk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb))))
+}
+
 void mkfk_trs_nsoc_(double2* fk, const double2* Gk, const double2* delta, const int64_t* Nk, const int64_t* Nw,
                     const int64_t* Norb) {
   ABI_TRY

@@ -1089,8 +1089,31 @@ double maxabs(const double2* a, const double2* b, long long n) {
 }
 }  // namespace
 
+void nonlin_bubbles(double2* xs_out, double2* xc_out, const double2* Gk, const double2* Fk, const double* Smat,
+                    const double* Cmat, const int64_t* olist, const double* prt_host, const int64_t* kmap,
+                    const int64_t* invk, double temp, int64_t Nkall, int64_t Nk, int64_t Nw, int64_t Nchi,
+                    int64_t Norb, int64_t Nx, int64_t Ny, int64_t Nz, bool singlet, bool vertex) {
+  PGB_CHECK(Norb <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  Inputs in;
+  upload_inputs(in, kmap, invk, olist, Nx, Ny, Nz, Nkall, Nk, Nw, Norb, Nchi, Smat, Cmat, nullptr, nullptr, nullptr);
+  const Geom& g = in.g;
+  const long long KE = g.K * Norb * Norb, KC = g.K * Nchi * Nchi;
+  std::vector<double> hprt(prt_host, prt_host + Norb);
+  DBuf<double2> G(KE), F(KE), XS(KC), XC(KC);
+  G.upload(Gk, KE);
+  F.upload(Fk, KE);
+  chi0<double>(g, in.p, G.p, temp, nullptr, XS.p);
+  chi0_ff<double>(g, in.p, F.p, hprt, temp, singlet, XC.p);
+  combine_sc(XS.p, XC.p, KC);
+  if (vertex) PGB_CHECK(vertex_sc(XS.p, XC.p, g.K, (int)Nchi, in.S.p, in.C.p, singlet), "zgesv failed in the SC vertex");
+  XS.download(xs_out, KC);
+  XC.download(xc_out, KC);
+  sync();
+}
+
 void run_nonlin_eliash(const NonlinArgs& a) {
   g_stats = LastStats{};
+  PGB_CHECK(a.Norb <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
   cudaStream_t st = ctx().stream;
   Inputs in;
   upload_inputs(in, a.kmap, a.invk, a.olist, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Smat, a.Cmat,
@@ -1125,10 +1148,12 @@ void run_nonlin_eliash(const NonlinArgs& a) {
     chi0<double>(g, in.p, G.p, a.temp, nullptr, XS.p);
     chi0_ff<double>(g, in.p, F.p, hprt, a.temp, singlet, XC.p);
     combine_sc(XS.p, XC.p, KC);
-    double sdw = 0, cdw = 0;
-    int qs = 0, qc = 0;
-    stoner<double>(g, XS.p, in.S.p, in.C.p, &sdw, &cdw, &qs, &qc);
-    ckchi_print(g, sdw, cdw, qs, qc);
+    if (ctx().verbose) {  // the Stoner check only prints
+      double sdw = 0, cdw = 0;
+      int qs = 0, qc = 0;
+      stoner<double>(g, XS.p, in.S.p, in.C.p, &sdw, &cdw, &qs, &qc);
+      ckchi_print(g, sdw, cdw, qs, qc);
+    }
     PGB_CHECK(vertex_sc(XS.p, XC.p, K, Nchi, in.S.p, in.C.p, singlet), "zgesv failed in the SC vertex");
   };
   int n_hist = 0, i_hist = 0, amp_phase = 1, npts = 0, n_polish = 0, n_anchor = 0;

@@ -146,6 +146,11 @@ void run_mkself(const MkselfArgs& a, int prec);
 template <typename R> void run_lin_eliash(const LinEliashArgs& a);
 void run_pipeline(const PipelineArgs& a, int prec);
 void run_nonlin_eliash(const NonlinArgs& a);
+// chi0_S / chi0_C of G and F (vertex: V_sigma / V_Delta instead), host arrays
+void nonlin_bubbles(double2* xs_out, double2* xc_out, const double2* Gk, const double2* Fk, const double* Smat,
+                    const double* Cmat, const int64_t* olist, const double* prt_host, const int64_t* kmap,
+                    const int64_t* invk, double temp, int64_t Nkall, int64_t Nk, int64_t Nw, int64_t Nchi,
+                    int64_t Norb, int64_t Nx, int64_t Ny, int64_t Nz, bool singlet, bool vertex);
 const LastStats& last_stats();
 
 }  // namespace pgb

@@ -1681,8 +1681,8 @@ void combine_sc(double2* gg, double2* ff, long long n) {
 //   V_sigma = 3/2 S - 1/2 C + 3/2 S chi_s + 1/2 C chi_c - 1/4 (S+C)(P+Q),
 //   V_Delta = V0 + cs S chi_s + cc C chi_c  (singlet V0=(S+C)/2, cs=3/2, cc=-1/2;
 //             triplet V0=(S-C)/2, cs=cc=-1/2).
-// Per warp, shared memory holds P (then chi_s), Q (then chi_c), P+Q and one
-// accumulation row per lane.
+// Per warp, shared memory holds P (then chi_s), Q (then chi_c), P+Q (N*N
+// each) and an N x 32 accumulation block, one column per lane.
 template <int N, int W>
 __global__ void __launch_bounds__(32 * W) k_vertex_sc(double2* XS, double2* XC, long long K, const double* S,
                                                       const double* C, int singlet) {
@@ -1691,11 +1691,12 @@ __global__ void __launch_bounds__(32 * W) k_vertex_sc(double2* XS, double2* XC, 
   double* sC = sS + N * N;
   double2* base = reinterpret_cast<double2*>(smsc + ((2 * N * N * sizeof(double) + 15) / 16) * 16);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double2* Pm = base + (size_t)w * (4 * N * N + 0);
+  constexpr int kWarpStride = 3 * N * N + 32 * N;
+  double2* Pm = base + (size_t)w * kWarpStride;
   double2* Qm = Pm + N * N;
   double2* X5 = Qm + N * N;
-  double2* Rb = X5 + N * N;  // [j][lane]
-  int* ints = reinterpret_cast<int*>(base + (size_t)W * 4 * N * N);
+  double2* Rb = X5 + N * N;  // [j][lane], N * 32
+  int* ints = reinterpret_cast<int*>(base + (size_t)W * kWarpStride);
   int* pv = ints + w * (N + 1);
   int* mp = ints + W * (N + 1) + w * 32;
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
@@ -1768,8 +1769,8 @@ __global__ void __launch_bounds__(32 * W) k_vertex_sc(double2* XS, double2* XC, 
 bool vertex_sc(double2* XS, double2* XC, long long K, int Nchi, const double* S, const double* C, bool singlet) {
   constexpr int W = 2;
   auto launch = [&](auto kernel, int n) {
-    const size_t smem = ((2 * (size_t)n * n * sizeof(double) + 15) / 16) * 16 + (size_t)W * 4 * n * n * sizeof(double2) +
-                        sizeof(int) * (W * (n + 1) + W * 32);
+    const size_t smem = ((2 * (size_t)n * n * sizeof(double) + 15) / 16) * 16 +
+                        (size_t)W * (3 * n * n + 32 * n) * sizeof(double2) + sizeof(int) * (W * (n + 1) + W * 32);
     PGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = std::min<long long>((K + W - 1) / W, (long long)ctx().num_sms * 16);
     kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(XS, XC, K, S, C, singlet ? 1 : 0);

@@ -56,6 +56,8 @@ _SIGNATURES = {
     + [_pi] * 11 + [_pd],
     "eliashberg": [_c128, _c128, _c128, _c128, _f64, _f64, _i64, _f64, _i64, _i64, _pd, _pd, _pd]
     + [_pi] * 10 + [_pb, _pb, _pi, _pd, _pb],
+    "pyrpa_gb_chi0sc": [_c128, _c128, _c128, _c128, _f64, _f64, _i64, _f64, _i64, _i64, _pd] + [_pi] * 10,
+    "pyrpa_gb_sc_dyson": [_c128, _c128, _c128, _c128, _pi, _pi, _pi],
     "mkfk_trs_nsoc_": [_c128, _c128, _c128, _pi, _pi, _pi],
     "get_initial_delta_": [_c128, _f64, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi],
     "remap_delta_": [_c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi],
@@ -488,6 +490,31 @@ def nonlinear_eliashberg(delta_init, Gk, hamk, Smat, Cmat, olist, plist, kmap, i
           byref(c_bool(bool(sw_sigma))), byref(c_bool(bool(sw_Vconst))), i64(m_diis), dbl(gap_min),
           byref(c_bool(bool(sw_amp_newton))))
     return delta, sigmak
+
+
+def get_chi0sc(Gk, Fk, Smat, Cmat, olist, plist, kmap, invk, Nx: int, Ny: int, Nz: int, temp: float, gap_sym: int,
+               vertex: bool = False):
+    """chi0_S, chi0_C = chi^GG +- chi^FF of the nonlinear loop (ffeliash.f90:454-489),
+    or with vertex=True its V_sigma, V_Delta (ffeliash.f90:379-452); (Nchi,Nchi,Nw,Nk)."""
+    Norb, Nchi = len(Gk), len(Smat)
+    Nk, Nw = Gk.shape[3], Gk.shape[2]
+    xs = np.zeros((Nchi, Nchi, Nw, Nk), dtype=np.complex128)
+    xc = np.zeros_like(xs)
+    _call("pyrpa_gb_chi0sc", xs, xc, np.ascontiguousarray(Gk), np.ascontiguousarray(Fk), Smat, Cmat, olist,
+          np.ascontiguousarray(plist, dtype=np.float64), kmap, invk, dbl(temp), i64(len(kmap)), i64(Nk), i64(Nw),
+          i64(Nchi), i64(Norb), i64(Nx), i64(Ny), i64(Nz), i64(gap_sym), i64(1 if vertex else 0))
+    return xs, xc
+
+
+def sc_dyson(G0, Fk, delta):
+    """One SC Dyson step of the nonlinear loop (ffeliash.f90:316-377):
+    G = G0 (1 + delta Fk^+), then F = -G0 delta G^+; returns (G, F)."""
+    Norb, Nw, Nk = len(G0), G0.shape[2], G0.shape[3]
+    G = np.zeros_like(G0)
+    F = np.array(Fk, dtype=np.complex128, order="C", copy=True)
+    _call("pyrpa_gb_sc_dyson", G, F, np.ascontiguousarray(G0), np.ascontiguousarray(delta), i64(Nk), i64(Nw),
+          i64(Norb))
+    return G, F
 
 
 def gen_Fk(Gk, delta, invk):

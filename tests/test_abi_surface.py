@@ -69,6 +69,29 @@ def test_header_declarations_are_exported(lib):
         assert hasattr(lib, d)
 
 
+def header_arity():
+    text = (ROOT / "include" / "fmod.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for name, params in re.findall(r"\bvoid\s+(\w+)\s*\(([^)]*)\)", text):
+        params = params.strip()
+        out[name] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_header_arity():
+    """Every argtypes list the wrappers bind has as many entries as the
+    declaration in include/fmod.h has parameters."""
+    from pyrpa_gb300 import flibs
+    arity = header_arity()
+    checked = 0
+    for name, types in flibs._SIGNATURES.items():
+        if name in arity:
+            assert len(types) == arity[name], (name, len(types), arity[name])
+            checked += 1
+    assert checked >= 25
+
+
 def test_irreducible_k_mesh_matches_oracle(lib):
     from pyrpa_gb300 import flibs as F
     for dims in [(2, 2, 1), (4, 4, 1), (8, 6, 1), (5, 5, 1), (6, 5, 1), (4, 4, 4), (6, 6, 3), (3, 3, 3),

@@ -55,7 +55,9 @@ def setup(Norb, dims, Nw, temp, mu, U, J, gap_sym, seed=0, complex_hop=False, ga
     hamk = O.gen_ham(klist, ham_r, rvec)
     eig, uni = O.get_eig(hamk)
     olist, site = O.get_chi_orb_list(Norb)
-    olist = np.asarray(olist)
+    # the library reads olist as the Fortran (Nchi, 2) array the reference's
+    # get_chi_orb_list returns; ctypes passes the memory as it is
+    olist = np.asfortranarray(olist)
     S, C = O.gen_SCmatrix(olist, site, U, J)
     G0 = O.gen_Green0(eig, uni, mu, temp, Nw)
     init = O.get_initial_gap(klist, Norb, gap_sym)
@@ -83,6 +85,45 @@ def run_both(F, m, **kw):
     st = F.last_stats()
     do, so, r = O.nonlinear_eliashberg(m["d0"].copy(), Go, *args_of(m), full=True, **kw)
     return (dg, sg, Gg, int(st["iterations"])), (do, so, Go, r)
+
+
+BLOCK_MODELS = {
+    "1orb": dict(Norb=1, dims=(8, 8, 1), Nw=16, temp=0.05, mu=-0.3, U=2.0, J=0.0, gap_sym=1),
+    "2orb": dict(Norb=2, dims=(4, 4, 1), Nw=16, temp=0.1, mu=0.0, U=1.0, J=0.1, gap_sym=1),
+    "3orb-cplx": dict(Norb=3, dims=(4, 6, 1), Nw=8, temp=0.1, mu=0.1, U=0.6, J=0.1, gap_sym=0, seed=3,
+                      complex_hop=True),
+    "2orb-3d": dict(Norb=2, dims=(4, 4, 4), Nw=4, temp=0.2, mu=0.0, U=1.0, J=0.1, gap_sym=0, seed=5),
+}
+
+
+def block_inputs(name, gap_sym, gap_max=0.3):
+    mk = dict(BLOCK_MODELS[name], gap_max=gap_max)
+    mk["gap_sym"] = gap_sym
+    m = setup(**mk)
+    Fk = O.mkfk_trs_nsoc(m["G0"], m["d0"])
+    return m, Fk
+
+
+@pytest.mark.parametrize("name", list(BLOCK_MODELS))
+@pytest.mark.parametrize("gap_sym", [0, 1, -1])
+@pytest.mark.parametrize("vertex", [False, True])
+def test_chi0sc_matches_oracle(F, name, gap_sym, vertex):
+    """chi0_S / chi0_C (and V_sigma / V_Delta) of a G and a finite F."""
+    m, Fk = block_inputs(name, gap_sym)
+    a = (m["G0"], Fk, m["S"], m["C"], m["olist"], m["plist"], m["kmap"], m["invk"], *m["dims"], m["temp"], gap_sym)
+    xs, xc = F.get_chi0sc(*a, vertex=vertex)
+    ys, yc = O.get_chi0sc(*a, vertex=vertex)
+    close(xs, ys, 1e-9, 2e-9)
+    close(xc, yc, 1e-9, 2e-9)
+
+
+@pytest.mark.parametrize("name", list(BLOCK_MODELS))
+def test_sc_dyson_matches_oracle(F, name):
+    m, Fk = block_inputs(name, BLOCK_MODELS[name]["gap_sym"])
+    G, Fn = F.sc_dyson(m["G0"], Fk, m["d0"])
+    Go, Fo = O.sc_dyson(m["G0"], Fk, m["d0"])
+    close(G, Go, 1e-12)
+    close(Fn, Fo, 1e-12)
 
 
 # 1 orbital, t = 1, t' = -0.25, mu = -0.3, T = 0.05, U = 2.5: Stoner factor 0.93
