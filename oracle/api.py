@@ -193,3 +193,89 @@ def nonlinear_eliashberg(delta_init, Gk, hamk, Smat, Cmat, olist, plist, kmap, i
     Gk[...] = r.G.T
     delta, sigma = np.ascontiguousarray(r.delta.T), np.ascontiguousarray(r.sigma.T)
     return (delta, sigma, r) if full else (delta, sigma)
+
+
+# ----------------------------------------------------------------- spin-orbit
+# Facades of the reference's spin-orbit wrappers (libs/flibs/_interaction.py:
+# gen_Vmatrix(_orb), _susceptibility.py: get_chi0_soc, get_chis_chic_soc,
+# _selfenergy.py: mkself_soc, _eliashberg.py: linearized_eliashberg_soc,
+# conv_delta_orb_to_band_soc, gen_Fk_soc), in the wrappers' array layouts.
+from . import soc_oracle as SO  # noqa: E402
+
+
+def gen_Vmatrix(olist, slist, site, invs, U, J):
+    return np.ascontiguousarray(SO.get_vmat_soc(np.asarray(olist), slist, np.asarray(site), invs, U, J).T)
+
+
+def gen_Vmatrix_orb(olist, slist, site, invs, Umat, Jmat):
+    V = SO.get_vmat_soc(np.asarray(olist), slist, np.asarray(site), invs, 0.0, 0.0, Umat=np.asarray(Umat).T,
+                        Jmat=np.asarray(Jmat).T)
+    return np.ascontiguousarray(V.T)
+
+
+def get_chi0_soc(Vmat, Gk, olist, slist, kmap, invk, invs, temp, Nx, Ny, Nz, full=False):
+    grid = _grid(kmap, invk, Nx, Ny, Nz)
+    ol = np.asarray(olist)
+    chi = SO.get_chi0_conv_soc(Gk.T, grid, ol, invs, slist, temp)
+    sg, sg2 = SO.sign_tables(ol, slist)
+    invschi = SO.get_invschi(ol, invs)
+    out = (np.ascontiguousarray(chi.T), np.ascontiguousarray(sg.T), np.ascontiguousarray(sg2.T), invschi)
+    return out + (SO.ckchi_soc(chi, np.asarray(Vmat).T),) if full else out
+
+
+def soc_orb_list(olist, slist, invs):
+    """orb_list of get_chis_chic_soc (libs/flibs/_susceptibility.py:544-555)."""
+    olist = np.asarray(olist)
+    slist = np.asarray(slist)
+    invs = np.asarray(invs)
+    orbs = np.where(slist == 1)[0]
+    o1, o2 = np.meshgrid(orbs, orbs)
+    pairs = np.array([o1.flatten(), o2.flatten()]).T
+    out = np.zeros(len(olist), dtype=np.int64)
+    for i, ol in enumerate(olist):
+        a = (ol[0] if slist[ol[0] - 1] == 1 else invs[ol[0] - 1]) - 1
+        b = (ol[1] if slist[ol[1] - 1] == 1 else invs[ol[1] - 1]) - 1
+        for j, pb in enumerate(pairs):
+            if a == pb[0] and b == pb[1]:
+                out[i] = j + 1
+                break
+    return out
+
+
+def get_chis_chic_soc(chi, Vmat, olist, slist, invs):
+    ol = np.asarray(olist)
+    orb_list = soc_orb_list(ol, slist, invs)
+    c, sz, pm = SO.get_chis_chic_soc(chi.T, np.asarray(Vmat).T, orb_list, ol, slist)
+    return np.ascontiguousarray(c.T), np.ascontiguousarray(sz.T), np.ascontiguousarray(pm.T)
+
+
+def mkself_soc(Vmat, kmap, invk, invs, olist, slist, hamk, eig, uni, mu, fill, temp, Nw, Nx, Ny, Nz,
+               sw_out=False, sw_in=False, sub_sigma=1, scf_loop=300, eps=1.0e-4, pp=0.3, m_diis=5,
+               sw_rescale=False, sigma_scale=1.0, full=False):
+    r = SO.mkself_soc(np.asarray(Vmat).T, np.asarray(kmap), np.asarray(invk), invs, np.asarray(olist), slist,
+                      hamk.transpose(0, 2, 1), eig, uni.transpose(0, 2, 1), mu, fill, temp, scf_loop, pp, eps,
+                      Nx, Ny, Nz, Nw, sub_sigma=sub_sigma, m_diis=m_diis, sw_rescale=sw_rescale)
+    sig = np.ascontiguousarray(r.sigma.T)
+    return (sig, r.mu, r) if full else (sig, r.mu)
+
+
+def linearized_eliashberg_soc(chi, Gk, uni, init_delta, Vmat, sgnsig, sgnsig2, plist, slist, olist, kmap, invk,
+                              invs, invschi, Nx, Ny, Nz, temp, gap_sym, eps=1.0e-4, itemax=300, arnoldi_m=10,
+                              full=False):
+    """Like the library, chi is overwritten with the pairing vertex."""
+    r, Vd = SO.lin_eliash_soc(chi.T, Gk.T, uni.transpose(0, 2, 1), np.asarray(init_delta).T, np.asarray(Vmat).T,
+                              np.asarray(olist), slist, np.asarray(kmap), np.asarray(invk), invs, temp, eps, Nx, Ny,
+                              Nz, itemax, gap_sym, arnoldi_m)
+    chi[...] = Vd.T
+    gap = np.ascontiguousarray(r.delta.T)
+    return (gap, r.lam, r) if full else gap
+
+
+def conv_delta_orb_to_band_soc(delta, uni, invk, invs, slist):
+    out = SO.conv_delta_orb_to_band_soc(delta.T, uni.transpose(0, 2, 1), np.asarray(invk), invs, slist)
+    return np.ascontiguousarray(out.T)
+
+
+def gen_Fk_soc(Gk, delta, invk, invs, slist, gap_sym):
+    F = SO.mkfk_trs_soc(Gk.T, delta.T, slist, np.asarray(invk), invs, gap_sym)
+    return np.ascontiguousarray(F.T)

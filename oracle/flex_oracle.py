@@ -590,10 +590,12 @@ class MkselfResult:
 
 def mkself(S_F, C_F, kmap, invk, olist, H_F, eig, U_F, mu_init, fill, temp, scf_loop,
            pp, eps, Nx, Ny, Nz, Nw, sub_sigma=1, m_diis=5, sw_rescale=True,
-           sw_tail=False, sigma_in=None, mu_old_in=None, sigma_scale=1.0, verbose=False):
+           sw_tail=False, sigma_in=None, mu_old_in=None, sigma_scale=1.0, verbose=False, hooks=None):
     """FLEX self-consistency loop, restated from fself.f90:287-446 with
     compare_sigma (:449-542), renew_mu (:544-660), get_rn (:662-687) and
-    precompute_eig_gkinv (:689-711).  sigma_in/mu_old_in emulate sw_in."""
+    precompute_eig_gkinv (:689-711).  sigma_in/mu_old_in emulate sw_in.
+    hooks (chi, stoner, vertex, sigma) replace the four physics steps; the
+    spin-orbit loop of fselfwithsoc.f90 passes its own."""
     grid = KGrid(kmap, invk, Nx, Ny, Nz)
     Nk = H_F.shape[0]
     No = H_F.shape[1]
@@ -736,15 +738,22 @@ def mkself(S_F, C_F, kmap, invk, olist, H_F, eig, U_F, mu_init, fill, temp, scf_
     it_done = 0
     for scf_i in range(1, scf_loop + 1):
         it_done = scf_i
-        if sw_tail:
+        if hooks is not None:
+            chi = hooks["chi"](G, mu)
+            stoner = hooks["stoner"](chi)
+        elif sw_tail:
             chi = chi0_tail(G, eig, U_F, mu, grid, olist, temp)
         else:
             chi = get_chi0_conv(G, grid, olist, temp)
-        stoner = ckchi(chi, S_F, C_F)[0]
+        if hooks is None:
+            stoner = ckchi(chi, S_F, C_F)[0]
         if sw_rescale and stoner >= 1.0:
             chi = chi * ((1.0 - 1.0e-4) / stoner)
-        V = vsigma_flex_nosoc(chi, S_F, C_F)
-        sig = calc_sigma(G, V, S_F, C_F, grid, olist, temp)
+        if hooks is not None:
+            sig = hooks["sigma"](G, hooks["vertex"](chi))
+        else:
+            V = vsigma_flex_nosoc(chi, S_F, C_F)
+            sig = calc_sigma(G, V, S_F, C_F, grid, olist, temp)
         if sub_sigma > 0:
             sig = hf_subtract(sig, sub_sigma)
         compare_sigma()

@@ -107,6 +107,36 @@ def random_hoppings(Norb, seed, shells=((1, 0, 0), (1, 1, 0), (2, 0, 0)), sigma=
     return rvec, ham_r
 
 
+def spin_orbit_hoppings(rvec, ham_r, alpha=0.0):
+    """Spin-orbital model of a spatial model: spin-up orbitals first, then
+    their spin-down partners (the default slist / invs of pyrpa's main.py),
+    plus a Rashba term alpha (sin ky s_x - sin kx s_y).  Returns
+    (rvec, ham_r, slist, invs) with invs 1-based.  The Rashba term keeps
+    time reversal, H(-k)_ab = s_a s_b H(k)_{b'a'}, which the reference's
+    irreducible-k scheme needs."""
+    n = ham_r.shape[1]
+    H = np.zeros((len(rvec), 2 * n, 2 * n), dtype=np.complex128)
+    H[:, :n, :n] = ham_r
+    H[:, n:, n:] = ham_r
+    if alpha:
+        sx = np.array([[0, 1], [1, 0]], dtype=np.complex128)
+        sy = np.array([[0, -1j], [1j, 0]], dtype=np.complex128)
+        for r, R in enumerate(np.asarray(rvec)):
+            for d, Mspin, sgn in ((0, sy, -1.0), (1, sx, 1.0)):
+                e = np.zeros(3)
+                e[d] = 1.0
+                if np.allclose(R, e):
+                    c = 0.5j
+                elif np.allclose(R, -e):
+                    c = -0.5j
+                else:
+                    continue
+                H[r] += np.kron(Mspin, np.eye(n)) * (alpha * sgn * c)
+    slist = np.array([1] * n + [-1] * n, dtype=np.int64)
+    invs = np.concatenate([np.arange(n, 2 * n), np.arange(n)]).astype(np.int64) + 1
+    return rvec, H, slist, invs
+
+
 def full_grid_dispersion_1orb(ham_r, rvec, Nx, Ny, Nz=1):
     """One-orbital band energy on the full grid [Nx,Ny,Nz]."""
     ix, iy, iz = np.meshgrid(np.arange(Nx), np.arange(Ny), np.arange(Nz), indexing="ij")
