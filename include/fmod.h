@@ -237,7 +237,58 @@ void pyrpa_gb_chi0sc(double* xs, double* xc, const double* Gk, const double* fk,
 void pyrpa_gb_sc_dyson(double* Gk, double* fk, const double* G0, const double* delta, const int64_t* Nk,
                        const int64_t* Nw, const int64_t* Norb);
 
-/* Symbols outside the accelerated path (transport, impurity, SOC, Eilenberger,
+/* ---- spin-orbit coupling.  Spin-orbital indices: slist(a) = +-1 spin label,
+ * invs(a) = 1-based spin partner; G(-k)_ab = s_a s_b G(k)_{invs b, invs a}.
+ * The engine covers Norb = 2 or 4 spin-orbitals (Nchi = 4 or 16), in FP64. */
+/* fUJ.f90:109-180 / 182-251: onsite vertex V (Nchi,Nchi) from U, J or Umat, Jmat (Norb,Norb) */
+void get_vmat_soc(double* Vmat, const int64_t* ol, const int64_t* sl, const int64_t* site, const int64_t* invs,
+                  const double* Uval, const double* Jval, const int64_t* Nchi, const int64_t* Norb);
+void get_vmat_soc_orb(double* Vmat, const int64_t* ol, const int64_t* sl, const int64_t* site,
+                      const int64_t* invs, const double* Umat, const double* Jmat, const int64_t* Nchi,
+                      const int64_t* Norb);
+/* fselfwithsoc.f90:1-153: the FLEX loop with the spin-orbit bubble, the vertex
+ * -V + V (I + chi0 V)^-1 chi0 V and the Sigma static slot -V (libs/flibs/_selfenergy.py:38-60) */
+void mkself_soc(double* sigmak, double* mu, const double* Vmat, const int64_t* kmap, const int64_t* invk,
+                const int64_t* invs, const int64_t* olist, const int64_t* slist, const double* hamk,
+                const double* eig, const double* uni, const double* mu_init, const double* rfill,
+                const double* temp, const int64_t* scf_loop, const double* pp, const double* eps,
+                const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb,
+                const int64_t* Nchi, const int64_t* Nx, const int64_t* Ny, const int64_t* Nz,
+                const int64_t* sub_sigma, const bool* sw_out, const bool* sw_in, const int64_t* m_diis,
+                const bool* sw_rescale, const double* sigma_scale);
+/* fchi0withsoc.f90:111-214 (libs/flibs/_susceptibility.py:141-159): chi (Nk,Nw,Nchi,Nchi) plus
+ * the outputs sgnsig (Norb,Norb), sgnsig2 (Nchi,Nchi) and invschi (Nchi, 1-based) */
+void get_chi0_soc(double* chi, double* sgnsig, double* sgnsig2, int64_t* invschi, const double* Vmat,
+                  const double* Gk, const int64_t* kmap, const int64_t* invk, const int64_t* invs,
+                  const int64_t* olist, const int64_t* slist, const double* temp, const int64_t* Nx,
+                  const int64_t* Ny, const int64_t* Nz, const int64_t* Nw, const int64_t* Nk,
+                  const int64_t* Nkall, const int64_t* Nchi, const int64_t* Norb);
+/* fchi0withsoc.f90:281-326: nu = 0 RPA channels chic, chiszz, chispm (Nk,Nchi/4,Nchi/4) */
+void get_chis_chic_soc(double* chic, double* chiszz, double* chispm, const double* chi, const double* Vmat,
+                       const int64_t* orb_list, const int64_t* olist, const int64_t* slist,
+                       const int64_t* invs, const int64_t* Nk, const int64_t* Nw, const int64_t* Nchi,
+                       const int64_t* Norb);
+/* feliashwithsoc.f90:1-424: delta (Nkall,Nw,Norb,Norb) on the full mesh; chi is overwritten
+ * with V_Delta = -V + V (I + chi0 V)^-1 chi0 V; two-pass Arnoldi (arnoldi_m > 0) or the
+ * shifted power method.  sgnsig, sgnsig2 and prt are not read (recomputed from slist);
+ * lambda goes to pyrpa_gb_last_stats. */
+void lin_eliash_soc(double* delta, double* chi, const double* Gk, const double* uni,
+                    const double* init_delta, const double* Vmat, const double* sgnsig, const double* sgnsig2,
+                    const double* prt, const int64_t* olist, const int64_t* slist, const int64_t* kmap,
+                    const int64_t* invk, const int64_t* invs, const int64_t* invschi, const double* temp,
+                    const double* eps, const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw,
+                    const int64_t* Nchi, const int64_t* Norb, const int64_t* Nx, const int64_t* Ny,
+                    const int64_t* Nz, const int64_t* itemax, const int64_t* gap_sym, const int64_t* arnoldi_m);
+/* feliashwithsoc.f90:426-518: F (Nkall,Nw,Norb,Norb) = -G(k) delta(k) G(-k)^+ and the spin-block fills */
+void mkfk_trs_soc_(double* fk, const double* Gk, const double* delta, const double* sgnsig, const int64_t* slist,
+                   const int64_t* invk, const int64_t* invs, const int64_t* Nkall, const int64_t* Nk,
+                   const int64_t* Nw, const int64_t* Norb, const int64_t* gap_sym);
+/* feliashwithsoc.f90:750-794: band-basis gap (Nkall,Norb,Norb) at the first frequency */
+void conv_delta_orb_to_band_soc(double* deltab, const double* delta, const double* uni, const int64_t* invk,
+                                const int64_t* invs, const int64_t* slist, const int64_t* Norb,
+                                const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw);
+
+/* Symbols outside the accelerated path (transport, impurity, Eilenberger,
  * real-frequency maps, Pade ...) are exported with no
  * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"
  * so that `import libs.flibs` binds every name it expects. */

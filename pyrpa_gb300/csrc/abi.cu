@@ -908,6 +908,164 @@ void pyrpa_gb_sc_dyson(double2* Gk, double2* fk, const double2* G0, const double
                                   nan_fill(fk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb))))
 }
 
+// ------------------------------------------------------------ spin-orbit --
+// Onsite vertex with spin-orbit coupling (fUJ.f90:109-180 and, with
+// orbital-dependent U/J, :182-251); host code, written as V(j,i).
+namespace {
+void vmat_soc(double* Vmat, const int64_t* ol, const int64_t* sl, const int64_t* site, const int64_t* invs,
+              double U, double J, const double* Umat, const double* Jmat, int64_t n, int64_t no) {
+  const double Up = U - 2 * J;
+  const bool orb = Umat != nullptr;
+  auto Uf = [&](int64_t a, int64_t b) { return Umat[a + no * b]; };  // 0-based
+  auto Jf = [&](int64_t a, int64_t b) { return Jmat[a + no * b]; };
+  auto inv = [&](int64_t a) { return invs[a] - 1; };
+  auto s = [&](int64_t a) { return sl[a]; };
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = 0; j < n; ++j) {
+      double v = 0.0;
+      const int64_t i1 = ol[i] - 1, i2 = ol[n + i] - 1, j1 = ol[j] - 1, j2 = ol[n + j] - 1;
+      PGB_CHECK(i1 >= 0 && i1 < no && i2 >= 0 && i2 < no && j1 >= 0 && j1 < no && j2 >= 0 && j2 < no,
+                "olist entry outside [1,Norb]");
+      if (site[i] == site[j]) {
+        if (s(i1) == s(i2) && s(j1) == s(j2)) {
+          if (s(i1) == s(j1)) {  // equal spins: (C-S)/2
+            if (i1 == j2 && j1 == i2) {
+              v = 0.0;
+            } else if (i1 == i2 && j1 == j2) {
+              v = orb ? Uf(i1, j1) - Jf(i1, j1) : Up - J;
+            } else if (i1 == j1 && i2 == j2) {
+              v = orb ? Jf(i1, i2) - Uf(i1, i2) : J - Up;
+            }
+          } else {  // opposite spins: (C+S)/2
+            if (i1 == i2 && j1 == j2) {
+              v = i1 == inv(j1) ? (orb ? Uf(i1, i1) : U) : (orb ? Uf(i1, j1) : Up);
+            } else if (i1 == inv(j1) && i2 == inv(j2)) {
+              v = orb ? Jf(i1, i2) : J;
+            } else if (i1 == inv(j2) && j1 == inv(i2)) {
+              v = orb ? Jf(i1, i2) : J;
+            }
+          }
+        } else if (s(i1) == s(j1) && s(i2) == s(j2)) {  // spin flip: -S
+          if (i1 == inv(i2) && j1 == inv(j2)) {
+            v = i1 == j1 ? -(orb ? Uf(i1, i1) : U) : -(orb ? Jf(i1, j1) : J);
+          } else if (i1 == j1 && i2 == j2) {
+            v = -(orb ? Uf(i1, i2) : Up);
+          } else if (i1 == inv(j2) && j1 == inv(i2)) {
+            v = -(orb ? Jf(i1, i2) : J);
+          }
+        }
+      }
+      Vmat[j + n * i] = v;
+    }
+}
+}  // namespace
+
+void get_vmat_soc(double* Vmat, const int64_t* ol, const int64_t* sl, const int64_t* site, const int64_t* invs,
+                  const double* Uval, const double* Jval, const int64_t* Nchi, const int64_t* Norb) {
+  ABI_TRY
+  vmat_soc(Vmat, ol, sl, site, invs, *Uval, *Jval, nullptr, nullptr, *Nchi, *Norb);
+  ABI_CATCH("get_vmat_soc", nan_fill(Vmat, (size_t)(*Nchi) * (*Nchi)))
+}
+
+void get_vmat_soc_orb(double* Vmat, const int64_t* ol, const int64_t* sl, const int64_t* site, const int64_t* invs,
+                      const double* Umat, const double* Jmat, const int64_t* Nchi, const int64_t* Norb) {
+  ABI_TRY
+  vmat_soc(Vmat, ol, sl, site, invs, 0.0, 0.0, Umat, Jmat, *Nchi, *Norb);
+  ABI_CATCH("get_vmat_soc_orb", nan_fill(Vmat, (size_t)(*Nchi) * (*Nchi)))
+}
+
+void mkself_soc(double2* sigmak, double* mu, const double* Vmat, const int64_t* kmap, const int64_t* invk,
+                const int64_t* invs, const int64_t* olist, const int64_t* slist, const double2* hamk, const double* eig,
+                const double2* uni, const double* mu_init, const double* rfill, const double* temp,
+                const int64_t* scf_loop, const double* pp, const double* eps, const int64_t* Nkall, const int64_t* Nk,
+                const int64_t* Nw, const int64_t* Norb, const int64_t* Nchi, const int64_t* Nx, const int64_t* Ny,
+                const int64_t* Nz, const int64_t* sub_sigma, const bool* sw_out, const bool* sw_in,
+                const int64_t* m_diis, const bool* sw_rescale, const double* sigma_scale) {
+  ABI_TRY
+  ensure_context();
+  MkselfArgs a{sigmak, mu, Vmat, Vmat, kmap, invk, olist, hamk, eig, uni, *mu_init, *rfill, *temp, *scf_loop, *pp,
+               *eps, *Nkall, *Nk, *Nw, *Norb, *Nchi, *Nx, *Ny, *Nz, *sub_sigma, *sw_out, *sw_in, *m_diis,
+               *sw_rescale, false, *sigma_scale};
+  run_mkself_soc(a, SocSpin{invs, slist});
+  ABI_CATCH("mkself_soc", (nan_fill(sigmak, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)), *mu = NAN))
+}
+
+void get_chi0_soc(double2* chi, double* sgnsig, double* sgnsig2, int64_t* invschi, const double* Vmat,
+                  const double2* Gk, const int64_t* kmap, const int64_t* invk, const int64_t* invs,
+                  const int64_t* olist, const int64_t* slist, const double* temp, const int64_t* Nx, const int64_t* Ny,
+                  const int64_t* Nz, const int64_t* Nw, const int64_t* Nk, const int64_t* Nkall, const int64_t* Nchi,
+                  const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t n = *Nchi, no = *Norb;
+  // sign tables and the spin-flipped chi index (fchi0withsoc.f90:136-154, 200-214)
+  for (int64_t j = 0; j < no; ++j)
+    for (int64_t i = 0; i < no; ++i) sgnsig[i + no * j] = (double)(slist[i] * slist[j]);
+  auto ps = [&](int64_t l) { return slist[olist[l] - 1] * slist[olist[n + l] - 1]; };
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = 0; i < n; ++i) sgnsig2[i + n * j] = (double)(ps(i) * ps(j));
+  for (int64_t l = 0; l < n; ++l) {
+    invschi[l] = 0;
+    const int64_t i = invs[olist[l] - 1], j = invs[olist[n + l] - 1];
+    for (int64_t m = 0; m < n; ++m)
+      if (olist[m] == i && olist[n + m] == j) {
+        invschi[l] = m + 1;
+        break;
+      }
+  }
+  run_chi0_soc(chi, Vmat, Gk, kmap, invk, olist, SocSpin{invs, slist}, *temp, *Nx, *Ny, *Nz, *Nw, *Nk, *Nkall, n, no);
+  ABI_CATCH("get_chi0_soc", nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)))
+}
+
+void get_chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const double2* chi, const double* Vmat,
+                       const int64_t* orb_list, const int64_t* olist, const int64_t* slist, const int64_t* invs,
+                       const int64_t* Nk, const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  (void)invs;
+  run_chis_chic_soc(chic, chiszz, chispm, chi, Vmat, orb_list, olist, slist, *Nk, *Nw, *Nchi, *Norb);
+  ABI_CATCH("get_chis_chic_soc", (nan_fill(chic, (size_t)(*Nk) * (*Nchi / 4) * (*Nchi / 4)),
+                                  nan_fill(chiszz, (size_t)(*Nk) * (*Nchi / 4) * (*Nchi / 4)),
+                                  nan_fill(chispm, (size_t)(*Nk) * (*Nchi / 4) * (*Nchi / 4))))
+}
+
+void lin_eliash_soc(double2* delta, double2* chi, const double2* Gk, const double2* uni, const double* init_delta,
+                    const double* Vmat, const double* sgnsig, const double* sgnsig2, const double* prt,
+                    const int64_t* olist, const int64_t* slist, const int64_t* kmap, const int64_t* invk,
+                    const int64_t* invs, const int64_t* invschi, const double* temp, const double* eps,
+                    const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw, const int64_t* Nchi,
+                    const int64_t* Norb, const int64_t* Nx, const int64_t* Ny, const int64_t* Nz,
+                    const int64_t* itemax, const int64_t* gap_sym, const int64_t* arnoldi_m) {
+  ABI_TRY
+  ensure_context();
+  (void)sgnsig;  // recomputed from slist
+  (void)sgnsig2;
+  (void)prt;
+  LinEliashSocArgs a{delta, chi, Gk, uni, init_delta, Vmat, olist, kmap, invk, invschi, SocSpin{invs, slist},
+                     *temp, *eps, *Nkall, *Nk, *Nw, *Nchi, *Norb, *Nx, *Ny, *Nz, *itemax, *gap_sym, *arnoldi_m};
+  run_lin_eliash_soc(a);
+  ABI_CATCH("lin_eliash_soc", nan_fill(delta, (size_t)(*Nkall) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+void mkfk_trs_soc_(double2* fk, const double2* Gk, const double2* delta, const double* sgnsig, const int64_t* slist,
+                   const int64_t* invk, const int64_t* invs, const int64_t* Nkall, const int64_t* Nk,
+                   const int64_t* Nw, const int64_t* Norb, const int64_t* gap_sym) {
+  ABI_TRY
+  ensure_context();
+  (void)sgnsig;
+  run_mkfk_soc(fk, Gk, delta, invk, SocSpin{invs, slist}, *Nkall, *Nk, *Nw, *Norb, *gap_sym);
+  ABI_CATCH("mkfk_trs_soc_", nan_fill(fk, (size_t)(*Nkall) * (*Nw) * (*Norb) * (*Norb)))
+}
+
+void conv_delta_orb_to_band_soc(double2* deltab, const double2* delta, const double2* uni, const int64_t* invk,
+                                const int64_t* invs, const int64_t* slist, const int64_t* Norb, const int64_t* Nkall,
+                                const int64_t* Nk, const int64_t* Nw) {
+  ABI_TRY
+  ensure_context();
+  run_orb_to_band_soc(deltab, delta, uni, invk, SocSpin{invs, slist}, *Norb, *Nkall, *Nk, *Nw);
+  ABI_CATCH("conv_delta_orb_to_band_soc", nan_fill(deltab, (size_t)(*Nkall) * (*Norb) * (*Norb)))
+}
+
 void mkfk_trs_nsoc_(double2* fk, const double2* Gk, const double2* delta, const int64_t* Nk, const int64_t* Nw,
                     const int64_t* Norb) {
   ABI_TRY
@@ -1014,17 +1172,14 @@ PGB_STUB(calc_sigma_hall)
 PGB_STUB(calc_tau_epa)
 PGB_STUB(calc_tdf)
 PGB_STUB(chiq_map)
-PGB_STUB(conv_delta_orb_to_band_soc)
 PGB_STUB(gen_dos)
 PGB_STUB(gen_green_inv_from_eig)
 PGB_STUB(gen_imp_ham)
 PGB_STUB(gen_tr_greenw_0)
 PGB_STUB(get_a_)
 PGB_STUB(get_band_to_orb_delta)
-PGB_STUB(get_chi0_soc)
 PGB_STUB(get_chi_irr)
 PGB_STUB(get_chi_irr_sc)
-PGB_STUB(get_chis_chic_soc)
 PGB_STUB(get_dft_imp_ham)
 PGB_STUB(get_eig_mlo)
 PGB_STUB(get_imass0)
@@ -1039,15 +1194,10 @@ PGB_STUB(get_tr_chi)
 PGB_STUB(get_tr_phi)
 PGB_STUB(get_veloc)
 PGB_STUB(get_vlm0)
-PGB_STUB(get_vmat_soc)
-PGB_STUB(get_vmat_soc_orb)
 PGB_STUB(get_vnm)
-PGB_STUB(lin_eliash_soc)
 PGB_STUB(matrix_riccati_batch)
 PGB_STUB(matrix_riccati_chords)
 PGB_STUB(mkbdghamk)
-PGB_STUB(mkfk_trs_soc_)
-PGB_STUB(mkself_soc)
 PGB_STUB(pade_with_trace)
 PGB_STUB(phiq_map)
 PGB_STUB(riccati_chords)

@@ -274,8 +274,13 @@ double stage_chi0(Inputs& in, const FlexParams& a, const double2* G, double mu, 
   double sdw = 0, cdw = 0;
   int qs = 0, qc = 0;
   tm.start();
-  stoner<R>(g, chi, in.S.p, in.C.p, &sdw, &cdw, &qs, &qc);
-  ckchi_print(g, sdw, cdw, qs, qc);
+  if (in.soc) {  // max Re eig(-chi0(q,0) V) (fchi0withsoc.f90:156-198)
+    stoner<R>(g, chi, in.Vneg.p, in.Vneg.p, &sdw, &cdw, &qs, &qc);
+    ckchi_print_soc(g, sdw, qs);
+  } else {
+    stoner<R>(g, chi, in.S.p, in.C.p, &sdw, &cdw, &qs, &qc);
+    ckchi_print(g, sdw, cdw, qs, qc);
+  }
   if (a.sw_rescale && sdw >= 1.0) {
     const double rt = 1.0 - 1.0e-4;
     log("[FLEX] Stoner factor=%10.6f >= 1: rescaling chi0 to%7.4f\n", sdw, rt);
@@ -288,14 +293,20 @@ template <typename R>
 void stage_vertex(Inputs& in, cx<R>* chi) {
   Timer tm;
   tm.start();
-  PGB_CHECK(vertex<R>(chi, in.g.K, in.g.K, in.Nchi, in.S.p, in.C.p, 0), "zgesv failed in V_sigma");
+  if (in.soc) {
+    PGB_CHECK((std::is_same<R, double>::value), "the spin-orbit loop runs in FP64");
+    PGB_CHECK(vertex_soc(reinterpret_cast<double2*>(chi), in.g.K, in.Nchi, in.V.p), "zgesv failed in V_sigma");
+  } else {
+    PGB_CHECK(vertex<R>(chi, in.g.K, in.g.K, in.Nchi, in.S.p, in.C.p, 0), "zgesv failed in V_sigma");
+  }
   g_stats.t_vertex += tm.stop();
 }
 template <typename R>
 void stage_sigma(Inputs& in, const FlexParams& a, const double2* G, const cx<R>* chi, double2* sig) {
   Timer tm;
   tm.start();
-  sigma<R>(in.g, in.p, G, chi, in.S.p, in.C.p, a.temp, sig);
+  if (in.soc) sigma<R>(in.g, in.p, G, chi, in.Vneg.p, nullptr, a.temp, sig);  // static slot -V
+  else sigma<R>(in.g, in.p, G, chi, in.S.p, in.C.p, a.temp, sig);
   g_stats.t_sigma += tm.stop();
 }
 
@@ -686,6 +697,115 @@ void run_mkself(const MkselfArgs& a, int prec) {
   sync();
 }
 
+// Two-pass Arnoldi of lin_eliash (feliash.f90:190-388, feliashwithsoc.f90:190-388):
+// pass 1 from the initial gap, exit at a Ritz value >= 0.1, else pass 2 with
+// the shift -lambda_- and that Ritz vector deflated.  apply_op/inner/norm/init
+// define the operator and the inner product of the caller's vector space of n
+// elements; the normalized Ritz vector goes to delta_out, lambda is returned.
+template <class Apply, class Inner, class Norm, class Init>
+double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm norm, Init init_vec,
+                        double2* delta_out) {
+  cudaStream_t st = ctx().stream;
+  double lambda_out = 0.0;
+  DBuf<double2> w(KE);
+  PGB_CHECK(m <= 64, "arnoldi_m above 64 is not supported");
+  std::vector<DBuf<double2>> V(m);
+  for (auto& v : V) v.alloc(KE);
+  auto arnoldi = [&](double shift, const double2* defl, std::vector<double2>& Hm, int& m_act) {
+    Hm.assign((size_t)(m + 1) * m, make_double2(0, 0));
+    m_act = m;
+    for (int j = 0; j < m; ++j) {
+      apply_op(w.p, V[j].p);
+      if (defl) {
+        axpy(w.p, make_double2(shift, 0), V[j].p, KE);
+        double2 h = inner(defl, w.p);
+        axpy(w.p, make_double2(-h.x, -h.y), defl, KE);
+      }
+      for (int ii = 0; ii <= j; ++ii) {
+        double2 h = inner(V[ii].p, w.p);
+        Hm[ii * m + j] = h;
+        axpy(w.p, make_double2(-h.x, -h.y), V[ii].p, KE);
+      }
+      const double beta = norm(w.p);
+      Hm[(j + 1) * m + j] = make_double2(beta, 0);
+      if (beta < 1.0e-14) {
+        m_act = j + 1;
+        break;
+      }
+      if (j < m - 1) {
+        PGB_CUDA(cudaMemcpyAsync(V[j + 1].p, w.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal(V[j + 1].p, 1.0 / beta, KE);
+      }
+    }
+  };
+  auto ritz = [&](double2* out, const std::vector<double2>& Hm, int m_act, double2 lam) {
+    std::vector<double2> Hs((size_t)m_act * m_act);
+    for (int i = 0; i < m_act; ++i)
+      for (int j = 0; j < m_act; ++j) Hs[i * m_act + j] = Hm[i * m + j];
+    std::vector<double2> y = eigvec(Hs, m_act, lam);
+    std::vector<const double2*> xs(m_act);
+    for (int i = 0; i < m_act; ++i) xs[i] = V[i].p;
+    lincomb(out, xs.data(), y.data(), m_act, KE);
+    scal(out, 1.0 / norm(out), KE);
+  };
+  auto ritz_values = [&](const std::vector<double2>& Hm, int m_act) {
+    std::vector<double2> Hs((size_t)m_act * m_act), ev;
+    for (int i = 0; i < m_act; ++i)
+      for (int j = 0; j < m_act; ++j) Hs[i * m_act + j] = Hm[i * m + j];
+    eig_small(Hs, m_act, ev);
+    return ev;
+  };
+  // pass 1: no shift
+  init_vec(V[0].p);
+  log("Arnoldi pass 1 (no shift): Krylov dim =%4d ...\n", m);
+  std::vector<double2> Hm;
+  int m_act = m;
+  arnoldi(0.0, nullptr, Hm, m_act);
+  std::vector<double2> ev = ritz_values(Hm, m_act);
+  int imin = 0, imax = 0;
+  for (int i = 1; i < m_act; ++i) {
+    if (ev[i].x < ev[imin].x) imin = i;
+    if (ev[i].x > ev[imax].x) imax = i;
+  }
+  const double lambda1 = ev[imin].x;
+  for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x);
+  log("  lambda_- =%12.6f\n", lambda1);
+  DBuf<double2> D(KE);
+  if (ev[imax].x >= 0.1) {
+    lambda_out = ev[imax].x;
+    log("  eliash   =%12.6f\n", lambda_out);
+    ritz(D.p, Hm, m_act, ev[imax]);
+  } else {
+    DBuf<double2> delta1(KE);
+    ritz(delta1.p, Hm, m_act, ev[imin]);
+    const double shift = -lambda1;
+    init_vec(V[0].p);
+    double2 h = inner(delta1.p, V[0].p);
+    axpy(V[0].p, make_double2(-h.x, -h.y), delta1.p, KE);
+    const double b0 = norm(V[0].p);
+    if (!(b0 >= 1.0e-14)) {
+      // the operator has no component outside the pass-1 direction
+      lambda_out = lambda1;
+      PGB_CUDA(cudaMemcpyAsync(D.p, delta1.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    } else {
+      scal(V[0].p, 1.0 / b0, KE);
+      log("Arnoldi pass 2 (shift=%10.6f): Krylov dim =%4d ...\n", shift, m);
+      arnoldi(shift, delta1.p, Hm, m_act);
+      ev = ritz_values(Hm, m_act);
+      imax = 0;
+      for (int i = 1; i < m_act; ++i)
+        if (ev[i].x > ev[imax].x) imax = i;
+      for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x - shift);
+      lambda_out = ev[imax].x - shift;
+      log("  eliash   =%12.6f\n", lambda_out);
+      ritz(D.p, Hm, m_act, ev[imax]);
+    }
+  }
+  PGB_CUDA(cudaMemcpyAsync(delta_out, D.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+  sync();
+  return lambda_out;
+}
+
 // ============================================================ lin_eliash ==
 // chi (device, cx<R>) is overwritten with the pairing vertex V_Delta; if
 // chi_host is given, V_Delta is also copied back there (feliash.f90:61).
@@ -719,7 +839,7 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
   const double weight = a.temp / (double)g.Nkall;
   const double scale = weight / (double)g.P;
   DeltaKernelCache<R> cache;
-  DBuf<double2> F(KE), w(KE);
+  DBuf<double2> F(KE);
   Timer ta;
   auto apply_op = [&](double2* out, const double2* v) {
     ta.start();
@@ -742,101 +862,7 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
   double lambda_out = 0.0;
   const int m = (int)a.arnoldi_m;
   if (m > 0) {
-    PGB_CHECK(m <= 64, "arnoldi_m above 64 is not supported");
-    std::vector<DBuf<double2>> V(m);
-    for (auto& v : V) v.alloc(KE);
-    auto arnoldi = [&](double shift, const double2* defl, std::vector<double2>& Hm, int& m_act) {
-      Hm.assign((size_t)(m + 1) * m, make_double2(0, 0));
-      m_act = m;
-      for (int j = 0; j < m; ++j) {
-        apply_op(w.p, V[j].p);
-        if (defl) {
-          axpy(w.p, make_double2(shift, 0), V[j].p, KE);
-          double2 h = inner(defl, w.p);
-          axpy(w.p, make_double2(-h.x, -h.y), defl, KE);
-        }
-        for (int ii = 0; ii <= j; ++ii) {
-          double2 h = inner(V[ii].p, w.p);
-          Hm[ii * m + j] = h;
-          axpy(w.p, make_double2(-h.x, -h.y), V[ii].p, KE);
-        }
-        const double beta = norm(w.p);
-        Hm[(j + 1) * m + j] = make_double2(beta, 0);
-        if (beta < 1.0e-14) {
-          m_act = j + 1;
-          break;
-        }
-        if (j < m - 1) {
-          PGB_CUDA(cudaMemcpyAsync(V[j + 1].p, w.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-          scal(V[j + 1].p, 1.0 / beta, KE);
-        }
-      }
-    };
-    auto ritz = [&](double2* out, const std::vector<double2>& Hm, int m_act, double2 lam) {
-      std::vector<double2> Hs((size_t)m_act * m_act);
-      for (int i = 0; i < m_act; ++i)
-        for (int j = 0; j < m_act; ++j) Hs[i * m_act + j] = Hm[i * m + j];
-      std::vector<double2> y = eigvec(Hs, m_act, lam);
-      std::vector<const double2*> xs(m_act);
-      for (int i = 0; i < m_act; ++i) xs[i] = V[i].p;
-      lincomb(out, xs.data(), y.data(), m_act, KE);
-      scal(out, 1.0 / norm(out), KE);
-    };
-    auto ritz_values = [&](const std::vector<double2>& Hm, int m_act) {
-      std::vector<double2> Hs((size_t)m_act * m_act), ev;
-      for (int i = 0; i < m_act; ++i)
-        for (int j = 0; j < m_act; ++j) Hs[i * m_act + j] = Hm[i * m + j];
-      eig_small(Hs, m_act, ev);
-      return ev;
-    };
-    // pass 1: no shift
-    init_vec(V[0].p);
-    log("Arnoldi pass 1 (no shift): Krylov dim =%4d ...\n", m);
-    std::vector<double2> Hm;
-    int m_act = m;
-    arnoldi(0.0, nullptr, Hm, m_act);
-    std::vector<double2> ev = ritz_values(Hm, m_act);
-    int imin = 0, imax = 0;
-    for (int i = 1; i < m_act; ++i) {
-      if (ev[i].x < ev[imin].x) imin = i;
-      if (ev[i].x > ev[imax].x) imax = i;
-    }
-    const double lambda1 = ev[imin].x;
-    for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x);
-    log("  lambda_- =%12.6f\n", lambda1);
-    DBuf<double2> D(KE);
-    if (ev[imax].x >= 0.1) {
-      lambda_out = ev[imax].x;
-      log("  eliash   =%12.6f\n", lambda_out);
-      ritz(D.p, Hm, m_act, ev[imax]);
-    } else {
-      DBuf<double2> delta1(KE);
-      ritz(delta1.p, Hm, m_act, ev[imin]);
-      const double shift = -lambda1;
-      init_vec(V[0].p);
-      double2 h = inner(delta1.p, V[0].p);
-      axpy(V[0].p, make_double2(-h.x, -h.y), delta1.p, KE);
-      const double b0 = norm(V[0].p);
-      if (!(b0 >= 1.0e-14)) {
-        // the operator has no component outside the pass-1 direction
-        lambda_out = lambda1;
-        PGB_CUDA(cudaMemcpyAsync(D.p, delta1.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-      } else {
-        scal(V[0].p, 1.0 / b0, KE);
-        log("Arnoldi pass 2 (shift=%10.6f): Krylov dim =%4d ...\n", shift, m);
-        arnoldi(shift, delta1.p, Hm, m_act);
-        ev = ritz_values(Hm, m_act);
-        imax = 0;
-        for (int i = 1; i < m_act; ++i)
-          if (ev[i].x > ev[imax].x) imax = i;
-        for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x - shift);
-        lambda_out = ev[imax].x - shift;
-        log("  eliash   =%12.6f\n", lambda_out);
-        ritz(D.p, Hm, m_act, ev[imax]);
-      }
-    }
-    PGB_CUDA(cudaMemcpyAsync(delta_out, D.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-    sync();
+    lambda_out = arnoldi_two_pass(m, KE, apply_op, inner, norm, init_vec, delta_out);
   } else {
     // shifted power method with deflation (feliash.f90:66-140)
     DBuf<double2> D(KE), nd(KE), d1(KE), tmp(KE);
@@ -1287,6 +1313,245 @@ void run_nonlin_eliash(const NonlinArgs& a) {
   Sig.download(a.sigmak, KE);
   G.download(a.Gk, KE);
   sync();
+}
+
+// ============================================================ spin-orbit ==
+namespace {
+// the maps of a full k list for build_full_mesh without a Geom: the
+// reference's invk alone (full-mesh kernels that need no FFT)
+void full_mesh_from_invk(FullMesh& fm, const int64_t* invk, int64_t Nkall, int64_t Nk) {
+  std::vector<int> irr(Nkall), flag(Nkall), minus(Nkall);
+  for (int64_t i = 0; i < Nkall; ++i) {
+    irr[i] = (int)invk[3 * i] - 1;
+    flag[i] = (int)invk[3 * i + 1];
+    minus[i] = (int)invk[3 * i + 2] - 1;
+    PGB_CHECK(irr[i] >= 0 && irr[i] < Nk, "invk(1,:) outside [1,Nk]");
+    PGB_CHECK(flag[i] == 0 || flag[i] == 1, "invk(2,:) must be 0 or 1");
+  }
+  fm.Nkall = Nkall;
+  fm.irr.alloc(Nkall);
+  fm.irr.upload(irr.data(), Nkall);
+  fm.flag.alloc(Nkall);
+  fm.flag.upload(flag.data(), Nkall);
+  fm.minus.alloc(Nkall);
+  fm.minus.upload(minus.data(), Nkall);
+}
+
+void spin_map(Geom& g, const SocSpin& sp, int64_t Norb) {
+  PGB_CHECK(Norb <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  for (int a = 0; a < Norb; ++a) {
+    PGB_CHECK(sp.invs[a] >= 1 && sp.invs[a] <= Norb, "invs entry outside [1,Norb]");
+    PGB_CHECK(sp.slist[a] == 1 || sp.slist[a] == -1, "slist entries must be +1 or -1");
+    g.spin.inv[a] = (int)sp.invs[a] - 1;
+    g.spin.sgn[a] = (int)sp.slist[a];
+  }
+  g.spin.on = 1;
+}
+
+void upload_soc(Inputs& in, const int64_t* kmap, const int64_t* invk, const int64_t* olist, const SocSpin& sp,
+                int64_t Nx, int64_t Ny, int64_t Nz, int64_t Nkall, int64_t Nk, int64_t Nw, int64_t Norb, int64_t Nchi,
+                const double* Vmat, const double2* hamk, const double* eig, const double2* uni) {
+  PGB_CHECK(Nchi == 4 || Nchi == 16, "the spin-orbit engine supports Nchi = 4 or 16 (2 or 4 spin-orbitals)");
+  upload_inputs(in, kmap, invk, olist, Nx, Ny, Nz, Nkall, Nk, Nw, Norb, Nchi, Vmat, Vmat, hamk, eig, uni);
+  build_pairs_soc(in.p, in.g, olist, (int)Norb, (int)Nchi, sp.invs, sp.slist);
+  in.soc = true;
+  const size_t n2 = (size_t)Nchi * Nchi;
+  std::vector<double> neg(Vmat, Vmat + n2);
+  for (auto& x : neg) x = -x;
+  in.V.alloc(n2);
+  in.V.upload(Vmat, n2);
+  in.Vneg.alloc(n2);
+  in.Vneg.upload(neg.data(), n2);
+}
+}  // namespace
+
+void run_mkself_soc(const MkselfArgs& a, const SocSpin& sp) {
+  g_stats = LastStats{};
+  Inputs in;
+  upload_soc(in, a.kmap, a.invk, a.olist, sp, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Smat, a.hamk,
+             a.eig, a.uni);
+  FlexParams prm{a.mu_init, a.fill, a.temp, a.scf_loop, a.pp, a.eps, a.sub_sigma, a.sw_out, a.sw_in, a.m_diis,
+                 a.sw_rescale, false, a.sigma_scale};
+  const long long KE = in.g.K * a.Norb * a.Norb;
+  DBuf<double2> sig(KE);
+  mkself_core(in, prm, sig.p, a.mu_out, nullptr, 0.0, 0.0, 64);
+  sig.download(a.sigmak, KE);
+  sync();
+}
+
+double run_chi0_soc(double2* chi_out, const double* Vmat, const double2* Gk, const int64_t* kmap,
+                    const int64_t* invk, const int64_t* olist, const SocSpin& sp, double temp, int64_t Nx, int64_t Ny,
+                    int64_t Nz, int64_t Nw, int64_t Nk, int64_t Nkall, int64_t Nchi, int64_t Norb) {
+  g_stats = LastStats{};
+  Inputs in;
+  upload_soc(in, kmap, invk, olist, sp, Nx, Ny, Nz, Nkall, Nk, Nw, Norb, Nchi, Vmat, nullptr, nullptr, nullptr);
+  const long long KE = in.g.K * Norb * Norb, KC = in.g.K * Nchi * Nchi;
+  DBuf<double2> G(KE), chi(KC);
+  G.upload(Gk, KE);
+  chi0<double>(in.g, in.p, G.p, temp, nullptr, chi.p);
+  double sdw = 0, cdw = 0;
+  int qs = 0, qc = 0;
+  stoner<double>(in.g, chi.p, in.Vneg.p, in.Vneg.p, &sdw, &cdw, &qs, &qc);
+  ckchi_print_soc(in.g, sdw, qs);
+  g_stats.stoner = sdw;
+  chi.download(chi_out, KC);
+  sync();
+  return sdw;
+}
+
+void run_lin_eliash_soc(const LinEliashSocArgs& a) {
+  g_stats = LastStats{};
+  cudaStream_t st = ctx().stream;
+  Inputs in;
+  upload_soc(in, a.kmap, a.invk, a.olist, a.sp, a.Nx, a.Ny, a.Nz, a.Nkall, a.Nk, a.Nw, a.Norb, a.Nchi, a.Vmat, nullptr,
+             nullptr, a.uni);
+  const Geom& g = in.g;
+  FullMesh fm;
+  build_full_mesh(fm, g, a.invk);
+  const int No = (int)a.Norb, Nchi = (int)a.Nchi;
+  const long long KE = g.K * No * No, KC = g.K * Nchi * Nchi, KF = fm.Nkall * g.Nw * No * No;
+  const int gap_sym = (int)a.gap_sym;
+  DBuf<double2> chi(KC), G(KE), F(KF), D(KF);
+  chi.upload(a.chi, KC);
+  {
+    Timer tv;
+    tv.start();
+    PGB_CHECK(vertex_soc(chi.p, g.K, Nchi, in.V.p), "zgesv failed in V_delta");  // chi -> V_Delta
+    g_stats.t_vertex += tv.stop();
+  }
+  chi.download(a.chi, KC);
+  G.upload(a.Gk, KE);
+  DBuf<double> init((size_t)a.Nk * No), ones(fm.Nkall);
+  init.upload(a.init_delta, (size_t)a.Nk * No);
+  {
+    std::vector<double> h1(fm.Nkall, 1.0);
+    ones.upload(h1.data(), fm.Nkall);
+  }
+  std::vector<double> hV(a.Vmat, a.Vmat + (size_t)Nchi * Nchi);
+  std::vector<int> invschi(Nchi);
+  for (int l = 0; l < Nchi; ++l) invschi[l] = (int)a.invschi[l];
+  const double scale = -a.temp / (double)g.Nkall;  // A v = -(T/Nkall) mkdelta_soc(mkfk_soc(v))
+  Timer ta;
+  auto apply_op = [&](double2* out, const double2* v) {
+    ta.start();
+    mkfk_soc(F.p, G.p, v, fm, g, gap_sym);
+    mkdelta_soc(g, in.p, fm, F.p, chi.p, hV, invschi, gap_sym, scale, out);
+    g_stats.t_apply += ta.stop();
+    g_stats.applies += 1;
+  };
+  const int Nkf = (int)fm.Nkall;
+  auto inner = [&](const double2* u, const double2* v) {  // 2 sum conj(u) v (feliashwithsoc.f90:400-424)
+    const double2 s = inner_w(u, v, ones.p, Nkf, KF);
+    return make_double2(2.0 * s.x, 2.0 * s.y);
+  };
+  auto norm = [&](const double2* f) { return std::sqrt(2.0 * inner_w(f, f, ones.p, Nkf, KF).x); };
+  auto init_vec = [&](double2* d) {
+    initial_delta_soc(d, init.p, in.uni.p, fm, g, gap_sym);
+    const double n2 = inner_w(d, d, ones.p, Nkf, KF).x;
+    PGB_CHECK(n2 > 0, "Error: get_initial_delta_soc norm <= 0");
+    scal(d, 1.0 / std::sqrt(2.0 * n2), KF);
+  };
+  double lam = 0.0;
+  if (a.arnoldi_m > 0) {
+    lam = arnoldi_two_pass((int)a.arnoldi_m, KF, apply_op, inner, norm, init_vec, D.p);
+  } else {
+    // shifted power method of lin_eliash_soc (feliashwithsoc.f90:60-110): pass 2
+    // runs with the shift |newdelta| of pass 1 and no deflation
+    DBuf<double2> nd(KF), tmp(KF);
+    double norm2 = 0.0, nrm = 1.0;
+    for (int i_eig = 1; i_eig <= 2; ++i_eig) {
+      init_vec(D.p);
+      int count = 0;
+      for (int it = 1; it <= a.itemax; ++it) {
+        apply_op(nd.p, D.p);
+        if (norm2 != 0.0) axpy(nd.p, make_double2(norm2, 0), D.p, KF);
+        nrm = norm(nd.p);
+        PGB_CHECK(nrm > 0, "Error: norm <= 0 in iter_loop");
+        const double inrm = 1.0 / nrm;
+        const double lam_rq = inner(D.p, nd.p).x;
+        PGB_CUDA(cudaMemcpyAsync(tmp.p, nd.p, KF * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal(tmp.p, inrm, KF);
+        axpy(tmp.p, make_double2(-1, 0), D.p, KF);
+        const double ep = norm(tmp.p);
+        axpy(tmp.p, make_double2(2, 0), D.p, KF);
+        const double en = norm(tmp.p);
+        const double verr = std::min(ep, en);
+        lam = lam_rq - norm2;
+        log("%3d lambda_elsh=%16.8E\n", it, lam);
+        if (verr < a.eps) {
+          if (lam > 0.1 || lam < 0.0) break;
+          if (verr < a.eps * 1.0e-2) ++count;
+          if (count > 30) break;
+        }
+        PGB_CUDA(cudaMemcpyAsync(D.p, nd.p, KF * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        scal(D.p, inrm, KF);
+      }
+      log(" eliash= %.15g\n", lam);
+      if (i_eig == 1 && lam > 0.0) break;
+      norm2 = nrm;
+    }
+    PGB_CUDA(cudaMemcpyAsync(D.p, nd.p, KF * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    scal(D.p, 1.0 / norm(D.p), KF);
+  }
+  g_stats.lambda = lam;
+  D.download(a.delta, KF);
+  sync();
+}
+
+void run_mkfk_soc(double2* fk, const double2* Gk, const double2* delta, const int64_t* invk, const SocSpin& sp,
+                  int64_t Nkall, int64_t Nk, int64_t Nw, int64_t Norb, int64_t gap_sym) {
+  Geom g;
+  g.Nk = (int)Nk;
+  g.Nw = (int)Nw;
+  g.Norb = (int)Norb;
+  spin_map(g, sp, Norb);
+  FullMesh fm;
+  full_mesh_from_invk(fm, invk, Nkall, Nk);
+  const long long KE = Nk * Nw * Norb * Norb, KF = Nkall * Nw * Norb * Norb;
+  DBuf<double2> G(KE), D(KF), F(KF);
+  G.upload(Gk, KE);
+  D.upload(delta, KF);
+  mkfk_soc(F.p, G.p, D.p, fm, g, (int)gap_sym);
+  F.download(fk, KF);
+  sync();
+}
+
+void run_orb_to_band_soc(double2* deltab, const double2* delta, const double2* uni, const int64_t* invk,
+                         const SocSpin& sp, int64_t Norb, int64_t Nkall, int64_t Nk, int64_t Nw) {
+  Geom g;
+  g.Nk = (int)Nk;
+  g.Nw = (int)Nw;
+  g.Norb = (int)Norb;
+  spin_map(g, sp, Norb);
+  FullMesh fm;
+  full_mesh_from_invk(fm, invk, Nkall, Nk);
+  const long long KF = Nkall * Nw * Norb * Norb, KU = Nk * Norb * Norb, KB = Nkall * Norb * Norb;
+  DBuf<double2> D(KF), U(KU), B(KB);
+  D.upload(delta, KF);
+  U.upload(uni, KU);
+  orb_to_band_soc(B.p, D.p, U.p, fm, g);
+  B.download(deltab, KB);
+  sync();
+}
+
+void run_chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const double2* chi, const double* Vmat,
+                       const int64_t* orb_list, const int64_t* olist, const int64_t* slist, int64_t Nk, int64_t Nw,
+                       int64_t Nchi, int64_t Norb) {
+  PGB_CHECK(Nchi % 4 == 0, "Nchi must be a multiple of 4 for the spin-orbit channels");
+  const long long K = Nk * Nw, KC = K * Nchi * Nchi;
+  std::vector<int> o1(Nchi), o2(Nchi), sl(Norb), ol(Nchi);
+  for (int64_t l = 0; l < Nchi; ++l) {
+    o1[l] = (int)olist[l] - 1;
+    o2[l] = (int)olist[Nchi + l] - 1;
+    PGB_CHECK(o1[l] >= 0 && o1[l] < Norb && o2[l] >= 0 && o2[l] < Norb, "olist entry outside [1,Norb]");
+    ol[l] = (int)orb_list[l];
+  }
+  for (int64_t a = 0; a < Norb; ++a) sl[a] = (int)slist[a];
+  DBuf<double2> X(KC);
+  DBuf<double> V((size_t)Nchi * Nchi);
+  X.upload(chi, KC);
+  V.upload(Vmat, (size_t)Nchi * Nchi);
+  chis_chic_soc(chic, chiszz, chispm, X.p, K, (int)Nk, (int)Nchi, V.p, o1, o2, sl, ol);
 }
 
 // The Eliashberg stage (final G, chi0, V_Delta, Arnoldi) runs in FP64 except

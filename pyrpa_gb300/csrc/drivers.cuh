@@ -95,6 +95,10 @@ struct Inputs {
   DBuf<double> S, C, eig;
   DBuf<double2> H, uni;
   int Norb = 1, Nchi = 1, Nk = 1, Nw = 1;
+  // spin-orbit runs: V and -V (Fortran order); the pairs and g.spin carry the
+  // spin partners (fselfwithsoc.f90)
+  bool soc = false;
+  DBuf<double> V, Vneg;
 };
 
 struct FlexParams {
@@ -146,6 +150,35 @@ void run_mkself(const MkselfArgs& a, int prec);
 template <typename R> void run_lin_eliash(const LinEliashArgs& a);
 void run_pipeline(const PipelineArgs& a, int prec);
 void run_nonlin_eliash(const NonlinArgs& a);
+
+// ---- spin-orbit coupling (fselfwithsoc.f90, fchi0withsoc.f90, feliashwithsoc.f90)
+struct SocSpin {
+  const int64_t *invs, *slist;     // (Norb) 1-based spin partner, +-1 spin label
+};
+// mkself_soc: the FLEX loop in FP64 with Vmat in place of Smat (Cmat unused)
+void run_mkself_soc(const MkselfArgs& a, const SocSpin& sp);
+// get_chi0_soc: bubble (Nk,Nw,Nchi,Nchi) and its Stoner factor max Re eig(-chi0 V)
+double run_chi0_soc(double2* chi_out, const double* Vmat, const double2* Gk, const int64_t* kmap,
+                    const int64_t* invk, const int64_t* olist, const SocSpin& sp, double temp, int64_t Nx, int64_t Ny,
+                    int64_t Nz, int64_t Nw, int64_t Nk, int64_t Nkall, int64_t Nchi, int64_t Norb);
+struct LinEliashSocArgs {
+  double2* delta;                  // out (Nkall,Nw,Norb,Norb)
+  double2* chi;                    // in (Nk,Nw,Nchi,Nchi); overwritten with V_Delta
+  const double2 *Gk, *uni;
+  const double *init_delta, *Vmat;
+  const int64_t *olist, *kmap, *invk, *invschi;
+  SocSpin sp;
+  double temp, eps;
+  int64_t Nkall, Nk, Nw, Nchi, Norb, Nx, Ny, Nz, itemax, gap_sym, arnoldi_m;
+};
+void run_lin_eliash_soc(const LinEliashSocArgs& a);
+void run_mkfk_soc(double2* fk, const double2* Gk, const double2* delta, const int64_t* invk, const SocSpin& sp,
+                  int64_t Nkall, int64_t Nk, int64_t Nw, int64_t Norb, int64_t gap_sym);
+void run_orb_to_band_soc(double2* deltab, const double2* delta, const double2* uni, const int64_t* invk,
+                         const SocSpin& sp, int64_t Norb, int64_t Nkall, int64_t Nk, int64_t Nw);
+void run_chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const double2* chi, const double* Vmat,
+                       const int64_t* orb_list, const int64_t* olist, const int64_t* slist, int64_t Nk, int64_t Nw,
+                       int64_t Nchi, int64_t Norb);
 // chi0_S / chi0_C of G and F (vertex: V_sigma / V_Delta instead), host arrays
 void nonlin_bubbles(double2* xs_out, double2* xc_out, const double2* Gk, const double2* Fk, const double* Smat,
                     const double* Cmat, const int64_t* olist, const double* prt_host, const int64_t* kmap,

@@ -72,6 +72,11 @@ void build_geom(Geom& g, const int64_t* kmap, const int64_t* invk, int64_t Nx, i
   PGB_CHECK(Nchi <= kMaxChi, "Nchi above the engine limit of 32 orbital pairs");
   g.Nx = (int)Nx; g.Ny = (int)Ny; g.Nz = (int)Nz; g.Nw = (int)Nw; g.Nk = (int)Nk;
   g.Norb = (int)Norb; g.Nchi = (int)Nchi;
+  for (int a = 0; a < kMaxOrb; ++a) {
+    g.spin.inv[a] = a;
+    g.spin.sgn[a] = 1;
+  }
+  g.spin.on = 0;
   g.Nkall = Nx * Ny * Nz;
   g.M = 2 * Nw;
   g.P = g.Nkall * g.M;
@@ -183,6 +188,61 @@ void build_pairs(Pairs& p, const int64_t* olist, int Norb, int Nchi, const int32
     }
 }
 
+void build_pairs_soc(Pairs& p, Geom& g, const int64_t* olist, int Norb, int Nchi, const int64_t* invs,
+                     const int64_t* slist) {
+  PGB_CHECK(Norb <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  for (int a = 0; a < Norb; ++a) {
+    PGB_CHECK(invs[a] >= 1 && invs[a] <= Norb, "invs entry outside [1,Norb]");
+    PGB_CHECK(slist[a] == 1 || slist[a] == -1, "slist entries must be +1 or -1");
+    g.spin.inv[a] = (int)invs[a] - 1;
+    g.spin.sgn[a] = (int)slist[a];
+  }
+  for (int a = 0; a < Norb; ++a)
+    PGB_CHECK(g.spin.inv[g.spin.inv[a]] == a, "invs is not an involution");
+  g.spin.on = 1;
+  std::vector<int> o1(Nchi), o2(Nchi);
+  for (int l = 0; l < Nchi; ++l) {
+    o1[l] = (int)olist[l] - 1;
+    o2[l] = (int)olist[Nchi + l] - 1;
+    PGB_CHECK(o1[l] >= 0 && o1[l] < Norb && o2[l] >= 0 && o2[l] < Norb, "olist entry outside [1,Norb]");
+  }
+  // chi_1234 = sgn chi*_{-4,-3,-2,-1}: pair (m1,l1) maps to (m2,l2) with
+  // (o1 l1, o2 l1, o1 m1, o2 m1) = (inv o2 m2, inv o1 m2, inv o2 l2, inv o1 l2)
+  const int* inv = g.spin.inv;
+  std::vector<int32_t> cmap(2 * (size_t)Nchi * Nchi, 0);
+  const int nirr = Nchi * (Nchi + 1) / 2;
+  std::vector<int32_t> irr(2 * (size_t)nirr, 0);
+  std::vector<char> is_irr((size_t)Nchi * Nchi, 0);
+  for (int l1 = 0; l1 < Nchi; ++l1)
+    for (int m1 = 0; m1 < Nchi; ++m1) {
+      bool done = false;
+      for (int l2 = 0; l2 < Nchi && !done; ++l2)
+        for (int m2 = 0; m2 < Nchi; ++m2) {
+          if (o1[l1] == inv[o2[m2]] && o2[l1] == inv[o1[m2]] && o1[m1] == inv[o2[l2]] && o2[m1] == inv[o1[l2]]) {
+            cmap[m1 + (size_t)Nchi * l1] = m2 + 1;
+            cmap[m1 + (size_t)Nchi * (l1 + Nchi)] = l2 + 1;
+            if (!is_irr[m2 + (size_t)Nchi * l2]) is_irr[m1 + (size_t)Nchi * l1] = 1;
+            done = true;
+            break;
+          }
+        }
+    }
+  int it = 0;
+  for (int l1 = 0; l1 < Nchi; ++l1)
+    for (int m1 = 0; m1 < Nchi; ++m1)
+      if (is_irr[m1 + (size_t)Nchi * l1]) {
+        PGB_CHECK(it < nirr, "more irreducible spin-orbit pairs than Nchi(Nchi+1)/2");
+        irr[it] = l1 + 1;
+        irr[it + nirr] = m1 + 1;
+        ++it;
+      }
+  build_pairs(p, olist, Norb, Nchi, irr.data(), cmap.data());
+  for (auto& c : p.chi) {
+    const int sg = g.spin.sgn[o1[c.l]] * g.spin.sgn[o2[c.l]] * g.spin.sgn[o1[c.m]] * g.spin.sgn[o2[c.m]];
+    c.pneg = sg < 0 ? 1 : 0;
+  }
+}
+
 // =============================================================== green ==
 __global__ void k_green0(double2* G, const double* eig, const double2* uni, double mu, double temp,
                          int Nk, int Nw, int No) {
@@ -272,9 +332,12 @@ bool invert_blocks(double2* G, long long nmat, int Norb, long long stride_mat, l
 // (at -k: conj G_ab).
 template <typename R>
 __global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, const int* grid_irr,
-                            const int* grid_flag, long long Nkall, int Nk, int Nw, int No, long long P) {
+                            const int* grid_flag, long long Nkall, int Nk, int Nw, int No, long long P,
+                            SpinMap sm) {
   const int e = elems[blockIdx.y];
   const int a = e % No, b = e / No;
+  const int ia = sm.inv[a], ib = sm.inv[b];
+  const double sg = (double)(sm.sgn[a] * sm.sgn[b]);
   cx<R>* o = out + (long long)blockIdx.y * P;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -283,10 +346,10 @@ __global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, cons
     const int k = grid_irr[gi], fl = grid_flag[gi];
     double2 v;
     if (n < Nw) {
-      v = fl ? G[fidx(k, n, b, a, Nk, Nw, No)] : G[fidx(k, n, a, b, Nk, Nw, No)];
+      v = fl ? sg * G[fidx(k, n, ib, ia, Nk, Nw, No)] : G[fidx(k, n, a, b, Nk, Nw, No)];
     } else {
       const int j = 2 * Nw - 1 - n;
-      v = conj(fl ? G[fidx(k, j, a, b, Nk, Nw, No)] : G[fidx(k, j, b, a, Nk, Nw, No)]);
+      v = fl ? sg * conj(G[fidx(k, j, ia, ib, Nk, Nw, No)]) : conj(G[fidx(k, j, b, a, Nk, Nw, No)]);
     }
     o[idx] = cmk<R>((R)v.x, (R)v.y);
   }
@@ -359,7 +422,7 @@ void pad_green_all(const Geom& g, const double2* G, cx<R>* out) {
   d.upload(h.data(), No2);
   dim3 grid(grid_1d(g.P, 256, 4096), No2);
   k_pad_green<R><<<grid, 256, 0, ctx().stream>>>(out, G, d.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk,
-                                                  g.Nw, g.Norb, g.P);
+                                                  g.Nw, g.Norb, g.P, g.spin);
   count_launch("pad_green");
 }
 
@@ -375,6 +438,7 @@ struct ChiDev {
   double2 J;
   int dm, dl, dm2, dl2;
   double2 dJ;
+  int pneg;  // partner = -conj (spin-orbit exchange sign)
 };
 
 template <typename R>
@@ -424,11 +488,11 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
     const int k = (int)(idx % Nk), j = (int)(idx / Nk);
     cx<R> v = t[irr_grid[k] + Nkall * j];
     if (sawc) v += J * sawc[j];
-    if (pr.self) v = conj(v);
+    if (pr.self) v = pr.pneg ? -conj(v) : conj(v);
     if (abs_below(v.x, kThresh)) v.x = 0;
     if (abs_below(v.y, kThresh)) v.y = 0;
     chi[fidx(k, j, pr.m, pr.l, Nk, Nw, Nchi)] = v;
-    if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = conj(v);
+    if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = pr.pneg ? -conj(v) : conj(v);
     if (pr.has_d) {
       const long long M = 2LL * Nw;
       cx<R> d = conj(t[irr_grid[k] + Nkall * ((M - j) % M)]);
@@ -557,7 +621,7 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
   for (size_t i = 0; i < p.chi.size(); ++i) {
     const ChiPair& c = p.chi[i];
     hp[i] = ChiDev{c.m, c.l, c.m2, c.l2, c.e13, c.e42, c.self, 0, make_double2(0, 0), 0, 0, 0, 0,
-                   make_double2(0, 0)};
+                   make_double2(0, 0), c.pneg};
   }
   // swapped partners: the relation chi_ml(q,nu) = conj chi_lm(q,-nu) is exact
   // for any G, while the exchange relation is imposed (the partner is written
@@ -571,7 +635,7 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
     cls[hp[i].m2 + (size_t)Nchi * hp[i].l2] = (int)i;
   }
   std::vector<int> derived(hp.size(), -1);  // source transform of a derived class
-  if (chi0_swap_enabled()) {
+  if (chi0_swap_enabled() && !g.spin.on) {  // the derivation assumes unsigned partners
     for (size_t i = 0; i < hp.size(); ++i) {
       const ChiDev& c = hp[i];
       if (c.self || derived[i] >= 0 || c.has_d || c.l == c.m) continue;
@@ -853,6 +917,10 @@ void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc) {
   auto kc = [&](int k, int c) { return (long long)g.h_kmap[3 * (long long)g.h_full_of_grid[g.h_irr_grid[k]] + c]; };
   log("SDW%4lld%4lld%4lld%12.8f\n", kc(qs, 0), kc(qs, 1), kc(qs, 2), sdw);
   log("CDW%4lld%4lld%4lld%12.8f\n", kc(qc, 0), kc(qc, 1), kc(qc, 2), cdw);
+}
+void ckchi_print_soc(const Geom& g, double v, int q) {  // fchi0withsoc.f90:189-197
+  auto kc = [&](int c) { return (long long)g.h_kmap[3 * (long long)g.h_full_of_grid[g.h_irr_grid[q]] + c]; };
+  log("SDW/CDW%4lld%4lld%4lld%12.8f\n", kc(0), kc(1), kc(2), v);
 }
 
 // ================================================================ vertex ==
@@ -2032,11 +2100,15 @@ void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, cons
   DBuf<cx<R>> F((size_t)No2 * g.P);
   pad_green_all<R>(g, G, F.p);
   fft.forward<R>(F.p, No2, st);
-  std::vector<double> hS(Nchi * Nchi), hC(Nchi * Nchi);
+  // static slot of V_sigma: 1.5 S - 0.5 C, or S itself when C is null (the
+  // spin-orbit loop passes -V there, fselfwithsoc.f90:588)
+  std::vector<double> hS(Nchi * Nchi), hC(Nchi * Nchi, 0.0);
   PGB_CUDA(cudaMemcpyAsync(hS.data(), S, sizeof(double) * hS.size(), cudaMemcpyDeviceToHost, st));
-  PGB_CUDA(cudaMemcpyAsync(hC.data(), C, sizeof(double) * hC.size(), cudaMemcpyDeviceToHost, st));
+  if (C) PGB_CUDA(cudaMemcpyAsync(hC.data(), C, sizeof(double) * hC.size(), cudaMemcpyDeviceToHost, st));
   sync();
-  auto stat = [&](int m, int l) { return 1.5 * hS[m + Nchi * l] - 0.5 * hC[m + Nchi * l]; };
+  auto stat = [&](int m, int l) {
+    return C ? 1.5 * hS[m + Nchi * l] - 0.5 * hC[m + Nchi * l] : hS[m + Nchi * l];
+  };
   // groups: output e = a + No*b with a <= b, together with its transpose
   struct Group { int e, et; std::vector<MirrorTerm> terms; };
   std::vector<Group> groups;
@@ -2687,4 +2759,477 @@ template void sigma<dfl>(const Geom&, const Pairs&, const double2*, const cx<dfl
 template void widen<dfl>(double2*, const cx<dfl>*, long long);
 template void narrow<dfl>(cx<dfl>*, const double2*, long long);
 
+}  // namespace pgb
+
+// ================================================== spin-orbit coupling ==
+// fchi0withsoc.f90, fselfwithsoc.f90, feliashwithsoc.f90, fUJ.f90:367-399.
+// The chi0 and Sigma stages run through chi0 / sigma above with the spin map
+// of Geom; this section holds the parts that differ in kind: the RPA vertex
+// -V (I + chi0 V)^-1, the nu = 0 channel sums, and the Eliashberg pieces,
+// whose gap lives on the full k mesh in the reference's full-list order.
+namespace pgb {
+
+void build_full_mesh(FullMesh& fm, const Geom& g, const int64_t* invk) {
+  const long long n = g.Nkall;
+  std::vector<int> irr(n), flag(n), minus(n), grid(n, -1);
+  for (long long i = 0; i < n; ++i) {
+    irr[i] = (int)invk[3 * i] - 1;
+    flag[i] = (int)invk[3 * i + 1];
+    minus[i] = (int)invk[3 * i + 2] - 1;
+    PGB_CHECK(minus[i] >= 0 && minus[i] < n, "invk(3,:) outside [1,Nkall]");
+  }
+  for (long long gi = 0; gi < n; ++gi) grid[g.h_full_of_grid[gi]] = (int)gi;
+  fm.Nkall = n;
+  fm.irr.alloc(n);
+  fm.irr.upload(irr.data(), n);
+  fm.flag.alloc(n);
+  fm.flag.upload(flag.data(), n);
+  fm.minus.alloc(n);
+  fm.minus.upload(minus.data(), n);
+  fm.grid.alloc(n);
+  fm.grid.upload(grid.data(), n);
+  fm.full.alloc(n);
+  fm.full.upload(g.h_full_of_grid.data(), n);
+}
+
+namespace {
+// V_sigma / V_Delta = -V + V (I + X V)^-1 X V = -V (I + X V)^-1 per (q, iw),
+// in place; one warp per matrix, row i on lane i (fUJ.f90:367-399)
+template <int N, int W>
+__global__ void __launch_bounds__(32 * W) k_vertex_soc(double2* chi, long long K, const double* V) {
+  extern __shared__ __align__(16) unsigned char smv[];
+  double* sV = reinterpret_cast<double*>(smv);  // row-major V
+  double2* base = reinterpret_cast<double2*>(smv + ((N * N * sizeof(double) + 15) / 16) * 16);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double2* Ai = base + (size_t)w * N * N;
+  int* ints = reinterpret_cast<int*>(base + (size_t)W * N * N);
+  int* pv = ints + w * (N + 1);
+  int* mp = ints + W * (N + 1) + w * 32;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) sV[(e % N) * N + e / N] = V[e];
+  __syncthreads();
+  const int i = lane < N ? lane : 0;
+  for (long long q = (long long)blockIdx.x * W + w; q < K; q += (long long)gridDim.x * W) {
+    double2 x[N], a[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) x[j] = chi[q + K * (i + N * j)];
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(i == j ? 1.0 : 0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < N; ++c) s += sV[c * N + j] * x[c];
+      a[j] = s;
+    }
+    const bool ok = warp_inverse<double, N>(a, pv, mp);
+    if (lane < N)
+      for (int j = 0; j < N; ++j) Ai[i * N + j] = a[j];
+    __syncwarp();
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(0.0, 0.0);
+      for (int c = 0; c < N; ++c) s += sV[i * N + c] * Ai[c * N + j];
+      if (lane < N) chi[q + K * (i + N * j)] = -s;
+    }
+    __syncwarp();
+    if (!ok && lane == 0) atomicExch(&g_err_dev, 6);
+  }
+}
+
+// Y = (I + chi0(q,0) V)^-1 chi0(q,0) per irreducible q (fchi0withsoc.f90:297-304)
+template <int N, int W>
+__global__ void __launch_bounds__(32 * W) k_rpa0_soc(double2* Y, const double2* chi, int Nk, long long K,
+                                                     const double* V) {
+  extern __shared__ __align__(16) unsigned char smr[];
+  double* sV = reinterpret_cast<double*>(smr);
+  int* ints = reinterpret_cast<int*>(smr + ((N * N * sizeof(double) + 15) / 16) * 16);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* pv = ints + w * (N + 1);
+  int* mp = ints + W * (N + 1) + w * 32;
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) sV[(e % N) * N + e / N] = V[e];
+  __syncthreads();
+  const int i = lane < N ? lane : 0;
+  for (int q = blockIdx.x * W + w; q < Nk; q += gridDim.x * W) {
+    double2 x[N], a[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) x[j] = chi[q + K * (i + N * j)];
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(i == j ? 1.0 : 0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < N; ++c) s += sV[c * N + j] * x[c];
+      a[j] = s;
+    }
+    const bool ok = warp_inverse<double, N>(a, pv, mp);
+    for (int j = 0; j < N; ++j) {
+      double2 s = mkc(0.0, 0.0);
+      for (int c = 0; c < N; ++c) s += pick<double, N>(a, c) * chi[q + K * (c + N * j)];
+      if (lane < N) Y[q + (long long)Nk * (i + N * j)] = s;
+    }
+    if (!ok && lane == 0) atomicExch(&g_err_dev, 7);
+  }
+}
+
+struct ChanTerm {
+  int m, l;
+  double coef;
+};
+// out[c][q] = sum of coef * Y(q, m, l) over the terms of output cell c
+__global__ void k_chan_sum(double2* out, const double2* Y, const int* start, const ChanTerm* terms, int Nk, int ncell,
+                           int N) {
+  const long long n = (long long)Nk * ncell;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(idx % Nk), c = (int)(idx / Nk);
+    double2 s = mkc(0.0, 0.0);
+    for (int t = start[c]; t < start[c + 1]; ++t) s += terms[t].coef * Y[q + (long long)Nk * (terms[t].m + N * terms[t].l)];
+    out[idx] = s;
+  }
+}
+
+// F = -G(k) Delta(k) G(-k)^H on the full mesh, G(-k) from the spin-orbit TRS
+// partner, then the spin-block fills of feliashwithsoc.f90:466-516
+__global__ void k_mkfk_soc(double2* F, const double2* G, const double2* D, const int* irr, const int* flag,
+                           long long Nkall, int Nk, int Nw, int No, SpinMap sm, int gap_sym) {
+  const long long n = Nkall * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long i = idx % Nkall;
+    const int j = (int)(idx / Nkall);
+    const int k = irr[i], fl = flag[i];
+    auto g1 = [&](int a, int c) {  // G(k)_{ac}
+      return fl ? (double)(sm.sgn[a] * sm.sgn[c]) * G[fidx(k, j, sm.inv[c], sm.inv[a], Nk, Nw, No)]
+                : G[fidx(k, j, a, c, Nk, Nw, No)];
+    };
+    auto g2 = [&](int b, int c) {  // G(-k)_{bc}
+      return fl ? G[fidx(k, j, c, b, Nk, Nw, No)]
+                : (double)(sm.sgn[b] * sm.sgn[c]) * G[fidx(k, j, sm.inv[b], sm.inv[c], Nk, Nw, No)];
+    };
+    double2 Cm[kMaxOrb * kMaxOrb], Fm[kMaxOrb * kMaxOrb];
+    for (int a = 0; a < No; ++a)
+      for (int c = 0; c < No; ++c) {
+        double2 s = mkc(0.0, 0.0);
+        for (int e = 0; e < No; ++e) s += g1(a, e) * D[fidx(i, j, e, c, Nkall, Nw, No)];
+        Cm[a * kMaxOrb + c] = s;
+      }
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 s = mkc(0.0, 0.0);
+        for (int c = 0; c < No; ++c) s += Cm[a * kMaxOrb + c] * conj(g2(b, c));
+        Fm[a * kMaxOrb + b] = -s;
+      }
+    auto f = [&](int a, int b) -> double2& { return Fm[a * kMaxOrb + b]; };
+    for (int l = 0; l < No; ++l) {
+      if (sm.sgn[l] != 1) continue;
+      for (int m = 0; m < No; ++m) {
+        if (sm.sgn[m] == 1) {
+          if (gap_sym < 0) {
+            f(sm.inv[l], sm.inv[m]) = -conj(f(m, l));
+          } else {
+            f(m, l) = mkc(0.0, 0.0);
+            f(sm.inv[l], sm.inv[m]) = mkc(0.0, 0.0);
+          }
+        } else if (sm.inv[m] == l) {
+          f(sm.inv[l], sm.inv[m]) = mkc(f(m, l).x, 0.0);
+        }
+      }
+    }
+    if (gap_sym != -10)
+      for (int l = 0; l < No; ++l) {
+        if (sm.sgn[l] != 1) continue;
+        for (int m = 0; m < No; ++m)
+          if (sm.sgn[m] == -1) f(sm.inv[m], sm.inv[l]) = gap_sym < 0 ? f(m, l) : -f(m, l);
+      }
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) F[fidx(i, j, a, b, Nkall, Nw, No)] = Fm[a * kMaxOrb + b];
+  }
+}
+
+// padded full-mesh F element (a, b): slot j = F(k, iw_j), slot 2Nw-1-j = -F_ba(-k, iw_j)
+// (feliashwithsoc.f90:594-601)
+__global__ void k_pad_ffull(double2* out, const double2* F, const int* full_of_grid, const int* minus,
+                            long long Nkall, int Nw, int No, long long P) {
+  const int e = blockIdx.y, a = e % No, b = e / No;
+  double2* o = out + (long long)e * P;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)(idx / Nkall);
+    const int i = full_of_grid[gi];
+    o[idx] = n < Nw ? F[fidx(i, n, a, b, Nkall, Nw, No)] : -F[fidx(minus[i], 2 * Nw - 1 - n, b, a, Nkall, Nw, No)];
+  }
+}
+
+struct SocBoson {
+  int m, l, ism, isl;
+  double stat, sg2;
+};
+// pairing-vertex pad of mkdelta_soc: at -q the spin-flipped pair times
+// sgnsig2(m,l); slot Nw = -V(m,l) (feliashwithsoc.f90:548-574)
+__global__ void k_pad_boson_socd(double2* out, const double2* V, const SocBoson* terms, const int* grid_irr,
+                                 const int* grid_flag, long long Nkall, int Nk, int Nw, int Nchi, long long P) {
+  const SocBoson t = terms[blockIdx.y];
+  double2* o = out + (long long)blockIdx.y * P;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long gi = idx % Nkall;
+    const int n = (int)(idx / Nkall);
+    const int k = grid_irr[gi], fl = grid_flag[gi];
+    double2 v;
+    if (n == Nw) {
+      v = mkc(t.stat, 0.0);
+    } else if (n < Nw) {
+      v = fl ? t.sg2 * V[fidx(k, n, t.isl, t.ism, Nk, Nw, Nchi)] : V[fidx(k, n, t.m, t.l, Nk, Nw, Nchi)];
+    } else {
+      const int j = 2 * Nw - n;
+      v = fl ? t.sg2 * conj(V[fidx(k, j, t.ism, t.isl, Nk, Nw, Nchi)]) : conj(V[fidx(k, j, t.l, t.m, Nk, Nw, Nchi)]);
+    }
+    o[idx] = v;
+  }
+}
+
+// T = sum_t W_t * FP_{ef_t}
+__global__ void k_prodsum(double2* T, const double2* W, const double2* FP, const int* ef, int nt, long long P) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double2 s = mkc(0.0, 0.0);
+    for (int t = 0; t < nt; ++t) s += W[(long long)t * P + idx] * FP[(long long)ef[t] * P + idx];
+    T[idx] = s;
+  }
+}
+
+// D(i, j) = scale * T(cell of i, j), every full k
+__global__ void k_scatter_full(double2* D, const double2* T, const int* grid_of_full, long long Nkall, int Nw,
+                               double scale) {
+  const long long n = Nkall * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long i = idx % Nkall, j = idx / Nkall;
+    D[idx] = scale * T[grid_of_full[i] + Nkall * j];
+  }
+}
+
+// spin-block fills of mkdelta_soc (feliashwithsoc.f90:622-662), per (k, iw)
+__global__ void k_sym_delta_soc(double2* D, long long Nkall, int Nw, int No, SpinMap sm, int gap_sym) {
+  const long long n = Nkall * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const long long i = idx % Nkall;
+    const int j = (int)(idx / Nkall);
+    auto d = [&](int a, int b) -> double2& { return D[fidx(i, j, a, b, Nkall, Nw, No)]; };
+    for (int l = 0; l < No; ++l) {
+      if (sm.sgn[l] != 1) continue;
+      for (int m = 0; m < No; ++m) {
+        if (sm.sgn[m] == 1) d(sm.inv[l], sm.inv[m]) = -conj(d(m, l));
+        else if (sm.inv[m] == l) d(l, m) = mkc(d(l, m).x, 0.0);
+        else if (l > sm.inv[m]) d(sm.inv[m], sm.inv[l]) = conj(d(l, m));
+      }
+    }
+    if (gap_sym == -10) continue;
+    for (int l = 0; l < No; ++l) {
+      if (sm.sgn[l] != 1) continue;
+      for (int m = 0; m < No; ++m)
+        if (sm.sgn[m] == -1) d(sm.inv[l], sm.inv[m]) = gap_sym > 0 ? -d(l, m) : d(l, m);
+    }
+  }
+}
+
+// band gap phi_n(k) to the orbital basis on the full mesh (feliashwithsoc.f90:690-725)
+__global__ void k_init_delta_soc(double2* D, const double* init, const double2* uni, const int* irr, const int* flag,
+                                 long long Nkall, int Nk, int Nw, int No, SpinMap sm, int gap_sym) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nkall;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = irr[i], fl = flag[i];
+    auto U = [&](int a, int n) { return uni[a + (long long)No * (n + (long long)No * k)]; };
+    for (int a = 0; a < No; ++a)
+      for (int b = 0; b < No; ++b) {
+        double2 s = mkc(0.0, 0.0);
+        for (int n = 0; n < No; ++n) {
+          const double ph = init[k + (long long)Nk * n];
+          if (fl == 0) s += (ph * (double)sm.sgn[b]) * (U(a, n) * conj(U(sm.inv[b], n)));
+          else s += (ph * (double)sm.sgn[a]) * (conj(U(sm.inv[a], n)) * U(b, n));
+        }
+        if (fl == 0) s = -s;
+        if (gap_sym > 0 && sm.sgn[a] * sm.sgn[b] >= 0) s = mkc(0.0, 0.0);
+        for (int j = 0; j < Nw; ++j) D[fidx(i, j, a, b, Nkall, Nw, No)] = s;
+      }
+  }
+}
+
+// orbital gap at the first frequency to the band basis (feliashwithsoc.f90:750-794)
+__global__ void k_orb_to_band_soc(double2* out, const double2* D, const double2* uni, const int* irr,
+                                  const int* flag, long long Nkall, int Nw, int No, SpinMap sm) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nkall;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int k = irr[i], fl = flag[i];
+    auto U = [&](int a, int n) { return uni[a + (long long)No * (n + (long long)No * k)]; };
+    for (int x = 0; x < No; ++x)
+      for (int y = 0; y < No; ++y) {
+        double2 s = mkc(0.0, 0.0);
+        for (int a = 0; a < No; ++a)
+          for (int b = 0; b < No; ++b) {
+            const double2 d = D[fidx(i, 0, a, b, Nkall, Nw, No)];
+            if (fl == 0) s += (double)sm.sgn[b] * (conj(U(a, x)) * d * U(sm.inv[b], y));
+            else s += (double)(-sm.sgn[a]) * (U(sm.inv[a], x) * d * conj(U(b, y)));
+          }
+        out[i + Nkall * (x + (long long)No * y)] = (fl == 0 || fl == 1) ? s : mkc(0.0, 0.0);
+      }
+  }
+}
+}  // namespace
+
+bool vertex_soc(double2* chi, long long K, int Nchi, const double* V) {
+  constexpr int W = 4;
+  auto launch = [&](auto kernel, int n) {
+    const size_t smem = ((size_t)n * n * sizeof(double) + 15) / 16 * 16 + (size_t)W * n * n * sizeof(double2) +
+                        sizeof(int) * (W * (n + 1) + W * 32);
+    PGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long blocks = std::min<long long>((K + W - 1) / W, (long long)ctx().num_sms * 16);
+    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(chi, K, V);
+  };
+  reset_err();
+  switch (Nchi) {
+    case 4: launch(k_vertex_soc<4, W>, 4); break;
+    case 16: launch(k_vertex_soc<16, W>, 16); break;
+    default: throw Error("the spin-orbit vertex supports Nchi = 4 or 16 (2 or 4 spin-orbitals)");
+  }
+  count_launch("vertex_soc");
+  return fetch_err() == 0;
+}
+
+void chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const double2* chi, long long K, int Nk, int Nchi,
+                   const double* V, const std::vector<int>& o1, const std::vector<int>& o2,
+                   const std::vector<int>& slist, const std::vector<int>& orb_list) {
+  constexpr int W = 4;
+  const int n4 = Nchi / 4;
+  DBuf<double2> Y((size_t)Nk * Nchi * Nchi);
+  auto launch = [&](auto kernel, int n) {
+    const size_t smem = ((size_t)n * n * sizeof(double) + 15) / 16 * 16 + sizeof(int) * (W * (n + 1) + W * 32);
+    const long long blocks = std::min<long long>((Nk + W - 1) / W, (long long)ctx().num_sms * 16);
+    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(Y.p, chi, Nk, K, V);
+  };
+  reset_err();
+  switch (Nchi) {
+    case 4: launch(k_rpa0_soc<4, W>, 4); break;
+    case 16: launch(k_rpa0_soc<16, W>, 16); break;
+    default: throw Error("get_chis_chic_soc supports Nchi = 4 or 16 (2 or 4 spin-orbitals)");
+  }
+  count_launch("rpa0_soc");
+  PGB_CHECK(fetch_err() == 0, "zgesv failed in get_chis_chic_soc");
+  // output cells: channel c (0 chic, 1 chiszz, 2 chispm) x (r, s); the reference
+  // accumulates cmat2(m,l) into cell (orb_list(l), orb_list(m)) by spin labels
+  const int ncell = 3 * n4 * n4;
+  std::vector<std::vector<ChanTerm>> cell(ncell);
+  auto s = [&](int a) { return slist[a]; };
+  for (int l = 0; l < Nchi; ++l)
+    for (int m = 0; m < Nchi; ++m) {
+      const int r = orb_list[l] - 1, c = orb_list[m] - 1;
+      PGB_CHECK(r >= 0 && r < n4 && c >= 0 && c < n4, "orb_list entry outside [1,Nchi/4]");
+      const int rc = r + n4 * c;
+      if (s(o1[l]) == s(o1[m]) && s(o2[l]) == s(o2[m]) && s(o1[l]) == -s(o2[l]) && s(o1[l]) == 1)
+        cell[2 * n4 * n4 + rc].push_back({m, l, 1.0});
+      if (s(o1[l]) == s(o2[l]) && s(o1[m]) == s(o2[m])) {
+        cell[rc].push_back({m, l, 0.5});
+        cell[n4 * n4 + rc].push_back({m, l, s(o1[l]) == s(o1[m]) ? 0.25 : -0.25});
+      }
+    }
+  std::vector<int> start(ncell + 1, 0);
+  std::vector<ChanTerm> flat;
+  for (int c = 0; c < ncell; ++c) {
+    start[c] = (int)flat.size();
+    flat.insert(flat.end(), cell[c].begin(), cell[c].end());
+  }
+  start[ncell] = (int)flat.size();
+  DBuf<int> dstart(ncell + 1);
+  dstart.upload(start.data(), ncell + 1);
+  DBuf<ChanTerm> dterms(std::max<size_t>(1, flat.size()));
+  if (!flat.empty()) dterms.upload(flat.data(), flat.size());
+  DBuf<double2> out((size_t)Nk * ncell);
+  k_chan_sum<<<grid_1d((long long)Nk * ncell, 256, 65536), 256, 0, ctx().stream>>>(out.p, Y.p, dstart.p, dterms.p,
+                                                                                   Nk, ncell, Nchi);
+  count_launch("chan_sum");
+  const size_t cs = (size_t)Nk * n4 * n4;
+  out.download(chic, cs);
+  PGB_CUDA(cudaMemcpyAsync(chiszz, out.p + cs, cs * sizeof(double2), cudaMemcpyDeviceToHost, ctx().stream));
+  PGB_CUDA(cudaMemcpyAsync(chispm, out.p + 2 * cs, cs * sizeof(double2), cudaMemcpyDeviceToHost, ctx().stream));
+  sync();
+}
+
+void mkfk_soc(double2* F, const double2* G, const double2* D, const FullMesh& fm, const Geom& g, int gap_sym) {
+  const long long n = fm.Nkall * g.Nw;
+  k_mkfk_soc<<<grid_1d(n, 128, 65536), 128, 0, ctx().stream>>>(F, G, D, fm.irr.p, fm.flag.p, fm.Nkall, g.Nk, g.Nw,
+                                                               g.Norb, g.spin, gap_sym);
+  count_launch("mkfk_soc");
+}
+
+void mkdelta_soc(const Geom& g, const Pairs& p, const FullMesh& fm, const double2* F, const double2* Vd,
+                 const std::vector<double>& Vmat, const std::vector<int>& invschi, int gap_sym, double scale,
+                 double2* out) {
+  cudaStream_t st = ctx().stream;
+  const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, (int)g.M, (int)sizeof(double2));
+  const int No = g.Norb, No2 = No * No, Nchi = g.Nchi;
+  const long long KF = fm.Nkall * g.Nw;
+  const int* s = g.spin.sgn;
+  const int* inv = g.spin.inv;
+  // terms grouped by output element (o1 l, o2 m) (feliashwithsoc.f90:538-545)
+  std::vector<std::vector<std::pair<SocBoson, int>>> groups(No2);
+  for (int l = 0; l < Nchi; ++l)
+    for (int m = 0; m < Nchi; ++m) {
+      const int o1l = p.o1[l], o2l = p.o2[l], o1m = p.o1[m], o2m = p.o2[m];
+      const bool mixed = s[o1l] * s[o2m] < 0;
+      if (!(gap_sym < 0 || (gap_sym > 0 && mixed))) continue;
+      if (!((gap_sym == -10 && mixed) || s[o1l] == 1)) continue;
+      if (!(s[o2m] == 1 || o1l >= inv[o2m])) continue;
+      const double sg2 = (double)(s[o1m] * s[o2m] * s[o1l] * s[o2l]);
+      PGB_CHECK(invschi[l] >= 1 && invschi[m] >= 1 && invschi[l] <= Nchi && invschi[m] <= Nchi,
+                "invschi entry outside [1,Nchi] (olist lacks a spin-flipped pair)");
+      SocBoson t{m, l, invschi[m] - 1, invschi[l] - 1, -Vmat[m + (size_t)Nchi * l], sg2};
+      groups[o1l + No * o2m].push_back({t, o2l + No * o1m});
+    }
+  DBuf<double2> FP((size_t)No2 * g.P);
+  dim3 gp(grid_1d(g.P, 256, 4096), No2);
+  k_pad_ffull<<<gp, 256, 0, st>>>(FP.p, F, fm.full.p, fm.minus.p, fm.Nkall, g.Nw, No, g.P);
+  count_launch("pad_ffull");
+  fft.forward<double>(FP.p, No2, st);
+  size_t maxt = 1;
+  for (auto& gr : groups) maxt = std::max(maxt, gr.size());
+  DBuf<double2> W(maxt * g.P), T(g.P);
+  DBuf<SocBoson> dt(maxt);
+  DBuf<int> def(maxt);
+  PGB_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)KF * No2, st));
+  for (int e = 0; e < No2; ++e) {
+    const int nt = (int)groups[e].size();
+    if (nt == 0) continue;
+    std::vector<SocBoson> ht(nt);
+    std::vector<int> hef(nt);
+    for (int t = 0; t < nt; ++t) {
+      ht[t] = groups[e][t].first;
+      hef[t] = groups[e][t].second;
+    }
+    dt.upload(ht.data(), nt);
+    def.upload(hef.data(), nt);
+    dim3 gw(grid_1d(g.P, 256, 4096), nt);
+    k_pad_boson_socd<<<gw, 256, 0, st>>>(W.p, Vd, dt.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, Nchi, g.P);
+    count_launch("pad_boson_socd");
+    fft.forward<double>(W.p, nt, st);
+    k_prodsum<<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(T.p, W.p, FP.p, def.p, nt, g.P);
+    count_launch("prodsum");
+    fft.backward<double>(T.p, 1, st);
+    k_scatter_full<<<grid_1d(KF, 256, 65536), 256, 0, st>>>(out + (size_t)e * KF, T.p, fm.grid.p, fm.Nkall, g.Nw,
+                                                            scale / (double)g.P);
+    count_launch("scatter_full");
+    sync();  // host term buffers are reused by the next element
+  }
+  k_sym_delta_soc<<<grid_1d(KF, 128, 65536), 128, 0, st>>>(out, fm.Nkall, g.Nw, No, g.spin, gap_sym);
+  count_launch("sym_delta_soc");
+}
+
+void initial_delta_soc(double2* D, const double* init, const double2* uni, const FullMesh& fm, const Geom& g,
+                       int gap_sym) {
+  k_init_delta_soc<<<grid_1d(fm.Nkall, 128, 65536), 128, 0, ctx().stream>>>(D, init, uni, fm.irr.p, fm.flag.p,
+                                                                             fm.Nkall, g.Nk, g.Nw, g.Norb, g.spin,
+                                                                             gap_sym);
+  count_launch("init_delta_soc");
+}
+
+void orb_to_band_soc(double2* out, const double2* D, const double2* uni, const FullMesh& fm, const Geom& g) {
+  k_orb_to_band_soc<<<grid_1d(fm.Nkall, 128, 65536), 128, 0, ctx().stream>>>(out, D, uni, fm.irr.p, fm.flag.p,
+                                                                              fm.Nkall, g.Nw, g.Norb, g.spin);
+  count_launch("orb_to_band_soc");
+}
 }  // namespace pgb

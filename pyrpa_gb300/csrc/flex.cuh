@@ -15,10 +15,21 @@
 
 #include "common.cuh"
 #include "fft.cuh"
+#include "linalg.cuh"
 
 namespace pgb {
 
+// Time-reversal partner of each orbital: G_ab(-k, iw) = sgn_a sgn_b G_{inv b, inv a}(k, iw).
+// Identity with sgn = +1 without spin-orbit coupling; with it, inv is the
+// spin partner and sgn the spin label (fchi0withsoc.f90:63-78).
+struct SpinMap {
+  int inv[kMaxOrb];
+  int sgn[kMaxOrb];
+  int on;
+};
+
 struct Geom {
+  SpinMap spin;
   int Nx = 1, Ny = 1, Nz = 1, Nw = 1, Nk = 1, Norb = 1, Nchi = 1;
   long long Nkall = 1, M = 2, P = 2, K = 1;
   std::vector<int> h_grid_irr, h_grid_flag, h_irr_grid;
@@ -39,6 +50,7 @@ struct ChiPair {
   int e13, e42;      // orbital elements a + Norb*b of G13 and G42
   int self;          // partner is the pair itself
   double2 J;         // tau=0 jump coefficient (tail reference only)
+  int pneg;          // the partner is -conj instead of conj (spin-orbit sign)
 };
 
 struct Term {  // one (m,l) term of a sigma / delta contraction
@@ -57,6 +69,10 @@ struct Pairs {
 // (get_chi0_conv_ passes them, 1-based, int32, Fortran layout).
 void build_pairs(Pairs& p, const int64_t* olist, int Norb, int Nchi, const int32_t* irr_chi = nullptr,
                  const int32_t* chi_map = nullptr);
+// spin-orbit variant: exchange map with spin flips (fchi0withsoc.f90:216-279),
+// partner signs sgnsig2, and the spin map of g
+void build_pairs_soc(Pairs& p, Geom& g, const int64_t* olist, int Norb, int Nchi, const int64_t* invs,
+                     const int64_t* slist);
 
 // ------------------------------------------------------------------ stages
 // All pointers are device pointers; R is the bulk (FFT/contraction) type.
@@ -157,9 +173,34 @@ bool vertex_sc(double2* XS, double2* XC, long long K, int Nchi, const double* S,
 
 // small host helpers
 void ckchi_print(const Geom& g, double sdw, double cdw, int qs, int qc);
+void ckchi_print_soc(const Geom& g, double v, int q);
 template <typename R> void widen(double2* out, const cx<R>* in, long long n);
 // out = in between any two bulk types (float, double, double-float)
 template <typename To, typename From> void convert(cx<To>* out, const cx<From>* in, long long n);
 template <typename R> void narrow(cx<R>* out, const double2* in, long long n);
 
+
+// ---------------------------------------------------- spin-orbit coupling --
+// Maps of the reference's full k list (kmap/invk order): irreducible index,
+// direct/TRS flag, index of -k, and mesh cell, per full index; full index per cell.
+struct FullMesh {
+  long long Nkall = 0;
+  DBuf<int> irr, flag, minus, grid, full;
+};
+void build_full_mesh(FullMesh& fm, const Geom& g, const int64_t* invk);
+// -V (I + chi0 V)^-1 in place on (K, Nchi, Nchi) matrices; false on a singular matrix
+bool vertex_soc(double2* chi, long long K, int Nchi, const double* V);
+// nu = 0 channel sums of get_chis_chic_soc into host arrays (Nk, Nchi/4, Nchi/4)
+void chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const double2* chi, long long K, int Nk, int Nchi,
+                   const double* V, const std::vector<int>& o1, const std::vector<int>& o2,
+                   const std::vector<int>& slist, const std::vector<int>& orb_list);
+// full-mesh anomalous Green function (mkfk_trs_soc)
+void mkfk_soc(double2* F, const double2* G, const double2* D, const FullMesh& fm, const Geom& g, int gap_sym);
+// out = scale * mkdelta_soc(F) on the full mesh (V_Delta in Vd, Vmat host Fortran order)
+void mkdelta_soc(const Geom& g, const Pairs& p, const FullMesh& fm, const double2* F, const double2* Vd,
+                 const std::vector<double>& Vmat, const std::vector<int>& invschi, int gap_sym, double scale,
+                 double2* out);
+void initial_delta_soc(double2* D, const double* init, const double2* uni, const FullMesh& fm, const Geom& g,
+                       int gap_sym);
+void orb_to_band_soc(double2* out, const double2* D, const double2* uni, const FullMesh& fm, const Geom& g);
 }  // namespace pgb

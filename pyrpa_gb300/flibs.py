@@ -59,6 +59,16 @@ _SIGNATURES = {
     "pyrpa_gb_chi0sc": [_c128, _c128, _c128, _c128, _f64, _f64, _i64, _f64, _i64, _i64, _pd] + [_pi] * 10,
     "pyrpa_gb_sc_dyson": [_c128, _c128, _c128, _c128, _pi, _pi, _pi],
     "mkfk_trs_nsoc_": [_c128, _c128, _c128, _pi, _pi, _pi],
+    "get_vmat_soc": [_f64, _i64, _i64, _i64, _i64, _pd, _pd, _pi, _pi],
+    "get_vmat_soc_orb": [_f64, _i64, _i64, _i64, _i64, _f64, _f64, _pi, _pi],
+    "mkself_soc": [_c128, _pd, _f64, _i64, _i64, _i64, _i64, _i64, _c128, _f64, _c128, _pd, _pd, _pd, _pi, _pd, _pd]
+    + [_pi] * 9 + [_pb, _pb, _pi, _pb, _pd],
+    "get_chi0_soc": [_c128, _f64, _f64, _i64, _f64, _c128, _i64, _i64, _i64, _i64, _i64, _pd] + [_pi] * 8,
+    "get_chis_chic_soc": [_c128, _c128, _c128, _c128, _f64, _i64, _i64, _i64, _i64] + [_pi] * 4,
+    "lin_eliash_soc": [_c128, _c128, _c128, _c128, _f64, _f64, _f64, _f64, _f64, _i64, _i64, _i64, _i64, _i64,
+                       _i64, _pd, _pd] + [_pi] * 11,
+    "mkfk_trs_soc_": [_c128, _c128, _c128, _f64, _i64, _i64, _i64] + [_pi] * 5,
+    "conv_delta_orb_to_band_soc": [_c128, _c128, _c128, _i64, _i64, _i64] + [_pi] * 4,
     "get_initial_delta_": [_c128, _f64, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi],
     "remap_delta_": [_c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi],
     "conv_delta_orb_to_band": [_c128, _c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi],
@@ -596,3 +606,125 @@ def flex_eliash(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, init_delta, plist
           i64(itemax), dbl(eps_eliash), np.asarray(coarse, dtype=np.int64))
     return dict(sigmak=sigmak, mu=mu_o.value, gap=gap, lam=lam.value, stoner=st.value,
                 h2d_ms=times[0], compute_ms=times[1], d2h_ms=times[2])
+
+
+# ------------------------------------------------------------- spin-orbit
+# Mirrors of the reference's spin-orbit wrappers (libs/flibs/_interaction.py:
+# gen_Vmatrix(_orb); _susceptibility.py: get_chi0_soc, get_chis_chic_soc;
+# _selfenergy.py: mkself_soc; _eliashberg.py: linearized_eliashberg_soc,
+# conv_delta_orb_to_band_soc, gen_Fk_soc), same arguments and layouts.
+def gen_Vmatrix(olist, slist, site, invs, U: float, J: float):
+    Nchi, Norb = len(olist), len(slist)
+    Vmat = np.zeros((Nchi, Nchi), dtype=np.float64)
+    _call("get_vmat_soc", Vmat, olist, np.asarray(slist, dtype=np.int64), np.asarray(site, dtype=np.int64),
+          np.asarray(invs, dtype=np.int64), dbl(U), dbl(J), i64(Nchi), i64(Norb))
+    return Vmat
+
+
+def gen_Vmatrix_orb(olist, slist, site, invs, Umat, Jmat):
+    Nchi, Norb = len(olist), len(Umat)
+    Vmat = np.zeros((Nchi, Nchi), dtype=np.float64)
+    _call("get_vmat_soc_orb", Vmat, olist, np.asarray(slist, dtype=np.int64), np.asarray(site, dtype=np.int64),
+          np.asarray(invs, dtype=np.int64), np.ascontiguousarray(Umat, dtype=np.float64),
+          np.ascontiguousarray(Jmat, dtype=np.float64), i64(Nchi), i64(Norb))
+    return Vmat
+
+
+def get_chi0_soc(Vmat, Gk, olist, slist, kmap, invk, invs, temp: float, Nx: int, Ny: int, Nz: int):
+    """(chi, sgnsig, sgnsig2, invschi) (libs/flibs/_susceptibility.py:496-528)."""
+    Norb, Nchi = len(slist), len(olist)
+    Nkall, Nk, Nw = len(kmap), Gk.shape[3], Gk.shape[2]
+    chi = np.zeros((Nchi, Nchi, Nw, Nk), dtype=np.complex128)
+    sgnsig = np.zeros((Norb, Norb), dtype=np.float64)
+    sgnsig2 = np.zeros((Nchi, Nchi), dtype=np.float64)
+    invschi = np.zeros(Nchi, dtype=np.int64)
+    _call("get_chi0_soc", chi, sgnsig, sgnsig2, invschi, np.ascontiguousarray(Vmat, dtype=np.float64),
+          np.ascontiguousarray(Gk), kmap, invk, np.asarray(invs, dtype=np.int64), olist,
+          np.asarray(slist, dtype=np.int64), dbl(temp), i64(Nx), i64(Ny), i64(Nz), i64(Nw), i64(Nk), i64(Nkall),
+          i64(Nchi), i64(Norb))
+    return chi, sgnsig, sgnsig2, invschi
+
+
+def get_chis_chic_soc(chi, Vmat, olist, slist, invs):
+    """(chic, chiszz, chispm) (libs/flibs/_susceptibility.py:530-566)."""
+    slist = np.asarray(slist, dtype=np.int64)
+    invs = np.asarray(invs, dtype=np.int64)
+    Norb, Nchi = len(slist), len(olist)
+    Nk, Nw = chi.shape[3], chi.shape[2]
+    orbs = np.where(slist == 1)[0]
+    o1, o2 = np.meshgrid(orbs, orbs)
+    orb_chi = np.array([o1.flatten(), o2.flatten()]).T
+    orb_list = np.zeros(Nchi, dtype=np.int64)
+    for i, ol in enumerate(np.asarray(olist)):
+        a = (ol[0] if slist[ol[0] - 1] == 1 else invs[ol[0] - 1]) - 1
+        b = (ol[1] if slist[ol[1] - 1] == 1 else invs[ol[1] - 1]) - 1
+        for j, ob in enumerate(orb_chi):
+            if a == ob[0] and b == ob[1]:
+                orb_list[i] = j + 1
+                break
+    n4 = Nchi // 4
+    chic = np.zeros((n4, n4, Nk), dtype=np.complex128)
+    chiszz = np.zeros_like(chic)
+    chispm = np.zeros_like(chic)
+    _call("get_chis_chic_soc", chic, chiszz, chispm, np.ascontiguousarray(chi),
+          np.ascontiguousarray(Vmat, dtype=np.float64), orb_list, olist, slist, invs, i64(Nk), i64(Nw), i64(Nchi),
+          i64(Norb))
+    return chic, chiszz, chispm
+
+
+def mkself_soc(Vmat, kmap, invk, invs, olist, slist, hamk, eig, uni, mu: float, fill: float, temp: float, Nw: int,
+               Nx: int, Ny: int, Nz: int, sw_out: bool, sw_in: bool, sub_sigma: int = 1, scf_loop: int = 300,
+               eps: float = 1.0e-4, pp: float = 0.3, m_diis: int = 5, sw_rescale: bool = False,
+               sigma_scale: float = 1.0):
+    """FLEX with spin-orbit coupling (libs/flibs/_selfenergy.py:129-175)."""
+    Nkall, Nk, Nchi = len(kmap), len(hamk), len(Vmat)
+    Norb = hamk.shape[1]
+    mu_self = c_double(0.0)
+    sigmak = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("mkself_soc", sigmak, byref(mu_self), np.ascontiguousarray(Vmat, dtype=np.float64), kmap, invk,
+          np.asarray(invs, dtype=np.int64), olist, np.asarray(slist, dtype=np.int64), np.ascontiguousarray(hamk),
+          np.ascontiguousarray(eig), np.ascontiguousarray(uni), dbl(mu), dbl(fill), dbl(temp), i64(scf_loop),
+          dbl(pp), dbl(eps), i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(Nchi), i64(Nx), i64(Ny), i64(Nz),
+          i64(sub_sigma), byref(c_bool(bool(sw_out))), byref(c_bool(bool(sw_in))), i64(m_diis),
+          byref(c_bool(bool(sw_rescale))), dbl(sigma_scale))
+    return sigmak, mu_self.value
+
+
+def linearized_eliashberg_soc(chi, Gk, uni, init_delta, Vmat, sgnsig, sgnsig2, plist, slist, olist, kmap, invk,
+                              invs, invschi, Nx: int, Ny: int, Nz: int, temp: float, gap_sym: int, eps: float = 1.0e-4,
+                              itemax: int = 300, arnoldi_m: int = 10):
+    """Gap on the full mesh (libs/flibs/_eliashberg.py:183-222); chi is
+    overwritten with V_Delta.  The reference's argtypes list for this call has
+    27 entries for the 28 Fortran arguments (prt is missing), so its own wrapper
+    raises TypeError; this one passes the Fortran signature.  lambda is in
+    last_stats()["lambda"]."""
+    Norb, Nchi = len(slist), len(Vmat)
+    Nkall, Nk, Nw = len(kmap), Gk.shape[3], Gk.shape[2]
+    delta = np.zeros((Norb, Norb, Nw, Nkall), dtype=np.complex128)
+    _call("lin_eliash_soc", delta, chi, np.ascontiguousarray(Gk), np.ascontiguousarray(uni),
+          np.ascontiguousarray(init_delta, dtype=np.float64), np.ascontiguousarray(Vmat, dtype=np.float64),
+          np.ascontiguousarray(sgnsig, dtype=np.float64), np.ascontiguousarray(sgnsig2, dtype=np.float64),
+          np.ascontiguousarray(plist, dtype=np.float64), olist, np.asarray(slist, dtype=np.int64), kmap, invk,
+          np.asarray(invs, dtype=np.int64), np.asarray(invschi, dtype=np.int64), dbl(temp), dbl(eps), i64(Nkall),
+          i64(Nk), i64(Nw), i64(Nchi), i64(Norb), i64(Nx), i64(Ny), i64(Nz), i64(itemax), i64(gap_sym),
+          i64(arnoldi_m))
+    return delta
+
+
+def conv_delta_orb_to_band_soc(delta, uni, invk, invs, slist):
+    Nkall, Nk, Nw, Norb = len(invk), len(uni), delta.shape[2], len(delta)
+    deltab = np.zeros((Norb, Norb, Nkall), dtype=np.complex128)
+    _call("conv_delta_orb_to_band_soc", deltab, np.ascontiguousarray(delta), np.ascontiguousarray(uni), invk,
+          np.asarray(invs, dtype=np.int64), np.asarray(slist, dtype=np.int64), i64(Norb), i64(Nkall), i64(Nk),
+          i64(Nw))
+    return deltab
+
+
+def gen_Fk_soc(Gk, delta, invk, invs, slist, gap_sym: int):
+    Nkall, Nk, Nw, Norb = len(invk), Gk.shape[3], delta.shape[2], len(delta)
+    Fk = np.zeros((Norb, Norb, Nw, Nkall), dtype=np.complex128)
+    slist = np.asarray(slist, dtype=np.int64)
+    sgnsig = np.outer(slist, slist).astype(np.float64)
+    _call("mkfk_trs_soc_", Fk, np.ascontiguousarray(Gk), np.ascontiguousarray(delta), sgnsig, slist, invk,
+          np.asarray(invs, dtype=np.int64), i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(gap_sym))
+    return Fk

@@ -115,3 +115,21 @@ def test_soc_arnoldi_and_power_method_agree(gap_sym):
     _, lam_a, ra = O.linearized_eliashberg_soc(chi.copy(), *args, eps=1e-10, arnoldi_m=60, full=True)
     _, lam_p, rp = O.linearized_eliashberg_soc(chi.copy(), *args, eps=1e-9, itemax=3000, arnoldi_m=0, full=True)
     assert abs(lam_a - lam_p) < 1e-6 * max(1.0, abs(lam_a)), (lam_a, lam_p)
+
+
+def test_library_vmat_soc_matches_oracle():
+    """get_vmat_soc / get_vmat_soc_orb are host code in the library: no GPU needed."""
+    from pyrpa_gb300 import build, flibs
+    if not build.LIB.exists():
+        build.build()
+    flibs.load_library()
+    olist, site = O.get_chi_orb_list(4)
+    olist = np.asfortranarray(olist)
+    _, _, slist, invs = M.spin_orbit_hoppings(*M.two_orbital_hoppings())
+    a = flibs.gen_Vmatrix(olist, slist, site, invs, 1.3, 0.2)
+    assert np.array_equal(a, O.gen_Vmatrix(olist, slist, site, invs, 1.3, 0.2))
+    rng = np.random.default_rng(0)
+    Um = rng.uniform(0.5, 1.5, (4, 4))
+    Jm = rng.uniform(0.0, 0.3, (4, 4))
+    b = flibs.gen_Vmatrix_orb(olist, slist, site, invs, Um, Jm)
+    assert np.array_equal(b, O.gen_Vmatrix_orb(olist, slist, site, invs, Um, Jm))
