@@ -69,3 +69,19 @@ def test_reference_wrappers_compute_host_entry_points(ref_flibs):
             assert np.array_equal(x, y)
         rvec, ham_r = M.random_hoppings(Norb, Norb)
         assert np.array_equal(ref_flibs.get_plist(rvec, ham_r), F.get_plist(rvec, ham_r))
+
+
+def test_reference_soc_wrappers_against_the_library(ref_flibs):
+    """The reference's spin-orbit wrappers bind to this library; the host-side
+    vertex matches this package's mirror.  lin_eliash_soc's argtypes in the
+    reference list 27 entries for the 28 Fortran arguments (prt is missing),
+    which the C ABI follows (28); its own call therefore fails in ctypes."""
+    from pyrpa_gb300 import flibs as F
+    lib = importlib.import_module("libs.flibs._loader")._lib
+    olist, site = F.get_chi_orb_list(4)
+    _, _, slist, invs = M.spin_orbit_hoppings(*M.two_orbital_hoppings())
+    a = ref_flibs.gen_Vmatrix(olist, slist, site, invs, 1.3, 0.2)
+    assert np.array_equal(a, F.gen_Vmatrix(olist, slist, site, invs, 1.3, 0.2))
+    assert len(lib.lin_eliash_soc.argtypes) == 27
+    for name in ("mkself_soc", "get_chi0_soc", "get_chis_chic_soc", "mkfk_trs_soc_", "conv_delta_orb_to_band_soc"):
+        assert len(getattr(lib, name).argtypes) == len(F._SIGNATURES[name]), name
