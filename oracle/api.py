@@ -279,3 +279,65 @@ def conv_delta_orb_to_band_soc(delta, uni, invk, invs, slist):
 def gen_Fk_soc(Gk, delta, invk, invs, slist, gap_sym):
     F = SO.mkfk_trs_soc(Gk.T, delta.T, slist, np.asarray(invk), invs, gap_sym)
     return np.ascontiguousarray(F.T)
+
+
+# ------------------------------------------------------- real-frequency maps
+# Facades of libs/flibs/_susceptibility.py (get_chi_irr, chis_qmap, get_tr_chi,
+# get_phi_irr, phi_qmap, get_tr_phi), _hamiltonian.py (get_qshift,
+# get_iqshift) and _green.py (get_a, get_QP, pade_with_trace), wrapper layouts.
+from . import realfreq_oracle as RF  # noqa: E402
+
+
+def get_qshift(klist, qpoint):
+    return RF.get_qshift(qpoint, klist)
+
+
+def get_iqshift(klist, qpoint):
+    return RF.get_iqshift(qpoint, klist)
+
+
+def get_chi_irr(uni, eig, ffermi, qshift, olist, wlist, idelta, temp):
+    chi = RF.get_chi_irr(uni.transpose(0, 2, 1), eig, ffermi, qshift, np.asarray(olist), np.asarray(wlist),
+                         idelta, idelta * 1e-3, temp)
+    return np.ascontiguousarray(chi.T)
+
+
+def chis_qmap(uni, eig, ffermi, klist, Smat, olist, Nx, Ny, temp, ecut, idelta):
+    return RF.chiq_map(uni.transpose(0, 2, 1), eig, ffermi, np.asarray(klist), np.asarray(Smat).T,
+                       np.asarray(olist), temp, ecut, idelta, idelta * 1e-3, Nx, Ny)
+
+
+def get_tr_chi(chis, chi0, olist):
+    ol = np.asarray(olist)
+    trs, tr0, orb = RF.get_tr_chi(chis.T, chi0.T, ol, int(ol.max()))
+    return trs, tr0, np.ascontiguousarray(orb.T)
+
+
+def get_phi_irr(uni, eig, ffermi, qshift, olist, wlist, idelta, mu, temp):
+    phi = RF.get_phi_irr(uni.transpose(0, 2, 1), eig, ffermi, qshift, np.asarray(olist), np.asarray(wlist),
+                         idelta, idelta * 1e-3, mu, temp)
+    return np.ascontiguousarray(phi.T)
+
+
+def phi_qmap(uni, eig, ffermi, klist, olist, Nx, Ny, mu, temp, ecut, idelta, sw_omega):
+    return RF.phiq_map(uni.transpose(0, 2, 1), eig, ffermi, np.asarray(klist), np.asarray(olist), mu, temp, ecut,
+                       idelta, idelta * 1e-3, Nx, Ny, sw_omega)
+
+
+def get_tr_phi(phi, olist):
+    ol = np.asarray(olist)
+    tr, orb = RF.get_tr_phi(phi.T, ol, int(ol.max()))
+    return tr, np.ascontiguousarray(orb.T)
+
+
+def get_a(inp_data, xlist):
+    return RF.get_a(xlist, inp_data)
+
+
+def get_QP(a, xlist, wlist):
+    P, Q = RF.get_QP(a, xlist, wlist)
+    return Q, P  # the reference wrapper returns (Q, P)
+
+
+def pade_with_trace(A, iwlist, wlist):
+    return np.ascontiguousarray(RF.pade_with_trace(A.T, iwlist, wlist).T)
