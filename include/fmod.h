@@ -288,8 +288,45 @@ void conv_delta_orb_to_band_soc(double* deltab, const double* delta, const doubl
                                 const int64_t* invs, const int64_t* slist, const int64_t* Norb,
                                 const int64_t* Nkall, const int64_t* Nk, const int64_t* Nw);
 
-/* Symbols outside the accelerated path (transport, impurity, Eilenberger,
- * real-frequency maps, Pade ...) are exported with no
+/* ---- real-frequency maps and Pade (fchi.f90:1-318, fphi.f90:1-305, fpade.f90).
+ * Band data in the wrappers' layouts: uni (Norb,Norb,Nk), eig/ffermi (Norb,Nk),
+ * klist (3,Nk), all on the k list the maps sum over. */
+/* 1-based index of k+q (get_qshift_) / -k+q (get_iqshift_) on klist; a miss gives 1 */
+void get_qshift_(const double* qpoint, const double* klist, int64_t* qshift, const int64_t* Nk);
+void get_iqshift_(const double* qpoint, const double* klist, int64_t* qshift, const int64_t* Nk);
+/* chi0(q, w + i idelta) (Nchi,Nchi,Nw) of the band-basis Lindhard sum at one q */
+void get_chi_irr(double* chi, const double* uni, const double* eig, const double* ffermi, const int64_t* qshift,
+                 const int64_t* ol, const double* wl, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nk,
+                 const int64_t* Nw, const double* idelta, const double* eps, const double* temp);
+/* particle-particle analog phi0(q, w) (Nchi,Nchi,Nw) */
+void get_phi_irr(double* phi, const double* uni, const double* eig, const double* ffermi, const int64_t* qshift,
+                 const int64_t* ol, const double* wl, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nk,
+                 const int64_t* Nw, const double* idelta, const double* eps, const double* mu, const double* temp);
+/* (ll,mm) sums of chi_s = (I - chi0 S)^-1 chi0 and chi0 at w = ecut over q = (i/Nx, j/Ny, 0);
+ * trchis, trchi (Ny,Nx).  Nchi = 1, 4, 9, 16 or 25. */
+void chiq_map(double* trchis, double* trchi, const double* uni, const double* eig, const double* ffermi,
+              const double* klist, const double* Smat, const int64_t* ol, const double* temp, const double* ecut,
+              const double* idelta, const double* eps, const int64_t* Nx, const int64_t* Ny, const int64_t* Nk,
+              const int64_t* Norb, const int64_t* Nchi);
+/* trace of phi over q = (i/Nx, j/Ny, 0) (trphi (Ny,Nx)); w = ecut + i idelta if *sw_omega, else 0 */
+void phiq_map(double* trphi, const double* uni, const double* eig, const double* ffermi, const double* klist,
+              const int64_t* ol, const double* mu, const double* temp, const double* ecut, const double* idelta,
+              const double* eps, const int64_t* Nx, const int64_t* Ny, const int64_t* Nk, const int64_t* Norb,
+              const int64_t* Nchi, const bool* sw_omega);
+/* orbital traces per frequency (host code) */
+void get_tr_chi(double* trchis, double* trchi0, double* chis_orb, const double* chis, const double* chi0,
+                const int64_t* olist, const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb);
+void get_tr_phi(double* trphi, double* phi_orb, const double* phi, const int64_t* olist, const int64_t* Nw,
+                const int64_t* Nchi, const int64_t* Norb);
+/* continued-fraction coefficients and P_N, Q_N of one series (host code) */
+void get_a_(double* a, const double* xn, const double* inp_data, const int64_t* Np);
+void get_qp_(double* P, double* Q, const double* a, const double* xn, const double* wlist, const int64_t* Nw,
+             const int64_t* Np);
+/* arrayout (Nw,Nk) = sum over orbitals of the Pade continuation of arrayin(k,:,o,o) (Nk,Niw,Norb,Norb) */
+void pade_with_trace(const double* arrayin, double* arrayout, const double* iwlist, const double* wlist,
+                     const int64_t* Nk, const int64_t* Niw, const int64_t* Nw, const int64_t* Norb);
+
+/* Symbols outside the accelerated path (transport, impurity, Eilenberger ...) are exported with no
  * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"
  * so that `import libs.flibs` binds every name it expects. */
 

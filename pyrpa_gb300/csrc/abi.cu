@@ -908,6 +908,297 @@ void pyrpa_gb_sc_dyson(double2* Gk, double2* fk, const double2* G0, const double
                                   nan_fill(fk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb))))
 }
 
+// -------------------------------------------------------- real frequency --
+// k+q lookups (fchi.f90:1-93, fphi.f90:1-87): coordinates keyed at 2^-20 as
+// int(x*2^20 + 0.5) mod 2^20 (Fortran truncation and sign of the dividend); a
+// repeated key keeps the last index; a miss falls back to index 1.
+namespace {
+constexpr int64_t kKeyScale = 1048576;
+int64_t kkey(const double* x) {
+  int64_t k[3];
+  for (int c = 0; c < 3; ++c) {
+    const int64_t i = (int64_t)(x[c] * (double)kKeyScale + 0.5);  // truncation toward zero
+    k[c] = i % kKeyScale;                                            // C++ %: sign of the dividend
+  }
+  return k[0] + k[1] * kKeyScale + k[2] * kKeyScale * kKeyScale;
+}
+void kq_lookup(int64_t* out, const double* qpoint, const double* klist, int64_t Nk, bool minus_k) {
+  std::unordered_map<int64_t, int64_t> table;
+  table.reserve((size_t)Nk * 2);
+  for (int64_t j = 0; j < Nk; ++j) table[kkey(klist + 3 * j)] = j + 1;
+  int64_t nmiss = 0;
+  for (int64_t i = 0; i < Nk; ++i) {
+    double t[3];
+    for (int c = 0; c < 3; ++c) {
+      t[c] = (minus_k ? 1.0 - klist[3 * i + c] : klist[3 * i + c]) + qpoint[c];
+      if (t[c] >= 1.0) t[c] -= 1.0;
+      else if (t[c] < 0.0) t[c] += 1.0;
+    }
+    auto it = table.find(kkey(t));
+    if (it == table.end()) {
+      out[i] = 1;
+      ++nmiss;
+    } else {
+      out[i] = it->second;
+    }
+  }
+  if (nmiss > 0)
+    log("WARNING(get_%sqshift): %lld of %lld k+q points not found on the k-mesh.\n", minus_k ? "i" : "",
+        (long long)nmiss, (long long)Nk);
+}
+
+struct RfInputs {
+  DBuf<double2> uni;
+  DBuf<double> eig, ff;
+  std::vector<int> o1, o2;
+};
+void rf_upload(RfInputs& r, const double2* uni, const double* eig, const double* ffermi, const int64_t* ol,
+               int64_t Nchi, int64_t Norb, int64_t Nk) {
+  PGB_CHECK(Norb <= kMaxOrb && Nchi <= kMaxChi, "Norb or Nchi above the engine limits");
+  r.uni.alloc((size_t)Norb * Norb * Nk);
+  r.uni.upload(uni, (size_t)Norb * Norb * Nk);
+  r.eig.alloc((size_t)Norb * Nk);
+  r.eig.upload(eig, (size_t)Norb * Nk);
+  r.ff.alloc((size_t)Norb * Nk);
+  r.ff.upload(ffermi, (size_t)Norb * Nk);
+  r.o1.resize(Nchi);
+  r.o2.resize(Nchi);
+  for (int64_t l = 0; l < Nchi; ++l) {
+    r.o1[l] = (int)ol[l] - 1;
+    r.o2[l] = (int)ol[Nchi + l] - 1;
+    PGB_CHECK(r.o1[l] >= 0 && r.o1[l] < Norb && r.o2[l] >= 0 && r.o2[l] < Norb, "olist entry outside [1,Norb]");
+  }
+}
+std::vector<int> qshift_0based(const int64_t* qs, int64_t Nk) {
+  std::vector<int> out(Nk);
+  for (int64_t i = 0; i < Nk; ++i) {
+    PGB_CHECK(qs[i] >= 1 && qs[i] <= Nk, "qshift entry outside [1,Nk]");
+    out[i] = (int)qs[i] - 1;
+  }
+  return out;
+}
+void rf_irr(double2* out, const double2* uni, const double* eig, const double* ffermi, const int64_t* qshift,
+            const int64_t* ol, const double* wl, int64_t Nchi, int64_t Norb, int64_t Nk, int64_t Nw, double idelta,
+            double eps, double mu, double temp, bool phi) {
+  RfInputs r;
+  rf_upload(r, uni, eig, ffermi, ol, Nchi, Norb, Nk);
+  std::vector<int> qs = qshift_0based(qshift, Nk);
+  DBuf<int> dq(Nk);
+  dq.upload(qs.data(), Nk);
+  std::vector<RfJob> jobs(Nw);
+  for (int64_t w = 0; w < Nw; ++w) jobs[w] = RfJob{wl[w], idelta, 0};
+  DBuf<double2> d((size_t)Nchi * Nchi * Nw);
+  bubble_rf(d.p, r.uni.p, r.eig.p, r.ff.p, dq.p, jobs, r.o1, r.o2, (int)Nk, (int)Norb, (int)Nchi, mu, temp, eps, phi);
+  d.download(out, (size_t)Nchi * Nchi * Nw);
+  sync();
+}
+// q = ((i-1)/Nx, (j-1)/Ny, 0) in the reference's (i, j) order, job index i*Ny + j
+std::vector<int> map_qshifts(const double* klist, int64_t Nx, int64_t Ny, int64_t Nk, bool minus_k) {
+  std::vector<int> all((size_t)Nx * Ny * Nk);
+  std::vector<int64_t> one(Nk);
+  for (int64_t i = 0; i < Nx; ++i)
+    for (int64_t j = 0; j < Ny; ++j) {
+      const double q[3] = {(double)i / (double)Nx, (double)j / (double)Ny, 0.0};
+      kq_lookup(one.data(), q, klist, Nk, minus_k);
+      for (int64_t k = 0; k < Nk; ++k) all[(size_t)(i * Ny + j) * Nk + k] = (int)one[k] - 1;
+    }
+  return all;
+}
+}  // namespace
+
+void get_qshift_(const double* qpoint, const double* klist, int64_t* qshift, const int64_t* Nk) {
+  ABI_TRY
+  kq_lookup(qshift, qpoint, klist, *Nk, false);
+  ABI_CATCH("get_qshift_", (void)0)
+}
+
+void get_iqshift_(const double* qpoint, const double* klist, int64_t* qshift, const int64_t* Nk) {
+  ABI_TRY
+  kq_lookup(qshift, qpoint, klist, *Nk, true);
+  ABI_CATCH("get_iqshift_", (void)0)
+}
+
+void get_chi_irr(double2* chi, const double2* uni, const double* eig, const double* ffermi, const int64_t* qshift,
+                 const int64_t* ol, const double* wl, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nk,
+                 const int64_t* Nw, const double* idelta, const double* eps, const double* temp) {
+  ABI_TRY
+  ensure_context();
+  rf_irr(chi, uni, eig, ffermi, qshift, ol, wl, *Nchi, *Norb, *Nk, *Nw, *idelta, *eps, 0.0, *temp, false);
+  ABI_CATCH("get_chi_irr", nan_fill(chi, (size_t)(*Nchi) * (*Nchi) * (*Nw)))
+}
+
+void get_phi_irr(double2* phi, const double2* uni, const double* eig, const double* ffermi, const int64_t* qshift,
+                 const int64_t* ol, const double* wl, const int64_t* Nchi, const int64_t* Norb, const int64_t* Nk,
+                 const int64_t* Nw, const double* idelta, const double* eps, const double* mu, const double* temp) {
+  ABI_TRY
+  ensure_context();
+  rf_irr(phi, uni, eig, ffermi, qshift, ol, wl, *Nchi, *Norb, *Nk, *Nw, *idelta, *eps, *mu, *temp, true);
+  ABI_CATCH("get_phi_irr", nan_fill(phi, (size_t)(*Nchi) * (*Nchi) * (*Nw)))
+}
+
+void chiq_map(double2* trchis, double2* trchi, const double2* uni, const double* eig, const double* ffermi,
+              const double* klist, const double* Smat, const int64_t* ol, const double* temp, const double* ecut,
+              const double* idelta, const double* eps, const int64_t* Nx, const int64_t* Ny, const int64_t* Nk,
+              const int64_t* Norb, const int64_t* Nchi) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nq = (*Nx) * (*Ny), n = *Nchi;
+  RfInputs r;
+  rf_upload(r, uni, eig, ffermi, ol, n, *Norb, *Nk);
+  std::vector<int> qs = map_qshifts(klist, *Nx, *Ny, *Nk, false);
+  DBuf<int> dq(qs.size());
+  dq.upload(qs.data(), qs.size());
+  std::vector<RfJob> jobs(nq);
+  for (int64_t q = 0; q < nq; ++q) jobs[q] = RfJob{*ecut, *idelta, q * (*Nk)};
+  DBuf<double2> chi((size_t)n * n * nq), ts(nq), t0(nq);
+  bubble_rf(chi.p, r.uni.p, r.eig.p, r.ff.p, dq.p, jobs, r.o1, r.o2, (int)*Nk, (int)*Norb, (int)n, 0.0, *temp, *eps,
+            false);
+  std::vector<int> dmask(n);
+  for (int64_t l = 0; l < n; ++l) dmask[l] = r.o1[l] == r.o2[l] ? 1 : 0;
+  DBuf<int> dm(n);
+  dm.upload(dmask.data(), n);
+  DBuf<double> S((size_t)n * n);
+  S.upload(Smat, (size_t)n * n);
+  rpa_trace(ts.p, t0.p, chi.p, S.p, dm.p, (int)n, (int)nq);
+  ts.download(trchis, nq);  // trchis(Ny, Nx): element (j, i) at j + Ny i = job i*Ny + j
+  t0.download(trchi, nq);
+  sync();
+  ABI_CATCH("chiq_map", (nan_fill(trchis, (size_t)(*Nx) * (*Ny)), nan_fill(trchi, (size_t)(*Nx) * (*Ny))))
+}
+
+void phiq_map(double2* trphi, const double2* uni, const double* eig, const double* ffermi, const double* klist,
+              const int64_t* ol, const double* mu, const double* temp, const double* ecut, const double* idelta,
+              const double* eps, const int64_t* Nx, const int64_t* Ny, const int64_t* Nk, const int64_t* Norb,
+              const int64_t* Nchi, const bool* sw_omega) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nq = (*Nx) * (*Ny), n = *Nchi;
+  RfInputs r;
+  rf_upload(r, uni, eig, ffermi, ol, n, *Norb, *Nk);
+  std::vector<int> qs = map_qshifts(klist, *Nx, *Ny, *Nk, true);
+  DBuf<int> dq(qs.size());
+  dq.upload(qs.data(), qs.size());
+  const double wre = *sw_omega ? *ecut : 0.0, wim = *sw_omega ? *idelta : 0.0;
+  std::vector<RfJob> jobs(nq);
+  for (int64_t q = 0; q < nq; ++q) jobs[q] = RfJob{wre, wim, q * (*Nk)};
+  DBuf<double2> phi((size_t)n * n * nq), tr(nq);
+  bubble_rf(phi.p, r.uni.p, r.eig.p, r.ff.p, dq.p, jobs, r.o1, r.o2, (int)*Nk, (int)*Norb, (int)n, *mu, *temp, *eps,
+            true);
+  trace_jobs(tr.p, phi.p, (int)n, (int)nq);
+  tr.download(trphi, nq);
+  sync();
+  ABI_CATCH("phiq_map", nan_fill(trphi, (size_t)(*Nx) * (*Ny)))
+}
+
+// orbital traces of chi_s / chi_0 / phi per frequency (fchi.f90:160-196, fphi.f90:164-193)
+void get_tr_chi(double2* trchis, double2* trchi0, double2* chis_orb, const double2* chis, const double2* chi0,
+                const int64_t* olist, const int64_t* Nw, const int64_t* Nchi, const int64_t* Norb) {
+  ABI_TRY
+  const int64_t nw = *Nw, n = *Nchi, no = *Norb;
+  for (int64_t i = 0; i < nw; ++i) {
+    trchis[i] = mkc(0.0, 0.0);
+    trchi0[i] = mkc(0.0, 0.0);
+    for (int64_t o = 0; o < no + 2; ++o) chis_orb[o + (no + 2) * i] = mkc(0.0, 0.0);
+  }
+  for (int64_t i = 0; i < nw; ++i)
+    for (int64_t j = 0; j < n; ++j) {
+      if (olist[j] != olist[n + j]) continue;
+      for (int64_t k = 0; k < n; ++k) {
+        if (olist[k] != olist[n + k]) continue;
+        const double2 cs = chis[k + n * (j + n * i)];
+        trchis[i] += cs;
+        trchi0[i] += chi0[k + n * (j + n * i)];
+        if (olist[j] == olist[k]) {
+          PGB_CHECK(olist[j] >= 1 && olist[j] <= no, "olist entry outside [1,Norb]");
+          chis_orb[(olist[j] - 1) + (no + 2) * i] = cs;
+        }
+        if (olist[k] == 2 && olist[j] == 3) chis_orb[no + (no + 2) * i] = cs;
+        if (olist[k] == 2 && olist[j] == 4) chis_orb[no + 1 + (no + 2) * i] = cs;
+      }
+    }
+  ABI_CATCH("get_tr_chi", (void)0)
+}
+
+void get_tr_phi(double2* trphi, double2* phi_orb, const double2* phi, const int64_t* olist, const int64_t* Nw,
+                const int64_t* Nchi, const int64_t* Norb) {
+  ABI_TRY
+  const int64_t nw = *Nw, n = *Nchi, no = *Norb;
+  for (int64_t i = 0; i < nw; ++i) {
+    trphi[i] = mkc(0.0, 0.0);
+    for (int64_t o = 0; o < no + 2; ++o) phi_orb[o + (no + 2) * i] = mkc(0.0, 0.0);
+  }
+  for (int64_t i = 0; i < nw; ++i)
+    for (int64_t j = 0; j < n; ++j) {
+      trphi[i] += phi[j + n * (j + n * i)];
+      if (olist[j] != olist[n + j]) continue;
+      for (int64_t k = 0; k < n; ++k) {
+        if (olist[k] != olist[n + k]) continue;
+        const double2 v = phi[k + n * (j + n * i)];
+        if (olist[j] == olist[k]) {
+          PGB_CHECK(olist[j] >= 1 && olist[j] <= no, "olist entry outside [1,Norb]");
+          phi_orb[(olist[j] - 1) + (no + 2) * i] = v;
+        }
+        if (olist[k] == 2 && olist[j] == 3) phi_orb[no + (no + 2) * i] = v;
+        if (olist[k] == 2 && olist[j] == 4) phi_orb[no + 1 + (no + 2) * i] = v;
+      }
+    }
+  ABI_CATCH("get_tr_phi", (void)0)
+}
+
+// Pade continued fraction of one series (fpade.f90:1-55), host code: the
+// coefficients need Np^2/2 operations.  Only the entries j >= i of g_i are
+// formed, the ones the later steps read.
+void get_a_(double2* a, const double2* xn, const double2* inp, const int64_t* Np) {
+  ABI_TRY
+  const int64_t n = *Np;
+  std::vector<double2> g(inp, inp + n);
+  if (n > 0) a[0] = g[0];
+  for (int64_t i = 1; i < n; ++i) {
+    const double2 gp = g[i - 1], xp = xn[i - 1];
+    for (int64_t j = i; j < n; ++j) {
+      const double2 gj = g[j];
+      g[j] = (gj.x == 0.0 && gj.y == 0.0) ? mkc(0.0, 0.0) : cdiv(gp - gj, (xn[j] - xp) * gj);
+    }
+    a[i] = g[i];
+  }
+  ABI_CATCH("get_a_", (void)0)
+}
+
+void get_qp_(double2* P, double2* Q, const double2* a, const double2* xn, const double2* wlist, const int64_t* Nw,
+             const int64_t* Np) {
+  ABI_TRY
+  for (int64_t w = 0; w < *Nw; ++w) {
+    double2 P0 = mkc(0.0, 0.0), P1 = a[0], Q0 = mkc(1.0, 0.0), Q1 = mkc(1.0, 0.0);
+    for (int64_t i = 1; i < *Np; ++i) {
+      const double2 t = a[i] * (wlist[w] - xn[i - 1]);
+      const double2 p = P1 + t * P0, q = Q1 + t * Q0;
+      P0 = P1;
+      P1 = p;
+      Q0 = Q1;
+      Q1 = q;
+    }
+    P[w] = P1;
+    Q[w] = Q1;
+  }
+  ABI_CATCH("get_qp_", (void)0)
+}
+
+void pade_with_trace(const double2* arrayin, double2* arrayout, const double2* iwlist, const double2* wlist,
+                     const int64_t* Nk, const int64_t* Niw, const int64_t* Nw, const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, np = *Niw, nw = *Nw, no = *Norb;
+  PGB_CHECK(np >= 1, "pade_with_trace needs at least one Matsubara point");
+  DBuf<double2> A((size_t)nk * np * no * no), xn(np), wl(nw), out((size_t)nw * nk);
+  A.upload(arrayin, (size_t)nk * np * no * no);
+  xn.upload(iwlist, np);
+  wl.upload(wlist, nw);
+  pade_trace(out.p, A.p, xn.p, wl.p, (int)nk, (int)np, (int)nw, (int)no);
+  out.download(arrayout, (size_t)nw * nk);
+  sync();
+  ABI_CATCH("pade_with_trace", nan_fill(arrayout, (size_t)(*Nw) * (*Nk)))
+}
+
 // ------------------------------------------------------------ spin-orbit --
 // Onsite vertex with spin-orbit coupling (fUJ.f90:109-180 and, with
 // orbital-dependent U/J, :182-251); host code, written as V(j,i).
@@ -1171,35 +1462,24 @@ PGB_STUB(calc_lij_wl)
 PGB_STUB(calc_sigma_hall)
 PGB_STUB(calc_tau_epa)
 PGB_STUB(calc_tdf)
-PGB_STUB(chiq_map)
 PGB_STUB(gen_dos)
 PGB_STUB(gen_green_inv_from_eig)
 PGB_STUB(gen_imp_ham)
 PGB_STUB(gen_tr_greenw_0)
-PGB_STUB(get_a_)
 PGB_STUB(get_band_to_orb_delta)
-PGB_STUB(get_chi_irr)
 PGB_STUB(get_chi_irr_sc)
 PGB_STUB(get_dft_imp_ham)
 PGB_STUB(get_eig_mlo)
 PGB_STUB(get_imass0)
 PGB_STUB(get_imassk)
-PGB_STUB(get_iqshift_)
-PGB_STUB(get_phi_irr)
-PGB_STUB(get_qp_)
-PGB_STUB(get_qshift_)
 PGB_STUB(get_spectrum_spaghetti)
 PGB_STUB(get_tau)
-PGB_STUB(get_tr_chi)
-PGB_STUB(get_tr_phi)
 PGB_STUB(get_veloc)
 PGB_STUB(get_vlm0)
 PGB_STUB(get_vnm)
 PGB_STUB(matrix_riccati_batch)
 PGB_STUB(matrix_riccati_chords)
 PGB_STUB(mkbdghamk)
-PGB_STUB(pade_with_trace)
-PGB_STUB(phiq_map)
 PGB_STUB(riccati_chords)
 PGB_STUB(solve_cpa_array)
 

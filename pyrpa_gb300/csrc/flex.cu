@@ -3233,3 +3233,234 @@ void orb_to_band_soc(double2* out, const double2* D, const double2* uni, const F
   count_launch("orb_to_band_soc");
 }
 }  // namespace pgb
+
+// ======================================================= real frequency ==
+// Band-basis Lindhard sums on the real axis (fchi.f90:95-318, fphi.f90:89-305)
+// and Pade continuation (fpade.f90).  The reference adds rank-1 terms
+// w_klm B B^T (N^6 per k); here chi_{ab,cd} = sum_k sum_lm P_ac,l(k+q) w_lm
+// Q_bd,m(k) is contracted as (P W) Q^T (N^5 per k) in shared memory, one
+// CTA per (q, w) job and one thread per output element.
+namespace pgb {
+namespace {
+template <int PHI>
+__global__ void k_bubble_rf(double2* out, const double2* uni, const double* eig, const double* ff, const int* qsh,
+                            const RfJob* jobs, const int* o1, const int* o2, int Nk, int No, int Nchi, double mu,
+                            double temp, double eps) {
+  extern __shared__ __align__(16) unsigned char smb[];
+  const int N2 = No * No, N3 = N2 * No;
+  double2* Uk = reinterpret_cast<double2*>(smb);  // [a + No n]
+  double2* Uq = Uk + N2;
+  double2* W = Uq + N2;   // [l + No m]
+  double2* P = W + N2;    // [(a + No c) + N2 l]
+  double2* Q = P + N3;    // [(b + No d) + N2 m]
+  double2* T = Q + N3;    // [(a + No c) + N2 m]
+  double* e_k = reinterpret_cast<double*>(T + N3);
+  double* e_q = e_k + No;
+  double* f_k = e_q + No;
+  double* f_q = f_k + No;
+  const RfJob jb = jobs[blockIdx.x];
+  const int* qs = qsh + jb.qoff;
+  const int t = threadIdx.x, nt = blockDim.x;
+  const bool active = t < Nchi * Nchi;
+  const int i = t % Nchi, j = t / Nchi;
+  const int ac = active ? o1[i] + No * o1[j] : 0, bd = active ? o2[i] + No * o2[j] : 0;
+  const double temp_safe = fmax(temp, 1.0e-12);
+  double2 acc = mkc(0.0, 0.0);
+  for (int k = 0; k < Nk; ++k) {
+    const int kq = qs[k];
+    for (int e = t; e < N2; e += nt) {
+      Uk[e] = uni[e + (long long)N2 * k];
+      Uq[e] = uni[e + (long long)N2 * kq];
+    }
+    for (int e = t; e < No; e += nt) {
+      e_k[e] = eig[e + (long long)No * k];
+      e_q[e] = eig[e + (long long)No * kq];
+      f_k[e] = ff[e + (long long)No * k];
+      f_q[e] = ff[e + (long long)No * kq];
+    }
+    __syncthreads();
+    for (int e = t; e < N2; e += nt) {  // weight of band pair (l at k+q, m at k)
+      const int l = e % No, m = e / No;
+      double2 w = mkc(0.0, 0.0);
+      if (PHI) {
+        const double den = jb.w - e_k[m] - e_q[l] + 2.0 * mu;
+        if (!(fabs(den) < eps && jb.delta < eps)) w = cdiv(mkc(-(1.0 - f_q[l] - f_k[m]), 0.0), mkc(den, jb.delta));
+      } else {
+        const double de = e_k[m] - e_q[l];
+        if (fabs(jb.w) < 1.0e-12 && fabs(de) < 1.0e-9) w = mkc(f_k[m] * (1.0 - f_k[m]) / temp_safe, 0.0);
+        else if (fabs(f_q[l] - f_k[m]) > eps) w = cdiv(mkc(f_q[l] - f_k[m], 0.0), mkc(jb.w + de, jb.delta));
+      }
+      W[e] = w;
+    }
+    for (int e = t; e < N3; e += nt) {
+      const int pr = e % N2, n = e / N2, a = pr % No, c = pr / No;
+      P[e] = conj(Uq[a + No * n]) * Uq[c + No * n];
+      Q[e] = Uk[a + No * n] * conj(Uk[c + No * n]);
+    }
+    __syncthreads();
+    for (int e = t; e < N3; e += nt) {
+      const int pr = e % N2, m = e / N2;
+      double2 s = mkc(0.0, 0.0);
+      for (int l = 0; l < No; ++l) s += P[pr + N2 * l] * W[l + No * m];
+      T[e] = s;
+    }
+    __syncthreads();
+    if (active)
+      for (int m = 0; m < No; ++m) acc += T[ac + N2 * m] * Q[bd + N2 * m];
+    __syncthreads();
+  }
+  if (active) out[i + (long long)Nchi * (j + (long long)Nchi * blockIdx.x)] = (1.0 / (double)Nk) * acc;
+}
+
+// chi_s = (I - chi0 S)^-1 chi0 per q and the (ll, mm) sums of chi_s and chi0
+// (fchi.f90:289-314); one warp per q
+template <int N>
+__global__ void k_rpa_trace(double2* trs, double2* tr0, const double2* chi, const double* S, const int* dmask,
+                            int Nq) {
+  __shared__ int piv[4][N + 1], map[4][32];
+  __shared__ double sS[N * N];
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) sS[(e % N) * N + e / N] = S[e];
+  __syncthreads();
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = lane < N ? lane : 0;
+  for (int q = blockIdx.x * 4 + w; q < Nq; q += gridDim.x * 4) {
+    const double2* X = chi + (long long)N * N * q;  // X(i, j) at i + N j
+    double2 a[N];
+    for (int jj = 0; jj < N; ++jj) {
+      double2 s = mkc(i == jj ? 1.0 : 0.0, 0.0);
+      for (int c = 0; c < N; ++c) s -= sS[c * N + jj] * X[i + N * c];
+      a[jj] = s;
+    }
+    const bool ok = warp_inverse<double, N>(a, piv[w], map[w]);
+    double2 s_s = mkc(0.0, 0.0), s_0 = mkc(0.0, 0.0);
+    if (lane < N && dmask[i])
+      for (int jj = 0; jj < N; ++jj) {
+        if (!dmask[jj]) continue;
+        double2 v = mkc(0.0, 0.0);
+        for (int c = 0; c < N; ++c) v += pick<double, N>(a, c) * X[c + N * jj];
+        s_s += v;
+        s_0 += X[i + N * jj];
+      }
+    for (int off = 16; off > 0; off >>= 1) {
+      s_s.x += __shfl_xor_sync(0xffffffffu, s_s.x, off);
+      s_s.y += __shfl_xor_sync(0xffffffffu, s_s.y, off);
+      s_0.x += __shfl_xor_sync(0xffffffffu, s_0.x, off);
+      s_0.y += __shfl_xor_sync(0xffffffffu, s_0.y, off);
+    }
+    if (lane == 0) {
+      trs[q] = s_s;
+      tr0[q] = s_0;
+      if (!ok) atomicExch(&g_err_dev, 8);
+    }
+  }
+}
+
+__global__ void k_trace_jobs(double2* tr, const double2* m, int N, int Nq) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Nq; q += gridDim.x * blockDim.x) {
+    double2 s = mkc(0.0, 0.0);
+    for (int l = 0; l < N; ++l) s += m[l + (long long)N * (l + (long long)N * q)];
+    tr[q] = s;
+  }
+}
+
+// Pade: coefficients of series (k, o) = A(k, :, o, o) (fpade.f90:1-27); only the
+// entries j >= i of g_i are formed, the ones later steps read
+__global__ void k_pade_coef(double2* a, double2* g, const double2* A, const double2* xn, int Nk, int Np, int No) {
+  const long long ns = (long long)Nk * No;
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < ns; s += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(s % Nk), o = (int)(s / Nk);
+    double2* gs = g + s * Np;
+    double2* as = a + s * Np;
+    for (int jj = 0; jj < Np; ++jj) gs[jj] = A[k + (long long)Nk * (jj + (long long)Np * (o + (long long)No * o))];
+    as[0] = gs[0];
+    for (int ii = 1; ii < Np; ++ii) {
+      const double2 gp = gs[ii - 1], xp = xn[ii - 1];
+      for (int jj = ii; jj < Np; ++jj) {
+        const double2 gj = gs[jj];
+        gs[jj] = (gj.x == 0.0 && gj.y == 0.0) ? mkc(0.0, 0.0) : cdiv(gp - gj, (xn[jj] - xp) * gj);
+      }
+      as[ii] = gs[ii];
+    }
+  }
+}
+
+// out(w, k) = sum_o P_N / Q_N of series (k, o) at wl(w) (fpade.f90:29-129)
+__global__ void k_pade_eval(double2* out, const double2* a, const double2* xn, const double2* wl, int Nk, int Np,
+                            int Nw, int No) {
+  const long long n = (long long)Nk * Nw;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int w = (int)(idx % Nw), k = (int)(idx / Nw);
+    const double2 z = wl[w];
+    double2 sum = mkc(0.0, 0.0);
+    for (int o = 0; o < No; ++o) {
+      const double2* as = a + ((long long)k + (long long)Nk * o) * Np;
+      double2 P0 = mkc(0.0, 0.0), P1 = as[0], Q0 = mkc(1.0, 0.0), Q1 = mkc(1.0, 0.0);
+      for (int ii = 1; ii < Np; ++ii) {
+        const double2 tt = as[ii] * (z - xn[ii - 1]);
+        const double2 P = P1 + tt * P0, Q = Q1 + tt * Q0;
+        P0 = P1;
+        P1 = P;
+        Q0 = Q1;
+        Q1 = Q;
+      }
+      sum += cdiv(P1, Q1);
+    }
+    out[w + (long long)Nw * k] = sum;
+  }
+}
+}  // namespace
+
+void bubble_rf(double2* out, const double2* uni, const double* eig, const double* ff, const int* qsh,
+               const std::vector<RfJob>& jobs, const std::vector<int>& o1, const std::vector<int>& o2, int Nk, int No,
+               int Nchi, double mu, double temp, double eps, bool phi) {
+  PGB_CHECK(No <= kMaxOrb && Nchi <= kMaxChi, "Norb or Nchi above the engine limits");
+  DBuf<RfJob> dj(jobs.size());
+  dj.upload(jobs.data(), jobs.size());
+  DBuf<int> d1(Nchi), d2(Nchi);
+  d1.upload(o1.data(), Nchi);
+  d2.upload(o2.data(), Nchi);
+  const int threads = std::max(32, ((Nchi * Nchi + 31) / 32) * 32);
+  const size_t smem = (3 * (size_t)No * No + 3 * (size_t)No * No * No) * sizeof(double2) + 4 * (size_t)No * sizeof(double);
+  const long long nj = (long long)jobs.size();
+  for (long long j0 = 0; j0 < nj; j0 += 65535) {  // grid.x stays within one launch's limit
+    const int nb = (int)std::min<long long>(65535, nj - j0);
+    if (phi)
+      k_bubble_rf<1><<<nb, threads, smem, ctx().stream>>>(out + (size_t)Nchi * Nchi * j0, uni, eig, ff, qsh, dj.p + j0,
+                                                         d1.p, d2.p, Nk, No, Nchi, mu, temp, eps);
+    else
+      k_bubble_rf<0><<<nb, threads, smem, ctx().stream>>>(out + (size_t)Nchi * Nchi * j0, uni, eig, ff, qsh, dj.p + j0,
+                                                         d1.p, d2.p, Nk, No, Nchi, mu, temp, eps);
+    count_launch(phi ? "bubble_rf_phi" : "bubble_rf");
+  }
+}
+
+void rpa_trace(double2* trs, double2* tr0, const double2* chi, const double* S, const int* dmask, int Nchi, int Nq) {
+  reset_err();
+  const unsigned blocks = (unsigned)std::min<long long>((Nq + 3) / 4, 65535LL);
+  switch (Nchi) {
+    case 1: k_rpa_trace<1><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
+    case 4: k_rpa_trace<4><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
+    case 9: k_rpa_trace<9><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
+    case 16: k_rpa_trace<16><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
+    case 25: k_rpa_trace<25><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
+    default: throw Error("chiq_map supports Nchi = Norb^2 with Norb <= 5");
+  }
+  count_launch("rpa_trace");
+  PGB_CHECK(fetch_err() == 0, "zgesv failed in chiq_map");
+}
+
+void trace_jobs(double2* tr, const double2* m, int Nchi, int Nq) {
+  k_trace_jobs<<<grid_1d(Nq, 128, 65536), 128, 0, ctx().stream>>>(tr, m, Nchi, Nq);
+  count_launch("trace_jobs");
+}
+
+void pade_trace(double2* out, const double2* A, const double2* xn, const double2* wl, int Nk, int Np, int Nw, int No) {
+  const long long ns = (long long)Nk * No;
+  DBuf<double2> a((size_t)ns * Np), g((size_t)ns * Np);
+  k_pade_coef<<<grid_1d(ns, 64, 65536), 64, 0, ctx().stream>>>(a.p, g.p, A, xn, Nk, Np, No);
+  count_launch("pade_coef");
+  k_pade_eval<<<grid_1d((long long)Nk * Nw, 128, 65536), 128, 0, ctx().stream>>>(out, a.p, xn, wl, Nk, Np, Nw, No);
+  count_launch("pade_eval");
+}
+}  // namespace pgb

@@ -203,4 +203,17 @@ void mkdelta_soc(const Geom& g, const Pairs& p, const FullMesh& fm, const double
 void initial_delta_soc(double2* D, const double* init, const double2* uni, const FullMesh& fm, const Geom& g,
                        int gap_sym);
 void orb_to_band_soc(double2* out, const double2* D, const double2* uni, const FullMesh& fm, const Geom& g);
+
+// ------------------------------------------------------- real frequency --
+struct RfJob {
+  double w, delta;  // real frequency and broadening of one (q, w) job
+  long long qoff;   // offset of its k+q (or -k+q) index list, 0-based entries
+};
+// chi (or phi) matrices (Nchi, Nchi) of each job, (1/Nk) sum over the k list
+void bubble_rf(double2* out, const double2* uni, const double* eig, const double* ff, const int* qsh,
+               const std::vector<RfJob>& jobs, const std::vector<int>& o1, const std::vector<int>& o2, int Nk, int No,
+               int Nchi, double mu, double temp, double eps, bool phi);
+void rpa_trace(double2* trs, double2* tr0, const double2* chi, const double* S, const int* dmask, int Nchi, int Nq);
+void trace_jobs(double2* tr, const double2* m, int Nchi, int Nq);
+void pade_trace(double2* out, const double2* A, const double2* xn, const double2* wl, int Nk, int Np, int Nw, int No);
 }  // namespace pgb

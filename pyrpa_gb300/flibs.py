@@ -60,6 +60,17 @@ _SIGNATURES = {
     "pyrpa_gb_sc_dyson": [_c128, _c128, _c128, _c128, _pi, _pi, _pi],
     "mkfk_trs_nsoc_": [_c128, _c128, _c128, _pi, _pi, _pi],
     "get_vmat_soc": [_f64, _i64, _i64, _i64, _i64, _pd, _pd, _pi, _pi],
+    "get_qshift_": [_f64, _f64, _i64, _pi],
+    "get_iqshift_": [_f64, _f64, _i64, _pi],
+    "get_chi_irr": [_c128, _c128, _f64, _f64, _i64, _i64, _f64, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
+    "get_phi_irr": [_c128, _c128, _f64, _f64, _i64, _i64, _f64, _pi, _pi, _pi, _pi, _pd, _pd, _pd, _pd],
+    "chiq_map": [_c128, _c128, _c128, _f64, _f64, _f64, _f64, _i64, _pd, _pd, _pd, _pd] + [_pi] * 5,
+    "phiq_map": [_c128, _c128, _f64, _f64, _f64, _i64, _pd, _pd, _pd, _pd, _pd] + [_pi] * 5 + [_pb],
+    "get_tr_chi": [_c128, _c128, _c128, _c128, _c128, _i64, _pi, _pi, _pi],
+    "get_tr_phi": [_c128, _c128, _c128, _i64, _pi, _pi, _pi],
+    "get_a_": [_c128, _c128, _c128, _pi],
+    "get_qp_": [_c128, _c128, _c128, _c128, _c128, _pi, _pi],
+    "pade_with_trace": [_c128, _c128, _c128, _c128, _pi, _pi, _pi, _pi],
     "get_vmat_soc_orb": [_f64, _i64, _i64, _i64, _i64, _f64, _f64, _pi, _pi],
     "mkself_soc": [_c128, _pd, _f64, _i64, _i64, _i64, _i64, _i64, _c128, _f64, _c128, _pd, _pd, _pd, _pi, _pd, _pd]
     + [_pi] * 9 + [_pb, _pb, _pi, _pb, _pd],
@@ -728,3 +739,114 @@ def gen_Fk_soc(Gk, delta, invk, invs, slist, gap_sym: int):
     _call("mkfk_trs_soc_", Fk, np.ascontiguousarray(Gk), np.ascontiguousarray(delta), sgnsig, slist, invk,
           np.asarray(invs, dtype=np.int64), i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(gap_sym))
     return Fk
+
+
+# ------------------------------------------------------- real-frequency maps
+# Mirrors of libs/flibs/_hamiltonian.py (get_qshift, get_iqshift),
+# _susceptibility.py (get_chi_irr, chis_qmap, get_tr_chi, get_phi_irr,
+# phi_qmap, get_tr_phi) and _green.py (get_a, get_QP, pade_with_trace).
+def get_qshift(klist, qpoint):
+    Nk = len(klist)
+    qshift = np.zeros(Nk, dtype=np.int64)
+    _call("get_qshift_", np.ascontiguousarray(qpoint, dtype=np.float64), np.ascontiguousarray(klist, dtype=np.float64),
+          qshift, i64(Nk))
+    return qshift
+
+
+def get_iqshift(klist, qpoint):
+    Nk = len(klist)
+    qshift = np.zeros(Nk, dtype=np.int64)
+    _call("get_iqshift_", np.ascontiguousarray(qpoint, dtype=np.float64),
+          np.ascontiguousarray(klist, dtype=np.float64), qshift, i64(Nk))
+    return qshift
+
+
+def get_chi_irr(uni, eig, ffermi, qshift, olist, wlist, idelta: float, temp: float):
+    """chi0(q, w) [Nw, Nchi, Nchi] (libs/flibs/_susceptibility.py:271-293)."""
+    Nk, Nw = len(eig), len(wlist)
+    Norb, Nchi = eig.shape[1], len(olist)
+    chi = np.zeros((Nw, Nchi, Nchi), dtype=np.complex128)
+    _call("get_chi_irr", chi, np.ascontiguousarray(uni), np.ascontiguousarray(eig), np.ascontiguousarray(ffermi),
+          np.ascontiguousarray(qshift, dtype=np.int64), olist, np.ascontiguousarray(wlist, dtype=np.float64),
+          i64(Nchi), i64(Norb), i64(Nk), i64(Nw), dbl(idelta), dbl(idelta * 1e-3), dbl(temp))
+    return chi
+
+
+def chis_qmap(uni, eig, ffermi, klist, Smat, olist, Nx: int, Ny: int, temp: float, ecut: float, idelta: float):
+    """(chis, chi) maps [Nx, Ny] (libs/flibs/_susceptibility.py:295-324)."""
+    Nk = len(eig)
+    Norb, Nchi = eig.shape[1], len(olist)
+    chi = np.zeros((Nx, Ny), dtype=np.complex128)
+    chis = np.zeros((Nx, Ny), dtype=np.complex128)
+    _call("chiq_map", chis, chi, np.ascontiguousarray(uni), np.ascontiguousarray(eig), np.ascontiguousarray(ffermi),
+          np.ascontiguousarray(klist, dtype=np.float64), np.ascontiguousarray(Smat, dtype=np.float64), olist,
+          dbl(temp), dbl(ecut), dbl(idelta), dbl(idelta * 1e-3), i64(Nx), i64(Ny), i64(Nk), i64(Norb), i64(Nchi))
+    return chis, chi
+
+
+def get_tr_chi(chis, chi0, olist):
+    Nchi, Nw, Norb = len(olist), len(chi0), int(np.asarray(olist).max())
+    trchis = np.zeros(Nw, dtype=np.complex128)
+    trchi0 = np.zeros(Nw, dtype=np.complex128)
+    chis_orb = np.zeros((Nw, Norb + 2), dtype=np.complex128)
+    _call("get_tr_chi", trchis, trchi0, chis_orb, np.ascontiguousarray(chis), np.ascontiguousarray(chi0), olist,
+          i64(Nw), i64(Nchi), i64(Norb))
+    return trchis, trchi0, chis_orb
+
+
+def get_phi_irr(uni, eig, ffermi, qshift, olist, wlist, idelta: float, mu: float, temp: float):
+    Nk, Nw = len(eig), len(wlist)
+    Norb, Nchi = eig.shape[1], len(olist)
+    phi = np.zeros((Nw, Nchi, Nchi), dtype=np.complex128)
+    _call("get_phi_irr", phi, np.ascontiguousarray(uni), np.ascontiguousarray(eig), np.ascontiguousarray(ffermi),
+          np.ascontiguousarray(qshift, dtype=np.int64), olist, np.ascontiguousarray(wlist, dtype=np.float64),
+          i64(Nchi), i64(Norb), i64(Nk), i64(Nw), dbl(idelta), dbl(idelta * 1e-3), dbl(mu), dbl(temp))
+    return phi
+
+
+def phi_qmap(uni, eig, ffermi, klist, olist, Nx: int, Ny: int, mu: float, temp: float, ecut: float, idelta: float,
+             sw_omega: bool):
+    Nk = len(eig)
+    Norb, Nchi = eig.shape[1], len(olist)
+    phi = np.zeros((Nx, Ny), dtype=np.complex128)
+    _call("phiq_map", phi, np.ascontiguousarray(uni), np.ascontiguousarray(eig), np.ascontiguousarray(ffermi),
+          np.ascontiguousarray(klist, dtype=np.float64), olist, dbl(mu), dbl(temp), dbl(ecut), dbl(idelta),
+          dbl(idelta * 1e-3), i64(Nx), i64(Ny), i64(Nk), i64(Norb), i64(Nchi), byref(c_bool(bool(sw_omega))))
+    return phi
+
+
+def get_tr_phi(phi, olist):
+    Nchi, Nw, Norb = len(olist), len(phi), int(np.asarray(olist).max())
+    trphi = np.zeros(Nw, dtype=np.complex128)
+    phi_orb = np.zeros((Nw, Norb + 2), dtype=np.complex128)
+    _call("get_tr_phi", trphi, phi_orb, np.ascontiguousarray(phi), olist, i64(Nw), i64(Nchi), i64(Norb))
+    return trphi, phi_orb
+
+
+def get_a(inp_data, xlist):
+    Np = len(inp_data)
+    a = np.zeros(Np, dtype=np.complex128)
+    _call("get_a_", a, np.ascontiguousarray(xlist, dtype=np.complex128),
+          np.ascontiguousarray(inp_data, dtype=np.complex128), i64(Np))
+    return a
+
+
+def get_QP(a, xlist, wlist):
+    """(Q, P), in the reference wrapper's return order (libs/flibs/_green.py:190-204)."""
+    Nw, Np = len(wlist), len(a)
+    Q = np.zeros(Nw, dtype=np.complex128)
+    P = np.zeros(Nw, dtype=np.complex128)
+    _call("get_qp_", P, Q, np.ascontiguousarray(a, dtype=np.complex128),
+          np.ascontiguousarray(xlist, dtype=np.complex128), np.ascontiguousarray(wlist, dtype=np.complex128),
+          i64(Nw), i64(Np))
+    return Q, P
+
+
+def pade_with_trace(A, iwlist, wlist):
+    """[Nk, Nw] (libs/flibs/_green.py:206-220)."""
+    Nk, Nw, Niw = A.shape[3], len(wlist), len(iwlist)
+    Norb = A.shape[0]
+    B = np.zeros((Nk, Nw), dtype=np.complex128)
+    _call("pade_with_trace", np.ascontiguousarray(A), B, np.ascontiguousarray(iwlist, dtype=np.complex128),
+          np.ascontiguousarray(wlist, dtype=np.complex128), i64(Nk), i64(Niw), i64(Nw), i64(Norb))
+    return B

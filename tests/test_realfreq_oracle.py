@@ -100,3 +100,43 @@ def test_pade_with_trace_reproduces_the_green_function():
     out = O.pade_with_trace(G, iw, w)                         # [k, w]
     exact = np.sum(1.0 / (w[None, :, None] + mu - eig[:, None, :]), axis=2)
     assert np.abs(out - exact).max() < 1e-8 * np.abs(exact).max()
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from pyrpa_gb300 import build, flibs
+    if not build.LIB.exists():
+        build.build()
+    flibs.load_library()
+    return flibs
+
+
+def test_library_host_entries_match_oracle(lib):
+    """get_qshift_/get_iqshift_, get_tr_chi/get_tr_phi, get_a_/get_qp_ are host
+    code in the library."""
+    F = lib
+    rng = np.random.default_rng(7)
+    kl = full_mesh(6, 5)
+    for q in (np.zeros(3), np.array([2 / 6, 3 / 5, 0.0]), np.array([0.5, 0.1, 0.0])):  # the last misses the mesh
+        assert np.array_equal(F.get_qshift(kl, q), O.get_qshift(kl, q))
+        assert np.array_equal(F.get_iqshift(kl, q), O.get_iqshift(kl, q))
+    olist = np.asfortranarray(O.get_chi_orb_list(4)[0])
+    n = len(olist)
+    chis = rng.standard_normal((5, n, n)) + 1j * rng.standard_normal((5, n, n))
+    chi0 = rng.standard_normal((5, n, n)) + 1j * rng.standard_normal((5, n, n))
+    for a, b in zip(F.get_tr_chi(chis, chi0, olist), O.get_tr_chi(chis, chi0, olist)):
+        assert np.abs(a - b).max() < 1e-13
+    for a, b in zip(F.get_tr_phi(chis, olist), O.get_tr_phi(chis, olist)):
+        assert np.abs(a - b).max() < 1e-13
+    iw = 1j * np.pi * 0.05 * (2 * np.arange(10) + 1)
+    # more poles than half the points: the continued fraction does not
+    # terminate (a terminated one continues with 0/0 noise after 2n+1 terms)
+    poles = rng.uniform(-1, 1, 8)
+    data = np.sum(rng.uniform(0.1, 1, 8)[None, :] / (iw[:, None] - poles[None, :]), axis=1)
+    a1, a2 = F.get_a(data, iw), O.get_a(data, iw)
+    # the recursion amplifies rounding: a 1e-15 relative change of the data
+    # moves the last of these coefficients by 1e-7 relative
+    assert (np.abs(a1 - a2) / np.abs(a2)).max() < 1e-5
+    w = np.linspace(-1, 1, 9) + 0.01j
+    for x, y in zip(F.get_QP(a2, iw, w), O.get_QP(a2, iw, w)):
+        assert np.abs(x - y).max() < 1e-12 * np.abs(y).max()
