@@ -49,7 +49,8 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     p.add_argument("--precision", default="mixed", choices=["mixed", "32", "64"],
-                   help="mixed: FP32 bulk to the FP32 rounding floor, then FP64 bulk to eps")
+                   help="mixed: FP32 bulk to the FP32 rounding floor, then double-float bulk with the "
+                        "FP64 vertex to eps")
     p.add_argument("--eps", type=float, default=1.0e-4)
     p.add_argument("--scf-loop", type=int, default=300)
     p.add_argument("--no-tail", action="store_true")
@@ -280,7 +281,8 @@ def main():
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
                    "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, double-float chi0 "
                                           f"and Sigma with FP32 vertex for {int(stats['iterations_fp64_fp32vertex'])}, "
-                                          f"then FP64 bulk to eps; Eliashberg stage FP64",
+                                          f"then double-float chi0 and Sigma with FP64 vertex to eps; Eliashberg "
+                                          f"stage double-float chi0 and contractions with FP64 V_Delta",
                                  "32": "FP32 bulk", "64": "FP64"}[a.precision]})
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,

@@ -378,6 +378,15 @@ int mix_finish_bulk() {
   return (s && std::string(s) == "fp64") ? 64 : 48;
 }
 
+// Bulk of the judging phase of the mixed schedule: double-float chi0 and
+// Sigma with the FP64 vertex (default; about 1e-14 relative, 1.2 s less per
+// iteration on c2 than FP64 bulk), or FP64 throughout with
+// PYRPA_GB_JUDGE_BULK=fp64.
+bool mix_judge_df() {
+  const char* s = std::getenv("PYRPA_GB_JUDGE_BULK");
+  return !(s && std::string(s) == "fp64");
+}
+
 // PYRPA_GB_MIX_DIIS=keep keeps the FP32-phase DIIS history across the switch
 // to FP64 bulk (default: a fresh history)
 bool mix_diis_reset() {
@@ -599,17 +608,19 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
   //   1  chi0 and Sigma on FP64 bulk, the stages in finish_mask (default the
   //      vertex) still on FP32: the FP32 rounding floor of the residual comes
   //      from the chi0 and Sigma convolutions, not from the vertex solve;
-  //   2  everything on FP64.
+  //   2  the judging phase: FP64, or (default in the mixed mode) double-float
+  //      chi0 and Sigma with the FP64 vertex.
   // A phase ends when the residual is below eps, below kMixSwitch (phase 0
   // only) or, once it is below kMixStallFrom, has not reached a new minimum
   // for kMixStall iterations.  Convergence is declared only in phase 2.
   const int finish_mask = mix_finish_mask();
   const int finish_bulk = mix_finish_bulk();
   int phase = (prec == kPrecMixed || prec == 32) ? 0 : 2;
+  const bool judge_df = prec == kPrecMixed && mix_judge_df();
   auto prec_of = [&](int ph) {
     if (prec == kPrecDF) return StagePrec{48, 64, 48};
     auto pick = [&](int bit, int other) { return (ph == 0 ? mask32 : finish_mask) & bit ? 32 : other; };
-    if (ph == 2) return StagePrec{64, 64, 64};
+    if (ph == 2) return judge_df ? StagePrec{48, 64, 48} : StagePrec{64, 64, 64};
     const int other = ph == 0 ? 64 : finish_bulk;
     return StagePrec{pick(1, other), pick(2, 64), pick(4, other)};
   };
@@ -806,6 +817,22 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   return lambda_out;
 }
 
+// V_Delta of a double-float bubble: the vertex solve runs in FP64 and the
+// result goes back to double-float for the FFT contractions of mkdelta
+template <typename R>
+bool vertex_delta(cx<R>* chi, long long K, int Nchi, const double* S, const double* C, int mode) {
+  if constexpr (std::is_same<R, dfl>::value) {
+    const long long n = K * Nchi * Nchi;
+    DBuf<double2> t(n);
+    widen<dfl>(t.p, chi, n);
+    const bool ok = vertex<double>(t.p, K, K, Nchi, S, C, mode);
+    narrow<dfl>(chi, t.p, n);
+    return ok;
+  } else {
+    return vertex<R>(chi, K, K, Nchi, S, C, mode);
+  }
+}
+
 // ============================================================ lin_eliash ==
 // chi (device, cx<R>) is overwritten with the pairing vertex V_Delta; if
 // chi_host is given, V_Delta is also copied back there (feliash.f90:61).
@@ -825,7 +852,7 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
   {
     Timer tv;
     tv.start();
-    PGB_CHECK(vertex<R>(chi, K, K, Nchi, S.p, C.p, singlet ? 1 : 2), "zgesv failed in V_delta");
+    PGB_CHECK(vertex_delta<R>(chi, K, Nchi, S.p, C.p, singlet ? 1 : 2), "zgesv failed in V_delta");
     g_stats.t_vertex += tv.stop();
     if (chi_host) {
       DBuf<double2> tmp(KC);
@@ -1557,11 +1584,16 @@ void run_chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const do
 // The Eliashberg stage (final G, chi0, V_Delta, Arnoldi) runs in FP64 except
 // in the pure FP32 mode or with PYRPA_GB_ELIASH=fp32: with FP32 bulk there,
 // lambda of the 5-orbital 64x64x2048 model moved by 3.6e-6 relative.
+// Eliashberg-stage bulk (final chi0, V_Delta contractions, Arnoldi applies):
+// FP32 in the FP32 mode or with PYRPA_GB_ELIASH=fp32; double-float in the
+// mixed mode (the V_Delta solve itself in FP64) unless PYRPA_GB_ELIASH=fp64;
+// FP64 otherwise.
 void run_pipeline(const PipelineArgs& a, int prec) {
   const char* e = std::getenv("PYRPA_GB_ELIASH");
-  const bool eliash32 = (prec == 32) || (e && std::string(e) == "fp32");
-  if (!eliash32) run_pipeline_impl<double>(a, prec);
-  else run_pipeline_impl<float>(a, prec);
+  const std::string ev = e ? e : "";
+  if (prec == 32 || ev == "fp32") run_pipeline_impl<float>(a, prec);
+  else if (prec == kPrecMixed && ev != "fp64") run_pipeline_impl<dfl>(a, prec);
+  else run_pipeline_impl<double>(a, prec);
 }
 
 }  // namespace pgb

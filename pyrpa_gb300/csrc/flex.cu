@@ -2758,6 +2758,8 @@ template void sigma<dfl>(const Geom&, const Pairs&, const double2*, const cx<dfl
                          double, double2*);
 template void widen<dfl>(double2*, const cx<dfl>*, long long);
 template void narrow<dfl>(cx<dfl>*, const double2*, long long);
+template void mkdelta<dfl>(const Geom&, const Pairs&, const double2*, const cx<dfl>*, const double*, const double*,
+                           const double*, bool, double, double2*, DeltaKernelCache<dfl>*);
 
 }  // namespace pgb
 
