@@ -758,7 +758,14 @@ void get_vsigma_flex_nosoc_(double2* chi, const double* Smat, const double* Cmat
   X.upload(chi, K * n * n);
   S.upload(Smat, n * n);
   C.upload(Cmat, n * n);
-  PGB_CHECK(vertex<double>(X.p, K, K, (int)n, S.p, C.p, 0), "zgesv failed in V_sigma");
+  if (ctx().precision == kPrecDF) {  // the double-float solve of the mixed schedule's judging phase
+    DBuf<cdf> Xd(K * n * n);
+    narrow<dfl>(Xd.p, X.p, K * n * n);
+    PGB_CHECK(vertex<dfl>(Xd.p, K, K, (int)n, S.p, C.p, 0), "zgesv failed in V_sigma");
+    widen<dfl>(X.p, Xd.p, K * n * n);
+  } else {
+    PGB_CHECK(vertex<double>(X.p, K, K, (int)n, S.p, C.p, 0), "zgesv failed in V_sigma");
+  }
   X.download(chi, K * n * n);
   sync();
   ABI_CATCH("get_vsigma_flex_nosoc_", nan_fill(chi, (size_t)(*Nk) * (*Nw) * (*Nchi) * (*Nchi)))

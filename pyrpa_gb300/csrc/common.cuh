@@ -148,6 +148,43 @@ __host__ __device__ __forceinline__ cdf conj(cdf a) { return mkc(a.x, -a.y); }
 // a * (s i), s = +-1 (a sign change, no rounding)
 __host__ __device__ __forceinline__ cdf muli(cdf a, dfl s) { return s.hi > 0.f ? mkc(-a.y, a.x) : mkc(a.y, -a.x); }
 
+// Comparisons, division and the helpers the warp Gauss-Jordan elimination
+// uses for every bulk type (mad = multiply-add: one rounding in float and
+// double, the double-float product and sum otherwise).
+__host__ __device__ __forceinline__ bool operator>(dfl a, dfl b) { return b < a; }
+__host__ __device__ __forceinline__ bool operator==(dfl a, dfl b) { return a.hi == b.hi && a.lo == b.lo; }
+// Dekker's division: a float quotient, the double-float remainder a - b q1,
+// one float correction
+__host__ __device__ __forceinline__ dfl operator/(dfl a, dfl b) {
+  const float q1 = a.hi / b.hi;
+  const dfl r = a - b * dfl(q1);
+  const float q2 = r.hi / b.hi;
+  return fast_two_sum(q1, q2);
+}
+__host__ __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
+__host__ __device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
+__host__ __device__ __forceinline__ dfl mad(dfl a, dfl b, dfl c) { return a * b + c; }
+__host__ __device__ __forceinline__ dfl cabs1(cdf a) { return dabs(a.x) + dabs(a.y); }
+__host__ __device__ __forceinline__ cdf cdiv(cdf a, cdf b) {  // same scaling as the double version
+  const dfl s = dabs(b.x) + dabs(b.y);
+  const dfl bx = b.x / s, by = b.y / s;
+  const dfl d = bx * bx + by * by;
+  const dfl ax = a.x / s, ay = a.y / s;
+  return mkc((ax * bx + ay * by) / d, (ay * bx - ax * by) / d);
+}
+#ifdef __CUDACC__
+__device__ __forceinline__ float shfl_idx(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double shfl_idx(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ dfl shfl_idx(dfl v, int src) {
+  return dfl(__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src));
+}
+__device__ __forceinline__ float shfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ dfl shfl_xor(dfl v, int m) {
+  return dfl(__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m));
+}
+#endif
+
 // ---------------------------------------------------------------- errors --
 struct Error : std::runtime_error {
   explicit Error(const std::string& s) : std::runtime_error(s) {}

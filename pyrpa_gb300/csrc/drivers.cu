@@ -342,7 +342,7 @@ void convert_chi(void* out, int to, const void* in, int from, long long n) {
 double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, const StagePrec& sp, ChiBufs& b,
                  double2* sig) {
   const long long KC = in.g.K * in.Nchi * in.Nchi;
-  PGB_CHECK(sp.vertex == 32 || sp.vertex == 64, "the vertex stage runs in FP32 or FP64");
+  PGB_CHECK(sp.vertex == 32 || sp.vertex == 64 || sp.vertex == 48, "the vertex stage runs in FP32, FP64 or double-float");
   void* c0 = b.get(sp.chi0, KC);
   double sdw = 0;
   if (sp.chi0 == 32) sdw = stage_chi0<float>(in, a, G, mu, (float2*)c0);
@@ -351,6 +351,7 @@ double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, c
   void* cv = b.get(sp.vertex, KC);
   convert_chi(cv, sp.vertex, c0, sp.chi0, KC);
   if (sp.vertex == 32) stage_vertex<float>(in, (float2*)cv);
+  else if (sp.vertex == 48) stage_vertex<dfl>(in, (cdf*)cv);
   else stage_vertex<double>(in, (double2*)cv);
   void* cs = b.get(sp.sigma, KC);
   convert_chi(cs, sp.sigma, cv, sp.vertex, KC);
@@ -378,13 +379,16 @@ int mix_finish_bulk() {
   return (s && std::string(s) == "fp64") ? 64 : 48;
 }
 
-// Bulk of the judging phase of the mixed schedule: double-float chi0 and
-// Sigma with the FP64 vertex (default; about 1e-14 relative, 1.2 s less per
-// iteration on c2 than FP64 bulk), or FP64 throughout with
-// PYRPA_GB_JUDGE_BULK=fp64.
-bool mix_judge_df() {
+// Stage types of the judging phase of the mixed schedule
+// (PYRPA_GB_JUDGE_BULK): "df" (default) double-float chi0, vertex and Sigma,
+// about 1e-13 relative; "df64" the same with the FP64 vertex; "fp64" FP64
+// throughout.
+StagePrec mix_judge_prec() {
   const char* s = std::getenv("PYRPA_GB_JUDGE_BULK");
-  return !(s && std::string(s) == "fp64");
+  const std::string v = s ? s : "df";
+  if (v == "fp64") return StagePrec{64, 64, 64};
+  if (v == "df64") return StagePrec{48, 64, 48};
+  return StagePrec{48, 48, 48};
 }
 
 // PYRPA_GB_MIX_DIIS=keep keeps the FP32-phase DIIS history across the switch
@@ -608,19 +612,19 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
   //   1  chi0 and Sigma on FP64 bulk, the stages in finish_mask (default the
   //      vertex) still on FP32: the FP32 rounding floor of the residual comes
   //      from the chi0 and Sigma convolutions, not from the vertex solve;
-  //   2  the judging phase: FP64, or (default in the mixed mode) double-float
-  //      chi0 and Sigma with the FP64 vertex.
+  //   2  the judging phase: FP64, or in the mixed mode the stage types of
+  //      mix_judge_prec (default double-float throughout).
   // A phase ends when the residual is below eps, below kMixSwitch (phase 0
   // only) or, once it is below kMixStallFrom, has not reached a new minimum
   // for kMixStall iterations.  Convergence is declared only in phase 2.
   const int finish_mask = mix_finish_mask();
   const int finish_bulk = mix_finish_bulk();
   int phase = (prec == kPrecMixed || prec == 32) ? 0 : 2;
-  const bool judge_df = prec == kPrecMixed && mix_judge_df();
+  const StagePrec judge = prec == kPrecMixed ? mix_judge_prec() : StagePrec{64, 64, 64};
   auto prec_of = [&](int ph) {
     if (prec == kPrecDF) return StagePrec{48, 64, 48};
     auto pick = [&](int bit, int other) { return (ph == 0 ? mask32 : finish_mask) & bit ? 32 : other; };
-    if (ph == 2) return judge_df ? StagePrec{48, 64, 48} : StagePrec{64, 64, 64};
+    if (ph == 2) return judge;
     const int other = ph == 0 ? 64 : finish_bulk;
     return StagePrec{pick(1, other), pick(2, 64), pick(4, other)};
   };
@@ -817,11 +821,13 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   return lambda_out;
 }
 
-// V_Delta of a double-float bubble: the vertex solve runs in FP64 and the
-// result goes back to double-float for the FFT contractions of mkdelta
+// V_Delta in the bulk type of the Eliashberg stage; for double-float the
+// solve runs in double-float, or in FP64 with PYRPA_GB_ELIASH=df64
 template <typename R>
 bool vertex_delta(cx<R>* chi, long long K, int Nchi, const double* S, const double* C, int mode) {
+  const char* e = std::getenv("PYRPA_GB_ELIASH");
   if constexpr (std::is_same<R, dfl>::value) {
+    if (!(e && std::string(e) == "df64")) return vertex<dfl>(chi, K, K, Nchi, S, C, mode);
     const long long n = K * Nchi * Nchi;
     DBuf<double2> t(n);
     widen<dfl>(t.p, chi, n);
@@ -1584,15 +1590,15 @@ void run_chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const do
 // The Eliashberg stage (final G, chi0, V_Delta, Arnoldi) runs in FP64 except
 // in the pure FP32 mode or with PYRPA_GB_ELIASH=fp32: with FP32 bulk there,
 // lambda of the 5-orbital 64x64x2048 model moved by 3.6e-6 relative.
-// Eliashberg-stage bulk (final chi0, V_Delta contractions, Arnoldi applies):
-// FP32 in the FP32 mode or with PYRPA_GB_ELIASH=fp32; double-float in the
-// mixed mode (the V_Delta solve itself in FP64) unless PYRPA_GB_ELIASH=fp64;
-// FP64 otherwise.
+// Eliashberg-stage bulk (final chi0, V_Delta, Arnoldi applies): FP32 in the
+// FP32 mode or with PYRPA_GB_ELIASH=fp32; double-float in the mixed mode
+// unless PYRPA_GB_ELIASH=fp64 (df64: double-float with the FP64 V_Delta
+// solve); FP64 otherwise.
 void run_pipeline(const PipelineArgs& a, int prec) {
   const char* e = std::getenv("PYRPA_GB_ELIASH");
   const std::string ev = e ? e : "";
   if (prec == 32 || ev == "fp32") run_pipeline_impl<float>(a, prec);
-  else if (prec == kPrecMixed && ev != "fp64") run_pipeline_impl<dfl>(a, prec);
+  else if (prec == kPrecMixed && ev != "fp64") run_pipeline_impl<dfl>(a, prec);  // "df64": FP64 V_Delta solve
   else run_pipeline_impl<double>(a, prec);
 }
 

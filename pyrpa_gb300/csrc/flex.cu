@@ -1036,7 +1036,7 @@ __device__ __forceinline__ bool warp_inverse(cx<R> (&a)[N], int* piv, int* map) 
     int key = (lane < N && label >= k) ? label : 1 << 20;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      const R ov = __shfl_xor_sync(0xffffffffu, v, off);
+      const R ov = shfl_xor(v, off);
       const int ok2 = __shfl_xor_sync(0xffffffffu, key, off);
       if (ov > v || (ov == v && ok2 < key)) { v = ov; key = ok2; }
     }
@@ -1047,7 +1047,7 @@ __device__ __forceinline__ bool warp_inverse(cx<R> (&a)[N], int* piv, int* map) 
     if (lane == 0) piv[k] = plabel;
     const unsigned m = __ballot_sync(0xffffffffu, label == k && lane < N);
     const int src = __ffs(m) - 1;
-    const cx<R> pv = cmk<R>(__shfl_sync(0xffffffffu, ak.x, src), __shfl_sync(0xffffffffu, ak.y, src));
+    const cx<R> pv = cmk<R>(shfl_idx(ak.x, src), shfl_idx(ak.y, src));
     const cx<R> ip = ok ? cdiv(cmk<R>(1, 0), pv) : cmk<R>(0, 0);
     const bool is_piv = (label == k);
     // new row = base + f * (pivot row): the pivot lane scales (base 0, f = 1/p),
@@ -1055,9 +1055,9 @@ __device__ __forceinline__ bool warp_inverse(cx<R> (&a)[N], int* piv, int* map) 
     const cx<R> f = is_piv ? ip : -(ak * ip);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
-      const R sx = __shfl_sync(0xffffffffu, a[j].x, src), sy = __shfl_sync(0xffffffffu, a[j].y, src);
+      const R sx = shfl_idx(a[j].x, src), sy = shfl_idx(a[j].y, src);
       const R bx = is_piv ? (R)0 : a[j].x, by = is_piv ? (R)0 : a[j].y;
-      const cx<R> nv = cmk<R>(fma(f.x, sx, fma(-f.y, sy, bx)), fma(f.x, sy, fma(f.y, sx, by)));
+      const cx<R> nv = cmk<R>(mad(f.x, sx, mad(-f.y, sy, bx)), mad(f.x, sy, mad(f.y, sx, by)));
       a[j] = (j == k) ? f : nv;
     }
   }
@@ -1077,7 +1077,7 @@ __device__ __forceinline__ bool warp_inverse(cx<R> (&a)[N], int* piv, int* map) 
   __syncwarp();
   const int from = (lane < N) ? map[lane] : lane;
 #pragma unroll
-  for (int j = 0; j < N; ++j) a[j] = cmk<R>(__shfl_sync(0xffffffffu, a[j].x, from), __shfl_sync(0xffffffffu, a[j].y, from));
+  for (int j = 0; j < N; ++j) a[j] = cmk<R>(shfl_idx(a[j].x, from), shfl_idx(a[j].y, from));
   __syncwarp();
   return ok;
 }
@@ -1387,6 +1387,16 @@ bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double
       DBuf<R> dc(consts.size());
       dc.upload(consts.data(), consts.size());
       reset_err();
+      if constexpr (std::is_same<R, dfl>::value) {
+        switch (n) {
+          case 1: vertex_vs_launch<R, 1>(chi, nmat, estride, dc.p, mode); break;
+          case 4: vertex_vs_launch<R, 4>(chi, nmat, estride, dc.p, mode); break;
+          case 9: vertex_vs_launch<R, 9>(chi, nmat, estride, dc.p, mode); break;
+          case 16: vertex_vs_launch<R, 16>(chi, nmat, estride, dc.p, mode); break;
+          case 25: vertex_vs_launch<R, 25>(chi, nmat, estride, dc.p, mode); break;
+        }
+        return fetch_err() == 0;
+      }
       switch (n) {
         case 1: vertex_reg_launch<R, 1>(chi, nmat, estride, dc.p, mode); break;
         case 4: vertex_reg_launch<R, 4>(chi, nmat, estride, dc.p, mode); break;
@@ -1407,6 +1417,9 @@ bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double
       return fetch_err() == 0;
     }
   }
+  if constexpr (std::is_same<R, dfl>::value) {
+    throw Error("the double-float vertex supports Nchi = 1, 4, 9, 16 or 25 with invertible S and C");
+  } else {
   const size_t head = ((size_t)3 * n * n * sizeof(double) + 15) / 16 * 16;
   const size_t per_warp = (size_t)4 * n * n * sizeof(cx<R>);
   int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - head) / per_warp));
@@ -1422,6 +1435,7 @@ bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double
                                                                                      n, S, C, mode, warps);
   count_launch("vertex");
   return fetch_err() == 0;
+  }
 }
 
 template <typename R> __global__ void k_scale(cx<R>* a, long long n, R s) {
@@ -2760,6 +2774,7 @@ template void widen<dfl>(double2*, const cx<dfl>*, long long);
 template void narrow<dfl>(cx<dfl>*, const double2*, long long);
 template void mkdelta<dfl>(const Geom&, const Pairs&, const double2*, const cx<dfl>*, const double*, const double*,
                            const double*, bool, double, double2*, DeltaKernelCache<dfl>*);
+template bool vertex<dfl>(cx<dfl>*, long long, long long, int, const double*, const double*, int);
 
 }  // namespace pgb
 

@@ -334,7 +334,7 @@ def test_fp32_bulk_path(F):
 
 # ---------------------------------------------- register vertex, 16 and 25 pairs
 @pytest.mark.parametrize("Norb", [4, 5])
-@pytest.mark.parametrize("mode", ["fp64", "fp32", "fp32-reg"])
+@pytest.mark.parametrize("mode", ["fp64", "fp32", "fp32-reg", "df"])
 def test_vertex_large_orbital_counts(F, Norb, mode):
     """V_sigma and V_Delta for Nchi = 16 and 25 (the register kernels with the
     shared-memory accumulator in FP64) against the oracle."""
@@ -346,7 +346,7 @@ def test_vertex_large_orbital_counts(F, Norb, mode):
     cs = (Nchi, Nchi, Nchi, Nchi)
     chis = 0.05 * (rng.standard_normal(cs) + 1j * rng.standard_normal(cs))
     chi = 0.05 * (rng.standard_normal((Nchi, Nchi, 2, Nk)) + 1j * rng.standard_normal((Nchi, Nchi, 2, Nk)))
-    prec, tol = (64, (1e-11, 1e-14)) if mode == "fp64" else (32, (2e-5, 1e-8))
+    prec, tol = {"fp64": (64, (1e-11, 1e-14)), "df": (48, (1e-11, 1e-14))}.get(mode, (32, (2e-5, 1e-8)))
     old = os.environ.get("PYRPA_GB_VERTEX")
     F.set_precision(prec)
     try:
@@ -370,6 +370,22 @@ def test_vertex_large_orbital_counts(F, Norb, mode):
                                 m["invk"], 2, 2, 1, m["temp"], gap_sym, eps=1e-6, itemax=2, arnoldi_m=2)
         vd = FO.vdelta_nsoc_flex(chi.T, m["S"].T, m["C"].T, gap_sym >= 0).T
         close(c1, vd, 1e-11, 1e-14)
+
+
+@pytest.mark.parametrize("Norb", [1, 2, 3])
+def test_double_float_vertex_small_orbital_counts(F, Norb):
+    """The double-float V_sigma solve (precision 48 at get_vsigma) for Nchi = 1, 4, 9."""
+    m = build_model(Norb, 2, 2, 1, 2, 0.2, 0.0, seed=11, U=1.0, J=0.15)
+    rng = np.random.default_rng(Norb)
+    Nchi = Norb * Norb
+    cs = (Nchi, Nchi, Nchi, Nchi)
+    chis = 0.05 * (rng.standard_normal(cs) + 1j * rng.standard_normal(cs))
+    F.set_precision(48)
+    try:
+        v = F.get_Vsigma_nosoc_flex(chis.copy(), m["S"], m["C"])
+    finally:
+        F.set_precision(64)
+    close(v, O.get_Vsigma_nosoc_flex(chis.copy(), m["S"], m["C"]), 1e-11, 1e-14)
 
 
 # ------------------------------------------------------ mixed FP32/FP64 schedule
