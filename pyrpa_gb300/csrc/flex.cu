@@ -1180,7 +1180,8 @@ __global__ void __launch_bounds__(32 * W) k_vertex_reg(cx<R>* chi, long long nma
 // matrix holds X until both inversions are done, then X(S+C) as the scratch
 // of the sandwich term, then the result.
 template <typename R, int N, int W>
-__global__ void __launch_bounds__(32 * W) k_vertex_vs(cx<R>* chi, long long nmat, long long estride,
+__global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(cx<R>* chi, long long nmat,
+                                                                                 long long estride,
                                                       const R* consts, int mode) {
   constexpr int T = W;
   constexpr int TP = T + 1;
@@ -1330,7 +1331,9 @@ bool vertex_reg_launch(cx<R>* chi, long long nmat, long long estride, const R* d
 
 template <typename R, int N>
 bool vertex_vs_launch(cx<R>* chi, long long nmat, long long estride, const R* dconsts, int mode) {
-  constexpr int warps = 6;
+  // FP32: 8 warps a CTA held to 128 registers (no spills), two CTAs and 16
+  // warps per SM against 12 with 168 registers; 8-byte types keep 6 warps
+  constexpr int warps = sizeof(R) == 4 ? 8 : 6;
   const size_t smem = vertex_vs_smem<R, N, warps>();
   static bool attr = false;
   if (!attr) {
