@@ -150,8 +150,9 @@ __device__ void four_step_twiddle(cx<R>* buf, const PassDesc& d, long long o, bo
   const int L = d.L;
   for (int e = threadIdx.x; e < nl * L; e += blockDim.x) {
     const int b = e / L, p = e - b * L;
+    // p < L2 and k1 < L1, so p * k1 < L1 * L2 = Lfull: no reduction needed
     const long long k1 = ((contig ? o + b : o) % d.tw_L1);
-    const int t = (int)(((long long)p * k1) % d.tw_Lfull);
+    const int t = (int)((long long)p * k1);
     if (t) buf[e] = buf[e] * twid<R>(full_tab<R>(d), t, sign);
   }
 }
@@ -261,7 +262,8 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
     if (contig) { n2 = it % B; b = it / B; } else { b = it % nl; n2 = it / nl; }
     if (b >= nact) continue;
     cx<R> v[A];
-    // four-step twiddle exponent p * k1 mod Lfull in 32 bits (p < 64, k1 < L1 <= Lfull)
+    // four-step twiddle exponent p * k1: p < L2 and k1 < L1, so the product is
+    // below Lfull = L1 * L2 and indexes the table without a reduction
     const int k1o = tw4 ? (int)((contig ? o + b : o) % d.tw_L1) : 0;
 #pragma unroll
     for (int n1 = 0; n1 < A; ++n1) {
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
       const long long addr = contig ? base + (long long)b * L + p : base + (long long)p * d.S + b;
       v[n1] = arr[addr];
       if (tw4 && !d.tw_post) {
-        const int t = (p * k1o) % d.tw_Lfull;
+        const int t = p * k1o;
         if (t) v[n1] = v[n1] * twid<R>(full_tab<R>(d), t, sign);
       }
     }
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
       const int q = k1 + A * k2;
       cx<R> w = u[k2];
       if (tw4 && d.tw_post) {
-        const int t = (q * k1o) % d.tw_Lfull;
+        const int t = q * k1o;  // q < L2, k1o < L1
         if (t) w = w * twid<R>(full_tab<R>(d), t, sign);
       }
       const long long addr = contig ? base + (long long)b * L + q : base + (long long)q * d.S + b;
