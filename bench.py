@@ -49,8 +49,7 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
     p.add_argument("--precision", default="mixed", choices=["mixed", "32", "64"],
-                   help="mixed: FP32 bulk to the FP32 rounding floor, then double-float bulk with the "
-                        "FP64 vertex to eps")
+                   help="mixed: FP32 bulk to the FP32 rounding floor, then double-float bulk to eps")
     p.add_argument("--eps", type=float, default=1.0e-4)
     p.add_argument("--scf-loop", type=int, default=300)
     p.add_argument("--no-tail", action="store_true")
@@ -224,7 +223,8 @@ def main():
                 gap_sym=c["gap_sym"], eps=a.eps, scf_loop=a.scf_loop, sw_tail=tail, sw_rescale=True, coarse=coarse)
     config["warm_start"] = ("none (cold G0 start)" if coarse == (1, 1) else
                             f"coarse-mesh seed: {c['Nx'] // coarse[0]}x{c['Ny'] // coarse[0]} k mesh, "
-                            f"{c['Nw'] // coarse[1]} frequencies, FP32 bulk, interpolated to the full mesh")
+                            f"{c['Nw'] // coarse[1]} frequencies, FP32 bulk (itself seeded one level further "
+                            f"down), interpolated to the full mesh")
 
     def solve():
         return F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
@@ -281,8 +281,8 @@ def main():
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
                    "precision": {"mixed": f"FP32 bulk for {int(stats['iterations_fp32'])} iterations, double-float chi0 "
                                           f"and Sigma with FP32 vertex for {int(stats['iterations_fp64_fp32vertex'])}, "
-                                          f"then double-float chi0 and Sigma with FP64 vertex to eps; Eliashberg "
-                                          f"stage double-float chi0 and contractions with FP64 V_Delta",
+                                          f"then double-float chi0, vertex and Sigma to eps; Eliashberg stage "
+                                          f"double-float (chi0, V_Delta, contractions)",
                                  "32": "FP32 bulk", "64": "FP64"}[a.precision]})
     line = {
         "metric": METRIC, "value": value, "unit": "s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,

@@ -991,13 +991,25 @@ void run_lin_eliash(const LinEliashArgs& a) {
 // H, its eigenvalues and eigenvectors on the coarse mesh are those of the fine
 // mesh at the same k (transposed / conjugated at -k), so no hopping data is
 // needed.
-void coarse_seed(Inputs& in, const PipelineArgs& a, const FlexParams& prm, DBuf<double2>& seed, double* mu_seed) {
+// Band data of one mesh on the host, in the C-ABI layouts (H, U: (No,No,Nk), e: (No,Nk))
+struct HostBands {
+  const double2* hamk;
+  const double2* uni;
+  const double* eig;
+};
+
+// Sigma seed of the fine problem `in` from the same model solved on the mesh
+// and Matsubara set divided by (kdiv, wdiv), FP32 bulk down to its rounding
+// floor.  While the coarse problem is itself large (>= 8 points per divided
+// axis and >= 128 frequencies after another division), its own solve starts
+// from a seed made the same way one level further down.
+void coarse_seed_level(Inputs& in, const HostBands& hb, int64_t kdiv, int64_t wdiv, const FlexParams& prm,
+                       DBuf<double2>& seed, double* mu_seed, int depth) {
   const Geom& g = in.g;
   const int No = in.Norb;
-  auto div = [&](int n) { return (a.coarse_kdiv > 1 && n % a.coarse_kdiv == 0 && n / a.coarse_kdiv >= 2)
-                                     ? n / (int)a.coarse_kdiv : n; };
+  auto div = [&](int n) { return (kdiv > 1 && n % kdiv == 0 && n / kdiv >= 2) ? n / (int)kdiv : n; };
   const int Nxc = div(g.Nx), Nyc = div(g.Ny), Nzc = g.Nz > 1 ? div(g.Nz) : 1;
-  const int Nwc = std::max(1, g.Nw / (int)std::max<int64_t>(1, a.coarse_wdiv));
+  const int Nwc = std::max(1, g.Nw / (int)std::max<int64_t>(1, wdiv));
   std::vector<int64_t> kmap_c, invk_c;
   const int64_t Nkc = make_irr_mesh(Nxc, Nyc, Nzc, kmap_c, invk_c);
   Inputs ic;
@@ -1016,11 +1028,11 @@ void coarse_seed(Inputs& in, const PipelineArgs& a, const FlexParams& prm, DBuf<
     const long long gf = fx * x + (long long)g.Nx * (fy * y + (long long)g.Ny * fz * z);
     const int kf = g.h_grid_irr[gf], fl = g.h_grid_flag[gf];
     for (int e = 0; e < No * No; ++e) {
-      const double2 h = a.hamk[e + (size_t)No * No * kf], u = a.uni[e + (size_t)No * No * kf];
+      const double2 h = hb.hamk[e + (size_t)No * No * kf], u = hb.uni[e + (size_t)No * No * kf];
       hc[e + (size_t)No * No * j] = fl ? conj(h) : h;  // H(-k) = H(k)^* under time reversal
       uc[e + (size_t)No * No * j] = fl ? conj(u) : u;
     }
-    for (int n = 0; n < No; ++n) ec[n + (size_t)No * j] = a.eig[n + (size_t)No * kf];
+    for (int n = 0; n < No; ++n) ec[n + (size_t)No * j] = hb.eig[n + (size_t)No * kf];
   }
   ic.H.alloc(hc.size());
   ic.H.upload(hc.data(), hc.size());
@@ -1037,15 +1049,30 @@ void coarse_seed(Inputs& in, const PipelineArgs& a, const FlexParams& prm, DBuf<
   FlexParams pc = prm;
   pc.eps = prm.eps;
   pc.stop_at_fp32_floor = true;
+  // one level further down while the coarse problem is still large
+  DBuf<double2> seed_c;
+  double mu_cc = 0.0;
+  const bool nest = depth < 1 && kdiv > 1 && Nxc / kdiv >= 8 && Nyc / kdiv >= 8 && Nwc / std::max<int64_t>(1, wdiv) >= 128;
+  int iters_below = 0;
+  if (nest) {
+    const HostBands hbc{hc.data(), uc.data(), ec.data()};
+    coarse_seed_level(ic, hbc, kdiv, wdiv, prm, seed_c, &mu_cc, depth + 1);
+    iters_below = g_stats.iterations_coarse;
+  }
   DBuf<double2> sc((size_t)ic.g.K * No * No);
   double mu_c = 0;
   log("[FLEX] warm start on the %dx%dx%d mesh with %d frequencies\n", Nxc, Nyc, Nzc, Nwc);
-  mkself_core(ic, pc, sc.p, &mu_c, nullptr, 0.0, 0.0, kPrecMixed);
-  g_stats.iterations_coarse = g_stats.iterations;
+  mkself_core(ic, pc, sc.p, &mu_c, nest ? seed_c.p : nullptr, mu_cc, mu_cc, kPrecMixed);
+  g_stats.iterations_coarse = g_stats.iterations + iters_below;
   g_stats.iterations = g_stats.iterations32 = 0;
   seed.alloc((size_t)g.K * No * No);
-  sigma_interp(ic.g, g, sc.p, seed.p, No, a.temp);
+  sigma_interp(ic.g, g, sc.p, seed.p, No, prm.temp);
   *mu_seed = mu_c;
+}
+
+void coarse_seed(Inputs& in, const PipelineArgs& a, const FlexParams& prm, DBuf<double2>& seed, double* mu_seed) {
+  const HostBands hb{a.hamk, a.uni, a.eig};
+  coarse_seed_level(in, hb, a.coarse_kdiv, a.coarse_wdiv, prm, seed, mu_seed, 0);
 }
 
 template <typename R>
