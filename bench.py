@@ -170,6 +170,16 @@ def cpu_seconds(cfg, tail, iters, applies, rate):
 
 
 # ------------------------------------------------------------------ main
+def max_over_ranks(values, dist):
+    """Replicas: every rank solved its own instance; the job's time is the
+    slowest rank's (all-reduce MAX, then a barrier)."""
+    import torch
+    t = torch.tensor(values, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return [float(x) for x in t]
+
+
 def main():
     a = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -253,11 +263,7 @@ def main():
     stats = F.last_stats()
     value, e2e = max(dev), max(wall)
     if dist is not None:
-        import torch
-        t = torch.tensor([value, e2e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        value, e2e = float(t[0]), float(t[1])
-        dist.barrier()
+        value, e2e = max_over_ranks([value, e2e], dist)
     if rank != 0:
         return 0
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
