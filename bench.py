@@ -282,6 +282,7 @@ def main():
     rate, cores, npairs, cwall = cpu_pair_rate(c, a.cpu_pairs)
     cpu_v = cpu_seconds(c, tail, iters, applies, rate)
     config.update({"flex_iterations": iters, "eliashberg_applications": applies, "lambda": res["lam"],
+                   "lambda_top4": [float(x) for x in F.last_ritz(4)],
                    "warm_start_iterations": int(stats["iterations_coarse"]),
                    "warm_start_ms": stats["t_warm_ms"],
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],

@@ -164,6 +164,12 @@ void pyrpa_gb_kernel_launches(int64_t* n);
  * iterations of the mixed schedule's middle phase (FP64 chi0 and Sigma, FP32
  * vertex) (18 doubles) */
 void pyrpa_gb_last_stats(double* out);
+/* real parts of the Ritz values of the last Arnoldi pass of lin_eliash /
+ * lin_eliash_soc / pyrpa_gb_flex_eliash, on the operator's scale (the pass-2
+ * shift undone), largest first: *count of them are kept (at most 16), the
+ * first min(*n, *count) go to out.  The first is lambda.  No counterpart in
+ * the reference, which prints the Ritz values (feliash.f90:309-312, 365-368). */
+void pyrpa_gb_last_ritz(double* out, const int64_t* n, int64_t* count);
 void pyrpa_gb_device_info(int64_t* num_sms, int64_t* device);
 /* live timing of the FFT pass kernel: when on, every pass launch is bracketed
  * by CUDA events on the library stream; pyrpa_gb_fft_stats returns and resets

@@ -447,6 +447,11 @@ void pyrpa_gb_last_stats(double* out) {
                         (double)s.iterations_coarse, s.t_warm, s.t_stoner, (double)s.iterations_finish32};
   memcpy(out, v, sizeof(v));
 }
+void pyrpa_gb_last_ritz(double* out, const int64_t* n, int64_t* count) {
+  const LastStats& s = last_stats();
+  *count = s.nritz;
+  for (int64_t i = 0; i < std::min<int64_t>(*n, s.nritz); ++i) out[i] = s.ritz[i];
+}
 void pyrpa_gb_fft_profile(const int64_t* on) { fft_profile_enable(*on != 0); }
 void pyrpa_gb_fft_stats(double* out) {
   ABI_TRY fft_profile_collect(&out[0], &out[1], &out[2]);

@@ -786,6 +786,14 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x);
   log("  lambda_- =%12.6f\n", lambda1);
   DBuf<double2> D(KE);
+  auto keep_ritz = [&](const std::vector<double2>& e, double shift) {
+    std::vector<double> r;
+    for (const auto& z : e) r.push_back(z.x - shift);
+    std::sort(r.begin(), r.end(), [](double x, double y) { return x > y; });
+    g_stats.nritz = (int)std::min<size_t>(r.size(), 16);
+    for (int i = 0; i < g_stats.nritz; ++i) g_stats.ritz[i] = r[i];
+  };
+  keep_ritz(ev, 0.0);
   if (ev[imax].x >= 0.1) {
     lambda_out = ev[imax].x;
     log("  eliash   =%12.6f\n", lambda_out);
@@ -812,6 +820,7 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
         if (ev[i].x > ev[imax].x) imax = i;
       for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x - shift);
       lambda_out = ev[imax].x - shift;
+      keep_ritz(ev, shift);
       log("  eliash   =%12.6f\n", lambda_out);
       ritz(D.p, Hm, m_act, ev[imax]);
     }
@@ -1614,13 +1623,11 @@ void run_chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const do
   chis_chic_soc(chic, chiszz, chispm, X.p, K, (int)Nk, (int)Nchi, V.p, o1, o2, sl, ol);
 }
 
-// The Eliashberg stage (final G, chi0, V_Delta, Arnoldi) runs in FP64 except
-// in the pure FP32 mode or with PYRPA_GB_ELIASH=fp32: with FP32 bulk there,
-// lambda of the 5-orbital 64x64x2048 model moved by 3.6e-6 relative.
 // Eliashberg-stage bulk (final chi0, V_Delta, Arnoldi applies): FP32 in the
 // FP32 mode or with PYRPA_GB_ELIASH=fp32; double-float in the mixed mode
 // unless PYRPA_GB_ELIASH=fp64 (df64: double-float with the FP64 V_Delta
-// solve); FP64 otherwise.
+// solve); FP64 otherwise.  With FP32 bulk there, lambda of the 5-orbital
+// 64x64x2048 model moved by 3.6e-6 relative.
 void run_pipeline(const PipelineArgs& a, int prec) {
   const char* e = std::getenv("PYRPA_GB_ELIASH");
   const std::string ev = e ? e : "";

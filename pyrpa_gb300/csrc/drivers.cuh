@@ -128,6 +128,10 @@ struct LastStats {
   // milliseconds on the device (CUDA events on the library stream)
   double t_chi0 = 0, t_vertex = 0, t_sigma = 0, t_diis = 0, t_mu = 0, t_dyson = 0, t_apply = 0;
   double t_stoner = 0;  // Stoner factor (and the sw_rescale clamp) of the FLEX loop
+  // real parts of the last Arnoldi pass's Ritz values on the operator's own
+  // scale (the pass-2 shift undone), largest first
+  double ritz[16] = {0};
+  int nritz = 0;
 };
 
 // bulk type of each stage of a FLEX iteration: 32 FP32, 64 FP64, 48 double-float

@@ -89,6 +89,7 @@ _SIGNATURES = {
     "pyrpa_gb_regrid_sigma": [_c128, _c128, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
     "pyrpa_gb_wannier_r": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _pi, _pi],
     "pyrpa_gb_set_precision": [_pi],
+    "pyrpa_gb_last_ritz": [_f64, _pi, _pi],
     "pyrpa_gb_get_precision": [_pi],
     "pyrpa_gb_set_verbose": [_pi],
     "pyrpa_gb_last_error": [POINTER(c_char), _pi, _pi],
@@ -182,6 +183,15 @@ def last_stats() -> dict:
             "t_sigma_ms", "t_diis_ms", "t_mu_ms", "t_dyson_ms", "t_apply_ms", "iterations_fp32",
             "iterations_coarse", "t_warm_ms", "t_stoner_ms", "iterations_fp64_fp32vertex"]
     return dict(zip(keys, out[: len(keys)].tolist()))
+
+
+def last_ritz(n: int = 4):
+    """Largest real parts of the last Arnoldi pass's Ritz values (the first is
+    lambda); fewer than n when the Krylov space was smaller."""
+    out = np.zeros(max(1, n))
+    count = c_int64(0)
+    load_library().pyrpa_gb_last_ritz(out, i64(n), byref(count))
+    return out[: min(n, count.value)].copy()
 
 
 def fft_profile(on: bool) -> None:
