@@ -356,6 +356,65 @@ void pyrpa_gb_wannier_r(double* out, const double* data, const int64_t* kmap, co
                         const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* Nk_data,
                         const int64_t* Nw, const int64_t* Norb, const int64_t* Ncut);
 
+/* ------------------------------------------------ coarse-mesh seed --- */
+/* No counterpart in the reference (a pyrpa user seeds mkself by hand through
+ * sigma.bin, fself.f90:742-780).  sig_c (Nk_c,Nw_c,Norb,Norb) on the coarse
+ * irreducible mesh (kmap_c, invk_c) -> sig_f (Nk_f,Nw_f,Norb,Norb) on the fine
+ * one: Fourier interpolation over k (each coarse axis divides the fine one;
+ * an even axis's Nyquist plane is split in half), and for n >= Nw_c the
+ * c0 + c1/(i w) tail through the coarse frequencies 3 Nw_c / 4 and Nw_c - 2
+ * (0-based), as plibs.regrid_sigma_bin (libs/plibs/_calc.py:52-182) extends
+ * its tail.  Norb <= 8. */
+void pyrpa_gb_sigma_interp(double* sig_f, const double* sig_c, const int64_t* kmap_c, const int64_t* invk_c,
+                           const int64_t* Nx_c, const int64_t* Ny_c, const int64_t* Nz_c, const int64_t* Nk_c,
+                           const int64_t* Nw_c, const int64_t* kmap_f, const int64_t* invk_f, const int64_t* Nx_f,
+                           const int64_t* Ny_f, const int64_t* Nz_f, const int64_t* Nk_f, const int64_t* Nw_f,
+                           const int64_t* Norb, const double* temp);
+
+/* ----------------------------------------------- learned warm start --- */
+/* No counterpart in the reference.  A network refines the interpolated seed
+ * Sigma before the fine FLEX loop.  One row per (k, n, band i, band j) of the
+ * fine mesh: 16 features of U^dagger Sigma_seed U, the band energies, w_n and
+ * the model's descriptors desc[9] = {U, J, T, fill, Stoner factor of the
+ * coarse solve, mu of the coarse solve, band width W, max |Sigma_seed|,
+ * Norb} -> 16 -> 64 -> 64 -> 2 (tanh) -> the band-basis correction in units
+ * of max |Sigma_seed|.  FP32 weights (5378, flat: W1[64][16], b1, W2[64][64],
+ * b2, W3[2][64], b3), bf16 inputs and activations, FP32 gradients, Adam.
+ * A handle names one network with its training rows in HBM.  Arrays in the
+ * layouts above: sigma (Nk,Nw,Norb,Norb), uni (Norb,Norb,Nk), eig (Norb,Nk);
+ * kn [npairs][2] = (k, n) 0-based.  Norb <= 8. */
+void pyrpa_gb_lws_create(int64_t* handle);
+void pyrpa_gb_lws_destroy(const int64_t* handle);
+/* theta[n], n = 5378; setting the parameters resets the Adam state */
+void pyrpa_gb_lws_set_params(const int64_t* handle, const float* theta, const int64_t* n);
+void pyrpa_gb_lws_get_params(const int64_t* handle, float* theta, const int64_t* n);
+/* appends npairs * Norb^2 rows (features of sig_seed, targets sig_fine - sig_seed) */
+void pyrpa_gb_lws_add_samples(const int64_t* handle, const double* sig_seed, const double* sig_fine,
+                              const double* uni, const double* eig, const int64_t* kn, const int64_t* npairs,
+                              const int64_t* Nk, const int64_t* Nw, const int64_t* Nw_c, const int64_t* Norb,
+                              const double* desc);
+void pyrpa_gb_lws_clear_samples(const int64_t* handle);
+void pyrpa_gb_lws_num_samples(const int64_t* handle, int64_t* rows);
+/* x [rows][16] (the bf16 features as float), t [rows][2] when sig_fine is not NULL */
+void pyrpa_gb_lws_features(float* x, float* t, const double* sig_seed, const double* sig_fine, const double* uni,
+                           const double* eig, const int64_t* kn, const int64_t* npairs, const int64_t* Nk,
+                           const int64_t* Nw, const int64_t* Nw_c, const int64_t* Norb, const double* desc);
+/* y [rows][2] of x [rows][16] */
+void pyrpa_gb_lws_forward(const int64_t* handle, const float* x, const int64_t* rows, float* y);
+/* mean over the training rows of sum (y - t)^2, and its gradient grad[5378] */
+void pyrpa_gb_lws_loss_grad(const int64_t* handle, double* loss, float* grad);
+/* one Adam step with the whole training set's gradient; loss before the step */
+void pyrpa_gb_lws_step(const int64_t* handle, const double* lr, const double* beta1, const double* beta2,
+                       const double* eps, double* loss);
+/* steps Adam steps on batches drawn uniformly with replacement (mt19937_64(seed)); loss[steps] */
+void pyrpa_gb_lws_train(const int64_t* handle, const int64_t* steps, const int64_t* batch, const double* lr,
+                        const double* beta1, const double* beta2, const double* eps, const int64_t* seed,
+                        double* loss);
+/* sigma (in place) += U (max|sigma| * y) U^dagger at every (k, n) */
+void pyrpa_gb_lws_apply(const int64_t* handle, double* sigma, const double* uni, const double* eig,
+                        const int64_t* Nk, const int64_t* Nw, const int64_t* Nw_c, const int64_t* Norb,
+                        const double* desc);
+
 /* Allocation-free variant of get_eig_or_tr_chi.  No counterpart in the reference.
  * All pointers are DEVICE pointers in the layouts of get_eig_or_tr_chi: chi
  * (Nk,Nchi,Nchi) complex128, invk (3,Nkall) int64, chiqout (Nkall) complex128.

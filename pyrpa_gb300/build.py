@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libfmod.so"
-SOURCES = ["fft.cu", "flex.cu", "drivers.cu", "abi.cu"]
+SOURCES = ["fft.cu", "flex.cu", "drivers.cu", "lws.cu", "abi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

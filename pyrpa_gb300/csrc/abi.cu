@@ -22,6 +22,7 @@
 #include "drivers.cuh"
 #include "flex.cuh"
 #include "linalg.cuh"
+#include "lws.cuh"
 
 namespace pgb {
 
@@ -79,6 +80,11 @@ template <typename T> void nan_fill(T* p, size_t n) {
   const double q = std::numeric_limits<double>::quiet_NaN();
   double* d = reinterpret_cast<double*>(p);
   for (size_t i = 0; i < n * sizeof(T) / sizeof(double); ++i) d[i] = q;
+}
+
+void nan_fill_f(float* p, size_t n) {
+  if (!p) return;
+  for (size_t i = 0; i < n; ++i) p[i] = std::numeric_limits<float>::quiet_NaN();
 }
 
 // FP32 bulk for every entry point except FP64 mode (the mixed schedule only
@@ -869,6 +875,106 @@ void pyrpa_gb_wannier_r(double2* out, const double2* data, const int64_t* kmap, 
   o.download(out, n_out);
   sync();
   ABI_CATCH("pyrpa_gb_wannier_r", nan_fill(out, (size_t)((*Nx) * (*Ny) * (*Nz) * std::min(*Ncut, *Nw) * (*Norb) * (*Norb))))
+}
+
+// ------------------------------------------------- coarse-mesh seed --
+void pyrpa_gb_sigma_interp(double2* sig_f, const double2* sig_c, const int64_t* kmap_c, const int64_t* invk_c,
+                           const int64_t* Nx_c, const int64_t* Ny_c, const int64_t* Nz_c, const int64_t* Nk_c,
+                           const int64_t* Nw_c, const int64_t* kmap_f, const int64_t* invk_f, const int64_t* Nx_f,
+                           const int64_t* Ny_f, const int64_t* Nz_f, const int64_t* Nk_f, const int64_t* Nw_f,
+                           const int64_t* Norb, const double* temp) {
+  ABI_TRY
+  ensure_context();
+  const int64_t no = *Norb;
+  PGB_CHECK(no >= 1 && no <= 8, "Norb must be in [1, 8]");
+  PGB_CHECK(*Nw_c >= 1 && *Nw_f >= *Nw_c, "the fine Matsubara set must hold the coarse one");
+  const int64_t nchi = no * no <= kMaxChi ? no * no : 1;
+  Geom gc, gf;
+  build_geom(gc, kmap_c, invk_c, *Nx_c, *Ny_c, *Nz_c, *Nk_c, *Nw_c, no, nchi);
+  build_geom(gf, kmap_f, invk_f, *Nx_f, *Ny_f, *Nz_f, *Nk_f, *Nw_f, no, nchi);
+  const size_t nc = (size_t)(*Nk_c) * (*Nw_c) * no * no, nf = (size_t)(*Nk_f) * (*Nw_f) * no * no;
+  DBuf<double2> c(nc), f(nf);
+  c.upload(sig_c, nc);
+  sigma_interp(gc, gf, c.p, f.p, (int)no, *temp);
+  f.download(sig_f, nf);
+  sync();
+  ABI_CATCH("pyrpa_gb_sigma_interp", nan_fill(sig_f, (size_t)(*Nk_f) * (*Nw_f) * (*Norb) * (*Norb)))
+}
+
+// --------------------------------------------------- learned warm start --
+static LwsDesc lws_desc(const double* d) { return LwsDesc{d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]}; }
+
+void pyrpa_gb_lws_create(int64_t* handle) {
+  ABI_TRY *handle = lws_create();
+  ABI_CATCH("pyrpa_gb_lws_create", *handle = 0)
+}
+void pyrpa_gb_lws_destroy(const int64_t* handle) {
+  ABI_TRY lws_destroy(*handle);
+  ABI_CATCH("pyrpa_gb_lws_destroy", (void)0)
+}
+void pyrpa_gb_lws_set_params(const int64_t* handle, const float* theta, const int64_t* n) {
+  ABI_TRY ensure_context(); lws_set_params(lws_get(*handle), theta, *n);
+  ABI_CATCH("pyrpa_gb_lws_set_params", (void)0)
+}
+void pyrpa_gb_lws_get_params(const int64_t* handle, float* theta, const int64_t* n) {
+  ABI_TRY ensure_context(); lws_get_params(lws_get(*handle), theta, *n);
+  ABI_CATCH("pyrpa_gb_lws_get_params", nan_fill_f(theta, (size_t)*n))
+}
+void pyrpa_gb_lws_add_samples(const int64_t* handle, const double2* sig_seed, const double2* sig_fine,
+                              const double2* uni, const double* eig, const int64_t* kn, const int64_t* npairs,
+                              const int64_t* Nk, const int64_t* Nw, const int64_t* Nw_c, const int64_t* Norb,
+                              const double* desc) {
+  ABI_TRY
+  ensure_context();
+  lws_add_samples(lws_get(*handle), sig_seed, sig_fine, uni, eig, kn, *npairs, (int)*Nk, (int)*Nw, (int)*Nw_c,
+                  (int)*Norb, lws_desc(desc));
+  ABI_CATCH("pyrpa_gb_lws_add_samples", (void)0)
+}
+void pyrpa_gb_lws_clear_samples(const int64_t* handle) {
+  ABI_TRY ensure_context(); lws_clear_samples(lws_get(*handle));
+  ABI_CATCH("pyrpa_gb_lws_clear_samples", (void)0)
+}
+void pyrpa_gb_lws_num_samples(const int64_t* handle, int64_t* rows) {
+  ABI_TRY *rows = lws_get(*handle).M;
+  ABI_CATCH("pyrpa_gb_lws_num_samples", *rows = -1)
+}
+void pyrpa_gb_lws_features(float* x, float* t, const double2* sig_seed, const double2* sig_fine, const double2* uni,
+                           const double* eig, const int64_t* kn, const int64_t* npairs, const int64_t* Nk,
+                           const int64_t* Nw, const int64_t* Nw_c, const int64_t* Norb, const double* desc) {
+  ABI_TRY
+  lws_features_host(x, t, sig_seed, sig_fine, uni, eig, kn, *npairs, (int)*Nk, (int)*Nw, (int)*Nw_c, (int)*Norb,
+                    lws_desc(desc));
+  ABI_CATCH("pyrpa_gb_lws_features", nan_fill_f(x, (size_t)(*npairs) * (*Norb) * (*Norb) * kLwsNF))
+}
+void pyrpa_gb_lws_forward(const int64_t* handle, const float* x, const int64_t* rows, float* y) {
+  ABI_TRY ensure_context(); lws_forward_host(lws_get(*handle), x, *rows, y);
+  ABI_CATCH("pyrpa_gb_lws_forward", nan_fill_f(y, (size_t)(*rows) * 2))
+}
+void pyrpa_gb_lws_loss_grad(const int64_t* handle, double* loss, float* grad) {
+  ABI_TRY ensure_context(); *loss = lws_loss_grad(lws_get(*handle), grad);
+  ABI_CATCH("pyrpa_gb_lws_loss_grad", (*loss = std::numeric_limits<double>::quiet_NaN(),
+                                       nan_fill_f(grad, (size_t)kLwsNParam)))
+}
+void pyrpa_gb_lws_step(const int64_t* handle, const double* lr, const double* beta1, const double* beta2,
+                       const double* eps, double* loss) {
+  ABI_TRY ensure_context(); lws_step_full(lws_get(*handle), *lr, *beta1, *beta2, *eps, loss);
+  ABI_CATCH("pyrpa_gb_lws_step", *loss = std::numeric_limits<double>::quiet_NaN())
+}
+void pyrpa_gb_lws_train(const int64_t* handle, const int64_t* steps, const int64_t* batch, const double* lr,
+                        const double* beta1, const double* beta2, const double* eps, const int64_t* seed,
+                        double* loss) {
+  ABI_TRY
+  ensure_context();
+  lws_train(lws_get(*handle), *steps, *batch, *lr, *beta1, *beta2, *eps, (uint64_t)*seed, loss);
+  ABI_CATCH("pyrpa_gb_lws_train", nan_fill(loss, (size_t)std::max<int64_t>(0, *steps)))
+}
+void pyrpa_gb_lws_apply(const int64_t* handle, double2* sigma, const double2* uni, const double* eig,
+                        const int64_t* Nk, const int64_t* Nw, const int64_t* Nw_c, const int64_t* Norb,
+                        const double* desc) {
+  ABI_TRY
+  ensure_context();
+  lws_apply(lws_get(*handle), sigma, uni, eig, (int)*Nk, (int)*Nw, (int)*Nw_c, (int)*Norb, lws_desc(desc));
+  ABI_CATCH("pyrpa_gb_lws_apply", nan_fill(sigma, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
 }
 
 void eliashberg(double2* delta, double2* sigmak, double2* Gk, const double2* hamk, const double* Smat,

@@ -25,6 +25,8 @@ _c128 = np.ctypeslib.ndpointer(dtype=np.complex128)
 _f64 = np.ctypeslib.ndpointer(dtype=np.float64)
 _i64 = np.ctypeslib.ndpointer(dtype=np.int64)
 _i32 = np.ctypeslib.ndpointer(dtype=np.int32)
+_f32 = np.ctypeslib.ndpointer(dtype=np.float32)
+_vp = ctypes.c_void_p
 _pi = POINTER(c_int64)
 _pd = POINTER(c_double)
 _pb = POINTER(c_bool)
@@ -88,6 +90,21 @@ _SIGNATURES = {
     + [_pb, _pb, _pi, _pi, _pi, _pd, _i64],
     "pyrpa_gb_regrid_sigma": [_c128, _c128, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
     "pyrpa_gb_wannier_r": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _pi, _pi],
+    "pyrpa_gb_sigma_interp": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _i64, _i64, _pi, _pi, _pi, _pi, _pi,
+                              _pi, _pd],
+    "pyrpa_gb_lws_create": [_pi],
+    "pyrpa_gb_lws_destroy": [_pi],
+    "pyrpa_gb_lws_set_params": [_pi, _f32, _pi],
+    "pyrpa_gb_lws_get_params": [_pi, _f32, _pi],
+    "pyrpa_gb_lws_add_samples": [_pi, _c128, _c128, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi, _f64],
+    "pyrpa_gb_lws_clear_samples": [_pi],
+    "pyrpa_gb_lws_num_samples": [_pi, _pi],
+    "pyrpa_gb_lws_features": [_f32, _vp, _c128, _vp, _c128, _f64, _i64, _pi, _pi, _pi, _pi, _pi, _f64],
+    "pyrpa_gb_lws_forward": [_pi, _f32, _pi, _f32],
+    "pyrpa_gb_lws_loss_grad": [_pi, _pd, _f32],
+    "pyrpa_gb_lws_step": [_pi, _pd, _pd, _pd, _pd, _pd],
+    "pyrpa_gb_lws_train": [_pi, _pi, _pi, _pd, _pd, _pd, _pd, _pi, _f64],
+    "pyrpa_gb_lws_apply": [_pi, _c128, _c128, _f64, _pi, _pi, _pi, _pi, _f64],
     "pyrpa_gb_set_precision": [_pi],
     "pyrpa_gb_last_ritz": [_f64, _pi, _pi],
     "pyrpa_gb_get_precision": [_pi],
@@ -431,6 +448,24 @@ def regrid_sigma(sigmak, temp_old: float, temp_new: float, Nw_new: int, w_scale:
     out = np.zeros((Norb, Norb, Nw_new, Nk), dtype=np.complex128)
     _call("pyrpa_gb_regrid_sigma", out, sigmak, i64(Nk), i64(Nw_old), i64(Nw_new), i64(Norb), dbl(temp_old),
           dbl(temp_new), dbl(w_scale))
+    return out
+
+
+def sigma_interp(sigmak_c, kmap_c, invk_c, Nx_c: int, Ny_c: int, Nz_c: int, kmap_f, invk_f, Nx_f: int,
+                 Ny_f: int, Nz_f: int, Nk_f: int, Nw_f: int, temp: float):
+    """Sigma of a coarse solve [Norb, Norb, Nw_c, Nk_c] (the wrappers' layout)
+    on a finer irreducible mesh: Fourier interpolation over k (each coarse
+    axis length divides the fine one; Sigma(-k) = Sigma(k)^T fills the coarse
+    grid) and c0 + c1/(i w) through two interior coarse frequencies beyond
+    the coarse Matsubara set.  Returns [Norb, Norb, Nw_f, Nk_f].  This is the
+    seed step of the coarse-mesh warm start; the reference has none."""
+    sigmak_c = np.ascontiguousarray(sigmak_c, dtype=np.complex128)
+    Norb, _, Nw_c, Nk_c = sigmak_c.shape
+    out = np.zeros((Norb, Norb, Nw_f, Nk_f), dtype=np.complex128)
+    _call("pyrpa_gb_sigma_interp", out, sigmak_c, np.ascontiguousarray(kmap_c, dtype=np.int64),
+          np.ascontiguousarray(invk_c, dtype=np.int64), i64(Nx_c), i64(Ny_c), i64(Nz_c), i64(Nk_c), i64(Nw_c),
+          np.ascontiguousarray(kmap_f, dtype=np.int64), np.ascontiguousarray(invk_f, dtype=np.int64), i64(Nx_f),
+          i64(Ny_f), i64(Nz_f), i64(Nk_f), i64(Nw_f), i64(Norb), dbl(temp))
     return out
 
 
