@@ -392,7 +392,7 @@ StagePrec mix_judge_prec() {
 }
 
 // PYRPA_GB_MIX_DIIS=keep keeps the FP32-phase DIIS history across the switch
-// to FP64 bulk (default: a fresh history)
+// to the middle phase's wider bulk (default: a fresh history)
 bool mix_diis_reset() {
   const char* s = std::getenv("PYRPA_GB_MIX_DIIS");
   return !(s && std::string(s) == "keep");
@@ -408,9 +408,11 @@ int fp32_stage_mask() {
          (v.find("sigma") != std::string::npos ? 4 : 0);
 }
 
-// prec: 64 FP64 bulk, 32 FP32 bulk, kPrecMixed FP32 bulk until the residual
-// reaches the FP32 rounding floor, then FP64 bulk until eps (convergence is
-// only declared on an FP64 iteration).
+// prec: 64 FP64 bulk, 48 double-float chi0 and Sigma, 32 FP32 bulk,
+// kPrecMixed the three-phase schedule: FP32 bulk until the residual reaches
+// the FP32 rounding floor, then double-float chi0 and Sigma with an FP32
+// vertex, then the judging iterations (double-float throughout by default,
+// mix_judge_prec); convergence is only declared in the judging phase.
 void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_out, const double2* seed,
                  double seed_mu, double seed_mu_old, int prec) {
   cudaStream_t st = ctx().stream;

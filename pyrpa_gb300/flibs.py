@@ -170,10 +170,13 @@ MIXED = 3264
 
 
 def set_precision(bits: int) -> None:
-    """64: FP64 everywhere (the reference's arithmetic); 32: complex FP32 FFTs,
+    """64: FP64 everywhere (the reference's arithmetic); 48: double-float chi0
+    and Sigma convolutions, FP64 elsewhere; 32: complex FP32 FFTs,
     contractions and vertex solves, FP64 for G, Sigma, mu, DIIS and lambda;
-    3264 (MIXED): as 32, but the FLEX loop finishes on FP64 bulk once its
-    residual reaches the FP32 rounding floor."""
+    3264 (MIXED): the FLEX loop runs FP32 bulk to the FP32 rounding floor,
+    then double-float chi0 and Sigma with an FP32 vertex, then double-float
+    judging iterations; the fused solve's Eliashberg stage is double-float.
+    Other entry points run as in 32."""
     load_library().pyrpa_gb_set_precision(i64(bits))
 
 
