@@ -661,10 +661,10 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
         const int from = phase;
         phase = (phase == 0 && finish_mask != 0) ? 1 : 2;
         log("[FLEX] residual%9.2E: continuing with %s\n", esterr,
-            phase == 1 ? "chi0 and Sigma on FP64 bulk" : "FP64 bulk");
+            phase == 1 ? "wider chi0 and Sigma, FP32 vertex" : "the judging iterations");
         if (from == 0 && mix_diis_reset()) {
           // the FP32 entries carry the FP32 rounding floor in their residuals;
-          // the FP64 phases start a fresh history from the current Sigma
+          // the later phases start a fresh history from the current Sigma
           n_hist = 0;
           i_hist = 0;
         }
