@@ -19,10 +19,13 @@ pairs, keeps a copy of the parameters and runs the solves.
 
 The reference has no counterpart: a pyrpa user seeds mkself by hand through
 sigma.bin (fself.f90:742-780) after plibs.regrid_sigma_bin.
+
+    python -m pyrpa_gb300.warmstart --train 8 --test 4     # train and measure
 """
 from __future__ import annotations
 
 import ctypes
+import time
 from ctypes import byref, c_double, c_int64
 from pathlib import Path
 
@@ -253,3 +256,102 @@ def learned_seed(net: LearnedWarmStart, m: dict, coarse: dict):
     s = interpolated_seed(m, coarse)
     desc = seed_descriptors(m, coarse, s)
     return net.apply(s, m["uni"], m["eig"], coarse["model"]["cfg"]["Nw"], desc), coarse["mu"]
+
+
+# ---------------------------------------------------------- measurement
+def family(count: int, seed: int = 0, Norb: int = 5, N: int = 64, Nw: int = 2048):
+    """Models of the 5-orbital family on one mesh with the sweep's parameter
+    ranges (U / U_Stoner, T, filling), as sweep.Instance records."""
+    from . import sweep
+    return [sweep.Instance(index=x.index, Norb=Norb, N=N, Nw=Nw, seed=x.seed, u_frac=x.u_frac, temp=x.temp,
+                           n_per_orb=x.n_per_orb) for x in sweep.draw(count, seed)]
+
+
+def _prepared(inst, U: float) -> dict:
+    from . import models
+    return models.prepare("c2", Norb=inst.Norb, Nx=inst.N, Ny=inst.N, Nz=1, Nw=inst.Nw, temp=inst.temp,
+                          fill=inst.fill, U=U, J=U / 6.0, seed=inst.seed, bandwidth=4.0)
+
+
+def _fused(m: dict, eps: float, sigma_seed=None, mu_seed: float = 0.0) -> dict:
+    """The fused FLEX + Eliashberg solve of m from G0 or from a seed; FLEX
+    iterations and the device seconds of the FLEX stages."""
+    c = m["cfg"]
+    t0 = time.perf_counter()
+    r = F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["init"],
+                      m["plist"], m["mu"], c["fill"], c["temp"], c["Nw"], c["Nx"], c["Ny"], c["Nz"], c["gap_sym"],
+                      eps=eps, sigma_seed=sigma_seed, seed_mu=mu_seed, seed_mu_old=mu_seed)
+    wall = time.perf_counter() - t0
+    st = F.last_stats()
+    flex_ms = sum(st[k] for k in ("t_chi0_ms", "t_vertex_ms", "t_sigma_ms", "t_diis_ms", "t_mu_ms", "t_dyson_ms",
+                                  "t_stoner_ms"))
+    return dict(sigmak=r["sigmak"], mu=r["mu"], lam=r["lam"], iterations=int(st["iterations"]),
+                esterr=st["esterr"], flex_s=flex_ms / 1e3, wall_s=wall)
+
+
+def main(argv=None):
+    """Train the network on solved models of the family and time the fine
+    loop of held-out models from the interpolated and the learned seed,
+    beside the cold start."""
+    import argparse
+    import json
+
+    from . import sweep
+    ap = argparse.ArgumentParser(description="learned warm start: train and measure")
+    ap.add_argument("--train", type=int, default=8)
+    ap.add_argument("--test", type=int, default=4)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--mesh", type=int, default=64)
+    ap.add_argument("--nw", type=int, default=2048)
+    ap.add_argument("--kdiv", type=int, default=4)
+    ap.add_argument("--wdiv", type=int, default=4)
+    ap.add_argument("--eps", type=float, default=1e-6)
+    ap.add_argument("--pairs", type=int, default=200000, help="(k, n) pairs per training model")
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--batch", type=int, default=8192)
+    ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "64"])
+    ap.add_argument("--save", default=None)
+    a = ap.parse_args(argv)
+    F.load_library()
+    F.set_verbose(0)
+    F.set_precision(F.MIXED if a.precision == "mixed" else 64)
+    insts = family(a.train + a.test, a.seed, N=a.mesh, Nw=a.nw)
+    net = LearnedWarmStart(seed=a.seed)
+    held = []
+    for i, inst in enumerate(insts):
+        U = inst.u_frac * sweep.stoner_u(inst)
+        m = _prepared(inst, U)
+        coarse = coarse_solution(m, a.kdiv, a.wdiv, eps=a.eps)
+        cold = _fused(m, a.eps)
+        rec = dict(index=inst.index, U=U, temp=inst.temp, fill=inst.fill, cold_iterations=cold["iterations"],
+                   cold_flex_s=cold["flex_s"], coarse_iterations=coarse["iterations"])
+        if i < a.train:
+            rec["rows"] = add_training_solution(net, m, coarse, cold["sigmak"], a.pairs, seed=inst.index)
+        else:
+            held.append((inst, m, coarse, cold))
+        print(json.dumps(rec), flush=True)
+    t0 = time.perf_counter()
+    losses = net.train(a.steps, a.batch, a.lr, seed=a.seed)
+    print(json.dumps(dict(train_s=time.perf_counter() - t0, loss_first=float(losses[0]),
+                          loss_last=float(np.mean(losses[-50:])))), flush=True)
+    if a.save:
+        net.save(a.save)
+    for inst, m, coarse, cold in held:
+        s_int = interpolated_seed(m, coarse)
+        s_lrn, mu_c = learned_seed(net, m, coarse)
+        ri = _fused(m, a.eps, s_int, mu_c)
+        rl = _fused(m, a.eps, s_lrn, mu_c)
+        nrm = np.linalg.norm(cold["sigmak"])
+        print(json.dumps(dict(
+            index=inst.index, seed_err_interp=float(np.linalg.norm(s_int - cold["sigmak"]) / nrm),
+            seed_err_learned=float(np.linalg.norm(s_lrn - cold["sigmak"]) / nrm),
+            iterations=dict(cold=cold["iterations"], interp=ri["iterations"], learned=rl["iterations"]),
+            flex_s=dict(cold=cold["flex_s"], interp=ri["flex_s"], learned=rl["flex_s"]),
+            coarse_iterations=coarse["iterations"],
+            lambda_rel_diff=dict(interp=abs(ri["lam"] - cold["lam"]) / abs(cold["lam"]),
+                                 learned=abs(rl["lam"] - cold["lam"]) / abs(cold["lam"])))), flush=True)
+
+
+if __name__ == "__main__":
+    main()
