@@ -3,6 +3,8 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <cstdlib>
+#include <string>
 #include <tuple>
 
 #include "fft.cuh"
@@ -24,6 +26,10 @@ template <typename R> __device__ __forceinline__ const cx<R>* full_tab(const Pas
 template <> __device__ __forceinline__ const double2* full_tab<double>(const PassDesc& d) { return d.tw_full; }
 template <> __device__ __forceinline__ const float2* full_tab<float>(const PassDesc& d) { return d.tw_full_f; }
 template <> __device__ __forceinline__ const cdf* line_tab<dfl>(const PassDesc& d) { return d.tw_line_d; }
+template <typename R> __device__ __forceinline__ const cx<R>* line_tab_y(const PassDesc& d);
+template <> __device__ __forceinline__ const double2* line_tab_y<double>(const PassDesc& d) { return d.tw_line_y; }
+template <> __device__ __forceinline__ const float2* line_tab_y<float>(const PassDesc& d) { return d.tw_line_y_f; }
+template <> __device__ __forceinline__ const cdf* line_tab_y<dfl>(const PassDesc& d) { return d.tw_line_y_d; }
 template <> __device__ __forceinline__ const cdf* full_tab<dfl>(const PassDesc& d) { return d.tw_full_d; }
 // double-float roots: one 16-byte read-only load {re.hi, re.lo, im.hi, im.lo}
 template <> __device__ __forceinline__ cdf twid<dfl>(const cdf* tab, int t, int sign) {
@@ -141,6 +147,83 @@ __device__ void stage(const cx<R>* in, cx<R>* out, int L, int Ns, int nl, int si
     const int idxD = (j / Ns) * Ns * RAD + jj;
 #pragma unroll
     for (int r = 0; r < RAD; ++r) lo[idxD + r * Ns] = v[r];
+  }
+}
+
+// The same stage over nl lines whose line b starts at b * ls and whose
+// element j sits at j * es (the plane pass's rows and columns).
+template <typename R, int RAD>
+__device__ void stage_strided(const cx<R>* in, cx<R>* out, int L, int Ns, int nl, int es, int ls, int sign,
+                              const cx<R>* tab) {
+  const int nbf = L / RAD;
+  const int total = nl * nbf;
+  const int tstride = L / (Ns * RAD);
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int b = idx / nbf;
+    const int j = idx - b * nbf;
+    const cx<R>* li = in + (size_t)b * ls;
+    cx<R>* lo = out + (size_t)b * ls;
+    const int jj = j % Ns;
+    cx<R> v[RAD];
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) {
+      v[r] = li[(size_t)(j + r * nbf) * es];
+      if (r > 0 && jj > 0) v[r] = v[r] * twid<R>(tab, r * jj * tstride, sign);
+    }
+    Dft<R, RAD>::run(v, sign, tab, L);
+    const int idxD = (j / Ns) * Ns * RAD + jj;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) lo[(size_t)(idxD + r * Ns) * es] = v[r];
+  }
+}
+
+// All stages of one axis of the plane, ping-ponging in/out (swapped on return
+// so that `in` holds the result).
+template <typename R>
+__device__ void plane_axis(cx<R>*& in, cx<R>*& out, int L, int nl, int es, int ls, int nst, const int* radix,
+                           int sign, const cx<R>* tab) {
+  int Ns = 1;
+  for (int st = 0; st < nst; ++st) {
+    const int rad = radix[st];
+    switch (rad) {
+      case 2: stage_strided<R, 2>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      case 3: stage_strided<R, 3>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      case 4: stage_strided<R, 4>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      case 5: stage_strided<R, 5>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      case 7: stage_strided<R, 7>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      case 8: stage_strided<R, 8>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      case 11: stage_strided<R, 11>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      case 13: stage_strided<R, 13>(in, out, L, Ns, nl, es, ls, sign, tab); break;
+      default: break;
+    }
+    __syncthreads();
+    cx<R>* t = in;
+    in = out;
+    out = t;
+    Ns *= rad;
+  }
+}
+
+// x and y axes of one (x, y) plane per CTA: the plane is read once
+// (contiguous), transformed along its rows (stride 1) and columns (stride
+// nx + 1, the padded row length) in shared memory, and written once.
+template <typename R>
+__global__ void __launch_bounds__(256) fft_plane_kernel(cx<R>* data, long long P, PassDesc d, int sign) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = d.L, ny = d.ny, sx = nx + 1, n = nx * ny;
+  cx<R>* in = reinterpret_cast<cx<R>*>(smem_raw);
+  cx<R>* out = in + (size_t)ny * sx;
+  cx<R>* arr = data + (long long)blockIdx.y * P + (long long)blockIdx.x * n;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const int y = e / nx, x = e - y * nx;
+    in[y * sx + x] = arr[e];
+  }
+  __syncthreads();
+  plane_axis<R>(in, out, nx, ny, 1, sx, d.nst, d.radix, sign, line_tab<R>(d));
+  plane_axis<R>(in, out, ny, nx, sx, 1, d.nst_y, d.radix_y, sign, line_tab_y<R>(d));
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const int y = e / nx, x = e - y * nx;
+    arr[e] = in[y * sx + x];
   }
 }
 
@@ -470,6 +553,14 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
   return d;
 }
 
+constexpr int kMaxPlaneSide = 64;  // two padded 64 x 65 planes of 16-byte elements fit in 227 KB
+
+// PYRPA_GB_FFT_PLANE=1 transforms x and y in one plane pass
+bool plane_pass_enabled() {
+  const char* s = std::getenv("PYRPA_GB_FFT_PLANE");
+  return s && std::string(s) == "1";
+}
+
 int split_length(int n) {
   // L1 * L2 = n with both <= kMaxLine, L1 as close to sqrt(n) as possible
   int best = -1;
@@ -552,6 +643,29 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
     for (int p = 0; p < n; ++p) m.rev[p] = m.pos[(n - m.logical[p]) % n];
     S *= n;
   }
+  // x and y in one plane pass (opt-in)
+  if (plane_pass_enabled() && nx >= 2 && ny >= 2 && nx <= kMaxPlaneSide && ny <= kMaxPlaneSide) {
+    PassDesc pl{};
+    pl.plane = 1;
+    pl.L = nx;
+    pl.ny = ny;
+    pl.S = 1;
+    pl.O = P_ / ((long long)nx * ny);
+    pl.B = 1;
+    if (factor_line(nx, pl.radix, &pl.nst) && factor_line(ny, pl.radix_y, &pl.nst_y)) {
+      pl.tw_line = twiddle_table(nx);
+      pl.tw_line_f = twiddle_table_f(nx);
+      pl.tw_line_d = twiddle_table_d(nx);
+      pl.tw_line_y = twiddle_table(ny);
+      pl.tw_line_y_f = twiddle_table_f(ny);
+      pl.tw_line_y_d = twiddle_table_d(ny);
+      // sides <= 64 are direct passes, so x and y are the first two passes of every list
+      for (auto* v : {&fwd_, &bwd_, &fwd_space_, &bwd_space_}) {
+        v->erase(v->begin(), v->begin() + 2);
+        v->insert(v->begin(), pl);
+      }
+    }
+  }
   // device tables
   std::vector<int> h;
   for (int a = 0; a < 4; ++a) {
@@ -576,9 +690,10 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
     attr_set = true;
   }
   for (const PassDesc& d : passes) {
-    const long long tiles = (d.S == 1) ? (d.O + d.B - 1) / d.B : d.O * ((d.S + d.B - 1) / d.B);
-    const size_t smem = d.fa ? (size_t)d.B * d.fa * (d.fb + 1) * sizeof(cx<R>)
-                             : 2 * (size_t)d.B * d.L * sizeof(cx<R>);
+    const long long tiles = d.plane ? d.O : (d.S == 1) ? (d.O + d.B - 1) / d.B : d.O * ((d.S + d.B - 1) / d.B);
+    const size_t smem = d.plane ? 2 * (size_t)d.ny * (d.L + 1) * sizeof(cx<R>)
+                        : d.fa  ? (size_t)d.B * d.fa * (d.fb + 1) * sizeof(cx<R>)
+                                : 2 * (size_t)d.B * d.L * sizeof(cx<R>);
     for (int b0 = 0; b0 < nb; b0 += 65535) {
       const int nbb = std::min(65535, nb - b0);
       dim3 grid((unsigned)tiles, (unsigned)nbb);
@@ -589,7 +704,16 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
         pe.bytes = 2.0 * (double)nbb * (double)P_ * sizeof(cx<R>);
         PGB_CUDA(cudaEventRecord(pe.a, s));
       }
-      if (d.fa) launch_fast<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
+      if (d.plane) {
+        static bool plane_attr_set = false;
+        if (!plane_attr_set) {
+          PGB_CUDA(cudaFuncSetAttribute(fft_plane_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(2 * kMaxPlaneSide * (kMaxPlaneSide + 1) * sizeof(cx<R>))));
+          plane_attr_set = true;
+        }
+        fft_plane_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
+      }
+      else if (d.fa) launch_fast<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
       else fft_pass_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
       launch_check("fft_pass");
       if (g_prof) {

@@ -14,6 +14,9 @@
 // (L = L1*L2) with the twiddle multiply fused into the second pass; the
 // frequency index of such an axis is then stored digit-transposed, which
 // all pointwise kernels handle through the per-axis position tables below.
+// With PYRPA_GB_FFT_PLANE=1, meshes with 2 <= nx, ny <= 64 transform x and
+// y in one "plane pass" (one (x, y) plane per CTA in shared memory, rows
+// padded to nx + 1) instead of two passes.
 // Forward is exp(-2 pi i jk/L) (FFTW sign -1), backward exp(+...), both
 // unnormalized: the callers fold 1/P into their weights.
 #pragma once
@@ -42,6 +45,15 @@ struct PassDesc {
   const cdf* tw_line_d;    // and as double-float pairs for the double-float kernels
   const cdf* tw_full_d;
   int fa, fb;              // L = fa * fb for the two-level register kernel (0: Stockham kernel)
+  // plane pass: the x (length L) and y (length ny) axes of each (x, y) plane
+  // in one kernel; O = number of planes
+  int plane;
+  int ny;
+  int nst_y;
+  int radix_y[kMaxStages];
+  const double2* tw_line_y;
+  const float2* tw_line_y_f;
+  const cdf* tw_line_y_d;
 };
 
 // Position tables of one axis: pos[k] is where logical index k is stored,

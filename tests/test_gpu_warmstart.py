@@ -10,8 +10,8 @@ them to 2e-5.  The whole-set gradient agrees to 5e-3 relative (norm).  One
 Adam step from the device's own gradient repeats the oracle's float32
 operations one by one.
 
-These tests are opt-in (PYRPA_GB_LWS_TESTS=1) until the kernels have run on
-a GB300.
+These tests are opt-in (PYRPA_GB_PENDING_TESTS=1) until the kernels have
+run on a GB300.
 """
 import os
 
@@ -22,8 +22,9 @@ from oracle import flex_oracle as FO
 from oracle import warmstart_oracle as W
 
 pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("PYRPA_GB_LWS_TESTS") != "1",
-                                 reason="learned warm start kernels not yet run on a GB300 (PYRPA_GB_LWS_TESTS=1)")]
+              pytest.mark.skipif(os.environ.get("PYRPA_GB_PENDING_TESTS") != "1",
+                                 reason="learned warm start kernels not yet run on a GB300 "
+                                        "(PYRPA_GB_PENDING_TESTS=1)")]
 
 
 @pytest.fixture(scope="module")
