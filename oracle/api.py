@@ -130,13 +130,14 @@ def linearized_eliashberg(chi, Gk, uni, init_delta, Smat, Cmat, olist, plist, km
 
 
 def get_initial_gap(klist, Norb, gap_sym):
-    """Band-basis initial gap [Norb, Nk] (libs/plibs/_response.py:413-462)."""
+    """Band-basis initial gap [Norb, Nk] (libs/plibs/_response.py:415-462,
+    gap_symms): p+ip (gap_sym -3) is complex."""
     A = 2 * np.pi
     kx, ky, kz = klist[:, 0], klist[:, 1], klist[:, 2]
     rows = {0: np.ones(len(klist)), 1: np.cos(A * kx) - np.cos(A * ky),
             2: 2 * np.cos(A * kx) * np.cos(A * ky), 3: 2 * np.sin(A * kx) * np.sin(A * ky),
             4: 2 * np.sin(A * kx) * np.sin(A * kz), 5: 2 * np.sin(A * ky) * np.sin(A * kz),
-            -1: 2 * np.sin(A * kx), -2: 2 * np.sin(A * ky)}
+            -1: 2 * np.sin(A * kx), -2: 2 * np.sin(A * ky), -3: 2 * np.sin(A * kx) + 2j * np.sin(A * ky)}
     row = rows.get(gap_sym, np.zeros(len(klist)))
     return np.tile(row, (Norb, 1))
 

@@ -143,6 +143,16 @@ def i64(v):
     return byref(c_int64(int(v)))
 
 
+def _real_gap(init_delta):
+    """The band-basis initial gap as float64.  The Fortran dummy is real
+    (feliash.f90:38, 653) and the reference binds it as a float64 ndpointer,
+    which rejects a complex array (the p+ip gap of get_initial_gap)."""
+    a = np.asarray(init_delta)
+    if np.iscomplexobj(a):
+        raise TypeError("init_delta must be real (float64): the library takes a real band-basis gap")
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
 def dbl(v):
     return byref(c_double(float(v)))
 
@@ -527,7 +537,7 @@ def linearized_eliashberg(chi, Gk, uni, init_delta, Smat, Cmat, olist, plist, km
     delta = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
     lam = c_double(0.0)
     _call("lin_eliash", delta, chi, np.ascontiguousarray(Gk), np.ascontiguousarray(uni),
-          np.ascontiguousarray(init_delta, dtype=np.float64), Smat, Cmat, olist,
+          _real_gap(init_delta), Smat, Cmat, olist,
           np.ascontiguousarray(plist, dtype=np.float64), kmap, invk, dbl(temp), dbl(eps), i64(Nkall), i64(Nk),
           i64(Nw), i64(Nchi), i64(Norb), i64(Nx), i64(Ny), i64(Nz), i64(itemax), i64(gap_sym), i64(arnoldi_m),
           byref(lam))
@@ -597,7 +607,7 @@ def gen_Fk(Gk, delta, invk):
 def get_initial_delta(init_delta, uni, kmap, invk, Nw: int, gap_sym: int):
     Norb, Nk = init_delta.shape
     delta = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
-    _call("get_initial_delta_", delta, np.ascontiguousarray(init_delta, dtype=np.float64),
+    _call("get_initial_delta_", delta, _real_gap(init_delta),
           np.ascontiguousarray(uni), kmap, invk, i64(len(kmap)), i64(Nk), i64(Nw), i64(Norb), i64(gap_sym))
     return delta
 
@@ -620,13 +630,19 @@ def conv_delta_orb_to_band(delta, uni, invk, plist, gap_sym: int):
 
 
 def get_initial_gap(klist, Norb: int, gap_sym: int):
-    """Band-basis initial gap [Norb, Nk] (libs/plibs/_response.py:413-462)."""
+    """Band-basis initial gap [Norb, Nk] (libs/plibs/_response.py:415-462):
+    s, dx2-y2, s+-, dxy, dxz, dyz for gap_sym 0..5, px, py, p+ip (complex)
+    for -1, -2, -3; other values raise IndexError, as in the reference."""
     A = 2 * np.pi
     kx, ky, kz = klist[:, 0], klist[:, 1], klist[:, 2]
     rows = {0: np.ones(len(klist)), 1: np.cos(A * kx) - np.cos(A * ky), 2: 2 * np.cos(A * kx) * np.cos(A * ky),
             3: 2 * np.sin(A * kx) * np.sin(A * ky), 4: 2 * np.sin(A * kx) * np.sin(A * kz),
-            5: 2 * np.sin(A * ky) * np.sin(A * kz), -1: 2 * np.sin(A * kx), -2: 2 * np.sin(A * ky)}
-    return np.tile(rows.get(gap_sym, np.zeros(len(klist))), (Norb, 1))
+            5: 2 * np.sin(A * ky) * np.sin(A * kz), -1: 2 * np.sin(A * kx), -2: 2 * np.sin(A * ky),
+            -3: 2 * np.sin(A * kx) + 2j * np.sin(A * ky)}
+    if gap_sym not in rows:
+        # the reference looks the symmetry's label up in a list and fails there
+        raise IndexError(f"gap_sym {gap_sym} outside -3..5 (s, dx2-y2, s+-, dxy, dxz, dyz, px, py, p+ip)")
+    return np.tile(rows[gap_sym], (Norb, 1))
 
 
 # ------------------------------------------------ fused FLEX + Eliashberg
@@ -658,7 +674,7 @@ def flex_eliash(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, init_delta, plist
         seed_ptr = sigma_seed.ctypes.data_as(ctypes.c_void_p)
     _call("pyrpa_gb_flex_eliash", sigmak, byref(mu_o), gap, byref(lam), byref(st), times, Smat, Cmat, kmap, invk,
           olist, np.ascontiguousarray(hamk), np.ascontiguousarray(eig), np.ascontiguousarray(uni),
-          np.ascontiguousarray(init_delta, dtype=np.float64), np.ascontiguousarray(plist, dtype=np.float64),
+          _real_gap(init_delta), np.ascontiguousarray(plist, dtype=np.float64),
           seed_ptr, dbl(seed_mu), dbl(seed_mu_old), dbl(mu), dbl(fill), dbl(temp), i64(scf_loop), dbl(pp), dbl(eps),
           i64(Nkall), i64(Nk), i64(Nw), i64(Norb), i64(Nchi), i64(Nx), i64(Ny), i64(Nz), i64(sub_sigma),
           i64(m_diis), byref(c_bool(sw_rescale)), byref(c_bool(sw_tail)), i64(gap_sym), i64(arnoldi_m),
@@ -761,7 +777,7 @@ def linearized_eliashberg_soc(chi, Gk, uni, init_delta, Vmat, sgnsig, sgnsig2, p
     Nkall, Nk, Nw = len(kmap), Gk.shape[3], Gk.shape[2]
     delta = np.zeros((Norb, Norb, Nw, Nkall), dtype=np.complex128)
     _call("lin_eliash_soc", delta, chi, np.ascontiguousarray(Gk), np.ascontiguousarray(uni),
-          np.ascontiguousarray(init_delta, dtype=np.float64), np.ascontiguousarray(Vmat, dtype=np.float64),
+          _real_gap(init_delta), np.ascontiguousarray(Vmat, dtype=np.float64),
           np.ascontiguousarray(sgnsig, dtype=np.float64), np.ascontiguousarray(sgnsig2, dtype=np.float64),
           np.ascontiguousarray(plist, dtype=np.float64), olist, np.asarray(slist, dtype=np.int64), kmap, invk,
           np.asarray(invs, dtype=np.int64), np.asarray(invschi, dtype=np.int64), dbl(temp), dbl(eps), i64(Nkall),
