@@ -249,13 +249,23 @@ def get_scmat_orb(olist, site, Umat_py, Jmat_py):
 
 
 def get_chi_orb_list(Norb: int, site_prof=(1,)):
-    """Orbital-pair list as plibs.get_chi_orb_list builds it for one site
-    (libs/plibs/_response.py:382-410): pair l = (l % Norb + 1, l // Norb + 1)."""
-    if len(site_prof) != 1:
-        raise NotImplementedError
-    l = np.arange(Norb * Norb)
-    ol = np.stack([l % Norb + 1, l // Norb + 1], axis=1).astype(np.int64)
-    return ol, np.ones(Norb * Norb, dtype=np.int64)
+    """Orbital-pair list and site labels as plibs.get_chi_orb_list builds
+    them (libs/plibs/_response.py:382-413).  Within a site of ns orbitals
+    starting at orbital f, pair l = (f + l % ns, f + l // ns); one site spans
+    all orbitals with label 1, several sites are labelled by their first
+    orbital.  A profile that does not add up to Norb is refused (the
+    reference prints and exits)."""
+    prof = [int(x) for x in site_prof]
+    if len(prof) > 1 and sum(prof) != Norb:
+        raise SystemExit("site_prof doesn't correspond to Hamiltonian")
+    sites = [Norb] if len(prof) == 1 else prof
+    pairs, labels, first = [], [], 1
+    for ns in sites:
+        l = np.arange(ns * ns)
+        pairs.append(np.stack([first + l % ns, first + l // ns], axis=1))
+        labels.append(np.full(ns * ns, 1 if len(prof) == 1 else first))
+        first += ns
+    return np.concatenate(pairs).astype(np.int64), np.concatenate(labels).astype(np.int64)
 
 
 # --------------------------------------------------------------------------- #

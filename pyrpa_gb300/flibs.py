@@ -309,13 +309,30 @@ def get_plist(rvec, ham_r):
 
 # --------------------------------------------------------------- vertices
 def get_chi_orb_list(Norb: int, site_prof=(1,)):
-    """Orbital-pair list for one site, as plibs.get_chi_orb_list returns it: a
-    transposed view whose memory is Fortran olist(Nchi,2) (libs/plibs/_response.py:382-410)."""
-    if len(site_prof) != 1:
-        raise NotImplementedError("multi-site orbital-pair lists")
-    t = np.arange(Norb) + 1
-    o1, o2 = np.meshgrid(t, t)
-    return np.array([o1.flatten(), o2.flatten()]).T, np.ones(Norb * Norb, dtype=np.int64)
+    """Orbital-pair list and site labels as plibs.get_chi_orb_list returns
+    them (libs/plibs/_response.py:382-413).  One site: all Norb^2 pairs, pair
+    l = (l % Norb + 1, l // Norb + 1), site 1.  Several sites (orbital counts
+    in site_prof): the pairs within each site, labelled by the site's first
+    orbital.  The array's memory is the Fortran olist(Nchi,2) in both cases.
+    (The reference's several-site list is C-ordered, and the library would
+    read that memory as other pairs.)  A profile that does not add up to Norb
+    ends the program, as in the reference."""
+    prof = [int(x) for x in site_prof]
+    if len(prof) == 1:
+        t = np.arange(Norb) + 1
+        o1, o2 = np.meshgrid(t, t)
+        return np.array([o1.flatten(), o2.flatten()]).T, np.ones(Norb * Norb, dtype=np.int64)
+    if Norb != sum(prof):
+        print("site_prof doesn't correspond to Hamiltonian")
+        raise SystemExit
+    cols, site, n0 = [], [], 1
+    for ns in prof:
+        t = np.arange(ns) + n0
+        o1, o2 = np.meshgrid(t, t)
+        cols.append(np.array([o1.flatten(), o2.flatten()]))
+        site += [n0] * (ns * ns)
+        n0 += ns
+    return np.concatenate(cols, axis=1).T, np.array(site, dtype=np.int64)
 
 
 def gen_SCmatrix(olist, site, U: float, J: float):
