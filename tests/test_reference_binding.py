@@ -85,3 +85,24 @@ def test_reference_soc_wrappers_against_the_library(ref_flibs):
     assert len(lib.lin_eliash_soc.argtypes) == 27
     for name in ("mkself_soc", "get_chi0_soc", "get_chis_chic_soc", "mkfk_trs_soc_", "conv_delta_orb_to_band_soc"):
         assert len(getattr(lib, name).argtypes) == len(F._SIGNATURES[name]), name
+
+
+@pytest.mark.parametrize("Norb,prof", [(1, [1]), (3, [1]), (5, [1]), (4, [2, 2]), (5, [2, 1, 2])])
+def test_chi_map_matches_reference_port(ref_flibs, Norb, prof):
+    """The exchange-symmetry index map that get_chi0_conv_ takes, against the
+    reference's own Python port of fchi.f90 get_chi_map
+    (libs/flibs/_susceptibility.py:206-242)."""
+    from oracle import flex_oracle as FO
+    from pyrpa_gb300 import flibs as F
+    ref_port = importlib.import_module("libs.flibs._susceptibility")._get_chi_map
+    olist, _ = F.get_chi_orb_list(Norb, prof)
+    cmap_ref, irr_ref = ref_port(np.asarray(olist))
+    cmap, irr = F.chi_map_arrays(olist)
+    assert np.array_equal(cmap, cmap_ref) and np.array_equal(irr, irr_ref)
+    # the oracle's 0-based form: chi_map[m1, l1] = (m2, l2), irr = [(l1, m1)]
+    omap, oirr = FO.get_chi_map(np.asarray(olist))
+    n = len(olist)
+    for l1 in range(n):
+        for m1 in range(n):
+            assert tuple(omap[m1, l1]) == (cmap_ref[0, l1, m1] - 1, cmap_ref[1, l1, m1] - 1)
+    assert [(l + 1, m + 1) for (l, m) in oirr] == list(zip(irr_ref[0][:len(oirr)], irr_ref[1][:len(oirr)]))
