@@ -8,8 +8,9 @@ through the engine's C ABI (pyrpa_gb_flex_eliash, host buffers in and out).
   value        device seconds of the solve with the inputs already in HBM
                (CUDA events on the library stream, between upload and download)
   e2e          wall seconds of the whole ABI call from host buffers, copies included
-  roofline     the FFT pass kernel (the dominant kernel), timed live per launch
-               with CUDA events during the timed steps
+  roofline     the FFT passes (fft2_kernel<R, A, B>; every pass of the 64x64x4096
+               transforms), the kernel that moves the most bytes, timed live per
+               launch with CUDA events during the timed steps
   cpu_baseline the oracle's per-orbital-pair FFT convolution at full size on
                all host cores, extrapolated to one solve with this run's
                iteration and Eliashberg-application counts
@@ -298,7 +299,7 @@ def main():
         "config": config,
         "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": int(in_bytes), "d2h_bytes_per_step": int(out_bytes)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": "fft_pass_kernel", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "fft2_kernel (FFT passes)", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
                      "bytes_per_launch": per_launch_bytes, "launches": fft["launches"],
