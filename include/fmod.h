@@ -356,6 +356,15 @@ void pyrpa_gb_wannier_r(double* out, const double* data, const int64_t* kmap, co
                         const int64_t* Nx, const int64_t* Ny, const int64_t* Nz, const int64_t* Nk_data,
                         const int64_t* Nw, const int64_t* Norb, const int64_t* Ncut);
 
+/* ------------------------------------------------------ FFT tuning --- */
+/* No counterpart in the reference.  The settings the FFT autotuner
+ * (PYRPA_GB_FFT_TUNE=1) may try for one axis of length n with elem_bytes-byte
+ * elements: out[2i] = L1 (four-step split, 0 = one pass or the heuristic),
+ * out[2i+1] = lines per CTA (0 = the heuristic), the heuristic first; at most
+ * cap pairs are written, count = all of them.  Host only: needs no GPU. */
+void pyrpa_gb_fft_candidates(const int64_t* n, const int64_t* elem_bytes, int64_t* out, const int64_t* cap,
+                             int64_t* count);
+
 /* ------------------------------------------------ coarse-mesh seed --- */
 /* No counterpart in the reference (a pyrpa user seeds mkself by hand through
  * sigma.bin, fself.f90:742-780).  sig_c (Nk_c,Nw_c,Norb,Norb) on the coarse

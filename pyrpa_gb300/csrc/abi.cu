@@ -877,6 +877,19 @@ void pyrpa_gb_wannier_r(double2* out, const double2* data, const int64_t* kmap, 
   ABI_CATCH("pyrpa_gb_wannier_r", nan_fill(out, (size_t)((*Nx) * (*Ny) * (*Nz) * std::min(*Ncut, *Nw) * (*Norb) * (*Norb))))
 }
 
+// -------------------------------------------------------- FFT tuning --
+void pyrpa_gb_fft_candidates(const int64_t* n, const int64_t* elem_bytes, int64_t* out, const int64_t* cap,
+                             int64_t* count) {
+  ABI_TRY
+  const std::vector<AxisTune> c = fft_axis_candidates((int)*n, (int)*elem_bytes);
+  *count = (int64_t)c.size();
+  for (size_t i = 0; i < c.size() && (int64_t)i < *cap; ++i) {
+    out[2 * i] = c[i].L1;
+    out[2 * i + 1] = c[i].lines;
+  }
+  ABI_CATCH("pyrpa_gb_fft_candidates", *count = -1)
+}
+
 // ------------------------------------------------- coarse-mesh seed --
 void pyrpa_gb_sigma_interp(double2* sig_f, const double2* sig_c, const int64_t* kmap_c, const int64_t* invk_c,
                            const int64_t* Nx_c, const int64_t* Ny_c, const int64_t* Nz_c, const int64_t* Nk_c,

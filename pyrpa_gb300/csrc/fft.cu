@@ -523,7 +523,7 @@ bool factor_line(int L, int* radix, int* nst) {
   return n == 1;
 }
 
-PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
+PassDesc make_pass(int L, long long S, long long O, int elem_bytes, int lines = 0) {
   PassDesc d{};
   d.L = L;
   d.S = S;
@@ -531,6 +531,7 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
   if (fast_pair(L, &d.fa, &d.fb)) {
     long long nl = std::max(1, 2048 / L);
     nl = std::min(nl, 64LL);
+    if (lines > 0) nl = lines;
     nl = (S == 1) ? std::min(nl, O) : std::min(nl, S);
     d.B = (int)std::max(1LL, nl);
     d.tw_line = twiddle_table(L);
@@ -544,6 +545,7 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes) {
             "FFT length " + std::to_string(L) + " has a prime factor above 13 (unsupported)");
   long long B = std::max(1LL, 32768LL / ((long long)L * elem_bytes));
   B = std::min(B, 64LL);
+  if (lines > 0) B = lines;
   if (S == 1) B = std::min(B, O);
   else B = std::min(B, S);
   d.B = (int)std::max(1LL, B);
@@ -576,7 +578,7 @@ int split_length(int n) {
 
 }  // namespace
 
-FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
+FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes, const PlanTune* tune) {
   dims_[0] = nx;
   dims_[1] = ny;
   dims_[2] = nz;
@@ -593,8 +595,13 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
     m.logical.resize(n);
     m.rev.resize(n);
     int fa = 0, fb = 0, L1s = 0;
+    const AxisTune tn = tune ? tune->ax[a] : AxisTune{};
     const bool direct_fast = fast_pair(n, &fa, &fb);
-    if (n > 64 && !direct_fast) {
+    int ta, tb;
+    if (n > 64 && !direct_fast && tn.L1 > 0 && n % tn.L1 == 0 && n / tn.L1 <= 64 && fast_pair(tn.L1, &ta, &tb) &&
+        fast_pair(n / tn.L1, &ta, &tb)) {
+      L1s = tn.L1;
+    } else if (n > 64 && !direct_fast) {
       // four-step split into two lengths that both have a two-level kernel
       int best = -1;
       for (int a1 = 2; a1 <= 64; ++a1) {
@@ -606,7 +613,7 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
       L1s = best > 0 ? best : 0;
     }
     if (n > 1 && L1s == 0 && n <= kMaxLine) {
-      PassDesc p = make_pass(n, S, O, elem_bytes);
+      PassDesc p = make_pass(n, S, O, elem_bytes, tn.lines);
       fwd_.push_back(p);
       bwd_.push_back(p);
       if (a < 3) {
@@ -616,8 +623,8 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes) {
       for (int k = 0; k < n; ++k) m.pos[k] = k;
     } else if (n > 1) {
       const int L1 = L1s ? L1s : split_length(n), L2 = n / L1;
-      PassDesc pb = make_pass(L1, S * L2, O, elem_bytes);
-      PassDesc pa = make_pass(L2, S, O * L1, elem_bytes);
+      PassDesc pb = make_pass(L1, S * L2, O, elem_bytes, tn.lines);
+      PassDesc pa = make_pass(L2, S, O * L1, elem_bytes, tn.lines);
       pa.tw_L1 = L1;
       pa.tw_Lfull = n;
       pa.tw_full = twiddle_table(n);
@@ -771,6 +778,101 @@ void fft_profile_collect(double* launches, double* ms, double* bytes) {
   *bytes = b;
 }
 
+void FFT4D::release_tables() {
+  if (d_tables_) cudaFree(d_tables_);
+  d_tables_ = nullptr;
+}
+
+namespace {
+
+// shared memory of one pass of length L with `lines` lines per CTA, and
+// whether it fits that kernel's launch (48 KB for the two-level kernel,
+// 96 KB for the Stockham kernel, the limits the plan's launches use)
+bool pass_fits(int L, int lines, int elem_bytes) {
+  int a, b;
+  if (fast_pair(L, &a, &b)) return (long long)lines * a * (b + 1) * elem_bytes <= 48 * 1024;
+  return 2LL * lines * L * elem_bytes <= 96 * 1024;
+}
+
+bool tune_enabled() {
+  const char* s = std::getenv("PYRPA_GB_FFT_TUNE");
+  return s && std::string(s) == "1";
+}
+
+// the fastest of each axis's candidates, one axis after another, timed as
+// whole forward transforms of one scratch array (min of 3 after a warm-up)
+template <typename R>
+PlanTune tune_plan(int nx, int ny, int nz, int nt) {
+  const int dims[4] = {nx, ny, nz, nt};
+  const long long P = (long long)nx * ny * nz * nt;
+  cudaStream_t st = ctx().stream;
+  DBuf<cx<R>> x(P);
+  x.zero();
+  cudaEvent_t e0, e1;
+  PGB_CUDA(cudaEventCreate(&e0));
+  PGB_CUDA(cudaEventCreate(&e1));
+  PlanTune best{};
+  for (int a = 0; a < 4; ++a) {
+    const std::vector<AxisTune> cands = fft_axis_candidates(dims[a], (int)sizeof(cx<R>));
+    if (cands.size() < 2) continue;
+    float best_ms = 1e30f;
+    AxisTune pick = best.ax[a];
+    for (const AxisTune& c : cands) {
+      PlanTune trial = best;
+      trial.ax[a] = c;
+      FFT4D f(nx, ny, nz, nt, (int)sizeof(cx<R>), &trial);
+      float ms = 1e30f;
+      try {
+        f.forward<R>(x.p, 1, st);
+        for (int rep = 0; rep < 3; ++rep) {
+          PGB_CUDA(cudaEventRecord(e0, st));
+          f.forward<R>(x.p, 1, st);
+          PGB_CUDA(cudaEventRecord(e1, st));
+          PGB_CUDA(cudaEventSynchronize(e1));
+          float t = 0;
+          PGB_CUDA(cudaEventElapsedTime(&t, e0, e1));
+          ms = std::min(ms, t);
+        }
+      } catch (const Error&) {
+        ms = 1e30f;  // a candidate that does not launch is skipped
+      }
+      f.release_tables();
+      if (ms < best_ms) {
+        best_ms = ms;
+        pick = c;
+      }
+    }
+    best.ax[a] = pick;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
+}  // namespace
+
+std::vector<AxisTune> fft_axis_candidates(int n, int elem_bytes) {
+  std::vector<AxisTune> out;
+  if (n <= 1) return out;
+  out.push_back(AxisTune{});
+  int a, b;
+  std::vector<int> splits;
+  if (n > 64 && !fast_pair(n, &a, &b)) {
+    for (int l1 = 2; l1 <= 64; ++l1)
+      if (n % l1 == 0 && n / l1 <= 64 && fast_pair(l1, &a, &b) && fast_pair(n / l1, &a, &b)) splits.push_back(l1);
+  } else if (n <= kMaxLine) {
+    splits.push_back(0);
+  }
+  const int lines[] = {8, 16, 32, 64};
+  for (int l1 : splits)
+    for (int ln : lines) {
+      const bool fits = l1 ? (pass_fits(l1, ln, elem_bytes) && pass_fits(n / l1, ln, elem_bytes))
+                           : pass_fits(n, ln, elem_bytes);
+      if (fits) out.push_back(AxisTune{l1, ln});
+    }
+  return out;
+}
+
 const FFT4D& fft_plan(int nx, int ny, int nz, int nt, int elem_bytes) {
   static std::map<std::tuple<int, int, int, int, int>, FFT4D*> plans;
   static std::mutex mu;
@@ -778,7 +880,16 @@ const FFT4D& fft_plan(int nx, int ny, int nz, int nt, int elem_bytes) {
   auto key = std::make_tuple(nx, ny, nz, nt, elem_bytes);
   auto it = plans.find(key);
   if (it != plans.end()) return *it->second;
-  FFT4D* p = new FFT4D(nx, ny, nz, nt, elem_bytes);
+  FFT4D* p = nullptr;
+  if (tune_enabled() && (elem_bytes == 8 || elem_bytes == 16)) {
+    const PlanTune t = elem_bytes == 8 ? tune_plan<float>(nx, ny, nz, nt) : tune_plan<double>(nx, ny, nz, nt);
+    p = new FFT4D(nx, ny, nz, nt, elem_bytes, &t);
+    log("[FFT] tuned %dx%dx%dx%d (%d-byte): (L1, lines) = (%d,%d) (%d,%d) (%d,%d) (%d,%d)\n", nx, ny, nz, nt,
+        elem_bytes, t.ax[0].L1, t.ax[0].lines, t.ax[1].L1, t.ax[1].lines, t.ax[2].L1, t.ax[2].lines, t.ax[3].L1,
+        t.ax[3].lines);
+  } else {
+    p = new FFT4D(nx, ny, nz, nt, elem_bytes);
+  }
   plans[key] = p;
   return *p;
 }

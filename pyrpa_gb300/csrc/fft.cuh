@@ -56,6 +56,23 @@ struct PassDesc {
   const cdf* tw_line_y_d;
 };
 
+// Per-axis overrides of the plan's heuristics; 0 keeps the heuristic.
+// L1: the first length of a four-step split (axes > 64 without a direct
+// two-level kernel); lines: lines per CTA of every pass of the axis.
+struct AxisTune {
+  int L1 = 0;
+  int lines = 0;
+};
+struct PlanTune {
+  AxisTune ax[4];
+};
+
+// The settings an autotuner may try for one axis of length n with
+// elem-byte elements: the heuristic first, then every four-step split whose
+// two lengths have a two-level kernel, each with 8, 16, 32 or 64 lines per
+// CTA where the pass's shared memory fits its launch.
+std::vector<AxisTune> fft_axis_candidates(int n, int elem_bytes);
+
 // Position tables of one axis: pos[k] is where logical index k is stored,
 // rev[p] the position of logical -k for the value stored at position p.
 struct AxisMap {
@@ -66,7 +83,10 @@ struct AxisMap {
 class FFT4D {
  public:
   FFT4D() = default;
-  FFT4D(int nx, int ny, int nz, int nt, int elem_bytes);
+  // tune: per-axis overrides (null: the heuristics)
+  FFT4D(int nx, int ny, int nz, int nt, int elem_bytes, const PlanTune* tune = nullptr);
+  // frees the device position tables (plans made for timing only)
+  void release_tables();
   long long P() const { return P_; }
   const int* dims() const { return dims_; }
   // in-place transform of nb arrays stored back to back (stride P)
@@ -94,6 +114,9 @@ class FFT4D {
 };
 
 // Cached FFT plan for a grid (plans and twiddle tables live for the process).
+// With PYRPA_GB_FFT_TUNE=1 a new plan's per-axis settings are chosen by
+// timing the candidates of fft_axis_candidates on a scratch array (one axis
+// at a time, the others fixed at their best so far).
 const FFT4D& fft_plan(int nx, int ny, int nz, int nt, int elem_bytes);
 
 // Optional live timing of every FFT pass launch with CUDA events on the

@@ -90,6 +90,7 @@ _SIGNATURES = {
     + [_pb, _pb, _pi, _pi, _pi, _pd, _i64],
     "pyrpa_gb_regrid_sigma": [_c128, _c128, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
     "pyrpa_gb_wannier_r": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _pi, _pi],
+    "pyrpa_gb_fft_candidates": [_pi, _pi, _i64, _pi, _pi],
     "pyrpa_gb_sigma_interp": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _i64, _i64, _pi, _pi, _pi, _pi, _pi,
                               _pi, _pd],
     "pyrpa_gb_lws_create": [_pi],
@@ -479,6 +480,15 @@ def regrid_sigma(sigmak, temp_old: float, temp_new: float, Nw_new: int, w_scale:
     _call("pyrpa_gb_regrid_sigma", out, sigmak, i64(Nk), i64(Nw_old), i64(Nw_new), i64(Norb), dbl(temp_old),
           dbl(temp_new), dbl(w_scale))
     return out
+
+
+def fft_candidates(n: int, elem_bytes: int):
+    """(L1, lines) settings the FFT autotuner may try for an axis of length n
+    (PYRPA_GB_FFT_TUNE=1); (0, 0) is the heuristic.  Needs no GPU."""
+    out = np.zeros(2 * 64, dtype=np.int64)
+    count = c_int64(0)
+    _call("pyrpa_gb_fft_candidates", i64(n), i64(elem_bytes), out, i64(64), byref(count))
+    return [tuple(int(v) for v in out[2 * i: 2 * i + 2]) for i in range(min(64, count.value))]
 
 
 def sigma_interp(sigmak_c, kmap_c, invk_c, Nx_c: int, Ny_c: int, Nz_c: int, kmap_f, invk_f, Nx_f: int,

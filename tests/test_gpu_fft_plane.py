@@ -1,6 +1,6 @@
-"""GPU parity of the FFT plane pass (PYRPA_GB_FFT_PLANE=1: x and y of each
-(x, y) plane in one kernel) through chi0 and the FLEX loop, against the FP64
-oracle.  Mesh shapes here are used by no other test, so their FFT plans are
+"""GPU parity of the opt-in FFT variants through chi0 and the FLEX loop,
+against the FP64 oracle: the plane pass (PYRPA_GB_FFT_PLANE=1: x and y of
+each (x, y) plane in one kernel) and autotuned plans (PYRPA_GB_FFT_TUNE=1).  Mesh shapes here are used by no other test, so their FFT plans are
 built while the switch is on; it is cleared right after, so that plans made
 later take the default passes.
 
@@ -54,15 +54,28 @@ CASES = [(2, 6, 10, 1, 9, False), (1, 12, 12, 1, 7, False), (2, 10, 6, 2, 6, Fal
 
 @pytest.mark.parametrize("Norb,Nx,Ny,Nz,Nw,fp32", CASES)
 def test_plane_pass_matches_oracle(F, Norb, Nx, Ny, Nz, Nw, fp32):
+    _check(F, "PYRPA_GB_FFT_PLANE", Norb, Nx, Ny, Nz, Nw, fp32)
+
+
+# (Norb, Nx, Ny, Nz, Nw, FP32 run): Nw = 48 gives a 96-point axis with the splits 4x24 ... 24x4
+TUNED = [(1, 12, 10, 1, 48, False), (2, 10, 12, 1, 48, True)]
+
+
+@pytest.mark.parametrize("Norb,Nx,Ny,Nz,Nw,fp32", TUNED)
+def test_tuned_plan_matches_oracle(F, Norb, Nx, Ny, Nz, Nw, fp32):
+    _check(F, "PYRPA_GB_FFT_TUNE", Norb, Nx, Ny, Nz, Nw, fp32)
+
+
+def _check(F, switch, Norb, Nx, Ny, Nz, Nw, fp32):
     m = _model(F, Norb, Nx, Ny, Nz, Nw, seed=Nx + Ny + Nw)
     F.set_precision(32 if fp32 else 64)
-    os.environ["PYRPA_GB_FFT_PLANE"] = "1"
+    os.environ[switch] = "1"
     try:
         chi, st = F.get_chi0(m["S"], m["C"], m["Gk"], m["olist"], m["kmap"], m["invk"], m["temp"], Nx, Ny, Nz)
         sig, mu = F.mkself(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"],
                            0.5 * Norb, m["temp"], Nw, Nx, Ny, Nz, False, False, scf_loop=3, eps=1e-12, pp=0.5)
     finally:
-        os.environ.pop("PYRPA_GB_FFT_PLANE", None)
+        os.environ.pop(switch, None)
         F.set_precision(64)
     chio, sto = O.get_chi0(m["S"], m["C"], m["Gk"], m["olist"], m["kmap"], m["invk"], m["temp"], Nx, Ny, Nz)
     sigo, muo = O.mkself(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"],
