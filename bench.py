@@ -171,6 +171,34 @@ def cpu_seconds(cfg, tail, iters, applies, rate):
 
 
 # ------------------------------------------------------------------ main
+def solve_traffic(Norb: int, Nk: int, Nkall: int, Nw: int, stats: dict, precision: str) -> float:
+    """Algorithmic HBM bytes of one fine solve (the coarse warm start left
+    out), with P = Nkall 2Nw, K = Nk Nw, Nchi = Norb^2 and an ideal 4-D FFT of
+    two read-write sweeps:
+      per FLEX iteration        B [4P (2 Norb^2 + Nchi(Nchi+1)/2 + Nchi^2) + P Nchi^2 + 16 K Norb^2]
+                                + Bv 2 K Nchi^2
+      per Eliashberg application  Be [8P Norb^2 + 2P Nchi^2 + 4K Norb^2]
+    B, Bv and Be are the bytes of a complex chi0/Sigma, vertex and Eliashberg
+    element in each phase: 8 for FP32, 16 for FP64 and double-float."""
+    nchi = Norb * Norb
+    P, K = Nkall * 2 * Nw, Nk * Nw
+
+    def it_bytes(B, Bv):
+        return (B * (4 * P * (2 * Norb ** 2 + nchi * (nchi + 1) // 2 + nchi ** 2) + P * nchi ** 2
+                     + 16 * K * Norb ** 2) + Bv * 2 * K * nchi ** 2)
+
+    n = int(stats["iterations"])
+    if precision == "mixed":
+        n32, nmid = int(stats["iterations_fp32"]), int(stats["iterations_fp64_fp32vertex"])
+        flex = n32 * it_bytes(8, 8) + nmid * it_bytes(16, 8) + (n - n32 - nmid) * it_bytes(16, 16)
+        be = 16
+    elif precision == "32":
+        flex, be = n * it_bytes(8, 8), 8
+    else:
+        flex, be = n * it_bytes(16, 16), 16
+    return float(flex + int(stats["applies"]) * be * (8 * P * Norb ** 2 + 2 * P * nchi ** 2 + 4 * K * Norb ** 2))
+
+
 def max_over_ranks(values, dist):
     """Replicas: every rank solved its own instance; the job's time is the
     slowest rank's (all-reduce MAX, then a barrier)."""
@@ -280,6 +308,8 @@ def main():
                                         m["uni"], m["init"], m["plist"]))
     out_bytes = res["sigmak"].nbytes + res["gap"].nbytes
     iters, applies = int(stats["iterations"]), int(stats["applies"])
+    solve_bytes = solve_traffic(c["Norb"], len(m["klist"]), len(m["kmap"]), c["Nw"], stats, a.precision)
+    solve_s = value - stats["t_warm_ms"] / 1e3
     rate, cores, npairs, cwall = cpu_pair_rate(c, a.cpu_pairs)
     cpu_v = cpu_seconds(c, tail, iters, applies, rate)
     config.update({"flex_iterations": iters, "eliashberg_applications": applies, "lambda": res["lam"],
@@ -306,6 +336,11 @@ def main():
                      "avg_launch_ms": fft["ms"] / max(1, fft["launches"]),
                      "traffic": per_launch_bytes * traffic_per_byte,
                      "traffic_source": "ncu capture of one 64x64x4096 FP32 pass, scaled by bytes per launch"},
+        "solve_roofline": {"bound": "hbm", "bytes": solve_bytes, "seconds": solve_s,
+                           "achieved": solve_bytes / solve_s / 1e9 if solve_s > 0 else None, "peak": peak,
+                           "unit": "GB/s", "frac": solve_bytes / solve_s / 1e9 / peak if solve_s > 0 else None,
+                           "scope": "fine FLEX iterations and Eliashberg applications, algorithmic bytes with an "
+                                    "ideal two-sweep 4-D FFT; the coarse warm start is left out of bytes and time"},
         "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": cores, "kind": "port",
                          "sample": f"{npairs} full-size orbital-pair FFT convolutions (oracle, numpy) in {cwall:.1f} s "
                                    f"on {cores} spawned workers, extrapolated with this run's {iters} FLEX iterations "
