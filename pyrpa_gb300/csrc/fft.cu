@@ -13,6 +13,8 @@ namespace pgb {
 
 namespace {
 
+constexpr size_t kLongSmem = 200 * 1024;  // shared memory of one long-pass CTA at most
+
 // tab[t] = exp(-2 pi i t / L); sign < 0 uses it as is, sign > 0 its conjugate
 template <typename R>
 __device__ __forceinline__ cx<R> twid(const cx<R>* tab, int t, int sign) {
@@ -225,6 +227,124 @@ __global__ void __launch_bounds__(256) fft_plane_kernel(cx<R>* data, long long P
     const int y = e / nx, x = e - y * nx;
     arr[e] = in[y * sx + x];
   }
+}
+
+// One step of the long pass: length-G^2 DFTs of nl * ntask lines of shared
+// memory, done in place by groups of G threads.  Line c of line set b has its
+// elements at b * LS + c * cstride + i * estride.  Thread j of a group reads
+// the elements G i + j, runs a radix-G DFT over i, multiplies by w_L^(j kA)
+// and writes back the slots it read; thread kA then reads G kA + j, runs a
+// radix-G DFT over j and writes frequency kA + G kB (times w_M^(c k) when
+// tw_out).  The trip count is the same for every thread, so that all of
+// them reach each barrier.
+template <typename R, int G>
+__device__ void long_step(cx<R>* buf, int nl, int ntask, int LS, int cstride, int estride, int sign,
+                          const cx<R>* tabL, const cx<R>* tabM, bool tw_out) {
+  constexpr int L = G * G;
+  const int ngroups = blockDim.x / G;
+  const int group = threadIdx.x / G, lane = threadIdx.x - group * G;
+  const int total = nl * ntask;
+  for (int t0 = 0; t0 < total; t0 += ngroups) {
+    const int task = t0 + group;
+    const bool act = group < ngroups && task < total;
+    int base = 0, c = 0;
+    if (act) {
+      const int b = task / ntask;
+      c = task - b * ntask;
+      base = b * LS + c * cstride;
+    }
+    cx<R> v[G];
+    if (act) {
+#pragma unroll
+      for (int i = 0; i < G; ++i) v[i] = buf[base + estride * (G * i + lane)];
+      Dft<R, G>::run(v, sign, tabL, L);
+#pragma unroll
+      for (int k = 1; k < G; ++k)
+        if (lane) v[k] = v[k] * twid<R>(tabL, lane * k, sign);
+#pragma unroll
+      for (int k = 0; k < G; ++k) buf[base + estride * (G * k + lane)] = v[k];
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int j = 0; j < G; ++j) v[j] = buf[base + estride * (G * lane + j)];
+      Dft<R, G>::run(v, sign, tabL, L);
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int kb = 0; kb < G; ++kb) {
+        const int k = lane + G * kb;
+        cx<R> val = v[kb];
+        if (tw_out) {
+          const int t = c * k;  // c < L_other and k < L, so t < M
+          if (t) val = val * twid<R>(tabM, t, sign);
+        }
+        buf[base + estride * k] = val;
+      }
+    }
+  }
+}
+
+// A four-step axis of length M = L1 L2 (L1 = G1^2, L2 = G2^2) in one pass:
+// B adjacent lines (consecutive positions at stride 1, elements at stride S)
+// per CTA, each stored as L1 rows of L2 elements padded to L2 + 1.
+// Forward: columns (DFT over n1, twiddle w_M^(n2 k1)), then rows (over n2);
+// frequency k1 + L1 k2 ends in row k1, column k2.  Backward: rows (twiddle
+// w_M^(k1 n2)), then columns.
+template <typename R, int G1, int G2>
+__global__ void __launch_bounds__(256) fft_long_kernel(cx<R>* data, long long P, PassDesc d, int sign) {
+  constexpr int L1 = G1 * G1, L2 = G2 * G2, M = L1 * L2, RS = L2 + 1, LS = L1 * RS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* buf = reinterpret_cast<cx<R>*>(smem_raw);
+  cx<R>* arr = data + (long long)blockIdx.y * P;
+  const long long nsb = (d.S + d.B - 1) / d.B;
+  const long long o = blockIdx.x / nsb;
+  const long long s0 = (blockIdx.x - o * nsb) * d.B;
+  const int nl = (int)min((long long)d.B, d.S - s0);
+  const long long base = o * (long long)M * d.S + s0;
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+    const int p = e / nl, b = e - p * nl;
+    buf[b * LS + (p / L2) * RS + (p % L2)] = arr[base + (long long)p * d.S + b];
+  }
+  __syncthreads();
+  const cx<R>* t1 = line_tab<R>(d);
+  const cx<R>* t2 = line_tab_y<R>(d);
+  const cx<R>* tm = full_tab<R>(d);
+  if (sign < 0) {
+    long_step<R, G1>(buf, nl, L2, LS, 1, RS, sign, t1, tm, true);   // columns n2: over n1
+    __syncthreads();
+    long_step<R, G2>(buf, nl, L1, LS, RS, 1, sign, t2, tm, false);  // rows k1: over n2
+  } else {
+    long_step<R, G2>(buf, nl, L1, LS, RS, 1, sign, t2, tm, true);   // rows k1: over k2
+    __syncthreads();
+    long_step<R, G1>(buf, nl, L2, LS, 1, RS, sign, t1, tm, false);  // columns n2: over k1
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nl * M; e += blockDim.x) {
+    const int p = e / nl, b = e - p * nl;
+    arr[base + (long long)p * d.S + b] = buf[b * LS + (p / L2) * RS + (p % L2)];
+  }
+}
+
+template <typename R, int G1, int G2>
+void launch_long_one(const PassDesc& d, dim3 grid, size_t smem, cudaStream_t s, cx<R>* data, long long P, int sign) {
+  static bool attr = false;
+  if (!attr) {
+    PGB_CUDA(cudaFuncSetAttribute(fft_long_kernel<R, G1, G2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kLongSmem));
+    attr = true;
+  }
+  fft_long_kernel<R, G1, G2><<<grid, 256, smem, s>>>(data, P, d, sign);
+}
+
+template <typename R>
+void launch_long(const PassDesc& d, dim3 grid, size_t smem, cudaStream_t s, cx<R>* data, long long P, int sign) {
+  if (d.lp_L1 == 64 && d.lp_L2 == 64) return launch_long_one<R, 8, 8>(d, grid, smem, s, data, P, sign);
+  if (d.lp_L1 == 16 && d.lp_L2 == 64) return launch_long_one<R, 4, 8>(d, grid, smem, s, data, P, sign);
+  if (d.lp_L1 == 64 && d.lp_L2 == 16) return launch_long_one<R, 8, 4>(d, grid, smem, s, data, P, sign);
+  if (d.lp_L1 == 16 && d.lp_L2 == 16) return launch_long_one<R, 4, 4>(d, grid, smem, s, data, P, sign);
+  throw Error("no long-pass kernel for this axis split");
 }
 
 template <typename R>
@@ -557,6 +677,24 @@ PassDesc make_pass(int L, long long S, long long O, int elem_bytes, int lines = 
 
 constexpr int kMaxPlaneSide = 64;  // two padded 64 x 65 planes of 16-byte elements fit in 227 KB
 
+// PYRPA_GB_FFT_LONG=1 transforms four-step axes of length L1 L2 (L1, L2 in
+// {16, 64}) in one long pass
+bool long_pass_enabled() {
+  const char* s = std::getenv("PYRPA_GB_FFT_LONG");
+  return s && std::string(s) == "1";
+}
+
+bool long_split(int n, int* l1, int* l2) {
+  const int sp[4][2] = {{64, 64}, {16, 64}, {64, 16}, {16, 16}};
+  for (const auto& x : sp)
+    if (x[0] * x[1] == n) {
+      *l1 = x[0];
+      *l2 = x[1];
+      return true;
+    }
+  return false;
+}
+
 // PYRPA_GB_FFT_PLANE=1 transforms x and y in one plane pass
 bool plane_pass_enabled() {
   const char* s = std::getenv("PYRPA_GB_FFT_PLANE");
@@ -597,7 +735,7 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes, const PlanTune* tun
     int fa = 0, fb = 0, L1s = 0;
     const AxisTune tn = tune ? tune->ax[a] : AxisTune{};
     const bool direct_fast = fast_pair(n, &fa, &fb);
-    int ta, tb;
+    int ta, tb, lp1 = 0, lp2 = 0;
     if (n > 64 && !direct_fast && tn.L1 > 0 && n % tn.L1 == 0 && n / tn.L1 <= 64 && fast_pair(tn.L1, &ta, &tb) &&
         fast_pair(n / tn.L1, &ta, &tb)) {
       L1s = tn.L1;
@@ -621,6 +759,37 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes, const PlanTune* tun
         bwd_space_.push_back(p);
       }
       for (int k = 0; k < n; ++k) m.pos[k] = k;
+    } else if (n > 1 && long_pass_enabled() && long_split(n, &lp1, &lp2)) {
+      // the whole axis in one long pass, digit-transposed like the four-step split
+      const int L1 = lp1, L2 = lp2;
+      PassDesc lp{};
+      lp.lp = 1;
+      lp.L = n;
+      lp.lp_L1 = L1;
+      lp.lp_L2 = L2;
+      lp.S = S;
+      lp.O = O;
+      const long long fit = (long long)(kLongSmem / ((size_t)L1 * (L2 + 1) * elem_bytes));
+      // a power of two, so that each CTA's runs start on 32-byte sectors
+      long long nb = 1;
+      while (nb * 2 <= std::min({32LL, fit, S})) nb *= 2;
+      lp.B = (int)nb;
+      lp.tw_line = twiddle_table(L1);
+      lp.tw_line_f = twiddle_table_f(L1);
+      lp.tw_line_d = twiddle_table_d(L1);
+      lp.tw_line_y = twiddle_table(L2);
+      lp.tw_line_y_f = twiddle_table_f(L2);
+      lp.tw_line_y_d = twiddle_table_d(L2);
+      lp.tw_full = twiddle_table(n);
+      lp.tw_full_f = twiddle_table_f(n);
+      lp.tw_full_d = twiddle_table_d(n);
+      fwd_.push_back(lp);
+      bwd_.push_back(lp);
+      if (a < 3) {
+        fwd_space_.push_back(lp);
+        bwd_space_.push_back(lp);
+      }
+      for (int k = 0; k < n; ++k) m.pos[k] = (k / L1) + L2 * (k % L1);
     } else if (n > 1) {
       const int L1 = L1s ? L1s : split_length(n), L2 = n / L1;
       PassDesc pb = make_pass(L1, S * L2, O, elem_bytes, tn.lines);
@@ -697,8 +866,11 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
     attr_set = true;
   }
   for (const PassDesc& d : passes) {
-    const long long tiles = d.plane ? d.O : (d.S == 1) ? (d.O + d.B - 1) / d.B : d.O * ((d.S + d.B - 1) / d.B);
+    const long long tiles = d.plane ? d.O
+                            : d.lp ? d.O * ((d.S + d.B - 1) / d.B)
+                            : (d.S == 1) ? (d.O + d.B - 1) / d.B : d.O * ((d.S + d.B - 1) / d.B);
     const size_t smem = d.plane ? 2 * (size_t)d.ny * (d.L + 1) * sizeof(cx<R>)
+                        : d.lp  ? (size_t)d.B * d.lp_L1 * (d.lp_L2 + 1) * sizeof(cx<R>)
                         : d.fa  ? (size_t)d.B * d.fa * (d.fb + 1) * sizeof(cx<R>)
                                 : 2 * (size_t)d.B * d.L * sizeof(cx<R>);
     for (int b0 = 0; b0 < nb; b0 += 65535) {
@@ -720,6 +892,7 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
         }
         fft_plane_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
       }
+      else if (d.lp) launch_long<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
       else if (d.fa) launch_fast<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
       else fft_pass_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
       launch_check("fft_pass");

@@ -17,6 +17,10 @@
 // With PYRPA_GB_FFT_PLANE=1, meshes with 2 <= nx, ny <= 64 transform x and
 // y in one "plane pass" (one (x, y) plane per CTA in shared memory, rows
 // padded to nx + 1) instead of two passes.
+// With PYRPA_GB_FFT_LONG=1, axes of length L1 * L2 (L1, L2 in {16, 64})
+// that would take the two four-step passes take one "long pass" instead: a
+// CTA holds a few adjacent lines whole in shared memory, and the frequency
+// order (digit-transposed) is the same.
 // Forward is exp(-2 pi i jk/L) (FFTW sign -1), backward exp(+...), both
 // unnormalized: the callers fold 1/P into their weights.
 #pragma once
@@ -54,6 +58,10 @@ struct PassDesc {
   const double2* tw_line_y;
   const float2* tw_line_y_f;
   const cdf* tw_line_y_d;
+  // long pass: a four-step axis of length L = lp_L1 * lp_L2 in one kernel
+  // (B lines per CTA, tw_line* for lp_L1, tw_line_y* for lp_L2, tw_full* for L)
+  int lp;
+  int lp_L1, lp_L2;
 };
 
 // Per-axis overrides of the plan's heuristics; 0 keeps the heuristic.

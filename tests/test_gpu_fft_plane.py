@@ -1,6 +1,7 @@
 """GPU parity of the opt-in FFT variants through chi0 and the FLEX loop,
 against the FP64 oracle: the plane pass (PYRPA_GB_FFT_PLANE=1: x and y of
-each (x, y) plane in one kernel) and autotuned plans (PYRPA_GB_FFT_TUNE=1).  Mesh shapes here are used by no other test, so their FFT plans are
+each (x, y) plane in one kernel), the long pass (PYRPA_GB_FFT_LONG=1: a
+four-step axis in one kernel) and autotuned plans (PYRPA_GB_FFT_TUNE=1).  Mesh shapes here are used by no other test, so their FFT plans are
 built while the switch is on; it is cleared right after, so that plans made
 later take the default passes.
 
@@ -64,6 +65,16 @@ TUNED = [(1, 12, 10, 1, 48, False), (2, 10, 12, 1, 48, True)]
 @pytest.mark.parametrize("Norb,Nx,Ny,Nz,Nw,fp32", TUNED)
 def test_tuned_plan_matches_oracle(F, Norb, Nx, Ny, Nz, Nw, fp32):
     _check(F, "PYRPA_GB_FFT_TUNE", Norb, Nx, Ny, Nz, Nw, fp32)
+
+
+# (Norb, Nx, Ny, Nz, Nw, FP32 run): long axes 256 = 16 x 16, 1024 = 16 x 64, 4096 = 64 x 64
+LONG = [(2, 6, 10, 1, 128, False), (1, 10, 6, 1, 512, False), (1, 6, 10, 1, 2048, False),
+        (2, 10, 6, 1, 128, True)]
+
+
+@pytest.mark.parametrize("Norb,Nx,Ny,Nz,Nw,fp32", LONG)
+def test_long_pass_matches_oracle(F, Norb, Nx, Ny, Nz, Nw, fp32):
+    _check(F, "PYRPA_GB_FFT_LONG", Norb, Nx, Ny, Nz, Nw, fp32)
 
 
 def _check(F, switch, Norb, Nx, Ny, Nz, Nw, fp32):
