@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--cpu-pairs", type=int, default=0, help="orbital pairs in the CPU sample (0: one per core)")
     p.add_argument("--flex-iters", type=int, default=0)
     p.add_argument("--applies", type=int, default=0)
+    p.add_argument("--with-fp64", action="store_true",
+                   help="after the timed steps, solve once more in plain FP64 from G0 (the metric's denominator) "
+                        "and report its time and the lambda, Sigma and mu differences")
     return p.parse_args()
 
 
@@ -348,8 +351,25 @@ def main():
         "clocks": clk.summary(),
         "stages_ms": {k: v for k, v in stats.items() if k.startswith("t_")},
     }
+    if a.with_fp64:
+        line["plain_fp64"] = plain_fp64_comparison(F, solve_args=(m, call), res=res)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def plain_fp64_comparison(F, solve_args, res) -> dict:
+    """The same model solved in plain FP64 from G0 (no warm start), to the same
+    eps: its device seconds and how far the fast form's lambda, Sigma and mu
+    sit from it."""
+    m, call = solve_args
+    F.set_precision(64)
+    ref = F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
+                        m["init"], m["plist"], **dict(call, coarse=(1, 1)))
+    st = F.last_stats()
+    return {"seconds": ref["compute_ms"] / 1e3, "flex_iterations": int(st["iterations"]), "lambda": ref["lam"],
+            "lambda_rel_diff": abs(res["lam"] - ref["lam"]) / abs(ref["lam"]),
+            "sigma_max_rel_diff": float(np.abs(res["sigmak"] - ref["sigmak"]).max() / np.abs(ref["sigmak"]).max()),
+            "mu_diff": abs(res["mu"] - ref["mu"])}
 
 
 if __name__ == "__main__":
