@@ -273,23 +273,35 @@ def gen_kpoint_weight(invk, Nk: int):
     return w
 
 
-def gen_ham(klist, ham_r, rvec):
-    """k-space Hamiltonian [Nk,Norb,Norb] (libs/flibs/_hamiltonian.py:75-99)."""
+def gen_ham(klist, ham_r, rvec, Ovl_r=None):
+    """k-space Hamiltonian [Nk,Norb,Norb], and with overlap blocks Ovl_r also
+    the k-space overlap, (hamk, Ovlk) (libs/flibs/_hamiltonian.py:134-157)."""
     Nk, Nr, Norb = len(klist), len(rvec), ham_r.shape[1]
-    hamk = np.zeros((Nk, Norb, Norb), dtype=np.complex128)
-    _call("gen_ham", hamk, np.ascontiguousarray(klist, dtype=np.float64),
-          np.ascontiguousarray(ham_r, dtype=np.complex128), np.ascontiguousarray(rvec, dtype=np.float64),
-          i64(Nk), i64(Nr), i64(Norb))
-    return hamk
+
+    def transform(blocks):
+        out = np.zeros((Nk, Norb, Norb), dtype=np.complex128)
+        _call("gen_ham", out, np.ascontiguousarray(klist, dtype=np.float64),
+              np.ascontiguousarray(blocks, dtype=np.complex128), np.ascontiguousarray(rvec, dtype=np.float64),
+              i64(Nk), i64(Nr), i64(Norb))
+        return out
+
+    hamk = transform(ham_r)
+    return hamk if Ovl_r is None else (hamk, transform(Ovl_r))
 
 
-def get_eig(hamk):
-    """(eig[Nk,Norb] ascending, uni[Nk,Norb,Norb]) (libs/flibs/_hamiltonian.py:101-125)."""
+def get_eig(hamk, Ovlk=None, sw: bool = True):
+    """(eig[Nk,Norb] ascending, uni[Nk,Norb,Norb]), or eig alone when sw is
+    False (libs/flibs/_hamiltonian.py:160-185).  With an overlap Ovlk the
+    reference solves the generalized problem through get_eig_mlo, which this
+    library does not implement (the call raises)."""
     Nk, Norb = len(hamk), hamk.shape[1]
     eig = np.zeros((Nk, Norb))
     uni = np.zeros((Nk, Norb, Norb), dtype=np.complex128)
-    _call("get_eig", eig, uni, np.ascontiguousarray(hamk), i64(Nk), i64(Norb))
-    return eig, uni
+    if Ovlk is None:
+        _call("get_eig", eig, uni, np.ascontiguousarray(hamk), i64(Nk), i64(Norb))
+    else:
+        _call("get_eig_mlo")  # an exported stub: it reads no argument and reports the missing routine
+    return (eig, uni) if sw else eig
 
 
 def get_ffermi(eig, mu: float, temp: float):

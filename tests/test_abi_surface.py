@@ -143,3 +143,13 @@ def test_compute_entry_fails_loudly_without_gpu(lib):
         assert "no CUDA device" in str(e)
     else:
         assert np.isfinite(G).all()
+
+
+def test_non_orthogonal_basis_is_refused_loudly(lib):
+    """get_eig with an overlap (the reference's get_eig_mlo path,
+    libs/flibs/_hamiltonian.py:176-179) reaches the exported stub, which
+    reports the missing routine; no GPU is involved."""
+    from pyrpa_gb300 import flibs as F
+    hamk = np.tile(np.eye(2, dtype=np.complex128), (3, 1, 1))
+    with pytest.raises(RuntimeError, match="get_eig_mlo"):
+        F.get_eig(hamk, Ovlk=hamk)

@@ -1,0 +1,32 @@
+"""The Python mirror's optional arguments that call GPU entry points:
+gen_ham with overlap blocks returns (hamk, Ovlk) like the reference
+(libs/flibs/_hamiltonian.py:134-157), and get_eig(sw=False) returns the
+eigenvalues alone (:181-185).
+
+Opt-in (PYRPA_GB_PENDING_TESTS=1) until it has run on a GB300."""
+import os
+
+import numpy as np
+import pytest
+
+import _models as M
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(os.environ.get("PYRPA_GB_PENDING_TESTS") != "1",
+                                 reason="not yet run on a GB300 (PYRPA_GB_PENDING_TESTS=1)")]
+
+
+def test_gen_ham_overlap_and_eigenvalues_only():
+    from pyrpa_gb300 import build, flibs as F
+    if not build.LIB.exists():
+        build.build()
+    F.load_library()
+    rvec, ham_r = M.random_hoppings(2, 3)
+    klist, _, _ = F.gen_irr_k_TRS(4, 4, 1)
+    ovl = np.zeros_like(ham_r)
+    ovl[np.all(rvec == 0, axis=1)] = np.eye(2)
+    hamk, ovlk = F.gen_ham(klist, ham_r, rvec, Ovl_r=ovl)
+    assert np.array_equal(hamk, F.gen_ham(klist, ham_r, rvec))
+    assert np.allclose(ovlk, np.eye(2)[None])
+    eig, uni = F.get_eig(hamk)
+    assert np.array_equal(F.get_eig(hamk, sw=False), eig)
