@@ -332,6 +332,11 @@ void get_qp_(double* P, double* Q, const double* a, const double* xn, const doub
 void pade_with_trace(const double* arrayin, double* arrayout, const double* iwlist, const double* wlist,
                      const int64_t* Nk, const int64_t* Niw, const int64_t* Nw, const int64_t* Norb);
 
+/* fself.f90:85-129 gen_green_inv_from_eig: G^-1 from eig(Norb,Nk) and uni(Norb,Norb,Nk):
+ * Gk(Nk,Nw,Norb,Norb) = sum_n uni(m,n,k) conj(uni(l,n,k)) (iw + mu - eig(n,k)) - self */
+void gen_green_inv_from_eig(double* Gk, const double* self, const double* uni, const double* eig, const double* mu,
+                            const double* temp, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb);
+
 /* Symbols outside the accelerated path (transport, impurity, Eilenberger ...) are exported with no
  * arguments read and report "not part of the GB300 FLEX/RPA/Eliashberg engine"
  * so that `import libs.flibs` binds every name it expects. */

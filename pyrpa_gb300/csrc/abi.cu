@@ -644,6 +644,32 @@ void gen_green_inv_(double2* Gk, const double2* self, const double2* hamk, const
   ABI_CATCH("gen_green_inv_", nan_fill(Gk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
 }
 
+// fself.f90:85-129: G^-1(k, iw)_ml = sum_n U_mn conj(U_ln) (iw + mu - e_n) - Sigma_ml.  With U unitary
+// that is (iw + mu) delta_ml - H_ml - Sigma_ml for H = U diag(e) U^dagger, so H is rebuilt on the host
+// (Nk Norb^3 operations) and the G^-1 kernel of gen_green_inv_ does the rest.
+void gen_green_inv_from_eig(double2* Gk, const double2* self, const double2* uni, const double* eig,
+                            const double* mu, const double* temp, const int64_t* Nk, const int64_t* Nw,
+                            const int64_t* Norb) {
+  ABI_TRY
+  const int64_t nk = *Nk, no = *Norb;
+  PGB_CHECK(no >= 1 && no <= kMaxOrb, "Norb must be in [1, 8]");
+  std::vector<double2> h((size_t)no * no * nk);
+  for (int64_t k = 0; k < nk; ++k)
+    for (int64_t l = 0; l < no; ++l)
+      for (int64_t m = 0; m < no; ++m) {
+        double re = 0, im = 0;
+        for (int64_t n = 0; n < no; ++n) {
+          const double2 a = uni[m + no * n + no * no * k], b = uni[l + no * n + no * no * k];
+          const double e = eig[n + no * k];
+          re += e * (a.x * b.x + a.y * b.y);  // e * a * conj(b)
+          im += e * (a.y * b.x - a.x * b.y);
+        }
+        h[m + no * l + no * no * k] = make_double2(re, im);
+      }
+  gen_green_inv_(Gk, self, h.data(), mu, temp, Nk, Nw, Norb);
+  ABI_CATCH("gen_green_inv_from_eig", nan_fill(Gk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
+}
+
 void getinv_(double2* Gk, const int64_t* Nk, const int64_t* Nw, const int64_t* Norb) {
   ABI_TRY
   ensure_context();
@@ -1594,7 +1620,6 @@ PGB_STUB(calc_sigma_hall)
 PGB_STUB(calc_tau_epa)
 PGB_STUB(calc_tdf)
 PGB_STUB(gen_dos)
-PGB_STUB(gen_green_inv_from_eig)
 PGB_STUB(gen_imp_ham)
 PGB_STUB(gen_tr_greenw_0)
 PGB_STUB(get_band_to_orb_delta)

@@ -91,6 +91,7 @@ _SIGNATURES = {
     "pyrpa_gb_regrid_sigma": [_c128, _c128, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
     "pyrpa_gb_wannier_r": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _pi, _pi],
     "pyrpa_gb_fft_candidates": [_pi, _pi, _i64, _pi, _pi],
+    "gen_green_inv_from_eig": [_c128, _c128, _c128, _f64, _pd, _pd, _pi, _pi, _pi],
     "pyrpa_gb_sigma_interp": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _i64, _i64, _pi, _pi, _pi, _pi, _pi,
                               _pi, _pd],
     "pyrpa_gb_lws_create": [_pi],
@@ -369,6 +370,17 @@ def gen_Green0(eig, uni, mu: float, temp: float, Nw: int):
     Gk = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
     _call("gen_green0_", Gk, np.ascontiguousarray(eig), np.ascontiguousarray(uni), dbl(mu), dbl(temp),
           i64(Nk), i64(Nw), i64(Norb))
+    return Gk
+
+
+def gen_green_from_eig(selfen, eig, uni, mu: float, temp: float):
+    """Interacting G [Norb,Norb,Nw,Nk] from the band energies and eigenvectors
+    (libs/flibs/_green.py:119-139: gen_green_inv_from_eig, then getinv_)."""
+    Nk, Norb, Nw = len(eig), eig.shape[1], selfen.shape[2]
+    Gk = np.zeros((Norb, Norb, Nw, Nk), dtype=np.complex128)
+    _call("gen_green_inv_from_eig", Gk, np.ascontiguousarray(selfen), np.ascontiguousarray(uni),
+          np.ascontiguousarray(eig, dtype=np.float64), dbl(mu), dbl(temp), i64(Nk), i64(Nw), i64(Norb))
+    _call("getinv_", Gk, i64(Nk), i64(Nw), i64(Norb))
     return Gk
 
 

@@ -30,3 +30,24 @@ def test_gen_ham_overlap_and_eigenvalues_only():
     assert np.allclose(ovlk, np.eye(2)[None])
     eig, uni = F.get_eig(hamk)
     assert np.array_equal(F.get_eig(hamk, sw=False), eig)
+
+
+def test_green_from_eigenpairs_matches_oracle():
+    """gen_green_from_eig (fself.f90:85-129, then getinv_) equals G from H(k)
+    and Sigma: U (iw + mu - E) U^dagger - Sigma is (iw + mu) - H - Sigma."""
+    from oracle import api as O
+    from pyrpa_gb300 import build, flibs as F
+    if not build.LIB.exists():
+        build.build()
+    F.load_library()
+    F.set_precision(64)
+    rvec, ham_r = M.random_hoppings(3, 7, bandwidth=4.0)
+    klist, _, _ = O.gen_irr_k_TRS(6, 6, 1)
+    hamk = O.gen_ham(klist, ham_r, rvec)
+    eig, uni = O.get_eig(hamk)
+    rng = np.random.default_rng(3)
+    Nw, mu, temp = 16, 0.1, 0.05
+    sig = 0.1 * (rng.normal(size=(3, 3, Nw, len(klist))) + 1j * rng.normal(size=(3, 3, Nw, len(klist))))
+    got = F.gen_green_from_eig(sig, eig, uni, mu, temp)
+    ref = O.gen_green(sig, hamk, mu, temp)
+    assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max() + 2e-9
