@@ -35,3 +35,26 @@ def test_device_bytes_grow_with_size():
     assert 0 < S.device_bytes(base) < S.device_bytes(big)
     # the largest instance fits one GB300's HBM in complex128
     assert S.device_bytes(big, 16) < 200e9
+
+
+def test_run_records_failures_and_keeps_the_draw_order(monkeypatch):
+    """run() solves the largest footprint first, records a failing instance
+    instead of raising, and returns the results in draw order."""
+    from pyrpa_gb300 import flibs
+    calls = []
+
+    def fake_solve(inst, eps=1e-4, scf_loop=300):
+        calls.append(inst.index)
+        if inst.index == 2:
+            raise RuntimeError("singular G^-1 in the Dyson step")
+        return dict(index=inst.index, iterations=3)
+
+    monkeypatch.setattr(S, "solve", fake_solve)
+    monkeypatch.setattr(flibs, "load_library", lambda *a, **k: None)
+    monkeypatch.setattr(flibs, "set_verbose", lambda v: None)
+    insts = S.draw(6, seed=1)
+    res = S.run(insts)
+    assert calls == [x.index for x in sorted(insts, key=S.device_bytes, reverse=True)]
+    assert [r["index"] for r in res] == list(range(6))
+    assert "error" in res[2] and "Dyson" in res[2]["error"]
+    assert all("error" not in r for i, r in enumerate(res) if i != 2)
