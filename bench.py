@@ -42,8 +42,69 @@ METRIC = "time-to-converged FLEX Σ+λ, 5-orb 64²×2048: FP32+warm-start vs pla
 DEFAULT_COUNTS = {"c2": (30, 20), "c1": (30, 20), "c5": (30, 20)}
 
 
+# ------------------------------------------------------ profiling cases
+# Small launches of single engine kernels for ncu captures: each runs one ABI
+# call on a synthetic input larger than L2 (129 MB) but a few hundred MB at
+# most, so that a capture of one launch replays quickly.
+#   vertex  get_vsigma_flex_nosoc_ on a 5-orbital chi0 (Nchi = 25), 130
+#           irreducible q x 512 frequencies = 66,560 matrices
+#   chi0    get_chi0_tail on a 5-orbital 16x16 mesh with 512 frequencies
+#   flex    mkself, one FLEX iteration of the same model
+#   fft     get_chi0 of a 1-orbital 64x64 mesh with 2048 frequencies: FFT
+#           passes over 64x64x4096 arrays (134 MB in FP32)
+def _profile_model(F, models, Norb=5, N=16, Nw=512, temp=0.02):
+    rvec, ham_r = models.seeded_hoppings(Norb, 4, [(1, 0, 0), (1, 1, 0), (2, 0, 0)], dim=2, bandwidth=4.0)
+    klist, kmap, invk = F.gen_irr_k_TRS(N, N, 1)
+    hamk = F.gen_ham(klist, ham_r, rvec)
+    eig, uni = F.get_eig(hamk)
+    olist, site = F.get_chi_orb_list(Norb)
+    S, C = F.gen_SCmatrix(olist, site, 1.2, 0.2)
+    w = F.gen_kpoint_weight(invk, len(klist))
+    mu = models.bare_mu(eig, w, 0.6 * Norb, temp)
+    return dict(Norb=Norb, N=N, Nw=Nw, temp=temp, klist=klist, kmap=kmap, invk=invk, hamk=hamk, eig=eig, uni=uni,
+                olist=olist, S=S, C=C, mu=mu)
+
+
+def profile_case(case: str, precision: int, repeat: int) -> int:
+    sys.path.insert(0, str(ROOT))
+    from pyrpa_gb300 import flibs as F, models
+    F.load_library()
+    F.set_verbose(0)
+    F.set_precision(precision)
+    t0 = time.perf_counter()
+    for _ in range(repeat):
+        if case == "vertex":
+            Nchi, Nk, Nw = 25, 130, 512
+            rng = np.random.default_rng(0)
+            chi = 0.05 * (rng.standard_normal((Nchi, Nchi, Nw, Nk)) + 1j * rng.standard_normal((Nchi, Nchi, Nw, Nk)))
+            olist, site = F.get_chi_orb_list(5)
+            S, C = F.gen_SCmatrix(olist, site, 1.2, 0.2)
+            # the raw entry with explicit Nk, Nw (the Python wrapper reads
+            # them off the array the way the reference wrapper does)
+            F._call("get_vsigma_flex_nosoc_", chi, S, C, F.i64(Nk), F.i64(Nw), F.i64(Nchi))
+        elif case == "chi0":
+            m = _profile_model(F, models)
+            Gk = F.gen_Green0(m["eig"], m["uni"], m["mu"], m["temp"], m["Nw"])
+            F.get_chi0_tail(m["S"], m["C"], Gk, m["eig"], m["uni"], m["olist"], m["kmap"], m["invk"], m["mu"],
+                            m["temp"], m["N"], m["N"], 1)
+        elif case == "fft":
+            m = _profile_model(F, models, Norb=1, N=64, Nw=2048, temp=0.01)
+            Gk = F.gen_Green0(m["eig"], m["uni"], m["mu"], m["temp"], m["Nw"])
+            F.get_chi0(m["S"], m["C"], Gk, m["olist"], m["kmap"], m["invk"], m["temp"], m["N"], m["N"], 1)
+        else:
+            m = _profile_model(F, models)
+            F.mkself(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"],
+                     0.6 * m["Norb"], m["temp"], m["Nw"], m["N"], m["N"], 1, False, False, scf_loop=1, eps=1e-4,
+                     pp=0.5, sw_tail=True, sw_rescale=True)
+    print(f"{case}: {repeat} call(s) in {time.perf_counter() - t0:.3f} s", flush=True)
+    return 0
+
+
 def parse():
     p = argparse.ArgumentParser()
+    p.add_argument("--profile-case", choices=["vertex", "chi0", "flex", "fft"],
+                   help="run one small profiling case instead of the benchmark")
+    p.add_argument("--repeat", type=int, default=1, help="calls of the profiling case")
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=2)
     p.add_argument("--warmup", type=int, default=3)
@@ -214,6 +275,8 @@ def max_over_ranks(values, dist):
 
 def main():
     a = parse()
+    if a.profile_case:
+        return profile_case(a.profile_case, {"mixed": 32, "32": 32, "64": 64}[a.precision], a.repeat)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

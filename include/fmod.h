@@ -151,7 +151,9 @@ void pyrpa_gb_set_precision(const int64_t* bits);
 void pyrpa_gb_get_precision(int64_t* bits);
 /* 0 silences the progress lines the reference prints to stdout */
 void pyrpa_gb_set_verbose(const int64_t* level);
-/* message of the last failure (NUL-terminated, at most len bytes) and 1/0 */
+/* message of the last failure (NUL-terminated, at most len bytes) and its
+ * code: 0 none, 1 a failure of the library or the GPU, 2 an input the caller
+ * has to fix (the Python wrappers raise ValueError for 2, RuntimeError for 1) */
 void pyrpa_gb_last_error(char* buf, const int64_t* len, int64_t* code);
 void pyrpa_gb_clear_error(void);
 /* kernels this process has launched (all engine kernels, FFT passes included) */
@@ -350,6 +352,18 @@ void gen_green_inv_from_eig(double* Gk, const double* self, const double* uni, c
 void pyrpa_gb_regrid_sigma(double* out, const double* sigma, const int64_t* Nk, const int64_t* Nw_old,
                            const int64_t* Nw_new, const int64_t* Norb, const double* temp_old,
                            const double* temp_new, const double* w_scale);
+
+/* plibs.regrid_sigma_bin (libs/plibs/_calc.py:52-182) with its file handling:
+ * reads the io_sigma records of in_path (fself.f90:742-780), checks temp_old,
+ * Norb and Nw_old against the (temp, Nw, Norb, Nk) record when the file has
+ * one (NaN / 0 = take the file's value; Nw_new 0 = keep Nw_old), regrids as
+ * pyrpa_gb_regrid_sigma and writes mu, mu_OLD, the new Sigma and the record
+ * of the new mesh to out_path.  *Nk_out, *Nw_new_out = the written shape, or
+ * -1 with pyrpa_gb_last_error code 2 when the file or an argument is at fault. */
+void pyrpa_gb_regrid_sigma_file(const char* in_path, const char* out_path, const double* temp_old,
+                                const double* temp_new, const int64_t* Norb, const int64_t* Nw_old,
+                                const int64_t* Nw_new, const double* w_scale, int64_t* Nk_out,
+                                int64_t* Nw_new_out);
 
 /* The k -> R step of plibs.output_self_wannier / output_gap_wannier
  * (libs/plibs/_wannier_io.py:52-98): data in the wrappers' layout

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <limits>
 #include <map>
 #include <mutex>
@@ -67,10 +68,10 @@ std::mutex g_err_mu;
 std::string g_last_error;
 int64_t g_last_code = 0;
 
-void report(const char* fn, const char* what) {
+void report(const char* fn, const char* what, int64_t code = 1) {
   std::lock_guard<std::mutex> lk(g_err_mu);
   g_last_error = std::string(fn) + ": " + what;
-  g_last_code = 1;
+  g_last_code = code;
   fprintf(stderr, "pyrpa_gb300 error in %s: %s\n", fn, what);
   fflush(stderr);
 }
@@ -414,6 +415,10 @@ __global__ void k_map_full_checked(double2* out, const double2* vals, const int6
 
 #define ABI_TRY try {
 #define ABI_CATCH(name, onerr)            \
+  }                                       \
+  catch (const BadInput& e) {             \
+    report(name, e.what(), 2);            \
+    onerr;                                \
   }                                       \
   catch (const std::exception& e) {       \
     report(name, e.what());               \
@@ -880,6 +885,104 @@ void pyrpa_gb_regrid_sigma(double2* out, const double2* sig, const int64_t* Nk, 
   o.download(out, n_new);
   sync();
   ABI_CATCH("pyrpa_gb_regrid_sigma", nan_fill(out, (size_t)(*Nk) * (*Nw_new) * (*Norb) * (*Norb)))
+}
+
+}  // extern "C"
+
+namespace {
+
+// Every record of a gfortran sequential file (4-byte length, payload, the
+// same length again).  The scan stops at the first record whose markers
+// do not close, so a damaged tail reads as an absent footer.
+std::vector<std::string> sequential_records(const char* path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f.good()) throw BadInput(std::string("cannot open ") + path);
+  std::vector<std::string> out;
+  for (;;) {
+    int32_t head = 0, tail = -1;
+    if (!f.read(reinterpret_cast<char*>(&head), 4) || head < 0) break;
+    std::string body((size_t)head, '\0');
+    if (head && !f.read(&body[0], head)) break;
+    if (!f.read(reinterpret_cast<char*>(&tail), 4) || tail != head) break;
+    out.push_back(std::move(body));
+  }
+  return out;
+}
+
+void put_record(std::ofstream& f, const void* p, size_t n) {
+  if (n >= 2147483639ULL) throw Error("a sigma.bin record above 2 GiB is not supported");
+  const int32_t len = (int32_t)n;
+  f.write(reinterpret_cast<const char*>(&len), 4);
+  f.write(reinterpret_cast<const char*>(p), (std::streamsize)n);
+  f.write(reinterpret_cast<const char*>(&len), 4);
+}
+
+// |given - stored| <= 1e-8 |stored|: the footer agreement test of the seed regrid
+void footer_agrees(const char* what, double given, double stored) {
+  if (!(std::fabs(given - stored) <= 1e-8 * std::fabs(stored)))
+    throw BadInput(std::string(what) + " = " + std::to_string(given) + " disagrees with the value " +
+                   std::to_string(stored) + " stored in the file's (temp, Nw, Norb, Nk) record");
+}
+
+}  // namespace
+
+extern "C" {
+
+void pyrpa_gb_regrid_sigma_file(const char* in_path, const char* out_path, const double* temp_old,
+                                const double* temp_new, const int64_t* Norb, const int64_t* Nw_old,
+                                const int64_t* Nw_new, const double* w_scale, int64_t* Nk_out,
+                                int64_t* Nw_new_out) {
+  ABI_TRY
+  *Nk_out = *Nw_new_out = -1;
+  if (!std::isfinite(*temp_new)) throw BadInput("the target temperature temp_new must be given");
+  const std::vector<std::string> rec = sequential_records(in_path);
+  if (rec.size() < 3 || rec[0].size() != 8 || rec[1].size() != 8 || rec[2].size() % sizeof(double2))
+    throw BadInput(std::string(in_path) + " does not start with the mu, mu_OLD and Sigma records of io_sigma");
+  const bool footer = rec.size() >= 4 && rec[3].size() == 4 * sizeof(double);
+  double t_old = *temp_old;
+  int64_t nw_old = *Nw_old, norb = *Norb;
+  double meta[4] = {0, 0, 0, 0};
+  if (footer) {
+    memcpy(meta, rec[3].data(), sizeof(meta));
+    if (std::isfinite(t_old)) footer_agrees("temp_old", t_old, meta[0]);
+    if (nw_old > 0) footer_agrees("Nw_old", (double)nw_old, (double)std::llround(meta[1]));
+    if (norb > 0) footer_agrees("Norb", (double)norb, (double)std::llround(meta[2]));
+    t_old = meta[0];
+    nw_old = std::llround(meta[1]);
+    norb = std::llround(meta[2]);
+  } else if (!std::isfinite(t_old) || nw_old <= 0 || norb <= 0) {
+    throw BadInput(std::string(in_path) + " has no (temp, Nw, Norb, Nk) record, so temp_old, Norb and Nw_old "
+                   "have to be passed");
+  }
+  if (nw_old <= 0 || norb <= 0) throw BadInput("the stored Nw and Norb must be positive");
+  const int64_t nw_new = *Nw_new > 0 ? *Nw_new : nw_old;
+  const int64_t nvals = (int64_t)(rec[2].size() / sizeof(double2)), per_k = nw_old * norb * norb;
+  if (nvals % per_k)
+    throw BadInput("the Sigma record holds " + std::to_string(nvals) + " values, not a multiple of Nw_old*Norb^2 = " +
+                   std::to_string(per_k));
+  const int64_t nk = nvals / per_k;
+  if (footer && nk != std::llround(meta[3]))
+    throw BadInput("the Sigma record gives Nk = " + std::to_string(nk) + " but the file's last record says " +
+                   std::to_string(std::llround(meta[3])));
+  ensure_context();
+  DBuf<double2> s(nvals), o(nk * nw_new * norb * norb);
+  s.upload(reinterpret_cast<const double2*>(rec[2].data()), nvals);
+  regrid_sigma(o.p, s.p, (int)nk, (int)nw_old, (int)nw_new, (int)norb, t_old, *temp_new, *w_scale);
+  std::vector<double2> host((size_t)(nk * nw_new * norb * norb));
+  o.download(host.data(), (long long)host.size());
+  sync();
+  std::ofstream f(out_path, std::ios::binary | std::ios::trunc);
+  if (!f.good()) throw BadInput(std::string("cannot write ") + out_path);
+  put_record(f, rec[0].data(), 8);
+  put_record(f, rec[1].data(), 8);
+  put_record(f, host.data(), host.size() * sizeof(double2));
+  const double footer_new[4] = {*temp_new, (double)nw_new, (double)norb, (double)nk};
+  put_record(f, footer_new, sizeof(footer_new));
+  f.close();
+  if (!f) throw Error(std::string("writing ") + out_path + " failed");
+  *Nk_out = nk;
+  *Nw_new_out = nw_new;
+  ABI_CATCH("pyrpa_gb_regrid_sigma_file", (*Nk_out = -1, *Nw_new_out = -1))
 }
 
 void pyrpa_gb_wannier_r(double2* out, const double2* data, const int64_t* kmap, const int64_t* invk,

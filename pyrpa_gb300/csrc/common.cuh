@@ -189,6 +189,11 @@ __device__ __forceinline__ dfl shfl_xor(dfl v, int m) {
 struct Error : std::runtime_error {
   explicit Error(const std::string& s) : std::runtime_error(s) {}
 };
+// an argument or input file the caller has to fix (error code 2 at the ABI,
+// ValueError in the Python wrappers); every other failure is code 1
+struct BadInput : Error {
+  explicit BadInput(const std::string& s) : Error(s) {}
+};
 
 #define PGB_CUDA(call)                                                               \
   do {                                                                               \

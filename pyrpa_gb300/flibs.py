@@ -14,6 +14,7 @@ functions raise ``RuntimeError`` with the library's message.
 from __future__ import annotations
 
 import ctypes
+import os
 from ctypes import POINTER, byref, c_bool, c_char, c_double, c_int64
 from pathlib import Path
 
@@ -89,6 +90,7 @@ _SIGNATURES = {
                              _f64, _f64, ctypes.c_void_p, _pd, _pd, _pd, _pd, _pd, _pi, _pd, _pd] + [_pi] * 10
     + [_pb, _pb, _pi, _pi, _pi, _pd, _i64],
     "pyrpa_gb_regrid_sigma": [_c128, _c128, _pi, _pi, _pi, _pi, _pd, _pd, _pd],
+    "pyrpa_gb_regrid_sigma_file": [ctypes.c_char_p, ctypes.c_char_p, _pd, _pd, _pi, _pi, _pi, _pd, _pi, _pi],
     "pyrpa_gb_wannier_r": [_c128, _c128, _i64, _i64, _pi, _pi, _pi, _pi, _pi, _pi, _pi],
     "pyrpa_gb_fft_candidates": [_pi, _pi, _i64, _pi, _pi],
     "gen_green_inv_from_eig": [_c128, _c128, _c128, _f64, _pd, _pd, _pi, _pi, _pi],
@@ -169,12 +171,16 @@ def last_error() -> str:
 
 
 def _call(name, *args):
+    """Calls one entry point; a recorded failure becomes ValueError when the
+    library flags the input (error code 2), RuntimeError otherwise."""
     lib = load_library()
     lib.pyrpa_gb_clear_error()
     getattr(lib, name)(*args)
-    msg = last_error()
-    if msg:
-        raise RuntimeError(msg)
+    code = c_int64(0)
+    buf = ctypes.create_string_buffer(2048)
+    lib.pyrpa_gb_last_error(buf, i64(len(buf)), byref(code))
+    if code.value:
+        raise (ValueError if code.value == 2 else RuntimeError)(buf.value.decode(errors="replace"))
 
 
 # ------------------------------------------------------------------ control
@@ -504,6 +510,22 @@ def regrid_sigma(sigmak, temp_old: float, temp_new: float, Nw_new: int, w_scale:
     _call("pyrpa_gb_regrid_sigma", out, sigmak, i64(Nk), i64(Nw_old), i64(Nw_new), i64(Norb), dbl(temp_old),
           dbl(temp_new), dbl(w_scale))
     return out
+
+
+def regrid_sigma_file(path: str, out_path: str, temp_old, temp_new: float, Norb, Nw_old, Nw_new,
+                      w_scale: float = 1.0):
+    """Reads a sigma.bin seed, moves it onto Nw_new frequencies at temp_new and
+    writes it to out_path, all inside the library (record parsing, checks
+    against the file's (temp, Nw, Norb, Nk) record, the GPU regrid, the new
+    file).  None means "take it from the file" (temp_old, Norb, Nw_old) or
+    "keep Nw_old" (Nw_new).  Returns (Nk, Nw_new); ValueError for a file or
+    argument the caller has to fix."""
+    nk, nw = c_int64(-1), c_int64(-1)
+    _call("pyrpa_gb_regrid_sigma_file", os.fsencode(path), os.fsencode(out_path),
+          dbl(np.nan if temp_old is None else temp_old), dbl(np.nan if temp_new is None else temp_new),
+          i64(0 if Norb is None else Norb), i64(0 if Nw_old is None else Nw_old),
+          i64(0 if Nw_new is None else Nw_new), dbl(w_scale), byref(nk), byref(nw))
+    return int(nk.value), int(nw.value)
 
 
 def fft_candidates(n: int, elem_bytes: int):

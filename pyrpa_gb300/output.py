@@ -44,6 +44,6 @@ def output_gap_function(invk, kmap, gap, uni, plist, gap_sym, Nx: int, soc=False
                         if kx == Nx - 1:
                             f.write("\n")
             except IOError as e:
-                print(f"Error: Failed to write '{name}': {e}", flush=True)
+                print(f"output_gap_function: {name} not written ({e})", flush=True)
                 continue
     return 0

@@ -1,15 +1,16 @@
-"""Self-energy seeds: the reference's sigma.bin regrid with the compute on the GPU.
+"""Self-energy seeds on a new Matsubara mesh (plibs.regrid_sigma_bin).
 
-``regrid_sigma_bin`` has the signature and the file semantics of
-plibs.regrid_sigma_bin (libs/plibs/_calc.py:52-182): it reads the
-gfortran-sequential sigma.bin that mkself writes (mu, mu_OLD, sigmak in
-Fortran order and the (temp, Nw, Norb, Nk) footer), regrids Sigma along the
-Matsubara axis and writes the file back with a footer for the new mesh.  The
-regrid itself runs in libfmod.so (pyrpa_gb_regrid_sigma).
+``regrid_sigma_bin`` keeps the signature, defaults, return value and error
+cases of plibs.regrid_sigma_bin (libs/plibs/_calc.py:52-182), which a pyrpa
+script calls between two ``mkself`` runs at different temperatures.  All of
+the work happens in libfmod.so (``pyrpa_gb_regrid_sigma_file``): it parses the
+gfortran sequential records that io_sigma writes (mu, mu_OLD, Sigma in
+Fortran order, and the optional (temp, Nw, Norb, Nk) record), checks the
+arguments against that record, regrids on the GPU and writes the new file
+with the record of the new mesh.  Problems the caller has to fix arrive here
+as ValueError, as in the reference.
 """
 from __future__ import annotations
-
-import numpy as np
 
 from . import flibs
 
@@ -17,41 +18,10 @@ from . import flibs
 def regrid_sigma_bin(temp_old: float | None = None, temp_new: float | None = None, Norb: int | None = None,
                      Nw_old: int | None = None, Nw_new: int | None = None, w_scale: float | None = None,
                      path: str = "sigma.bin", out_path: str | None = None):
-    """Returns (Nk, Nw_new) like the reference; raises ValueError where it does."""
-    from scipy.io import FortranFile
+    """Regrid the sigma.bin at ``path`` onto Nw_new frequencies at temp_new
+    and write it to ``out_path`` (default: in place).  Arguments left None
+    are read from the file; returns (Nk, Nw_new)."""
     if temp_new is None:
-        raise ValueError("temp_new is required")
-    w_scale = 1.0 if w_scale is None else w_scale
-    with FortranFile(path, "r") as f:
-        mu = f.read_record(np.float64)
-        mu_old = f.read_record(np.float64)
-        flat = f.read_record(np.complex128)
-        try:
-            meta = f.read_record(np.float64)
-            if meta.size != 4:
-                meta = None
-        except Exception:
-            meta = None
-    if meta is not None:
-        stored = {"temp_old": meta[0], "Nw_old": int(round(meta[1])), "Norb": int(round(meta[2]))}
-        for name, given in (("temp_old", temp_old), ("Nw_old", Nw_old), ("Norb", Norb)):
-            if given is not None and not np.isclose(given, stored[name], rtol=1e-8, atol=0.0):
-                raise ValueError(f"{name}={given} contradicts the sigma.bin metadata footer ({stored[name]})")
-        temp_old, Nw_old, Norb = stored["temp_old"], stored["Nw_old"], stored["Norb"]
-    elif temp_old is None or Nw_old is None or Norb is None:
-        raise ValueError("sigma.bin carries no metadata footer: temp_old, Norb and Nw_old must be given")
-    Nw_new = Nw_old if Nw_new is None else Nw_new
-    Nk, rem = divmod(flat.size, Nw_old * Norb * Norb)
-    if rem:
-        raise ValueError(f"sigma.bin size {flat.size} is not divisible by Nw_old*Norb^2 = {Nw_old * Norb * Norb}")
-    if meta is not None and Nk != int(round(meta[3])):
-        raise ValueError(f"inferred Nk={Nk} contradicts the metadata footer ({int(round(meta[3]))})")
-    # Fortran (Nk, Nw, Norb, Norb) is the wrappers' [Norb, Norb, Nw, Nk] in C order
-    sig = flat.reshape((Norb, Norb, Nw_old, Nk))
-    out = flibs.regrid_sigma(sig, temp_old, temp_new, Nw_new, w_scale)
-    with FortranFile(out_path or path, "w") as f:
-        f.write_record(mu)
-        f.write_record(mu_old)
-        f.write_record(np.ascontiguousarray(out).ravel())
-        f.write_record(np.array([temp_new, float(Nw_new), float(Norb), float(Nk)]))
-    return Nk, Nw_new
+        raise ValueError("regrid_sigma_bin needs the target temperature temp_new")
+    return flibs.regrid_sigma_file(path, out_path or path, temp_old, temp_new, Norb, Nw_old, Nw_new,
+                                   1.0 if w_scale is None else w_scale)

@@ -4,8 +4,6 @@ each (x, y) plane in one kernel), the long pass (PYRPA_GB_FFT_LONG=1: a
 four-step axis in one kernel) and autotuned plans (PYRPA_GB_FFT_TUNE=1).  Mesh shapes here are used by no other test, so their FFT plans are
 built while the switch is on; it is cleared right after, so that plans made
 later take the default passes.
-
-Opt-in (PYRPA_GB_PENDING_TESTS=1) until the plane kernel has run on a GB300.
 """
 import os
 
@@ -15,9 +13,7 @@ import pytest
 import _models as M
 from oracle import api as O
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("PYRPA_GB_PENDING_TESTS") != "1",
-                                 reason="FFT plane kernel not yet run on a GB300 (PYRPA_GB_PENDING_TESTS=1)")]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")

@@ -1,19 +1,14 @@
 """The Python mirror's optional arguments that call GPU entry points:
 gen_ham with overlap blocks returns (hamk, Ovlk) like the reference
 (libs/flibs/_hamiltonian.py:134-157), and get_eig(sw=False) returns the
-eigenvalues alone (:181-185).
-
-Opt-in (PYRPA_GB_PENDING_TESTS=1) until it has run on a GB300."""
-import os
+eigenvalues alone (:181-185)."""
 
 import numpy as np
 import pytest
 
 import _models as M
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("PYRPA_GB_PENDING_TESTS") != "1",
-                                 reason="not yet run on a GB300 (PYRPA_GB_PENDING_TESTS=1)")]
+pytestmark = pytest.mark.gpu
 
 
 def test_gen_ham_overlap_and_eigenvalues_only():

@@ -1,10 +1,7 @@
 """GPU parity on a model of two sites (4 orbitals as [2, 2], Nchi = 8 pairs
 within the sites): chi0 and three FLEX iterations through the C ABI against
 the FP64 oracle, at the FP64 tolerances of the other parity tests.
-
-Opt-in (PYRPA_GB_PENDING_TESTS=1) until it has run on a GB300.
 """
-import os
 
 import numpy as np
 import pytest
@@ -12,9 +9,7 @@ import pytest
 import _models as M
 from oracle import api as O
 
-pytestmark = [pytest.mark.gpu,
-              pytest.mark.skipif(os.environ.get("PYRPA_GB_PENDING_TESTS") != "1",
-                                 reason="several-site orbital lists not yet run on a GB300 (PYRPA_GB_PENDING_TESTS=1)")]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
