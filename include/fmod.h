@@ -452,9 +452,12 @@ void pyrpa_gb_lws_apply(const int64_t* handle, double* sigma, const double* uni,
  * device array, so Nk is limited to 65,536 (larger Nk is rejected with an
  * error).  Nothing in the scratch has to start at zero: each call writes the
  * Nk values it reads.  An invk(1,i) outside [1,Nk] gives NaN at chiqout(i).
- * The first call on a device does a one-time set-up (it
- * looks up the scratch address and launches each kernel once, empty); make
- * that first call before any stream capture.  Calls whose work overlaps on
+ * The first call on a device does a one-time set-up: it looks up the
+ * scratch address and launches each kernel once, empty.  Under CUDA's lazy
+ * module loading (the default) that is when the library's module and the
+ * eigenvalue kernel's per-thread local memory are mapped on the device, so
+ * make that first call before the host's allocator reserves most of HBM, and
+ * before any stream capture; later calls take no device memory.  Calls whose work overlaps on
  * the device (different streams, or threads) share the one scratch array and
  * race: order them on one stream.  Returns 0 on success, 1 on an error whose
  * message pyrpa_gb_last_error returns. */

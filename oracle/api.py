@@ -54,6 +54,10 @@ def gen_green(selfen, hamk, mu, temp):
     return np.ascontiguousarray(O.gen_green_F(selfen.T, hamk.transpose(0, 2, 1), mu, temp).T)
 
 
+def gen_green_inv_from_eig(selfen, eig, uni, mu, temp):
+    return np.ascontiguousarray(O.gen_green_inv_from_eig_F(selfen.T, eig, uni.transpose(0, 2, 1), mu, temp).T)
+
+
 def _grid(kmap, invk, Nx, Ny, Nz):
     return O.KGrid(np.asarray(kmap), np.asarray(invk), Nx, Ny, Nz)
 

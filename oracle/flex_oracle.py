@@ -291,6 +291,14 @@ def gen_green_F(sigma_F, H_F, mu, temp):
     return np.linalg.inv(A)
 
 
+def gen_green_inv_from_eig_F(sigma_F, eig, U_F, mu, temp):
+    """G^-1[i,j,m,l] = sum_n U(m,n) U*(l,n) (mu + i w_j - e_n) - Sigma[i,j,m,l]
+    with the U given, unitary or not (fself.f90:85-129)."""
+    iw = mu + 1j * matsubara(temp, sigma_F.shape[1])
+    fac = iw[None, :, None] - eig[:, None, :]                   # [Nk,Nw,n]
+    return np.einsum("kmn,kln,kwn->kwml", U_F, np.conj(U_F), fac) - sigma_F
+
+
 # --------------------------------------------------------------------------- #
 #  chi0 (fchi.f90:319-918)
 # --------------------------------------------------------------------------- #

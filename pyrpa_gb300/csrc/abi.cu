@@ -132,6 +132,28 @@ __global__ void k_get_eig(double* eig, double2* uni, const double2* hk, int64_t 
   }
 }
 
+// G^-1(k, iw_j)_ml = sum_n U_mn conj(U_ln) (mu + i w_j - e_n) - Sigma_ml with
+// whatever U is given (fself.f90:85-129): U U^dagger multiplies i w + mu, so a
+// U that is not exactly unitary gives the reference's values too.  One thread
+// per (k, j), k fastest, so each (m, l) plane is written in coalesced runs.
+__global__ void k_green_inv_eig(double2* G, const double2* sig, const double2* uni, const double* eig, double mu,
+                                double temp, int64_t Nk, int64_t Nw, int No) {
+  const long long KW = Nk * Nw;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < KW; t += (long long)gridDim.x * blockDim.x) {
+    const long long i = t % Nk, j = t / Nk;
+    const double2 iw = make_double2(mu, (double)(2 * j + 1) * 3.141592653589793238462643383279 * temp);
+    const double2* U = uni + (long long)No * No * i;
+    const double* e = eig + (long long)No * i;
+    for (int l = 0; l < No; ++l)
+      for (int m = 0; m < No; ++m) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int n = 0; n < No; ++n) acc += (U[m + No * n] * conj(U[l + No * n])) * (iw - make_double2(e[n], 0.0));
+        const long long idx = t + KW * (m + (long long)No * l);
+        G[idx] = acc - sig[idx];
+      }
+  }
+}
+
 __global__ void k_ffermi(double* f, const double* eig, double mu, double itemp, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     f[i] = 0.5 - 0.5 * tanh((eig[i] - mu) * itemp);
@@ -393,8 +415,18 @@ auto chi0_fn() {
 // memory), and loops that enqueue work on their own stream and must not wait
 // for an allocation or a host copy on every call.  Its only scratch, one value
 // per irreducible q point, is the fixed array below.
+//
+// What the first call on a device takes: with CUDA's lazy module loading
+// (the default), the module that holds this array and these kernels, and the
+// local memory of the eigenvalue kernel (a 32x32 complex-double working matrix
+// per thread), are mapped on that device only when the module is first used.
+// The first call on each device therefore does a set-up (the array's address,
+// and one empty launch of each kernel) that takes that memory.  Make that
+// first call before the host's allocator reserves most of HBM, and before any
+// stream capture; later calls take nothing.
 namespace {
-// 65,536 irreducible q points at most: 1 MiB, reserved when the library loads
+// 65,536 irreducible q points at most: 1 MiB on every device that loads the
+// library, held until the process exits
 constexpr int64_t kNoAllocMaxNk = 65536;
 __device__ __align__(256) double2 g_noalloc_vals[kNoAllocMaxNk];
 constexpr int kNoAllocMaxDevices = 64;
@@ -656,22 +688,19 @@ void gen_green_inv_from_eig(double2* Gk, const double2* self, const double2* uni
                             const double* mu, const double* temp, const int64_t* Nk, const int64_t* Nw,
                             const int64_t* Norb) {
   ABI_TRY
-  const int64_t nk = *Nk, no = *Norb;
+  ensure_context();
+  const int64_t nk = *Nk, nw = *Nw, no = *Norb;
   PGB_CHECK(no >= 1 && no <= kMaxOrb, "Norb must be in [1, 8]");
-  std::vector<double2> h((size_t)no * no * nk);
-  for (int64_t k = 0; k < nk; ++k)
-    for (int64_t l = 0; l < no; ++l)
-      for (int64_t m = 0; m < no; ++m) {
-        double re = 0, im = 0;
-        for (int64_t n = 0; n < no; ++n) {
-          const double2 a = uni[m + no * n + no * no * k], b = uni[l + no * n + no * no * k];
-          const double e = eig[n + no * k];
-          re += e * (a.x * b.x + a.y * b.y);  // e * a * conj(b)
-          im += e * (a.y * b.x - a.x * b.y);
-        }
-        h[m + no * l + no * no * k] = make_double2(re, im);
-      }
-  gen_green_inv_(Gk, self, h.data(), mu, temp, Nk, Nw, Norb);
+  const long long KE = nk * nw * no * no;
+  DBuf<double2> s(KE), u(no * no * nk), G(KE);
+  DBuf<double> e(no * nk);
+  s.upload(self, KE);
+  u.upload(uni, no * no * nk);
+  e.upload(eig, no * nk);
+  k_green_inv_eig<<<g1(nk * nw, 128), 128, 0, ctx().stream>>>(G.p, s.p, u.p, e.p, *mu, *temp, nk, nw, (int)no);
+  launch_check("green_inv_eig");
+  G.download(Gk, KE);
+  sync();
   ABI_CATCH("gen_green_inv_from_eig", nan_fill(Gk, (size_t)(*Nk) * (*Nw) * (*Norb) * (*Norb)))
 }
 
@@ -1757,26 +1786,35 @@ int pyrpa_gb_eig_or_tr_chi_noalloc(void* chiqout_v, const void* chi_v, const int
     PGB_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kNoAllocMaxDevices) throw Error("device ordinal above 63");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // each launch is checked by its own return status, which leaves an error
+    // that the caller's earlier work left pending where it is
+    auto eig_launch = [&](double2* v, int64_t nk, int sw, unsigned grid) {
+      int n = (int)Nchi;
+      void* args[] = {(void*)&v, (void*)&chi, (void*)&nk, (void*)&n, (void*)&sw};
+      PGB_CUDA(cudaLaunchKernel((const void*)k_eig_or_tr, dim3(grid), dim3(32), args, 0, st));
+    };
+    auto map_launch = [&](const double2* v, int64_t nkall, unsigned grid, unsigned block) {
+      int64_t nk = Nk;
+      void* args[] = {(void*)&chiqout, (void*)&v, (void*)&invk, (void*)&nkall, (void*)&nk};
+      PGB_CUDA(cudaLaunchKernel((const void*)k_map_full_checked, dim3(grid), dim3(block), args, 0, st));
+    };
     double2* vals = nullptr;
     {
       std::lock_guard<std::mutex> lk(g_noalloc_mu);
       if (!g_noalloc_ptr[dev]) {
-        // set-up, once per device: the address of the scratch on this device,
-        // and one empty launch of each kernel, so that whatever the driver
-        // reserves for them (local memory of the eigenvalue kernel) is
-        // reserved now rather than on a later call
+        // set-up, once per device with that device current: the address of
+        // the scratch, and one empty launch of each kernel, so that what the
+        // module and its kernels need on this device is taken now
         void* p = nullptr;
         PGB_CUDA(cudaGetSymbolAddress(&p, g_noalloc_vals));
-        k_eig_or_tr<<<1, 32, 0, st>>>(static_cast<double2*>(p), chi, 0, (int)Nchi, 1);
-        k_map_full_checked<<<1, 32, 0, st>>>(chiqout, static_cast<double2*>(p), invk, 0, Nk);
-        PGB_CUDA(cudaGetLastError());
+        eig_launch(static_cast<double2*>(p), 0, 1, 1);
+        map_launch(static_cast<double2*>(p), 0, 1, 32);
         g_noalloc_ptr[dev] = static_cast<double2*>(p);
       }
       vals = g_noalloc_ptr[dev];
     }
-    k_eig_or_tr<<<g1(Nk, 32), 32, 0, st>>>(vals, chi, Nk, (int)Nchi, sw_eig ? 1 : 0);
-    k_map_full_checked<<<g1(Nkall, 256), 256, 0, st>>>(chiqout, vals, invk, Nkall, Nk);
-    PGB_CUDA(cudaGetLastError());
+    eig_launch(vals, Nk, sw_eig ? 1 : 0, (unsigned)g1(Nk, 32));
+    map_launch(vals, Nkall, (unsigned)g1(Nkall, 256), 256);
     ctx().kernel_launches += 2;
     return 0;
   } catch (const std::exception& e) {

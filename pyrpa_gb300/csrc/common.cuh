@@ -2,6 +2,7 @@
 // float2/double2, error reporting, the per-process CUDA context.
 #pragma once
 
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -246,7 +247,8 @@ struct Context {
   bool ready = false;
   int precision = 64;          // 64: FP64 bulk; 32: complex FP32 bulk with FP64 steps; 3264: mixed FLEX schedule
   int verbose = 1;             // progress prints like the reference's stdout
-  long long kernel_launches = 0;
+  // bumped by the entry points, some of which run on callers' own threads
+  std::atomic<long long> kernel_launches{0};
 };
 Context& ctx();
 void ensure_context();

@@ -1,0 +1,220 @@
+"""GPU parity against the FP64 oracle at the FFT sizes the benchmark runs.
+
+Every benchmark configuration transforms a Matsubara axis of 2048 or 4096
+points (2 Nw), which the engine splits four-step into two passes with the
+twiddle fused, and the 3-D configuration needs radix 3.  These tests put
+those code paths next to the oracle (oracle/flex_oracle.py) through the C
+ABI, at sizes the NumPy oracle finishes in about a minute each:
+
+* c1 in full (one orbital, t=1, t'=-0.25, n=0.85, T=0.02, U=3, 32x32 k
+  points, 1024 frequencies: a 2048-point axis).  mkself to eps 1e-8 with
+  sw_tail off and on must take the same iteration count, with mu to 1e-8 and
+  Sigma to 1e-7 of its maximum (the tolerances of the smaller FLEX tests:
+  33 DIIS steps amplify rounding).  At the converged solution, the
+  tail-corrected chi0, the RPA chi_s on every (q, i nu) slice, and lin_eliash
+  (gap_sym=1, the reference's 10-step Arnoldi, which is rounding-stable on
+  this model: a 1e-13 change of G moves the oracle's lambda by 3e-12) are
+  compared at the FP64 tolerances, lambda to 1e-8.  The fused fast form
+  (coarse-mesh warm start, mixed FP32 / double-float schedule) is held to the
+  spec accuracy, lambda within 1e-6 of the oracle's.
+* a 4096-point axis: a 3-orbital 16x16 model with 2048 frequencies, FP64
+  chi0 (tail-corrected) and two FLEX iterations.
+* 3-D with radix 3: a 2-orbital 6x6x6 model with 256 frequencies, mkself to
+  1e-8 (sw_tail on) and lin_eliash at a 20-step Arnoldi (10 steps stop 5%
+  short of the leading eigenvalue on this model, in the oracle as on the GPU).
+
+FP64 tolerances as everywhere: 1e-9 of the array maximum plus 2e-9 absolute
+(the reference zeroes real and imaginary parts below 1e-9).
+"""
+import numpy as np
+import pytest
+
+from oracle import api as O
+import _models as M
+
+pytestmark = pytest.mark.gpu
+
+RTOL64, ATOL64 = 1e-9, 2e-9
+
+
+@pytest.fixture(scope="module")
+def F():
+    from pyrpa_gb300 import build, flibs
+    if not build.LIB.exists():
+        build.build()
+    flibs.load_library()
+    flibs.set_verbose(0)
+    flibs.set_precision(64)
+    return flibs
+
+
+def close(a, b, rtol=RTOL64, atol=ATOL64):
+    a, b = np.asarray(a), np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    scale = max(np.abs(b).max(), 1e-300)
+    err = np.abs(a - b).max()
+    assert err <= rtol * scale + atol, f"max |diff| {err:.3e} vs scale {scale:.3e}"
+    return err / scale
+
+
+def _model(rvec, ham_r, Nx, Ny, Nz, Nw, temp, fill, U, J):
+    from pyrpa_gb300 import models
+    klist, kmap, invk = O.gen_irr_k_TRS(Nx, Ny, Nz)
+    hamk = O.gen_ham(klist, ham_r, rvec)
+    eig, uni = O.get_eig(hamk)
+    Norb = hamk.shape[1]
+    olist, site = O.get_chi_orb_list(Norb)
+    olist = np.asarray(olist)
+    S, C = O.gen_SCmatrix(olist, site, U, J)
+    w = O.gen_kpoint_weight(invk, len(klist))
+    mu = models.bare_mu(eig, w, fill, temp)
+    return dict(Norb=Norb, Nx=Nx, Ny=Ny, Nz=Nz, Nw=Nw, temp=temp, fill=fill, klist=klist, kmap=kmap, invk=invk,
+                hamk=hamk, eig=eig, uni=uni, olist=olist, S=S, C=C, mu=mu)
+
+
+def _mkself_args(m):
+    return (m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"], m["fill"],
+            m["temp"], m["Nw"], m["Nx"], m["Ny"], m["Nz"], False, False)
+
+
+# ------------------------------------------------------------------- c1
+@pytest.fixture(scope="module")
+def c1():
+    from pyrpa_gb300 import models
+    rvec, ham_r = models.square_t_tprime(1.0, -0.25)
+    return _model(rvec, ham_r, 32, 32, 1, 1024, 0.02, 0.425, 3.0, 0.0)
+
+
+_C1_ORACLE = {}
+
+
+def c1_oracle(m, tail):
+    """The oracle's mkself on c1 (cached per sw_tail), and for sw_tail on the
+    converged G, chi0 and the Eliashberg lambda and gap at gap_sym=1."""
+    if tail not in _C1_ORACLE:
+        kw = dict(eps=1e-8, pp=0.5, sw_rescale=True, sw_tail=tail)
+        sg, mu, r = O.mkself(*_mkself_args(m), **kw, full=True)
+        out = dict(sigma=sg, mu=mu, iterations=r.iterations, kw=kw)
+        if tail:
+            G = O.gen_green(sg, m["hamk"], mu, m["temp"])
+            chi, st = O.get_chi0_tail(m["S"], m["C"], G, m["eig"], m["uni"], m["olist"], m["kmap"], m["invk"], mu,
+                                      m["temp"], m["Nx"], m["Ny"], m["Nz"])
+            init = O.get_initial_gap(m["klist"], 1, 1)
+            gap, lam = O.linearized_eliashberg(chi.copy(), G, m["uni"], init, m["S"], m["C"], m["olist"], np.ones(1),
+                                               m["kmap"], m["invk"], m["Nx"], m["Ny"], m["Nz"], m["temp"], 1,
+                                               arnoldi_m=10)
+            out.update(G=G, chi=chi, stoner=st, init=init, gap=gap, lam=lam)
+        _C1_ORACLE[tail] = out
+    return _C1_ORACLE[tail]
+
+
+@pytest.mark.parametrize("tail", [False, True])
+def test_c1_mkself_matches_oracle(F, c1, tail):
+    o = c1_oracle(c1, tail)
+    sg, mu = F.mkself(*_mkself_args(c1), **o["kw"])
+    assert F.last_stats()["iterations"] == o["iterations"]
+    assert abs(mu - o["mu"]) < 1e-8
+    close(sg, o["sigma"], 1e-7, 1e-9)
+
+
+def test_c1_chi0_tail_and_chis_at_solution(F, c1):
+    """The 2048-point axis through the four-step passes: tail-corrected chi0 of
+    the converged G, then chi_s = (I - chi0 S)^-1 chi0 on all Nk x Nw slices."""
+    o = c1_oracle(c1, True)
+    m = c1
+    chi, st = F.get_chi0_tail(m["S"], m["C"], o["G"], m["eig"], m["uni"], m["olist"], m["kmap"], m["invk"], o["mu"],
+                              m["temp"], m["Nx"], m["Ny"], m["Nz"])
+    close(chi, o["chi"])
+    assert abs(st - o["stoner"]) <= 1e-9
+    slices = np.ascontiguousarray(o["chi"].reshape(1, 1, -1).transpose(2, 0, 1))
+    close(F.get_chis(slices, m["S"]), O.get_chis(slices, m["S"]), 1e-9, 1e-12)
+
+
+def test_c1_lin_eliash_matches_oracle(F, c1):
+    o = c1_oracle(c1, True)
+    m = c1
+    chi = o["chi"].copy()
+    gap, lam = F.linearized_eliashberg(chi, o["G"], m["uni"], o["init"], m["S"], m["C"], m["olist"], np.ones(1),
+                                       m["kmap"], m["invk"], m["Nx"], m["Ny"], m["Nz"], m["temp"], 1, arnoldi_m=10)
+    assert abs(lam - o["lam"]) <= 1e-8 * abs(o["lam"]), (lam, o["lam"])
+    ph = np.vdot(o["gap"].ravel(), gap.ravel())
+    close(gap, o["gap"] * ph / abs(ph), 1e-6, 1e-9)
+
+
+@pytest.mark.parametrize("form", ["fp64-cold", "mixed-warm"])
+def test_c1_fused_solve_against_oracle(F, c1, form):
+    """pyrpa_gb_flex_eliash (FLEX to 1e-8, G, tail chi0, lin_eliash) against the
+    oracle's step-by-step run.  The plain FP64 cold start follows the oracle to
+    the FP64 tolerances; the fast form (16x16x512 warm start, FP32 then
+    double-float bulk, double-float judging iteration) lands on the same fixed
+    point: Sigma to 1e-6 of its maximum, mu to 1e-7, lambda to 1e-6."""
+    o = c1_oracle(c1, True)
+    m = c1
+    F.set_precision(64 if form == "fp64-cold" else F.MIXED)
+    try:
+        r = F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], o["init"],
+                          np.ones(1), m["mu"], m["fill"], m["temp"], m["Nw"], m["Nx"], m["Ny"], m["Nz"], 1, eps=1e-8,
+                          pp=0.5, sw_rescale=True, sw_tail=True, arnoldi_m=10,
+                          coarse=(1, 1) if form == "fp64-cold" else (2, 2))
+    finally:
+        F.set_precision(64)
+    if form == "fp64-cold":
+        assert F.last_stats()["iterations"] == o["iterations"]
+        assert abs(r["mu"] - o["mu"]) < 1e-8
+        close(r["sigmak"], o["sigma"], 1e-7, 1e-9)
+        assert abs(r["lam"] - o["lam"]) <= 1e-8 * abs(o["lam"])
+    else:
+        assert abs(r["mu"] - o["mu"]) < 1e-7
+        close(r["sigmak"], o["sigma"], 1e-6, 1e-9)
+        assert abs(r["lam"] - o["lam"]) <= 1e-6 * abs(o["lam"]), (r["lam"], o["lam"])
+
+
+# ------------------------------------------------- 4096-point Matsubara axis
+@pytest.fixture(scope="module")
+def axis4096():
+    rvec, ham_r = M.random_hoppings(3, 11, bandwidth=4.0)
+    return _model(rvec, ham_r, 16, 16, 1, 2048, 0.01, 1.5, 0.8, 0.1)
+
+
+def test_chi0_tail_4096_axis(F, axis4096):
+    m = axis4096
+    G = O.gen_Green0(m["eig"], m["uni"], m["mu"], m["temp"], m["Nw"])
+    args = (m["S"], m["C"], G, m["eig"], m["uni"], m["olist"], m["kmap"], m["invk"], m["mu"], m["temp"], m["Nx"],
+            m["Ny"], m["Nz"])
+    chi, st = F.get_chi0_tail(*args)
+    chio, sto = O.get_chi0_tail(*args)
+    close(chi, chio)
+    assert abs(st - sto) <= 1e-9 * max(1.0, abs(sto))
+
+
+def test_two_flex_iterations_4096_axis(F, axis4096):
+    """Two iterations: chi0 (tail), vertex, Sigma, HF subtraction, linear
+    mixing, mu search, Dyson and the second chi0/Sigma on the new G."""
+    m = axis4096
+    kw = dict(eps=1e-8, pp=0.5, scf_loop=2, sw_rescale=True, sw_tail=True)
+    sg, mu = F.mkself(*_mkself_args(m), **kw)
+    sgo, muo = O.mkself(*_mkself_args(m), **kw)
+    assert abs(mu - muo) < 1e-9
+    close(sg, sgo)
+
+
+# --------------------------------------------------------- 3-D, radix 3
+def test_3d_radix3_flex_and_eliash(F):
+    rvec, ham_r = M.random_hoppings(2, 5, shells=((1, 0, 0), (1, 1, 0)), dim=3, bandwidth=3.0)
+    m = _model(rvec, ham_r, 6, 6, 6, 256, 0.03, 1.0, 1.0, 0.1)
+    kw = dict(eps=1e-8, pp=0.5, sw_rescale=True, sw_tail=True)
+    sg, mu = F.mkself(*_mkself_args(m), **kw)
+    sgo, muo, r = O.mkself(*_mkself_args(m), **kw, full=True)
+    assert F.last_stats()["iterations"] == r.iterations
+    assert abs(mu - muo) < 1e-8
+    close(sg, sgo, 1e-7, 1e-9)
+    G = O.gen_green(sgo, m["hamk"], muo, m["temp"])
+    chi, _ = O.get_chi0_tail(m["S"], m["C"], G, m["eig"], m["uni"], m["olist"], m["kmap"], m["invk"], muo, m["temp"],
+                             6, 6, 6)
+    init = O.get_initial_gap(m["klist"], 2, 0)
+    a = (m["uni"], init, m["S"], m["C"], m["olist"], np.ones(2), m["kmap"], m["invk"], 6, 6, 6, m["temp"], 0)
+    gap, lam = F.linearized_eliashberg(chi.copy(), G, *a, arnoldi_m=20)
+    gapo, lamo = O.linearized_eliashberg(chi.copy(), G, *a, arnoldi_m=20)
+    assert abs(lam - lamo) <= 1e-8 * abs(lamo), (lam, lamo)
+    ph = np.vdot(gapo.ravel(), gap.ravel())
+    close(gap, gapo * ph / abs(ph), 1e-6, 1e-9)

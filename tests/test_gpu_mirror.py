@@ -46,3 +46,26 @@ def test_green_from_eigenpairs_matches_oracle():
     got = F.gen_green_from_eig(sig, eig, uni, mu, temp)
     ref = O.gen_green(sig, hamk, mu, temp)
     assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max() + 2e-9
+
+
+def test_green_inverse_from_eigenpairs_with_non_unitary_vectors():
+    """gen_green_inv_from_eig takes the eigenvectors as given: with a U that is
+    not unitary the i w + mu term carries U U^dagger, as in fself.f90:85-129,
+    not the identity."""
+    from oracle import api as O
+    from pyrpa_gb300 import build, flibs as F
+    if not build.LIB.exists():
+        build.build()
+    F.load_library()
+    rng = np.random.default_rng(5)
+    rvec, ham_r = M.random_hoppings(3, 2, bandwidth=4.0)
+    klist, _, _ = O.gen_irr_k_TRS(4, 4, 1)
+    eig, uni = O.get_eig(O.gen_ham(klist, ham_r, rvec))
+    uni = uni + 0.05 * (rng.normal(size=uni.shape) + 1j * rng.normal(size=uni.shape))
+    Nw, mu, temp = 8, -0.2, 0.1
+    sig = 0.1 * (rng.normal(size=(3, 3, Nw, len(klist))) + 1j * rng.normal(size=(3, 3, Nw, len(klist))))
+    got = np.zeros_like(sig)
+    F._call("gen_green_inv_from_eig", got, sig, np.ascontiguousarray(uni), np.ascontiguousarray(eig), F.dbl(mu),
+            F.dbl(temp), F.i64(len(klist)), F.i64(Nw), F.i64(3))
+    ref = O.gen_green_inv_from_eig(sig, eig, uni, mu, temp)
+    assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
