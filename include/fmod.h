@@ -151,6 +151,13 @@ void pyrpa_gb_set_precision(const int64_t* bits);
 void pyrpa_gb_get_precision(int64_t* bits);
 /* 0 silences the progress lines the reference prints to stdout */
 void pyrpa_gb_set_verbose(const int64_t* level);
+/* Krylov convergence of lin_eliash (no counterpart in the reference): 0 (the
+ * default) runs the reference's two passes of exactly arnoldi_m steps
+ * (feliash.f90:190-388); tol > 0 restarts the pass that yields lambda from
+ * its Ritz vector, arnoldi_m steps at a time (at most 12 cycles), until the
+ * Ritz residual |A x - lambda x| / |lambda| = |h_{m+1,m} y_m| / |lambda| is
+ * below tol.  Also PYRPA_GB_ARNOLDI_TOL. */
+void pyrpa_gb_set_arnoldi_tol(const double* tol);
 /* message of the last failure (NUL-terminated, at most len bytes) and its
  * code: 0 none, 1 a failure of the library or the GPU, 2 an input the caller
  * has to fix (the Python wrappers raise ValueError for 2, RuntimeError for 1) */
@@ -164,7 +171,8 @@ void pyrpa_gb_kernel_launches(int64_t* n);
  * the FLEX iterations of a coarse-mesh warm start and its device milliseconds,
  * the device milliseconds of the Stoner factors in the FLEX loop, and the
  * iterations of the mixed schedule's middle phase (FP64 chi0 and Sigma, FP32
- * vertex) (18 doubles) */
+ * vertex), the Ritz residual |A x - lambda x| / |lambda| of the returned
+ * lambda and the Arnoldi cycles of its pass (20 doubles) */
 void pyrpa_gb_last_stats(double* out);
 /* real parts of the Ritz values of the last Arnoldi pass of lin_eliash /
  * lin_eliash_soc / pyrpa_gb_flex_eliash, on the operator's scale (the pass-2

@@ -125,10 +125,11 @@ def mkself(Smat, Cmat, kmap, invk, olist, hamk, eig, uni, mu, fill, temp, Nw, Nx
 
 def linearized_eliashberg(chi, Gk, uni, init_delta, Smat, Cmat, olist, plist, kmap, invk,
                           Nx, Ny, Nz, temp, gap_sym, eps=1.0e-5, itemax=300, arnoldi_m=10,
-                          full=False):
+                          full=False, arnoldi_tol=0.0):
     r = O.lin_eliash(chi.T, Gk.T, uni.transpose(0, 2, 1), np.asarray(init_delta).T,
                      Smat.T, Cmat.T, np.asarray(olist), np.asarray(plist), np.asarray(kmap),
-                     np.asarray(invk), temp, eps, Nx, Ny, Nz, itemax, gap_sym, arnoldi_m)
+                     np.asarray(invk), temp, eps, Nx, Ny, Nz, itemax, gap_sym, arnoldi_m,
+                     arnoldi_tol=arnoldi_tol)
     gap = np.ascontiguousarray(r.delta.T)
     return (gap, r.lam, r) if full else (gap, r.lam)
 

@@ -873,8 +873,12 @@ class LinEliashResult:
 
 
 def lin_eliash(chi, G, U_F, init_delta_F, S_F, C_F, olist, prt, kmap, invk, temp, eps,
-               Nx, Ny, Nz, itemax, gap_sym, arnoldi_m):
-    """feliash.f90:1-443 (V_Delta, then Arnoldi two-pass or shifted power method)."""
+               Nx, Ny, Nz, itemax, gap_sym, arnoldi_m, arnoldi_tol=0.0):
+    """feliash.f90:1-443 (V_Delta, then Arnoldi two-pass or shifted power method).
+    arnoldi_tol > 0 (the engine's pyrpa_gb_set_arnoldi_tol, not in the
+    reference) restarts the pass that gives lambda from its Ritz vector,
+    arnoldi_m steps at a time and at most 12 cycles, until the Ritz residual
+    |h_{m+1,m} y_m| / |lambda| is below the tolerance."""
     grid = KGrid(kmap, invk, Nx, Ny, Nz)
     Nk, Nw = G.shape[:2]
     Nkall = len(grid.ki)
@@ -918,7 +922,7 @@ def lin_eliash(chi, G, U_F, init_delta_F, S_F, C_F, olist, prt, kmap, invk, temp
             if j < arnoldi_m - 1:
                 V.append(w * (1.0 / beta))
         ev, vr = np.linalg.eig(H[:m_act, :m_act])
-        return V, ev, vr, m_act
+        return V, ev, vr, m_act, H
 
     def ritz(V, vr, idx, m_act):
         y = _zgeev_vector(vr[:, idx])
@@ -927,12 +931,27 @@ def lin_eliash(chi, G, U_F, init_delta_F, S_F, C_F, olist, prt, kmap, invk, temp
             d = d + y[ii] * V[ii]
         return d * (1.0 / norm(d))
 
-    V, ev, vr, m_act = arnoldi(init(), None, None)
+    def residual(H, vr, idx, m_act):
+        y = vr[:, idx]
+        return abs(H[m_act, m_act - 1]) * abs(y[m_act - 1]) / np.linalg.norm(y)
+
+    def converge(V, ev, vr, m_act, H, shift, defl):
+        s0 = 0.0 if shift is None else shift
+        idx = int(np.argmax(ev.real))
+        d, lam, res, cycles = ritz(V, vr, idx, m_act), float(ev[idx].real) - s0, residual(H, vr, idx, m_act), 1
+        while arnoldi_tol > 0 and res > arnoldi_tol * abs(lam) and cycles < 12:
+            V, ev, vr, m_act, H = arnoldi(d, shift, defl)
+            idx = int(np.argmax(ev.real))
+            d, lam, res = ritz(V, vr, idx, m_act), float(ev[idx].real) - s0, residual(H, vr, idx, m_act)
+            cycles += 1
+        return d, lam, ev
+
+    V, ev, vr, m_act, H = arnoldi(init(), None, None)
     idx = int(np.argmin(ev.real))
     lam1 = float(ev[idx].real)
     if ev.real.max() >= 0.1:
-        idx = int(np.argmax(ev.real))
-        return LinEliashResult(ritz(V, vr, idx, m_act), float(ev[idx].real), ev, None)
+        d, lam, ev = converge(V, ev, vr, m_act, H, None, None)
+        return LinEliashResult(d, lam, ev, None)
     delta1 = ritz(V, vr, idx, m_act)
     shift = -lam1
     v0 = init()
@@ -941,9 +960,9 @@ def lin_eliash(chi, G, U_F, init_delta_F, S_F, C_F, olist, prt, kmap, invk, temp
     if b < 1e-14:
         return LinEliashResult(delta1, lam1, ev, None)
     v0 = v0 * (1.0 / b)
-    V2, ev2, vr2, m_act2 = arnoldi(v0, shift, delta1)
-    idx = int(np.argmax(ev2.real))
-    return LinEliashResult(ritz(V2, vr2, idx, m_act2), float(ev2[idx].real) - shift, ev, ev2)
+    V2, ev2, vr2, m_act2, H2 = arnoldi(v0, shift, delta1)
+    d, lam, ev2 = converge(V2, ev2, vr2, m_act2, H2, shift, delta1)
+    return LinEliashResult(d, lam, ev, ev2)
 
 
 def _power_method(apply_op, inner, norm, init, eps, itemax, Vd):

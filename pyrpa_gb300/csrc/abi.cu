@@ -55,6 +55,7 @@ void ensure_context() {
     if (v == "48" || v == "df" || v == "DF") c.precision = kPrecDF;
   }
   if (const char* s = std::getenv("PYRPA_GB_VERBOSE")) c.verbose = std::atoi(s);
+  if (const char* s = std::getenv("PYRPA_GB_ARNOLDI_TOL")) c.arnoldi_tol = std::atof(s);
   c.ready = true;
 }
 
@@ -468,6 +469,13 @@ void pyrpa_gb_get_precision(int64_t* bits) {
   *bits = ctx().precision;
 }
 void pyrpa_gb_set_verbose(const int64_t* v) { ctx().verbose = (int)*v; }
+void pyrpa_gb_set_arnoldi_tol(const double* tol) {
+  ABI_TRY
+  PGB_CHECK(*tol >= 0.0, "the Arnoldi residual tolerance must be >= 0");
+  ensure_context();
+  ctx().arnoldi_tol = *tol;
+  ABI_CATCH("pyrpa_gb_set_arnoldi_tol", (void)0)
+}
 void pyrpa_gb_last_error(char* buf, const int64_t* len, int64_t* code) {
   std::lock_guard<std::mutex> lk(g_err_mu);
   if (buf && len && *len > 0) {
@@ -485,9 +493,10 @@ void pyrpa_gb_clear_error() {
 void pyrpa_gb_kernel_launches(int64_t* n) { *n = ctx().kernel_launches; }
 void pyrpa_gb_last_stats(double* out) {
   const LastStats& s = last_stats();
-  const double v[18] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
+  const double v[20] = {(double)s.iterations, s.esterr, s.stoner, s.mu, s.lambda, (double)s.applies, s.t_chi0,
                         s.t_vertex, s.t_sigma, s.t_diis, s.t_mu, s.t_dyson, s.t_apply, (double)s.iterations32,
-                        (double)s.iterations_coarse, s.t_warm, s.t_stoner, (double)s.iterations_finish32};
+                        (double)s.iterations_coarse, s.t_warm, s.t_stoner, (double)s.iterations_finish32,
+                        s.ritz_residual, (double)s.arnoldi_cycles};
   memcpy(out, v, sizeof(v));
 }
 void pyrpa_gb_last_ritz(double* out, const int64_t* n, int64_t* count) {

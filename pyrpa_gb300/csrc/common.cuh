@@ -247,6 +247,9 @@ struct Context {
   bool ready = false;
   int precision = 64;          // 64: FP64 bulk; 32: complex FP32 bulk with FP64 steps; 3264: mixed FLEX schedule
   int verbose = 1;             // progress prints like the reference's stdout
+  // 0: the reference's fixed Krylov size in lin_eliash; > 0: each Arnoldi pass
+  // restarts from its Ritz vector until |h_{m+1,m} y_m| / |lambda| < tol
+  double arnoldi_tol = 0.0;
   // bumped by the entry points, some of which run on callers' own threads
   std::atomic<long long> kernel_launches{0};
 };

@@ -728,6 +728,7 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   PGB_CHECK(m <= 64, "arnoldi_m above 64 is not supported");
   std::vector<DBuf<double2>> V(m);
   for (auto& v : V) v.alloc(KE);
+  DBuf<double2> D(KE);
   auto arnoldi = [&](double shift, const double2* defl, std::vector<double2>& Hm, int& m_act) {
     Hm.assign((size_t)(m + 1) * m, make_double2(0, 0));
     m_act = m;
@@ -755,6 +756,8 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
       }
     }
   };
+  // Ritz vector of lam into out (unit norm); returns the Ritz residual
+  // |h_{m+1,m}| |y_m| / |y| of the pair
   auto ritz = [&](double2* out, const std::vector<double2>& Hm, int m_act, double2 lam) {
     std::vector<double2> Hs((size_t)m_act * m_act);
     for (int i = 0; i < m_act; ++i)
@@ -764,6 +767,9 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
     for (int i = 0; i < m_act; ++i) xs[i] = V[i].p;
     lincomb(out, xs.data(), y.data(), m_act, KE);
     scal(out, 1.0 / norm(out), KE);
+    double yn = 0;
+    for (const auto& v : y) yn += abs2(v);
+    return Hm[(size_t)m_act * m + m_act - 1].x * std::sqrt(abs2(y[m_act - 1]) / std::max(yn, 1e-300));
   };
   auto ritz_values = [&](const std::vector<double2>& Hm, int m_act) {
     std::vector<double2> Hs((size_t)m_act * m_act), ev;
@@ -771,6 +777,30 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
       for (int j = 0; j < m_act; ++j) Hs[i * m_act + j] = Hm[i * m + j];
     eig_small(Hs, m_act, ev);
     return ev;
+  };
+  // with a tolerance set, restart a pass from its Ritz vector (in D) until the
+  // residual over |lambda| is below it; returns lambda on the operator's scale
+  const double tol = ctx().arnoldi_tol;
+  constexpr int kMaxCycles = 12;
+  auto converge = [&](double shift, const double2* defl, std::vector<double2>& Hm, int& m_act,
+                      std::vector<double2>& ev, int& imax, double res) {
+    int cycles = 1;
+    double lam = ev[imax].x - shift;
+    while (tol > 0.0 && res > tol * std::fabs(lam) && cycles < kMaxCycles) {
+      PGB_CUDA(cudaMemcpyAsync(V[0].p, D.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+      arnoldi(shift, defl, Hm, m_act);
+      ev = ritz_values(Hm, m_act);
+      imax = 0;
+      for (int i = 1; i < m_act; ++i)
+        if (ev[i].x > ev[imax].x) imax = i;
+      lam = ev[imax].x - shift;
+      res = ritz(D.p, Hm, m_act, ev[imax]);
+      ++cycles;
+      log("  restart %2d: lambda =%14.10f, residual %9.2e\n", cycles, lam, res / std::max(std::fabs(lam), 1e-300));
+    }
+    g_stats.ritz_residual = res / std::max(std::fabs(lam), 1e-300);
+    g_stats.arnoldi_cycles = cycles;
+    return lam;
   };
   // pass 1: no shift
   init_vec(V[0].p);
@@ -787,7 +817,6 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   const double lambda1 = ev[imin].x;
   for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x);
   log("  lambda_- =%12.6f\n", lambda1);
-  DBuf<double2> D(KE);
   auto keep_ritz = [&](const std::vector<double2>& e, double shift) {
     std::vector<double> r;
     for (const auto& z : e) r.push_back(z.x - shift);
@@ -797,9 +826,10 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   };
   keep_ritz(ev, 0.0);
   if (ev[imax].x >= 0.1) {
-    lambda_out = ev[imax].x;
+    const double res = ritz(D.p, Hm, m_act, ev[imax]);
+    lambda_out = converge(0.0, nullptr, Hm, m_act, ev, imax, res);
+    if (g_stats.arnoldi_cycles > 1) keep_ritz(ev, 0.0);
     log("  eliash   =%12.6f\n", lambda_out);
-    ritz(D.p, Hm, m_act, ev[imax]);
   } else {
     DBuf<double2> delta1(KE);
     ritz(delta1.p, Hm, m_act, ev[imin]);
@@ -811,6 +841,8 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
     if (!(b0 >= 1.0e-14)) {
       // the operator has no component outside the pass-1 direction
       lambda_out = lambda1;
+      g_stats.ritz_residual = 0.0;
+      g_stats.arnoldi_cycles = 1;
       PGB_CUDA(cudaMemcpyAsync(D.p, delta1.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     } else {
       scal(V[0].p, 1.0 / b0, KE);
@@ -821,10 +853,10 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
       for (int i = 1; i < m_act; ++i)
         if (ev[i].x > ev[imax].x) imax = i;
       for (int i = 0; i < m_act; ++i) log("%4d%14.6f\n", i + 1, ev[i].x - shift);
-      lambda_out = ev[imax].x - shift;
+      const double res = ritz(D.p, Hm, m_act, ev[imax]);
+      lambda_out = converge(shift, delta1.p, Hm, m_act, ev, imax, res);
       keep_ritz(ev, shift);
       log("  eliash   =%12.6f\n", lambda_out);
-      ritz(D.p, Hm, m_act, ev[imax]);
     }
   }
   PGB_CUDA(cudaMemcpyAsync(delta_out, D.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));

@@ -132,6 +132,10 @@ struct LastStats {
   // scale (the pass-2 shift undone), largest first
   double ritz[16] = {0};
   int nritz = 0;
+  // residual |A x - lambda x| / |lambda| of the returned Ritz pair and the
+  // Arnoldi cycles of the pass that produced it (restarts + 1)
+  double ritz_residual = 0;
+  int arnoldi_cycles = 0;
 };
 
 // bulk type of each stage of a FLEX iteration: 32 FP32, 64 FP64, 48 double-float

@@ -113,6 +113,7 @@ _SIGNATURES = {
     "pyrpa_gb_last_ritz": [_f64, _pi, _pi],
     "pyrpa_gb_get_precision": [_pi],
     "pyrpa_gb_set_verbose": [_pi],
+    "pyrpa_gb_set_arnoldi_tol": [_pd],
     "pyrpa_gb_last_error": [POINTER(c_char), _pi, _pi],
     "pyrpa_gb_clear_error": [],
     "pyrpa_gb_kernel_launches": [_pi],
@@ -215,11 +216,12 @@ def kernel_launches() -> int:
 
 
 def last_stats() -> dict:
-    out = np.zeros(18)
+    out = np.zeros(20)
     load_library().pyrpa_gb_last_stats(out)
     keys = ["iterations", "esterr", "stoner", "mu", "lambda", "applies", "t_chi0_ms", "t_vertex_ms",
             "t_sigma_ms", "t_diis_ms", "t_mu_ms", "t_dyson_ms", "t_apply_ms", "iterations_fp32",
-            "iterations_coarse", "t_warm_ms", "t_stoner_ms", "iterations_fp64_fp32vertex"]
+            "iterations_coarse", "t_warm_ms", "t_stoner_ms", "iterations_fp64_fp32vertex", "ritz_residual",
+            "arnoldi_cycles"]
     return dict(zip(keys, out[: len(keys)].tolist()))
 
 
@@ -230,6 +232,13 @@ def last_ritz(n: int = 4):
     count = c_int64(0)
     load_library().pyrpa_gb_last_ritz(out, i64(n), byref(count))
     return out[: min(n, count.value)].copy()
+
+
+def set_arnoldi_tol(tol: float) -> None:
+    """0: lin_eliash runs the reference's fixed arnoldi_m steps per pass; tol > 0
+    restarts the pass that gives lambda until the Ritz residual over |lambda|
+    is below tol (last_stats()["ritz_residual"], ["arnoldi_cycles"])."""
+    _call("pyrpa_gb_set_arnoldi_tol", dbl(tol))
 
 
 def fft_profile(on: bool) -> None:
