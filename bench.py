@@ -4,16 +4,25 @@ eigenvalue on one GB300, for the 5-orbital 64x64x2048 model (config c2).
 
 One step = one full solve of the reference's calc_lin_eliashberg_eq path
 (mkself to the residual eps -> G -> tail-corrected chi0 -> lin_eliash), run
-through the engine's C ABI (pyrpa_gb_flex_eliash, host buffers in and out).
+through the engine's C ABI (pyrpa_gb_flex_eliash, host buffers in and out),
+in the fast form: coarse-mesh warm start, FP32 then double-float bulk, a
+double-float judging iteration.  lin_eliash runs 20-step Arnoldi cycles,
+restarted until the Ritz residual is below 1e-10 of lambda: the reference's
+single 10-step pass stops 20% short of the leading eigenvalue on this model.
   value        device seconds of the solve with the inputs already in HBM
                (CUDA events on the library stream, between upload and download)
   e2e          wall seconds of the whole ABI call from host buffers, copies included
+  plain_fp64   after the timed steps, the same model solved once in plain FP64
+               from G0 (no warm start): the metric's denominator, with the
+               lambda, Sigma and mu differences of the fast form from it
   roofline     the FFT passes (fft2_kernel<R, A, B>; every pass of the 64x64x4096
                transforms), the kernel that moves the most bytes, timed live per
                launch with CUDA events during the timed steps
-  cpu_baseline the oracle's per-orbital-pair FFT convolution at full size on
-               all host cores, extrapolated to one solve with this run's
-               iteration and Eliashberg-application counts
+  cpu_baseline the oracle's restatement of the reference's CPU path, every
+               stage of a FLEX iteration and of an Eliashberg application timed
+               on a bounded full-size sample on all host cores and scaled to
+               one solve with the plain FP64 solve's iteration and application
+               counts (cpu_reference_estimate)
 Inputs are larger than L2 (every FFT array is >= 134 MB), so no L2 flush is
 needed between steps.  `--impl reference` prints the CPU line only.
 Under torchrun every rank solves its own copy of the model (replicas, no
@@ -36,10 +45,6 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 METRIC = "time-to-converged FLEX Σ+λ, 5-orb 64²×2048: FP32+warm-start vs plain FP64"
-# FLEX iterations and Eliashberg operator applications of one c2 solve as
-# measured by the GPU engine (FP32 bulk, eps 1e-4, DIIS 5, Arnoldi 10); the
-# CPU-only reference arm extrapolates with them.
-DEFAULT_COUNTS = {"c2": (30, 20), "c1": (30, 20), "c5": (30, 20)}
 
 
 # ------------------------------------------------------ profiling cases
@@ -117,12 +122,14 @@ def parse():
     p.add_argument("--no-tail", action="store_true")
     p.add_argument("--coarse", default="2,2",
                    help="warm start: k-mesh and frequency divisors of the coarse solve ('1,1' = cold start)")
-    p.add_argument("--cpu-pairs", type=int, default=0, help="orbital pairs in the CPU sample (0: one per core)")
-    p.add_argument("--flex-iters", type=int, default=0)
-    p.add_argument("--applies", type=int, default=0)
-    p.add_argument("--with-fp64", action="store_true",
-                   help="after the timed steps, solve once more in plain FP64 from G0 (the metric's denominator) "
-                        "and report its time and the lambda, Sigma and mu differences")
+    p.add_argument("--arnoldi-m", type=int, default=20, help="Krylov steps per Arnoldi cycle of lin_eliash")
+    p.add_argument("--arnoldi-tol", type=float, default=1.0e-10,
+                   help="restart the Arnoldi pass until the Ritz residual over |lambda| is below this "
+                        "(0: the reference's single fixed-size pass)")
+    p.add_argument("--no-fp64", action="store_true",
+                   help="skip the plain FP64 cold-start solve after the timed steps (the metric's denominator)")
+    p.add_argument("--flex-iters", type=int, default=0, help="reference arm: FLEX iterations to scale with")
+    p.add_argument("--applies", type=int, default=0, help="reference arm: Eliashberg applications to scale with")
     return p.parse_args()
 
 
@@ -184,54 +191,166 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------- CPU baseline
-def _cpu_pair_worker(args):
-    """One reference orbital-pair convolution at full grid size with the
-    oracle (pad G on the full grid, two forward 4-D FFTs, the G(r,t)G(-r,-t)
-    product, one backward FFT, gather to the irreducible mesh) on random data:
-    the unit of work of chi0_conv_acc / calc_sigma / mkdelta_nsoc."""
-    Nx, Ny, Nz, Nw, reps, seed = args
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
+# The reference's CPU path, restated by the oracle, timed stage by stage on a
+# bounded sample of the full-size workload and scaled to one solve.  Each unit
+# below is one piece of the reference's own loop structure at the full mesh:
+#   chi0    one bubble of one irreducible orbital pair of chi0_conv_acc
+#           (fchi.f90:508-613): pads, 2 forward 4-D FFTs, product, backward;
+#           with sw_tail a pair takes two (G and G0) and
+#   tailref the analytic tau reference of one pair (fchi.f90:637-850)
+#   sigma   one (l, m) pair of calc_sigma (fself.f90:159-285): 3 FFTs
+#   delta   one pair of mkdelta_nsoc (feliash.f90:486-635): 3 FFTs
+#   vertex  get_vsigma_flex_nosoc (fUJ.f90:318-365) on a slice of the (q, i nu)
+#           matrices
+#   mu      the zgeev of H + Sigma per (k, i w) of renew_mu (fself.f90:689-711)
+#           plus MU_EVALS fillings get_rn (fself.f90:662-687), on a slice
+#   dyson   gen_green_inv + getinv (fself.f90:43-157) on a slice
+#   diis    compare_sigma (fself.f90:449-542): the Gram matrix of a full
+#           history and the extrapolation, on a slice
+#   stoner  ckchi (fchi.f90:352-399): zgeev of chi0(q, 0) S at every q
+#   mkfk    mkfk_trs_nsoc (feliash.f90:445-484) on a slice
+# Every unit runs in its own spawned worker, all at once on the host cores,
+# and the solve's time is sum(units x seconds per unit) / workers, which
+# assumes the reference spreads each stage perfectly over the cores (its
+# FFTs are serial): a lower bound on the reference's time.
+MU_EVALS = 16          # fillings per renew_mu: bracket plus the inverse-quadratic search
+SLICE = 128            # the vertex, mu, Dyson, DIIS and mkfk samples are 1/SLICE of the full size
+# FLEX iterations and Eliashberg applications of the plain FP64 cold-start
+# GPU solve of each configuration (eps 1e-4, DIIS 5, pp 0.5, 20-step Arnoldi
+# cycles restarted to a Ritz residual of 1e-10), from that solve's own
+# statistics; the reference arm, which has no GPU run of its own, scales
+# with them
+PLAIN_FP64_COUNTS = {"c2": (24, 40), "c1": (11, 40), "c5": (29, 40)}
+
+
+def _cpu_unit(job):
+    kind, cfg, tail, seed = job
     sys.path.insert(0, str(ROOT))
     from oracle import flex_oracle as FO
-    klist, kmap, invk = FO.generate_irr_kpoint_inv(Nx, Ny, Nz)
-    grid = FO.KGrid(kmap, invk, Nx, Ny, Nz)
     rng = np.random.default_rng(seed)
-    G = (rng.standard_normal((len(klist), Nw, 1, 1)) + 1j * rng.standard_normal((len(klist), Nw, 1, 1)))
+    Nx, Ny, Nz, Nw, No, temp = cfg["Nx"], cfg["Ny"], cfg["Nz"], cfg["Nw"], cfg["Norb"], cfg["temp"]
+    nchi = No * No
+    K = FO.irr_k_count(Nx, Ny, Nz) * Nw
+
+    def crand(*shape):
+        return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+    if kind in ("chi0", "tailref", "sigma", "delta"):
+        klist, kmap, invk = FO.generate_irr_kpoint_inv(Nx, Ny, Nz)
+        grid = FO.KGrid(kmap, invk, Nx, Ny, Nz)
+        Nk = len(klist)
+        ol = np.array([[1, 1]])
+        one = np.ones((1, 1))
+        G = 0.1 * crand(Nk, Nw, 1, 1)
+        t0 = time.perf_counter()
+        if kind == "tailref":
+            chi_map, irr = FO.get_chi_map(ol)
+            U = np.ones((Nk, 1, 1), dtype=complex)
+            e = rng.uniform(-1, 1, (Nk, 1))
+            FO.gen_green0_F(e, U, 0.0, temp, Nw)
+            FO.chi0_ref_tau(np.zeros((Nk, Nw, 1, 1), dtype=complex), e, U, 0.0, grid, ol, temp, Nw, chi_map, irr)
+        elif kind == "chi0":
+            FO.get_chi0_conv(G, grid, ol, temp)
+        elif kind == "sigma":
+            FO.calc_sigma(G, 0.1 * crand(Nk, Nw, 1, 1), one, one, grid, ol, temp)
+        else:
+            FO.mkdelta_nsoc(G, 0.1 * crand(Nk, Nw, 1, 1), one, one, grid, np.ones(1), ol, True)
+        return kind, time.perf_counter() - t0, 1
+    n = max(1, K // SLICE)
+    if kind == "vertex":
+        S = rng.standard_normal((nchi, nchi))
+        S = 0.05 * (S + S.T)
+        chi = 0.05 * crand(n, 1, nchi, nchi)
+        t0 = time.perf_counter()
+        FO.vsigma_flex_nosoc(chi, S, 0.5 * S)
+        return kind, time.perf_counter() - t0, n
+    if kind == "stoner":
+        nq = FO.irr_k_count(Nx, Ny, Nz)
+        S = rng.standard_normal((nchi, nchi))
+        chi = 0.05 * crand(nq, 1, nchi, nchi)
+        t0 = time.perf_counter()
+        FO.ckchi(chi, S, 0.5 * S)
+        return kind, time.perf_counter() - t0, 1
+    A = crand(n, No, No)
+    if kind == "mu":
+        z = (0.1 + 1j * np.linspace(0.01, 10.0, n))[:, None]
+        e = rng.uniform(-1, 1, (n, No))
+        t0 = time.perf_counter()
+        lam = np.linalg.eigvals(A)
+        for _ in range(MU_EVALS):
+            np.sum((1.0 / (z - lam) - 1.0 / (z - e)).real)
+        return kind, time.perf_counter() - t0, n
+    if kind == "dyson":
+        t0 = time.perf_counter()
+        np.linalg.inv(A + 2j * np.eye(No))
+        return kind, time.perf_counter() - t0, n
+    if kind == "mkfk":
+        t0 = time.perf_counter()
+        FO.hermitize_lower(-(A @ A @ np.conj(np.swapaxes(A, -1, -2))))
+        return kind, time.perf_counter() - t0, n
+    # diis: Gram matrix of 5 residuals, extrapolation and the relative change
+    hist = [crand(n, No, No) for _ in range(5)]
     t0 = time.perf_counter()
-    for _ in range(reps):
-        A = np.fft.fftn(grid.pad_green(G, 0, 0))
-        B = np.fft.fftn(grid.pad_green(G, 0, 0))
-        tmp = np.fft.ifftn(-A * FO._reverse_all(B))
-        grid.gather_irr(tmp, Nw)
-    return time.perf_counter() - t0, reps
+    B = np.array([[np.sum(np.conj(a) * b).real for b in hist] for a in hist])
+    sd = sum(c * h for c, h in zip(np.linalg.solve(B + np.eye(5), np.ones(5)), hist))
+    np.abs((hist[0] - sd) / np.where(np.abs(sd) > 1e-10, sd, 1.0)).max()
+    return kind, time.perf_counter() - t0, n
 
 
-def cpu_pair_rate(cfg, npairs: int):
-    """Pairs per second on all host cores (spawned workers, one pair each)."""
+def _irr_count(cfg):
+    sys.path.insert(0, str(ROOT))
+    from oracle import flex_oracle as FO
+    return FO.irr_k_count(cfg["Nx"], cfg["Ny"], cfg["Nz"])
+
+
+def cpu_reference_estimate(cfg, tail: bool, iters: int, applies: int):
+    """Seconds of one solve on the host cores (see the table above), the
+    workers used and a description of what was timed."""
     cores = os.cpu_count() or 1
-    npairs = npairs or cores
-    work = [(cfg["Nx"], cfg["Ny"], cfg["Nz"], cfg["Nw"], 1, i) for i in range(npairs)]
+    No = cfg["Norb"]
+    nchi = No * No
+    nirr = nchi * (nchi + 1) // 2
+    K = _irr_count(cfg) * cfg["Nw"]
+    kinds = ["chi0", "sigma", "delta", "vertex", "mu", "dyson", "diis", "stoner", "mkfk"] + (["tailref"] if tail else [])
+    jobs = [(k, cfg, tail, i) for i, k in enumerate(kinds)]
+    jobs += [(k, cfg, tail, 100 + i) for i, k in enumerate((["chi0", "sigma"] * cores)[: max(0, cores - len(jobs))])]
     ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(processes=min(cores, npairs)) as pool:
-        res = pool.map(_cpu_pair_worker, work)
-    wall = time.perf_counter() - t0
-    return npairs / wall, min(cores, npairs), npairs, wall
-
-
-def pair_counts(cfg, tail: bool):
-    Nchi = cfg["Norb"] ** 2
-    nirr = Nchi * (Nchi + 1) // 2
-    per_iter = (3 * nirr if tail else nirr) + Nchi * Nchi
-    no = cfg["Norb"]
-    per_apply = sum(1 for a in range(no) for c in range(no) for b in range(no) for d in range(no) if a >= b)
-    final_chi0 = 3 * nirr if tail else nirr
-    return per_iter, per_apply, final_chi0
-
-
-def cpu_seconds(cfg, tail, iters, applies, rate):
-    per_iter, per_apply, final_chi0 = pair_counts(cfg, tail)
-    return (iters * per_iter + final_chi0 + applies * per_apply) / rate
+    # one BLAS / OpenMP thread per worker: the children read these when they
+    # import numpy, before any unit runs
+    saved = {k: os.environ.get(k) for k in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")}
+    os.environ.update({k: "1" for k in saved})
+    try:
+        t0 = time.perf_counter()
+        with ctx.Pool(processes=min(cores, len(jobs))) as pool:
+            res = pool.map(_cpu_unit, jobs)
+        wall = time.perf_counter() - t0
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    per = {}
+    for kind, sec, n in res:
+        per.setdefault(kind, []).append(sec / n)
+    u = {k: statistics.mean(v) for k, v in per.items()}
+    per_apply = sum(1 for a in range(No) for c in range(No) for b in range(No) for d in range(No) if a >= b)
+    # with sw_tail an irreducible pair is two bubbles (of G and of G0) and the tau reference
+    pair = 2 * u["chi0"] + u["tailref"] if tail else u["chi0"]
+    it = (nirr * pair + u["stoner"] + K * u["vertex"] + nchi * nchi * u["sigma"] + K * u["diis"]
+          + K * u["mu"] + K * u["dyson"])
+    final = K * u["dyson"] + nirr * pair + K * u["vertex"]
+    app = per_apply * u["delta"] + K * u["mkfk"]
+    total = (iters * it + final + applies * app) / cores
+    sample = (f"oracle (numpy FP64) on {cores} spawned workers, {wall:.1f} s: at the full {cfg['Nx']}x{cfg['Ny']}x"
+              f"{cfg['Nz']}x{cfg['Nw']} mesh one irreducible-pair chi0 bubble {u['chi0']:.2f} s"
+              f"{(', tau reference %.2f s' % u['tailref']) if tail else ''}, one Sigma pair {u['sigma']:.2f} s, "
+              f"one mkdelta pair {u['delta']:.2f} s, Stoner {u['stoner']:.2f} s; per (k,w) matrix (1/{SLICE} "
+              f"slices): vertex {u['vertex'] * 1e6:.1f} us, mu {u['mu'] * 1e6:.2f} us, Dyson "
+              f"{u['dyson'] * 1e6:.2f} us, DIIS {u['diis'] * 1e6:.2f} us, mkfk {u['mkfk'] * 1e6:.2f} us; per FLEX "
+              f"iteration {nirr} chi0 pairs + {nchi * nchi} Sigma pairs, per application {per_apply} mkdelta "
+              f"pairs; x {iters} FLEX iterations + {applies} Eliashberg applications, divided by {cores} workers")
+    return total, cores, sample
 
 
 # ------------------------------------------------------------------ main
@@ -298,20 +417,21 @@ def main():
     if a.impl == "reference":
         if rank != 0:
             return 0
-        iters, applies = (a.flex_iters or DEFAULT_COUNTS[a.config][0]), (a.applies or DEFAULT_COUNTS[a.config][1])
+        iters = a.flex_iters or PLAIN_FP64_COUNTS[a.config][0]
+        applies = a.applies or PLAIN_FP64_COUNTS[a.config][1]
         vals = []
         for i in range(a.warmup + a.steps):
-            rate, cores, npairs, wall = cpu_pair_rate(cfg, a.cpu_pairs)
+            v, cores, sample = cpu_reference_estimate(cfg, tail, iters, applies)
             if i >= a.warmup:
-                vals.append(cpu_seconds(cfg, tail, iters, applies, rate))
+                vals.append(v)
         v = statistics.mean(vals)
-        sample = (f"{npairs} full-size orbital-pair FFT convolutions per step on {cores} spawned numpy workers, "
-                  f"extrapolated with {iters} FLEX iterations and {applies} Eliashberg applications")
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": 0, "steps": a.steps,
                 "warmup": a.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
                 "vs_baseline": None, "dtype": "c128", "data": "synthetic seeded tight-binding model",
                 "config": config,
-                "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+                "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                                 "sample": sample + " (mean over the timed steps; the counts are those of the plain "
+                                                    "FP64 cold-start GPU solve of this configuration)"},
                 "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return 0
@@ -321,11 +441,16 @@ def main():
     F.load_library()
     F.set_verbose(0)
     F.set_precision({"mixed": F.MIXED, "32": 32, "64": 64}[a.precision])
+    F.set_arnoldi_tol(a.arnoldi_tol)
     m = models.prepare(a.config)
     c = m["cfg"]
     coarse = tuple(int(x) for x in a.coarse.split(","))
     call = dict(mu=m["mu"], fill=c["fill"], temp=c["temp"], Nw=c["Nw"], Nx=c["Nx"], Ny=c["Ny"], Nz=c["Nz"],
-                gap_sym=c["gap_sym"], eps=a.eps, scf_loop=a.scf_loop, sw_tail=tail, sw_rescale=True, coarse=coarse)
+                gap_sym=c["gap_sym"], eps=a.eps, scf_loop=a.scf_loop, sw_tail=tail, sw_rescale=True, coarse=coarse,
+                arnoldi_m=a.arnoldi_m)
+    config["arnoldi"] = (f"{a.arnoldi_m} steps a cycle, restarted until the Ritz residual is below "
+                         f"{a.arnoldi_tol:g} of lambda" if a.arnoldi_tol > 0 else
+                         f"the reference's two passes of {a.arnoldi_m} steps")
     config["warm_start"] = ("none (cold G0 start)" if coarse == (1, 1) else
                             f"coarse-mesh seed: {c['Nx'] // coarse[0]}x{c['Ny'] // coarse[0]} k mesh, "
                             f"{c['Nw'] // coarse[1]} frequencies, FP32 bulk (itself seeded one level further "
@@ -376,10 +501,14 @@ def main():
     iters, applies = int(stats["iterations"]), int(stats["applies"])
     solve_bytes = solve_traffic(c["Norb"], len(m["klist"]), len(m["kmap"]), c["Nw"], stats, a.precision)
     solve_s = value - stats["t_warm_ms"] / 1e3
-    rate, cores, npairs, cwall = cpu_pair_rate(c, a.cpu_pairs)
-    cpu_v = cpu_seconds(c, tail, iters, applies, rate)
+    ritz = [float(x) for x in F.last_ritz(4)]
+    fp64 = None if a.no_fp64 else plain_fp64_comparison(F, solve_args=(m, call), res=res)
+    cpu_counts = ((fp64["flex_iterations"], fp64["eliashberg_applications"]) if fp64
+                  else PLAIN_FP64_COUNTS[a.config])
+    cpu_v, cores, cpu_sample = cpu_reference_estimate(c, tail, *cpu_counts)
     config.update({"flex_iterations": iters, "eliashberg_applications": applies, "lambda": res["lam"],
-                   "lambda_top4": [float(x) for x in F.last_ritz(4)],
+                   "lambda_top4": ritz, "ritz_residual": stats["ritz_residual"],
+                   "arnoldi_cycles": int(stats["arnoldi_cycles"]),
                    "warm_start_iterations": int(stats["iterations_coarse"]),
                    "warm_start_ms": stats["t_warm_ms"],
                    "stoner": res["stoner"], "mu": res["mu"], "esterr": stats["esterr"],
@@ -408,14 +537,14 @@ def main():
                            "scope": "fine FLEX iterations and Eliashberg applications, algorithmic bytes with an "
                                     "ideal two-sweep 4-D FFT; the coarse warm start is left out of bytes and time"},
         "cpu_baseline": {"value": cpu_v, "unit": "s", "cores": cores, "kind": "port",
-                         "sample": f"{npairs} full-size orbital-pair FFT convolutions (oracle, numpy) in {cwall:.1f} s "
-                                   f"on {cores} spawned workers, extrapolated with this run's {iters} FLEX iterations "
-                                   f"and {applies} Eliashberg applications (FFT-pair work only)"},
+                         "sample": cpu_sample + (" (counts of this run's plain FP64 cold-start solve)" if fp64 else
+                                                 " (counts of an earlier plain FP64 cold-start solve)")},
         "clocks": clk.summary(),
         "stages_ms": {k: v for k, v in stats.items() if k.startswith("t_")},
     }
-    if a.with_fp64:
-        line["plain_fp64"] = plain_fp64_comparison(F, solve_args=(m, call), res=res)
+    if fp64:
+        line["plain_fp64"] = fp64
+        line["speedup_vs_plain_fp64"] = fp64["seconds"] / value
     print(json.dumps(line), flush=True)
     return 0
 
@@ -425,11 +554,17 @@ def plain_fp64_comparison(F, solve_args, res) -> dict:
     eps: its device seconds and how far the fast form's lambda, Sigma and mu
     sit from it."""
     m, call = solve_args
+    prec = F.get_precision()
     F.set_precision(64)
-    ref = F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
-                        m["init"], m["plist"], **dict(call, coarse=(1, 1)))
+    try:
+        ref = F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
+                            m["init"], m["plist"], **dict(call, coarse=(1, 1)))
+    finally:
+        F.set_precision(prec)
     st = F.last_stats()
-    return {"seconds": ref["compute_ms"] / 1e3, "flex_iterations": int(st["iterations"]), "lambda": ref["lam"],
+    return {"seconds": ref["compute_ms"] / 1e3, "flex_iterations": int(st["iterations"]),
+            "eliashberg_applications": int(st["applies"]), "lambda": ref["lam"],
+            "ritz_residual": st["ritz_residual"],
             "lambda_rel_diff": abs(res["lam"] - ref["lam"]) / abs(ref["lam"]),
             "sigma_max_rel_diff": float(np.abs(res["sigmak"] - ref["sigmak"]).max() / np.abs(ref["sigmak"]).max()),
             "mu_diff": abs(res["mu"] - ref["mu"])}
