@@ -147,6 +147,14 @@ void write_sigma_bin(double mu, double mu_old, const std::vector<double2>& sig, 
   write_record(f, meta, sizeof(meta));
 }
 
+// a seed of the FLEX loop must be finite: NaN or Inf would run the loop to
+// its iteration cap on a NaN residual
+void require_finite(const double2* v, size_t n, const char* what) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i].x) || !std::isfinite(v[i].y))
+      throw BadInput(std::string(what) + " holds NaN or Inf (element " + std::to_string(i) + ")");
+}
+
 void read_sigma_bin(double& mu, double& mu_old, std::vector<double2>& sig, double temp, int Nw, int Norb, int Nk) {
   std::ifstream f("sigma.bin", std::ios::binary);
   PGB_CHECK(f.good(), "sigma.bin not found in the working directory");
@@ -162,10 +170,12 @@ void read_sigma_bin(double& mu, double& mu_old, std::vector<double2>& sig, doubl
                 " bytes); convert the seed with plibs.regrid_sigma_bin first");
   }
   read_record(f, sig.data(), sig.size() * sizeof(double2));
+  require_finite(sig.data(), sig.size(), "the Sigma record of sigma.bin");
+  // the (temp, Nw, Norb, Nk) record is optional: a missing or truncated one
+  // is skipped, as the reference's read with iostat does (fself.f90:761-766)
   double meta[4];
-  int32_t m = 0;
-  if (f.read((char*)&m, 4) && m == 32) {
-    f.read((char*)meta, 32);
+  int32_t m = 0, m2 = 0;
+  if (f.read((char*)&m, 4) && m == 32 && f.read((char*)meta, 32) && f.read((char*)&m2, 4) && m2 == 32) {
     if ((int)std::lround(meta[1]) != Nw || (int)std::lround(meta[2]) != Norb || (int)std::lround(meta[3]) != Nk)
       throw Error("io_sigma: sigma.bin was written on a different mesh; convert the seed with "
                   "plibs.regrid_sigma_bin first");
@@ -1133,6 +1143,7 @@ void run_pipeline_impl(const PipelineArgs& a, int prec) {
   init.upload(a.init_delta, a.Nk * a.Norb);
   DBuf<double2> seed;
   if (a.sigma_seed) {
+    require_finite(a.sigma_seed, (size_t)KE, "the Sigma seed");
     seed.alloc(KE);
     seed.upload(a.sigma_seed, KE);
   }
