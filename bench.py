@@ -53,8 +53,10 @@ METRIC = "time-to-converged FLEX Σ+λ, 5-orb 64²×2048: FP32+warm-start vs pla
 # most, so that a capture of one launch replays quickly.
 #   vertex  get_vsigma_flex_nosoc_ on a 5-orbital chi0 (Nchi = 25), 130
 #           irreducible q x 512 frequencies = 66,560 matrices
-#   chi0    get_chi0_tail on a 5-orbital 16x16 mesh with 512 frequencies
-#   flex    mkself, one FLEX iteration of the same model
+#   chi0    get_chi0_tail on a 5-orbital mesh (default 16x16, 512 frequencies)
+#   flex    mkself, one FLEX iteration of the same model (--profile-mesh, --profile-nw)
+#   eliash  bare chi0 and a 4-step lin_eliash of the same model (V_Delta, mkfk,
+#           the mkdelta contraction)
 #   fft     get_chi0 of a 1-orbital 64x64 mesh with 2048 frequencies: FFT
 #           passes over 64x64x4096 arrays (134 MB in FP32)
 def _profile_model(F, models, Norb=5, N=16, Nw=512, temp=0.02):
@@ -70,7 +72,7 @@ def _profile_model(F, models, Norb=5, N=16, Nw=512, temp=0.02):
                 olist=olist, S=S, C=C, mu=mu)
 
 
-def profile_case(case: str, precision: int, repeat: int) -> int:
+def profile_case(case: str, precision: int, repeat: int, mesh: int = 16, nw: int = 512) -> int:
     sys.path.insert(0, str(ROOT))
     from pyrpa_gb300 import flibs as F, models
     F.load_library()
@@ -88,16 +90,23 @@ def profile_case(case: str, precision: int, repeat: int) -> int:
             # them off the array the way the reference wrapper does)
             F._call("get_vsigma_flex_nosoc_", chi, S, C, F.i64(Nk), F.i64(Nw), F.i64(Nchi))
         elif case == "chi0":
-            m = _profile_model(F, models)
+            m = _profile_model(F, models, N=mesh, Nw=nw)
             Gk = F.gen_Green0(m["eig"], m["uni"], m["mu"], m["temp"], m["Nw"])
             F.get_chi0_tail(m["S"], m["C"], Gk, m["eig"], m["uni"], m["olist"], m["kmap"], m["invk"], m["mu"],
                             m["temp"], m["N"], m["N"], 1)
+        elif case == "eliash":
+            m = _profile_model(F, models, N=mesh, Nw=nw)
+            Gk = F.gen_Green0(m["eig"], m["uni"], m["mu"], m["temp"], m["Nw"])
+            chi, _ = F.get_chi0(m["S"], m["C"], Gk, m["olist"], m["kmap"], m["invk"], m["temp"], m["N"], m["N"], 1)
+            init = F.get_initial_gap(m["klist"], m["Norb"], 0)
+            F.linearized_eliashberg(chi, Gk, m["uni"], init, m["S"], m["C"], m["olist"], np.ones(m["Norb"]),
+                                    m["kmap"], m["invk"], m["N"], m["N"], 1, m["temp"], 0, arnoldi_m=4)
         elif case == "fft":
             m = _profile_model(F, models, Norb=1, N=64, Nw=2048, temp=0.01)
             Gk = F.gen_Green0(m["eig"], m["uni"], m["mu"], m["temp"], m["Nw"])
             F.get_chi0(m["S"], m["C"], Gk, m["olist"], m["kmap"], m["invk"], m["temp"], m["N"], m["N"], 1)
         else:
-            m = _profile_model(F, models)
+            m = _profile_model(F, models, N=mesh, Nw=nw)
             F.mkself(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"], m["mu"],
                      0.6 * m["Norb"], m["temp"], m["Nw"], m["N"], m["N"], 1, False, False, scf_loop=1, eps=1e-4,
                      pp=0.5, sw_tail=True, sw_rescale=True)
@@ -107,15 +116,17 @@ def profile_case(case: str, precision: int, repeat: int) -> int:
 
 def parse():
     p = argparse.ArgumentParser()
-    p.add_argument("--profile-case", choices=["vertex", "chi0", "flex", "fft"],
+    p.add_argument("--profile-case", choices=["vertex", "chi0", "flex", "fft", "eliash"],
                    help="run one small profiling case instead of the benchmark")
     p.add_argument("--repeat", type=int, default=1, help="calls of the profiling case")
+    p.add_argument("--profile-mesh", type=int, default=16, help="k mesh side of the chi0 and flex cases")
+    p.add_argument("--profile-nw", type=int, default=512, help="Matsubara frequencies of the chi0 and flex cases")
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=2)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--config", default="c2", choices=["c1", "c2", "c5"])
-    p.add_argument("--precision", default="mixed", choices=["mixed", "32", "64"],
+    p.add_argument("--precision", default="mixed", choices=["mixed", "32", "64", "48"],
                    help="mixed: FP32 bulk to the FP32 rounding floor, then double-float bulk to eps")
     p.add_argument("--eps", type=float, default=1.0e-4)
     p.add_argument("--scf-loop", type=int, default=300)
@@ -394,8 +405,11 @@ def max_over_ranks(values, dist):
 
 def main():
     a = parse()
+    if a.precision == "48" and not a.profile_case:
+        raise SystemExit("--precision 48 (double-float chi0 and Sigma) is for the profiling cases only")
     if a.profile_case:
-        return profile_case(a.profile_case, {"mixed": 32, "32": 32, "64": 64}[a.precision], a.repeat)
+        return profile_case(a.profile_case, {"mixed": 32, "32": 32, "64": 64, "48": 48}[a.precision], a.repeat,
+                            a.profile_mesh, a.profile_nw)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
