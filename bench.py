@@ -231,7 +231,7 @@ SLICE = 128            # the vertex, mu, Dyson, DIIS and mkfk samples are 1/SLIC
 # cycles restarted to a Ritz residual of 1e-10), from that solve's own
 # statistics; the reference arm, which has no GPU run of its own, scales
 # with them
-PLAIN_FP64_COUNTS = {"c2": (24, 40), "c1": (11, 40), "c5": (29, 40)}
+PLAIN_FP64_COUNTS = {"c2": (24, 60), "c1": (11, 40), "c5": (29, 40)}
 
 
 def _cpu_unit(job):
