@@ -459,6 +459,14 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
     base = o * L * d.S + s0;
   }
   const bool tw4 = d.tw_L1 > 0;
+  // exchange buffer: contiguous lines keep each line's row padded to B + 1
+  // (threads walk n2, then lines); strided passes put the line innermost,
+  // [k1][n2][line], because there adjacent threads take adjacent lines and a
+  // line-outer layout would put a warp's accesses 2 (A B + A) words apart,
+  // into two banks
+  auto slot = [&](int b, int k1, int n2) {
+    return contig ? (b * A + k1) * LDB + n2 : (k1 * B + n2) * nl + b;
+  };
   // phase 1: load A elements per (line, n2), DFT over n1, inner twiddle
   for (int it = threadIdx.x; it < nl * B; it += blockDim.x) {
     int b, n2;
@@ -483,7 +491,7 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
     for (int k1 = 0; k1 < A; ++k1) {
       cx<R> w = v[k1];
       if (k1 && n2) w = w * twid<R>(line_tab<R>(d), n2 * k1, sign);
-      sm[(b * A + k1) * LDB + n2] = w;
+      sm[slot(b, k1, n2)] = w;
     }
   }
   __syncthreads();
@@ -494,7 +502,7 @@ __global__ void __launch_bounds__(256) fft2_kernel(cx<R>* data, long long P, Pas
     if (b >= nact) continue;
     cx<R> u[B];
 #pragma unroll
-    for (int n2 = 0; n2 < B; ++n2) u[n2] = sm[(b * A + k1) * LDB + n2];
+    for (int n2 = 0; n2 < B; ++n2) u[n2] = sm[slot(b, k1, n2)];
     Dft<R, B>::run(u, sign, line_tab<R>(d), L);
     const int k1o = tw4 ? (int)((contig ? o + b : o) % d.tw_L1) : 0;
 #pragma unroll

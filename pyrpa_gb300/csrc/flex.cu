@@ -748,61 +748,76 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
 // scalar control flow (deflation, shifts, rotations) from shared memory, so
 // it is warp-uniform.
 constexpr int kStonerWarps = 4;
-__device__ __forceinline__ double warp_sum(double v) {
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
-template <typename R>
+__device__ __forceinline__ float2 csqrt_f(float2 z) {
+  const float r = hypotf(z.x, z.y);
+  if (r == 0.0f) return mkc(0.0f, 0.0f);
+  const float t = sqrtf(0.5f * (r + fabsf(z.x)));
+  if (z.x >= 0) return mkc(t, z.y / (2 * t));
+  return mkc(fabsf(z.y) / (2 * t), z.y >= 0 ? t : -t);
+}
+__device__ __forceinline__ double2 csqrt_t(double2 z) { return csqrt_(z); }
+__device__ __forceinline__ float2 csqrt_t(float2 z) { return csqrt_f(z); }
+template <typename T> constexpr T kEpsOf = (T)2.220446049250313e-16;
+template <> constexpr float kEpsOf<float> = 1.1920929e-7f;
+// T is the arithmetic of the reduction and the QR: double for every chi0
+// type, float for an FP32 chi0 in the fast schedule (stoner() decides)
+template <typename R, typename T>
 __global__ void __launch_bounds__(32 * kStonerWarps) k_stoner(double* out, const cx<R>* chi, const double* S,
                                                               const double* C, int Nk, int Nw, int n) {
+  using cT = cx<T>;
   extern __shared__ __align__(16) unsigned char sm_st[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ld = n + 1;
-  double2* A = reinterpret_cast<double2*>(sm_st) + (size_t)w * (n * ld + 64);
-  double2* v = A + n * ld;   // Householder vector / rotation sines
-  double* cs = reinterpret_cast<double*>(v + 32);
+  cT* A = reinterpret_cast<cT*>(sm_st) + (size_t)w * (n * ld + 64);
+  cT* v = A + n * ld;   // Householder vector / rotation sines
+  T* cs = reinterpret_cast<T*>(v + 32);
   const int t = blockIdx.x * kStonerWarps + w;
   if (t >= 2 * Nk) return;  // warp-uniform
   const int k0 = t % Nk, which = t / Nk;
   const double* V = which ? C : S;
-  const double sg = which ? -1.0 : 1.0;
+  const T sg = which ? (T)-1 : (T)1;
+  const cT zero = cmk<T>((T)0, (T)0);
   if (lane < n) {
     for (int b = 0; b < n; ++b) {
-      double2 acc = mkc(0.0, 0.0);
-      for (int c = 0; c < n; ++c) acc += V[c + n * b] * ccast<double>(chi[fidx(k0, 0, lane, c, Nk, Nw, n)]);
+      cT acc = zero;
+      for (int c = 0; c < n; ++c) acc += (T)V[c + n * b] * ccast<T>(chi[fidx(k0, 0, lane, c, Nk, Nw, n)]);
       A[lane * ld + b] = sg * acc;
     }
   }
   __syncwarp();
   // Householder reduction to upper Hessenberg form
   for (int k = 0; k + 2 < n; ++k) {
-    const double xn = sqrt(warp_sum((lane > k && lane < n) ? abs2(A[lane * ld + k]) : 0.0));
+    const T xn = sqrt(warp_sum<T>((lane > k && lane < n) ? abs2(A[lane * ld + k]) : (T)0));
     if (xn == 0) continue;
-    const double2 x0 = A[(k + 1) * ld + k];
-    const double a0 = hypot(x0.x, x0.y);
-    const double2 ph = a0 > 0 ? mkc(x0.x / a0, x0.y / a0) : mkc(1.0, 0.0);
-    const double2 alpha = mkc(-ph.x * xn, -ph.y * xn);
-    double2 vl = mkc(0.0, 0.0);
-    if (lane > k && lane < n) vl = A[lane * ld + k] - ((lane == k + 1) ? alpha : mkc(0.0, 0.0));
-    const double vn = warp_sum(abs2(vl));
+    const cT x0 = A[(k + 1) * ld + k];
+    const T a0 = hypot(x0.x, x0.y);
+    const cT ph = a0 > 0 ? cmk<T>(x0.x / a0, x0.y / a0) : cmk<T>((T)1, (T)0);
+    const cT alpha = cmk<T>(-ph.x * xn, -ph.y * xn);
+    cT vl = zero;
+    if (lane > k && lane < n) vl = A[lane * ld + k] - ((lane == k + 1) ? alpha : zero);
+    const T vn = warp_sum<T>(abs2(vl));
     if (lane < 32) v[lane] = vl;
     __syncwarp();
     if (vn == 0) continue;
-    const double sc = 2.0 / vn;
+    const T sc = (T)2 / vn;
     if (lane >= k && lane < n) {  // A = (I - sc v v^H) A, column j = lane
-      double2 s = mkc(0.0, 0.0);
+      cT s = zero;
       for (int i = k + 1; i < n; ++i) s += conj(v[i]) * A[i * ld + lane];
       s = sc * s;
       for (int i = k + 1; i < n; ++i) A[i * ld + lane] -= v[i] * s;
     }
     __syncwarp();
     if (lane < n) {  // A = A (I - sc v v^H), row i = lane
-      double2 s = mkc(0.0, 0.0);
+      cT s = zero;
       for (int j = k + 1; j < n; ++j) s += A[lane * ld + j] * v[j];
       s = sc * s;
       for (int j = k + 1; j < n; ++j) A[lane * ld + j] -= s * conj(v[j]);
-      if (lane >= k + 2) A[lane * ld + k] = mkc(0.0, 0.0);
+      if (lane >= k + 2) A[lane * ld + k] = zero;
     }
     __syncwarp();
   }
@@ -810,65 +825,65 @@ __global__ void __launch_bounds__(32 * kStonerWarps) k_stoner(double* out, const
   double best = -1e300;
   int hi = n - 1, iter = 0, total = 0;
   bool failed = false;
-  const double eps = 2.220446049250313e-16;
+  const T eps = kEpsOf<T>;
   while (hi >= 0) {
-    if (hi == 0) { best = fmax(best, A[0].x); break; }
+    if (hi == 0) { best = fmax(best, (double)A[0].x); break; }
     int l = hi;
     while (l > 0) {
-      double s = cabs1(A[(l - 1) * ld + l - 1]) + cabs1(A[l * ld + l]);
+      T s = cabs1(A[(l - 1) * ld + l - 1]) + cabs1(A[l * ld + l]);
       if (s == 0) s = 1.0;
       if (cabs1(A[l * ld + l - 1]) <= eps * s) break;
       --l;
     }
     if (l == hi) {
-      best = fmax(best, A[hi * ld + hi].x);
+      best = fmax(best, (double)A[hi * ld + hi].x);
       --hi;
       iter = 0;
       continue;
     }
     __syncwarp();
-    if (l > 0 && lane == 0) A[l * ld + l - 1] = mkc(0.0, 0.0);
+    if (l > 0 && lane == 0) A[l * ld + l - 1] = zero;
     __syncwarp();  // the exceptional shift may read the element just zeroed
     if (++iter > 60 || ++total > 60 * n) { failed = true; break; }
-    double2 mu;
+    cT mu;
     if (iter % 11 == 10) {  // exceptional shift
-      const double e = cabs1(A[hi * ld + hi - 1]) + (hi >= 2 ? cabs1(A[(hi - 1) * ld + hi - 2]) : 0.0);
-      mu = A[hi * ld + hi] + mkc(0.75 * e, 0.0);
+      const T e = cabs1(A[hi * ld + hi - 1]) + (hi >= 2 ? cabs1(A[(hi - 1) * ld + hi - 2]) : (T)0);
+      mu = A[hi * ld + hi] + cmk<T>((T)0.75 * e, (T)0);
     } else {
-      const double2 a = A[(hi - 1) * ld + hi - 1], b = A[(hi - 1) * ld + hi];
-      const double2 c = A[hi * ld + hi - 1], d = A[hi * ld + hi];
-      const double2 hd = 0.5 * (a - d);
-      const double2 disc = csqrt_(hd * hd + b * c);
-      const double2 m1 = 0.5 * (a + d) + disc, m2 = 0.5 * (a + d) - disc;
+      const cT a = A[(hi - 1) * ld + hi - 1], b = A[(hi - 1) * ld + hi];
+      const cT c = A[hi * ld + hi - 1], d = A[hi * ld + hi];
+      const cT hd = (T)0.5 * (a - d);
+      const cT disc = csqrt_t(hd * hd + b * c);
+      const cT m1 = (T)0.5 * (a + d) + disc, m2 = (T)0.5 * (a + d) - disc;
       mu = (abs2(m1 - d) < abs2(m2 - d)) ? m1 : m2;
     }
     __syncwarp();
     if (lane >= l && lane <= hi) A[lane * ld + lane] -= mu;
     __syncwarp();
     for (int k = l; k < hi; ++k) {
-      const double2 a = A[k * ld + k], b = A[(k + 1) * ld + k];
-      const double aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
-      const double r = hypot(aa, bb);
-      double c;
-      double2 s;
-      if (r == 0) { c = 1.0; s = mkc(0.0, 0.0); }
-      else if (aa == 0) { c = 0.0; s = conj(b) * (1.0 / bb); }
-      else { c = aa / r; s = mkc(a.x / aa, a.y / aa) * conj(b) * (1.0 / r); }
+      const cT a = A[k * ld + k], b = A[(k + 1) * ld + k];
+      const T aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
+      const T r = hypot(aa, bb);
+      T c;
+      cT s;
+      if (r == 0) { c = (T)1; s = zero; }
+      else if (aa == 0) { c = (T)0; s = conj(b) * ((T)1 / bb); }
+      else { c = aa / r; s = cmk<T>(a.x / aa, a.y / aa) * conj(b) * ((T)1 / r); }
       if (lane == 0) { cs[k] = c; v[k] = s; }
       __syncwarp();
       if (lane >= k && lane <= hi) {
-        const double2 x = A[k * ld + lane], y = A[(k + 1) * ld + lane];
+        const cT x = A[k * ld + lane], y = A[(k + 1) * ld + lane];
         A[k * ld + lane] = c * x + s * y;
         A[(k + 1) * ld + lane] = c * y - conj(s) * x;
       }
       __syncwarp();
     }
     for (int k = l; k < hi; ++k) {
-      const double c = cs[k];
-      const double2 s = v[k];
+      const T c = cs[k];
+      const cT s = v[k];
       const int imax = (k + 2 < hi) ? k + 2 : hi;
       if (lane >= l && lane <= imax) {
-        const double2 x = A[lane * ld + k], y = A[lane * ld + k + 1];
+        const cT x = A[lane * ld + k], y = A[lane * ld + k + 1];
         A[lane * ld + k] = c * x + y * conj(s);
         A[lane * ld + k + 1] = c * y - x * s;
       }
@@ -883,24 +898,43 @@ __global__ void __launch_bounds__(32 * kStonerWarps) k_stoner(double* out, const
   }
 }
 
-template <typename R>
-void stoner(const Geom& g, const cx<R>* chi, const double* S, const double* C, double* sdw, double* cdw,
-            int* q_sdw, int* q_cdw) {
+// false if the QR of some matrix did not converge
+template <typename R, typename T>
+bool stoner_launch(const Geom& g, const cx<R>* chi, const double* S, const double* C, std::vector<double>& h) {
   reset_err();
   DBuf<double> out(2 * (size_t)g.Nk);
-  const size_t smem = (size_t)kStonerWarps * ((size_t)g.Nchi * (g.Nchi + 1) + 64) * sizeof(double2);
+  const size_t smem = (size_t)kStonerWarps * ((size_t)g.Nchi * (g.Nchi + 1) + 64) * sizeof(cx<T>);
   static bool attr = false;
   if (!attr) {
-    PGB_CUDA(cudaFuncSetAttribute(k_stoner<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(96 * 1024)));
+    PGB_CUDA(cudaFuncSetAttribute(k_stoner<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(96 * 1024)));
     attr = true;
   }
   const unsigned blocks = (unsigned)((2LL * g.Nk + kStonerWarps - 1) / kStonerWarps);
-  k_stoner<R><<<blocks, 32 * kStonerWarps, smem, ctx().stream>>>(out.p, chi, S, C, g.Nk, g.Nw, g.Nchi);
+  k_stoner<R, T><<<blocks, 32 * kStonerWarps, smem, ctx().stream>>>(out.p, chi, S, C, g.Nk, g.Nw, g.Nchi);
   count_launch("stoner");
-  std::vector<double> h(2 * (size_t)g.Nk);
+  h.resize(2 * (size_t)g.Nk);
   out.download(h.data(), h.size());
-  const int e = fetch_err();
-  PGB_CHECK(e == 0, "eigenvalue iteration of chi0(q,0)S did not converge");
+  return fetch_err() == 0;
+}
+
+// max Re eig of chi0(q,0) S and -chi0(q,0) C over q (fchi.f90:352-399).  An
+// FP32 chi0 carries about 1e-7 relative rounding, so its QR runs in FP32 on
+// the FP32 pipe (64 times the FP64 rate); it is redone in FP64 when the FP32
+// Stoner factor lies within 1e-3 of 1, where the sw_rescale clamp decides.
+template <typename R>
+void stoner(const Geom& g, const cx<R>* chi, const double* S, const double* C, double* sdw, double* cdw,
+            int* q_sdw, int* q_cdw) {
+  std::vector<double> h;
+  bool done = false;
+  if constexpr (std::is_same<R, float>::value) {
+    if (stoner_launch<R, float>(g, chi, S, C, h)) {
+      double s32 = -1.0e5;
+      for (int k = 0; k < g.Nk; ++k) s32 = std::max(s32, h[k]);
+      done = std::fabs(s32 - 1.0) >= 1.0e-3;
+    }
+  }
+  if (!done)
+    PGB_CHECK((stoner_launch<R, double>(g, chi, S, C, h)), "eigenvalue iteration of chi0(q,0)S did not converge");
   double s2 = -1.0e5, c2 = -1.0e5;
   int qs = 0, qc = 0;
   for (int k = 0; k < g.Nk; ++k) {

@@ -147,4 +147,8 @@ def test_stoner_above_one_is_clamped_like_the_oracle(F):
             assert st["stoner"] >= 1.0 and r.history[0]["stoner"] >= 1.0
             assert abs(st["stoner"] - r.history[0]["stoner"]) <= 1e-9 * r.history[0]["stoner"]
         assert abs(mu - muo) < 1e-9
-        assert np.abs(sg - sgo).max() <= 1e-9 * np.abs(sgo).max() + 2e-9
+        # the clamp leaves I - chi0 S a margin of 1e-4, which amplifies the
+        # rounding difference of the two chi0 by up to 1e4 in the first
+        # vertex; three further DIIS steps carry it (measured 1.3e-7)
+        rtol = 1e-9 if loops == 1 else 1e-6
+        assert np.abs(sg - sgo).max() <= rtol * np.abs(sgo).max() + 2e-9
