@@ -367,6 +367,10 @@ __global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, 
                             const int* grid_flag, long long Nkall, int Nk, int Nw, int Nchi, long long P) {
   const BosonTerm t = terms[blockIdx.y];
   cx<R>* o = out + (long long)blockIdx.y * P;
+  __shared__ R s_stat;  // converted once per block (see k_chi0_scatter)
+  if (threadIdx.x == 0) s_stat = (R)t.stat;
+  __syncthreads();
+  const R stat = s_stat;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
        idx += (long long)gridDim.x * blockDim.x) {
     const long long gi = idx % Nkall;
@@ -376,7 +380,7 @@ __global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, 
     if (n < Nw) {
       v = fl ? V[fidx(k, n, t.l, t.m, Nk, Nw, Nchi)] : V[fidx(k, n, t.m, t.l, Nk, Nw, Nchi)];
     } else if (n == Nw) {
-      v = cmk<R>((R)t.stat, (R)0);
+      v = cmk<R>(stat, (R)0);
     } else {
       const int j = 2 * Nw - n;
       v = conj(fl ? V[fidx(k, j, t.m, t.l, Nk, Nw, Nchi)] : V[fidx(k, j, t.l, t.m, Nk, Nw, Nchi)]);
@@ -481,7 +485,15 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
                                const cx<R>* sawc, long long Nkall, int Nk, int Nw, int Nchi, long long P) {
   const ChiDev pr = pairs[blockIdx.y];
   const cx<R>* t = tmp + (long long)blockIdx.y * P;
-  const cx<R> J = cmk<R>((R)pr.J.x, (R)pr.J.y);
+  // the pair's tau-jump coefficients, converted once per block: a double ->
+  // R conversion runs on the FP64 pipe (1/64 of the FP32 rate on GB300)
+  __shared__ cx<R> sJ[2];
+  if (threadIdx.x == 0) {
+    sJ[0] = cmk<R>((R)pr.J.x, (R)pr.J.y);
+    sJ[1] = cmk<R>((R)pr.dJ.x, (R)pr.dJ.y);
+  }
+  __syncthreads();
+  const cx<R> J = sJ[0], dJ = sJ[1];
   const long long K = (long long)Nk * Nw;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -496,7 +508,7 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
     if (pr.has_d) {
       const long long M = 2LL * Nw;
       cx<R> d = conj(t[irr_grid[k] + Nkall * ((M - j) % M)]);
-      if (sawc) d += cmk<R>((R)pr.dJ.x, (R)pr.dJ.y) * sawc[j];
+      if (sawc) d += dJ * sawc[j];
       if (abs_below(d.x, kThresh)) d.x = 0;
       if (abs_below(d.y, kThresh)) d.y = 0;
       chi[fidx(k, j, pr.dm, pr.dl, Nk, Nw, Nchi)] = d;
@@ -2115,7 +2127,10 @@ template <typename R>
 __global__ void k_contract_mirror(cx<R>* T0, cx<R>* T1, const cx<R>* W, const cx<R>* F, const cx<R>* D,
                                   const MirrorTerm* terms, int nt, long long P, long long Nkall, int Nx, int Ny,
                                   const int* rev_x, const int* rev_y, const int* rev_z, const int* log_t) {
-  const R nk = (R)(double)Nkall;
+  __shared__ R s_nk;  // converted once per block (see k_chi0_scatter)
+  if (threadIdx.x == 0) s_nk = (R)(double)Nkall;
+  __syncthreads();
+  const R nk = s_nk;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
        idx += (long long)gridDim.x * blockDim.x) {
     const long long s = idx % Nkall, pt = idx / Nkall;
