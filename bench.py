@@ -7,7 +7,7 @@ One step = one full solve of the reference's calc_lin_eliashberg_eq path
 through the engine's C ABI (pyrpa_gb_flex_eliash, host buffers in and out),
 in the fast form: coarse-mesh warm start, FP32 then double-float bulk, a
 double-float judging iteration.  lin_eliash runs 20-step Arnoldi cycles,
-restarted until the Ritz residual is below 1e-10 of lambda: the reference's
+restarted until the Ritz residual is below 1e-8 of lambda: the reference's
 single 10-step pass stops 20% short of the leading eigenvalue on this model.
   value        device seconds of the solve with the inputs already in HBM
                (CUDA events on the library stream, between upload and download)
@@ -134,7 +134,7 @@ def parse():
     p.add_argument("--coarse", default="2,2",
                    help="warm start: k-mesh and frequency divisors of the coarse solve ('1,1' = cold start)")
     p.add_argument("--arnoldi-m", type=int, default=20, help="Krylov steps per Arnoldi cycle of lin_eliash")
-    p.add_argument("--arnoldi-tol", type=float, default=1.0e-10,
+    p.add_argument("--arnoldi-tol", type=float, default=1.0e-8,
                    help="restart the Arnoldi pass until the Ritz residual over |lambda| is below this "
                         "(0: the reference's single fixed-size pass)")
     p.add_argument("--no-fp64", action="store_true",
