@@ -42,6 +42,11 @@ void gen_ham(double* ham_k, const double* klist, const double* ham_r, const doub
              const int64_t* Nk, const int64_t* Nr, const int64_t* Norb);
 /* fmod.f90:209-248 get_eig: eig(Norb,Nk) ascending, uni(Norb,Norb,Nk) eigenvectors in columns */
 void get_eig(double* eig, double* uni, const double* ham_k, const int64_t* Nk, const int64_t* Norb);
+/* fmod.f90:250-310 get_eig_mlo: eigenpairs in a non-orthogonal basis (overlap
+ * Ovlk(Norb,Norb,Nk)) by canonical orthogonalization; basis directions with
+ * overlap eigenvalue <= 1e-8 are dropped and leave an eigenvalue 0 */
+void get_eig_mlo(double* eig, double* uni, const double* ham_k, const double* Ovlk, const int64_t* Nk,
+                 const int64_t* Norb);
 /* fmod.f90:312-340 get_ffermi */
 void get_ffermi(double* ffermi, const double* eig, const double* mu, const double* temp,
                 const int64_t* Nk, const int64_t* Norb);

@@ -30,6 +30,11 @@ def get_eig(hamk):
     return w, np.ascontiguousarray(v.transpose(0, 2, 1))
 
 
+def get_eig_mlo(hamk, Ovlk):
+    w, v = O.get_eig_mlo_F(hamk.transpose(0, 2, 1), Ovlk.transpose(0, 2, 1))
+    return w, np.ascontiguousarray(v.transpose(0, 2, 1))
+
+
 def get_ffermi(eig, mu, temp):
     return O.get_ffermi(eig, mu, temp)
 

@@ -171,6 +171,24 @@ def get_eig_F(H_F: np.ndarray):
     return w, v
 
 
+def _upper_hermitian(A):
+    """The Hermitian matrix zheev('V','U') sees: A's upper triangle."""
+    return np.triu(A) + np.conj(np.swapaxes(np.triu(A, 1), -1, -2))
+
+
+def get_eig_mlo_F(H_F: np.ndarray, S_F: np.ndarray):
+    """(eig[Nk,Norb], U_F[Nk,Norb,Norb]) in a non-orthogonal basis by canonical
+    orthogonalization (fmod.f90:250-310): S = V_s diag(s) V_s^H, X = V_s
+    diag(1/sqrt(s)) with the columns of s <= 1e-8 zeroed, H_orth = X^H H X,
+    H_orth = V diag(e) V^H, U = X V.  Eigenvector phases follow numpy."""
+    s, Vs = np.linalg.eigh(_upper_hermitian(S_F))
+    keep = s > 1.0e-8
+    X = Vs * np.where(keep, 1.0 / np.sqrt(np.where(keep, s, 1.0)), 0.0)[:, None, :]
+    Ho = _upper_hermitian(np.conj(np.swapaxes(X, -1, -2)) @ (H_F @ X))
+    e, V = np.linalg.eigh(Ho)
+    return e, X @ V
+
+
 def get_ffermi(eig: np.ndarray, mu: float, temp: float) -> np.ndarray:
     """fmod.f90:312-340."""
     t = max(temp, 1e-12)

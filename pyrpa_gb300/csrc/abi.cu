@@ -155,6 +155,50 @@ __global__ void k_green_inv_eig(double2* G, const double2* sig, const double2* u
   }
 }
 
+// get_eig_mlo (fmod.f90:250-310): canonical orthogonalization of a
+// non-orthogonal basis.  Per k: S = V_s diag(s) V_s^H from S's upper triangle
+// (zheev 'U'), X = V_s diag(1/sqrt(s)) with the columns of s <= 1e-8 set to
+// zero (near-linear dependence), H_orth = X^H H X (its upper triangle), then
+// H_orth = V diag(e) V^H and uni = X V.  A discarded direction leaves an
+// eigenvalue 0 in eig, as in the reference.
+__global__ void k_get_eig_mlo(double* eig, double2* uni, const double2* hk, const double2* sk, int64_t Nk, int No) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nk; i += (long long)gridDim.x * blockDim.x) {
+    double2 A[kMaxOrb * kMaxOrb], V[kMaxOrb * kMaxOrb], X[kMaxOrb * kMaxOrb], T[kMaxOrb * kMaxOrb];
+    double w[kMaxOrb];
+    const double2* h = hk + (long long)No * No * i;
+    const double2* s = sk + (long long)No * No * i;
+    for (int r = 0; r < No; ++r)
+      for (int c = 0; c < No; ++c) A[r * No + c] = r <= c ? s[r + No * c] : conj(s[c + No * r]);
+    jacobi_herm(A, No, w, V);
+    for (int j = 0; j < No; ++j) {
+      const double sc = w[j] > 1.0e-8 ? 1.0 / sqrt(w[j]) : 0.0;
+      for (int r = 0; r < No; ++r) X[r * No + j] = sc * V[r * No + j];
+    }
+    for (int r = 0; r < No; ++r)  // T = H X (the full H, as the reference's zgemm reads it)
+      for (int c = 0; c < No; ++c) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int k = 0; k < No; ++k) acc += h[r + No * k] * X[k * No + c];
+        T[r * No + c] = acc;
+      }
+    for (int r = 0; r < No; ++r)  // upper triangle of X^H T, Hermitian
+      for (int c = r; c < No; ++c) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int k = 0; k < No; ++k) acc += conj(X[k * No + r]) * T[k * No + c];
+        A[r * No + c] = r == c ? make_double2(acc.x, 0.0) : acc;
+        if (r != c) A[c * No + r] = conj(acc);
+      }
+    jacobi_herm(A, No, w, V);
+    for (int n = 0; n < No; ++n) {
+      eig[n + (long long)No * i] = w[n];
+      for (int m = 0; m < No; ++m) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int k = 0; k < No; ++k) acc += X[m * No + k] * V[k * No + n];
+        uni[m + No * (n + (long long)No * i)] = acc;
+      }
+    }
+  }
+}
+
 __global__ void k_ffermi(double* f, const double* eig, double mu, double itemp, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     f[i] = 0.5 - 0.5 * tanh((eig[i] - mu) * itemp);
@@ -640,6 +684,24 @@ void get_eig(double* eig, double2* uni, const double2* ham_k, const int64_t* Nk,
   u.download(uni, no * no * nk);
   sync();
   ABI_CATCH("get_eig", (nan_fill(eig, (size_t)(*Norb) * (*Nk)), nan_fill(uni, (size_t)(*Norb) * (*Norb) * (*Nk))))
+}
+
+void get_eig_mlo(double* eig, double2* uni, const double2* ham_k, const double2* Ovlk, const int64_t* Nk,
+                 const int64_t* Norb) {
+  ABI_TRY
+  ensure_context();
+  const int64_t nk = *Nk, no = *Norb;
+  PGB_CHECK(no <= kMaxOrb, "Norb above the engine limit of 8 orbitals");
+  DBuf<double2> hk(no * no * nk), sk(no * no * nk), u(no * no * nk);
+  DBuf<double> e(no * nk);
+  hk.upload(ham_k, no * no * nk);
+  sk.upload(Ovlk, no * no * nk);
+  k_get_eig_mlo<<<g1(nk, 64), 64, 0, ctx().stream>>>(e.p, u.p, hk.p, sk.p, nk, (int)no);
+  launch_check("get_eig_mlo");
+  e.download(eig, no * nk);
+  u.download(uni, no * no * nk);
+  sync();
+  ABI_CATCH("get_eig_mlo", (nan_fill(eig, (size_t)(*Norb) * (*Nk)), nan_fill(uni, (size_t)(*Norb) * (*Norb) * (*Nk))))
 }
 
 void get_ffermi(double* ffermi, const double* eig, const double* mu, const double* temp, const int64_t* Nk,
@@ -1766,7 +1828,6 @@ PGB_STUB(gen_tr_greenw_0)
 PGB_STUB(get_band_to_orb_delta)
 PGB_STUB(get_chi_irr_sc)
 PGB_STUB(get_dft_imp_ham)
-PGB_STUB(get_eig_mlo)
 PGB_STUB(get_imass0)
 PGB_STUB(get_imassk)
 PGB_STUB(get_spectrum_spaghetti)

@@ -537,6 +537,117 @@ bool fast_pair(int L, int* a, int* b) {
   return true;
 }
 
+// x and y of each (x, y) plane of side L = A B in one pass (nx == ny == L):
+// the plane is read once into shared memory, both axes are transformed there
+// with the two-level register scheme of fft2_kernel (radix A, twiddle, radix
+// B; natural order out), and the plane is written once.  Rows are padded to
+// L + 1 and every phase runs the line index fastest across threads, so the
+// row-wise (stride L + 1) and column-wise (stride 1) accesses are free of
+// bank conflicts for 8- and 16-byte elements.  Each thread keeps its phase
+// inputs in registers across the barriers, so the exchange of a phase
+// reuses the plane buffer: L (L + 1) elements of shared memory in all.
+template <typename R, int A, int B>
+__global__ void __launch_bounds__(256) fft_xy_kernel(cx<R>* data, long long P, PassDesc d, int sign) {
+  constexpr int L = A * B, RS = L + 1;
+  constexpr int NI1 = (L * B + 255) / 256, NI2 = (L * A + 255) / 256;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cx<R>* sm = reinterpret_cast<cx<R>*>(smem_raw);
+  cx<R>* g = data + (long long)blockIdx.y * P + (long long)blockIdx.x * (L * L);
+  const cx<R>* tab = line_tab<R>(d);
+  for (int e = threadIdx.x; e < L * L; e += blockDim.x) sm[(e / L) * RS + (e % L)] = g[e];
+  __syncthreads();
+#pragma unroll 1
+  for (int axis = 0; axis < 2; ++axis) {
+    // axis 0: line l = row y, position p = x; axis 1: line l = column x, p = y
+    const int es = axis == 0 ? 1 : RS, ls = axis == 0 ? RS : 1;
+    cx<R> v[NI1][A];
+#pragma unroll
+    for (int i = 0; i < NI1; ++i) {
+      const int it = threadIdx.x + 256 * i;
+      if (it < L * B) {
+        const int l = it % L, n2 = it / L;
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) v[i][n1] = sm[l * ls + (B * n1 + n2) * es];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NI1; ++i) {
+      const int it = threadIdx.x + 256 * i;
+      if (it < L * B) {
+        const int l = it % L, n2 = it / L;
+        Dft<R, A>::run(v[i], sign, tab, L);
+#pragma unroll
+        for (int k1 = 0; k1 < A; ++k1) {
+          cx<R> w = v[i][k1];
+          if (k1 && n2) w = w * twid<R>(tab, n2 * k1, sign);
+          sm[(k1 * B + n2) * L + l] = w;
+        }
+      }
+    }
+    __syncthreads();
+    cx<R> u[NI2][B];
+#pragma unroll
+    for (int j = 0; j < NI2; ++j) {
+      const int it = threadIdx.x + 256 * j;
+      if (it < L * A) {
+        const int l = it % L, k1 = it / L;
+#pragma unroll
+        for (int n2 = 0; n2 < B; ++n2) u[j][n2] = sm[(k1 * B + n2) * L + l];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NI2; ++j) {
+      const int it = threadIdx.x + 256 * j;
+      if (it < L * A) {
+        const int l = it % L, k1 = it / L;
+        Dft<R, B>::run(u[j], sign, tab, L);
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) sm[l * ls + (k1 + A * k2) * es] = u[j][k2];
+      }
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < L * L; e += blockDim.x) g[e] = sm[(e / L) * RS + (e % L)];
+}
+
+template <typename R>
+void launch_xy(const PassDesc& d, dim3 grid, cudaStream_t s, cx<R>* data, long long P, int sign) {
+  const size_t smem = (size_t)d.L * (d.L + 1) * sizeof(cx<R>);
+#define PGB_XY(A_, B_)                                                                              \
+  if (d.fa == A_ && d.fb == B_) {                                                                   \
+    static bool attr = false;                                                                       \
+    if (!attr) {                                                                                    \
+      PGB_CUDA(cudaFuncSetAttribute(fft_xy_kernel<R, A_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                    (int)smem));                                                     \
+      attr = true;                                                                                  \
+    }                                                                                               \
+    fft_xy_kernel<R, A_, B_><<<grid, 256, smem, s>>>(data, P, d, sign);                             \
+    return;                                                                                         \
+  }
+  PGB_XY(8, 8) PGB_XY(4, 8) PGB_XY(8, 4) PGB_XY(4, 4) PGB_XY(3, 8) PGB_XY(8, 3) PGB_XY(2, 8) PGB_XY(8, 2)
+  PGB_XY(3, 4) PGB_XY(4, 3) PGB_XY(2, 4) PGB_XY(4, 2)
+#undef PGB_XY
+  throw Error("no x-y plane FFT kernel for this side");
+}
+
+// the sides the x-y plane pass takes (square planes; 16-byte elements of a
+// 64 x 64 plane fill 66.6 KB of shared memory)
+bool xy_side(int L, int* a, int* b) {
+  if (!fast_pair(L, a, b)) return false;
+  const int ok[][2] = {{8, 8}, {4, 8}, {8, 4}, {4, 4}, {3, 8}, {8, 3}, {2, 8}, {8, 2}, {3, 4}, {4, 3}, {2, 4}, {4, 2}};
+  for (const auto& x : ok)
+    if (x[0] == *a && x[1] == *b) return true;
+  return false;
+}
+
+// the x-y plane pass is on unless PYRPA_GB_FFT_XY=0
+bool xy_pass_enabled() {
+  const char* s = std::getenv("PYRPA_GB_FFT_XY");
+  return !(s && std::string(s) == "0");
+}
+
 template <typename R>
 void launch_fast(const PassDesc& d, dim3 grid, size_t smem, cudaStream_t s, cx<R>* data, long long P, int sign) {
 #define PGB_FAST(A_, B_)                                                                    \
@@ -827,8 +938,23 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes, const PlanTune* tun
     for (int p = 0; p < n; ++p) m.rev[p] = m.pos[(n - m.logical[p]) % n];
     S *= n;
   }
-  // x and y in one plane pass (opt-in)
-  if (plane_pass_enabled() && nx >= 2 && ny >= 2 && nx <= kMaxPlaneSide && ny <= kMaxPlaneSide) {
+  // x and y of square planes in one two-level pass (default), else the
+  // opt-in Stockham plane pass
+  int xa = 0, xb = 0;
+  if (xy_pass_enabled() && !plane_pass_enabled() && nx == ny && nx > 1 && xy_side(nx, &xa, &xb)) {
+    PassDesc xy = fwd_[0];
+    xy.xy = 1;
+    xy.L = nx;
+    xy.S = 1;
+    xy.O = P_ / ((long long)nx * ny);
+    xy.B = 1;
+    xy.fa = xa;
+    xy.fb = xb;
+    for (auto* v : {&fwd_, &bwd_, &fwd_space_, &bwd_space_}) {
+      v->erase(v->begin(), v->begin() + 2);
+      v->insert(v->begin(), xy);
+    }
+  } else if (plane_pass_enabled() && nx >= 2 && ny >= 2 && nx <= kMaxPlaneSide && ny <= kMaxPlaneSide) {
     PassDesc pl{};
     pl.plane = 1;
     pl.L = nx;
@@ -874,7 +1000,7 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
     attr_set = true;
   }
   for (const PassDesc& d : passes) {
-    const long long tiles = d.plane ? d.O
+    const long long tiles = (d.plane || d.xy) ? d.O
                             : d.lp ? d.O * ((d.S + d.B - 1) / d.B)
                             : (d.S == 1) ? (d.O + d.B - 1) / d.B : d.O * ((d.S + d.B - 1) / d.B);
     const size_t smem = d.plane ? 2 * (size_t)d.ny * (d.L + 1) * sizeof(cx<R>)
@@ -900,6 +1026,7 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
         }
         fft_plane_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
       }
+      else if (d.xy) launch_xy<R>(d, grid, s, data + (long long)b0 * P_, P_, sign);
       else if (d.lp) launch_long<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
       else if (d.fa) launch_fast<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
       else fft_pass_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);

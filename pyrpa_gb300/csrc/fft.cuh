@@ -62,6 +62,9 @@ struct PassDesc {
   // (B lines per CTA, tw_line* for lp_L1, tw_line_y* for lp_L2, tw_full* for L)
   int lp;
   int lp_L1, lp_L2;
+  // x-y plane pass: both axes of each square (x, y) plane of side L = fa fb
+  // in one kernel (fft_xy_kernel); O = number of planes
+  int xy;
 };
 
 // Per-axis overrides of the plan's heuristics; 0 keeps the heuristic.

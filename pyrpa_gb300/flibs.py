@@ -39,6 +39,7 @@ _SIGNATURES = {
     "get_kweight": [_f64, _i64, _pi, _pi],
     "gen_ham": [_c128, _f64, _c128, _f64, _pi, _pi, _pi],
     "get_eig": [_f64, _c128, _c128, _pi, _pi],
+    "get_eig_mlo": [_f64, _c128, _c128, _c128, _pi, _pi],
     "get_ffermi": [_f64, _f64, _pd, _pd, _pi, _pi],
     "get_parity_prop": [_f64, _f64, _c128, _pi, _pi],
     "get_scmat": [_f64, _f64, _i64, _i64, _pd, _pd, _pi],
@@ -308,15 +309,16 @@ def gen_ham(klist, ham_r, rvec, Ovl_r=None):
 def get_eig(hamk, Ovlk=None, sw: bool = True):
     """(eig[Nk,Norb] ascending, uni[Nk,Norb,Norb]), or eig alone when sw is
     False (libs/flibs/_hamiltonian.py:160-185).  With an overlap Ovlk the
-    reference solves the generalized problem through get_eig_mlo, which this
-    library does not implement (the call raises)."""
+    generalized problem goes through get_eig_mlo (canonical orthogonalization,
+    fmod.f90:250-310)."""
     Nk, Norb = len(hamk), hamk.shape[1]
     eig = np.zeros((Nk, Norb))
     uni = np.zeros((Nk, Norb, Norb), dtype=np.complex128)
     if Ovlk is None:
         _call("get_eig", eig, uni, np.ascontiguousarray(hamk), i64(Nk), i64(Norb))
     else:
-        _call("get_eig_mlo")  # an exported stub: it reads no argument and reports the missing routine
+        _call("get_eig_mlo", eig, uni, np.ascontiguousarray(hamk), np.ascontiguousarray(Ovlk, dtype=np.complex128),
+              i64(Nk), i64(Norb))
     return (eig, uni) if sw else eig
 
 

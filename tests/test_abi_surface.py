@@ -145,11 +145,15 @@ def test_compute_entry_fails_loudly_without_gpu(lib):
         assert np.isfinite(G).all()
 
 
-def test_non_orthogonal_basis_is_refused_loudly(lib):
+def test_non_orthogonal_basis_runs_on_the_gpu(lib):
     """get_eig with an overlap (the reference's get_eig_mlo path,
-    libs/flibs/_hamiltonian.py:176-179) reaches the exported stub, which
-    reports the missing routine; no GPU is involved."""
+    libs/flibs/_hamiltonian.py:176-179) binds the six-argument routine; without
+    a GPU it fails loudly instead of falling back to the CPU."""
     from pyrpa_gb300 import flibs as F
     hamk = np.tile(np.eye(2, dtype=np.complex128), (3, 1, 1))
-    with pytest.raises(RuntimeError, match="get_eig_mlo"):
-        F.get_eig(hamk, Ovlk=hamk)
+    try:
+        eig, uni = F.get_eig(hamk, Ovlk=hamk)
+    except RuntimeError as e:
+        assert "CUDA device" in str(e)
+    else:
+        assert np.allclose(eig, 1.0)
