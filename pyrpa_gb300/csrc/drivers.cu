@@ -408,6 +408,26 @@ bool mix_diis_reset() {
   return !(s && std::string(s) == "keep");
 }
 
+// The judging phase of the mixed schedule.  Its DIIS history starts fresh
+// (PYRPA_GB_JUDGE_DIIS=keep carries the middle phase's over): the middle
+// phase's iterates come from the FP32 vertex, whose fixed point differs from
+// the FP64 one near the magnetic instability, and an extrapolation over them
+// passes eps with that bias still in Sigma.  PYRPA_GB_JUDGE_MIN is the least
+// number of judging iterations, PYRPA_GB_JUDGE_EPS_FACTOR scales eps for the
+// judging phase's convergence test (<= 1).
+struct JudgeRule {
+  bool fresh = true;
+  int min_iterations = 1;
+  double eps_factor = 1.0;
+};
+JudgeRule judge_rule() {
+  JudgeRule r;
+  if (const char* s = std::getenv("PYRPA_GB_JUDGE_DIIS")) r.fresh = std::string(s) != "keep";
+  if (const char* s = std::getenv("PYRPA_GB_JUDGE_MIN")) r.min_iterations = std::max(1, std::atoi(s));
+  if (const char* s = std::getenv("PYRPA_GB_JUDGE_EPS_FACTOR")) r.eps_factor = std::min(1.0, std::atof(s));
+  return r;
+}
+
 // Stages that the FP32 phase of the FLEX loop runs in FP32 (default all):
 // PYRPA_GB_FP32_STAGES is a comma list of chi0, vertex, sigma.
 int fp32_stage_mask() {
@@ -643,6 +663,8 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
   ChiBufs bufs;
   double best = 1e300;
   int since_best = 0;
+  const JudgeRule judge_r = judge_rule();
+  int judged = 0;  // iterations of the mixed schedule's judging phase
   for (it = 1; it <= a.scf_loop; ++it) {
     log("iter=%5d\n", it);
     maxchi0s = flex_bulk(in, a, G.p, mu, prec_of(phase), bufs, sig.p);
@@ -655,8 +677,11 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
     g_stats.stoner = maxchi0s;
     if (phase == 0) g_stats.iterations32 = it;
     if (phase == 1) ++g_stats.iterations_finish32;
-    if (prec != kPrecMixed || phase == 2) {
+    if (prec != kPrecMixed) {
       if (esterr < a.eps) break;
+    } else if (phase == 2) {
+      ++judged;
+      if (esterr < a.eps * judge_r.eps_factor && judged >= judge_r.min_iterations) break;
     } else {
       // the stall count starts once the residual is out of the initial transient
       if (esterr < best * 0.9) {
@@ -672,9 +697,10 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
         phase = (phase == 0 && finish_mask != 0) ? 1 : 2;
         log("[FLEX] residual%9.2E: continuing with %s\n", esterr,
             phase == 1 ? "wider chi0 and Sigma, FP32 vertex" : "the judging iterations");
-        if (from == 0 && mix_diis_reset()) {
-          // the FP32 entries carry the FP32 rounding floor in their residuals;
-          // the later phases start a fresh history from the current Sigma
+        if ((from == 0 && mix_diis_reset()) || (phase == 2 && judge_r.fresh)) {
+          // the FP32 entries carry the FP32 rounding floor in their residuals,
+          // the middle phase's the FP32 vertex's fixed point: the later phases
+          // start a fresh history from the current Sigma
           n_hist = 0;
           i_hist = 0;
         }
