@@ -349,15 +349,40 @@ void convert_chi(void* out, int to, const void* in, int from, long long n) {
   else convert<dfl, double>((cdf*)out, (const double2*)in, n);
 }
 
+// Bosonic frequencies whose vertex the middle phase of the mixed schedule
+// solves in double-float although the rest of its vertex is FP32
+// (PYRPA_GB_MID_DF_NU; 0 = none).  Near the magnetic instability the
+// matrices I - chi0 S of the lowest frequencies are the ill-conditioned ones,
+// and an FP32 solve of them moves the middle phase's fixed point.
+int mid_df_nu() {
+  const char* s = std::getenv("PYRPA_GB_MID_DF_NU");
+  return s ? std::max(0, std::atoi(s)) : kMidDfNu;
+}
+
 double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, const StagePrec& sp, ChiBufs& b,
                  double2* sig) {
-  const long long KC = in.g.K * in.Nchi * in.Nchi;
+  const long long K = in.g.K, KC = K * in.Nchi * in.Nchi;
   PGB_CHECK(sp.vertex == 32 || sp.vertex == 64 || sp.vertex == 48, "the vertex stage runs in FP32, FP64 or double-float");
   void* c0 = b.get(sp.chi0, KC);
   double sdw = 0;
   if (sp.chi0 == 32) sdw = stage_chi0<float>(in, a, G, mu, (float2*)c0);
   else if (sp.chi0 == 64) sdw = stage_chi0<double>(in, a, G, mu, (double2*)c0);
   else sdw = stage_chi0<dfl>(in, a, G, mu, (cdf*)c0);
+  // middle phase: the lowest frequencies' vertex in double-float, from the
+  // double-float chi0, into a compact buffer [element][matrix]
+  const long long nlow = (sp.chi0 == 48 && sp.vertex == 32 && sp.sigma == 48 && !in.soc)
+                             ? std::min<long long>((long long)mid_df_nu() * in.Nk, K) : 0;
+  DBuf<cdf> low;
+  const size_t nel = (size_t)in.Nchi * in.Nchi;
+  if (nlow > 0) {
+    Timer tl;
+    tl.start();
+    low.alloc(nlow * (long long)nel);
+    PGB_CUDA(cudaMemcpy2DAsync(low.p, nlow * sizeof(cdf), c0, K * sizeof(cdf), nlow * sizeof(cdf), nel,
+                               cudaMemcpyDeviceToDevice, ctx().stream));
+    PGB_CHECK(vertex<dfl>(low.p, nlow, nlow, in.Nchi, in.S.p, in.C.p, 0), "zgesv failed in V_sigma");
+    g_stats.t_vertex += tl.stop();
+  }
   void* cv = b.get(sp.vertex, KC);
   convert_chi(cv, sp.vertex, c0, sp.chi0, KC);
   if (sp.vertex == 32) stage_vertex<float>(in, (float2*)cv);
@@ -365,6 +390,9 @@ double flex_bulk(Inputs& in, const FlexParams& a, const double2* G, double mu, c
   else stage_vertex<double>(in, (double2*)cv);
   void* cs = b.get(sp.sigma, KC);
   convert_chi(cs, sp.sigma, cv, sp.vertex, KC);
+  if (nlow > 0)
+    PGB_CUDA(cudaMemcpy2DAsync(cs, K * sizeof(cdf), low.p, nlow * sizeof(cdf), nlow * sizeof(cdf), nel,
+                               cudaMemcpyDeviceToDevice, ctx().stream));
   if (sp.sigma == 32) stage_sigma<float>(in, a, G, (const float2*)cs, sig);
   else if (sp.sigma == 64) stage_sigma<double>(in, a, G, (const double2*)cs, sig);
   else stage_sigma<dfl>(in, a, G, (const cdf*)cs, sig);

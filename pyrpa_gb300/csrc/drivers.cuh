@@ -149,6 +149,7 @@ constexpr int kPrecDF = 48;  // double-float chi0 and Sigma convolutions, FP64 e
 constexpr double kMixSwitch = 2.0e-3;  // residual at which the mixed schedule leaves FP32
 constexpr int kMixStall = 6;           // or after this many FP32 iterations without a new minimum
 constexpr double kMixStallFrom = 0.1;  //   counted once the residual has been below this
+constexpr int kMidDfNu = 0;            // middle phase: bosonic frequencies with a double-float vertex
 
 // the reference's irreducible TRS mesh (generate_irr_kpoint_inv): kmap and
 // invk (3 per full point), returns Nk
