@@ -293,7 +293,13 @@ template <typename T> struct DBuf {
   }
 };
 
-inline void sync() { PGB_CUDA(cudaStreamSynchronize(ctx().stream)); }
+// throws if a TMA-staged FFT pass gave up a bounded wait since the last call
+// (the flag is in mapped host memory: reading it costs no transfer)
+void fft_raise_pending();
+inline void sync() {
+  PGB_CUDA(cudaStreamSynchronize(ctx().stream));
+  fft_raise_pending();
+}
 
 void log(const char* fmt, ...);
 

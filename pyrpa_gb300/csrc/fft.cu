@@ -7,6 +7,9 @@
 #include <string>
 #include <tuple>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "fft.cuh"
 
 namespace pgb {
@@ -537,6 +540,181 @@ bool fast_pair(int L, int* a, int* b) {
   return true;
 }
 
+// ------------------------------------------------ TMA-staged strided pass
+// A strided pass of the two-level kernel whose tiles move by TMA.  The pass's
+// data is a 2-D tensor: dim0 = the S contiguous elements of a row (counted in
+// 8-byte words), dim1 = the rows (stride S elements) of all arrays of the
+// launch.  A tile is the box of kTmaLines adjacent lines x L points; it lands
+// in shared memory as [point][line], so the phase-1 reads and the phase-2
+// writes (line fastest across threads) are conflict-free, and the tile goes
+// back by a TMA store from the same buffer.  A CTA is persistent over tiles
+// and double-buffers them: the load of tile i + 2 is issued as soon as the
+// store of tile i has read its buffer.  Every wait on an mbarrier is bounded
+// (kTmaWaitCycles); a CTA that gives up sets the mapped host flag, waits
+// (bounded) for its own loads still in flight and returns, and the host
+// raises at its next synchronization.
+constexpr int kTmaLines = 32;
+constexpr long long kTmaWaitCycles = 4000000000LL;  // about 2 s at 2 GHz
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; false if the limit was reached
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > kTmaWaitCycles) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];"
+               ::"l"(map), "r"(x), "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+
+template <typename R, int A, int B>
+__global__ void __launch_bounds__(256) fft2_tma_kernel(const __grid_constant__ CUtensorMap map, PassDesc d,
+                                                       long long nsb, long long ntiles, long long rows_per_array,
+                                                       int sign, volatile int* err) {
+  constexpr int L = A * B, NL = kTmaLines;
+  constexpr int W = (int)(sizeof(cx<R>) / 8);  // 8-byte words per element
+  constexpr unsigned kTileBytes = (unsigned)(L * NL * sizeof(cx<R>));
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  cx<R>* bufs = reinterpret_cast<cx<R>*>(smem_raw);  // [2][L][NL]
+  cx<R>* xch = bufs + 2 * L * NL;                     // [A][B][NL]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(xch + L * NL);
+  const long long per_array = d.O * nsb;
+  auto coord = [&](long long t, int& x, int& y, long long& o) {
+    const long long a = t / per_array, rem = t - a * per_array;
+    o = rem / nsb;
+    x = (int)((rem - o * nsb) * NL * W);
+    y = (int)(a * rows_per_array + o * L);
+  };
+  const long long step = gridDim.x;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0]);
+    mbar_init(&bar[1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int k = 0; k < 2; ++k) {
+      const long long t = blockIdx.x + k * step;
+      if (t < ntiles) {
+        int x, y;
+        long long o;
+        coord(t, x, y, o);
+        mbar_expect_tx(&bar[k], kTileBytes);
+        tma_load_2d(bufs + k * L * NL, &map, x, y, &bar[k]);
+      }
+    }
+  }
+  __syncthreads();
+  const bool tw4 = d.tw_L1 > 0;
+  unsigned parity[2] = {0u, 0u};
+  bool bad = false;
+  int it = 0;
+  for (long long t = blockIdx.x; t < ntiles; t += step, ++it) {
+    const int cur = it & 1;
+    cx<R>* buf = bufs + cur * L * NL;
+    bool ok = mbar_wait(&bar[cur], parity[cur]);
+    if (__syncthreads_or(!ok)) {
+      bad = true;
+      break;
+    }
+    parity[cur] ^= 1u;
+    int x, y;
+    long long o;
+    coord(t, x, y, o);
+    const int k1o = tw4 ? (int)(o % d.tw_L1) : 0;
+    // phase 1: A points per (line, n2), DFT over n1, inner twiddle
+    for (int item = threadIdx.x; item < NL * B; item += blockDim.x) {
+      const int b = item % NL, n2 = item / NL;
+      cx<R> v[A];
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) {
+        const int p = B * n1 + n2;
+        v[n1] = buf[p * NL + b];
+        if (tw4 && !d.tw_post) {
+          const int tt = p * k1o;
+          if (tt) v[n1] = v[n1] * twid<R>(full_tab<R>(d), tt, sign);
+        }
+      }
+      Dft<R, A>::run(v, sign, line_tab<R>(d), L);
+#pragma unroll
+      for (int k1 = 0; k1 < A; ++k1) {
+        cx<R> w = v[k1];
+        if (k1 && n2) w = w * twid<R>(line_tab<R>(d), n2 * k1, sign);
+        xch[(k1 * B + n2) * NL + b] = w;
+      }
+    }
+    __syncthreads();
+    // phase 2: DFT over n2, X[k1 + A k2] back into the tile buffer
+    for (int item = threadIdx.x; item < NL * A; item += blockDim.x) {
+      const int b = item % NL, k1 = item / NL;
+      cx<R> u[B];
+#pragma unroll
+      for (int n2 = 0; n2 < B; ++n2) u[n2] = xch[(k1 * B + n2) * NL + b];
+      Dft<R, B>::run(u, sign, line_tab<R>(d), L);
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) {
+        const int q = k1 + A * k2;
+        cx<R> w = u[k2];
+        if (tw4 && d.tw_post) {
+          const int tt = q * k1o;
+          if (tt) w = w * twid<R>(full_tab<R>(d), tt, sign);
+        }
+        buf[q * NL + b] = w;
+      }
+    }
+    // the generic-proxy writes of the tile become visible to the TMA store
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store_2d(&map, x, y, buf);
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      const long long tn = t + 2 * step;
+      if (tn < ntiles) {
+        // the buffer is reloaded only after the store has read it
+        asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        int xn, yn;
+        long long on;
+        coord(tn, xn, yn, on);
+        mbar_expect_tx(&bar[cur], kTileBytes);
+        tma_load_2d(buf, &map, xn, yn, &bar[cur]);
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (bad) {
+      *err = 1;
+      // the loads this CTA issued and has not consumed: tiles it + 0 and
+      // it + 1 of the loop, each bounded
+      for (int k = 0; k < 2; ++k) {
+        const long long t = blockIdx.x + (long long)(it + k) * step;
+        if (t < ntiles) mbar_wait(&bar[(it + k) & 1], parity[(it + k) & 1]);
+      }
+    }
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  }
+}
+
 // x and y of each (x, y) plane of side L = A B in one pass (nx == ny == L):
 // the plane is read once into shared memory, both axes are transformed there
 // with the two-level register scheme of fft2_kernel (radix A, twiddle, radix
@@ -610,6 +788,93 @@ __global__ void __launch_bounds__(256) fft_xy_kernel(cx<R>* data, long long P, P
     __syncthreads();
   }
   for (int e = threadIdx.x; e < L * L; e += blockDim.x) g[e] = sm[(e / L) * RS + (e % L)];
+}
+
+// cuTensorMapEncodeTiled from the driver, through the runtime's entry-point
+// query (no link against libcuda)
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// the timeout flag of the TMA passes, in mapped pinned host memory
+volatile int* g_tma_flag_h = nullptr;
+int* g_tma_flag_d = nullptr;
+int* tma_flag() {
+  if (!g_tma_flag_h) {
+    void* h = nullptr;
+    PGB_CUDA(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped));
+    *static_cast<volatile int*>(h) = 0;
+    void* dptr = nullptr;
+    PGB_CUDA(cudaHostGetDevicePointer(&dptr, h, 0));
+    g_tma_flag_d = static_cast<int*>(dptr);
+    g_tma_flag_h = static_cast<volatile int*>(h);
+  }
+  return g_tma_flag_d;
+}
+
+// PYRPA_GB_FFT_TMA=1 stages the strided two-level passes by TMA
+bool tma_pass_enabled() {
+  const char* s = std::getenv("PYRPA_GB_FFT_TMA");
+  return s && std::string(s) == "1";
+}
+
+template <typename R, int A, int B>
+void launch_tma_ab(const CUtensorMap& map, const PassDesc& d, long long nsb, long long ntiles, long long rows,
+                   cudaStream_t s, int sign) {
+  constexpr int L = A * B;
+  const size_t smem = (size_t)3 * L * kTmaLines * sizeof(cx<R>) + 2 * sizeof(uint64_t);
+  static int per_sm = 0;
+  if (!per_sm) {
+    PGB_CUDA(cudaFuncSetAttribute(fft2_tma_kernel<R, A, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fft2_tma_kernel<R, A, B>, 256, smem));
+    per_sm = std::max(1, per_sm);
+  }
+  const long long grid = std::max(1LL, std::min<long long>(ntiles, (long long)ctx().num_sms * per_sm));
+  fft2_tma_kernel<R, A, B><<<(unsigned)grid, 256, smem, s>>>(map, d, nsb, ntiles, rows, sign, tma_flag());
+}
+
+template <typename R>
+void launch_tma(const PassDesc& d, long long nbb, cudaStream_t s, cx<R>* data, long long P, int sign) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tma_encoder();
+  PGB_CHECK(enc != nullptr, "cuTensorMapEncodeTiled is not available from the driver");
+  constexpr int W = (int)(sizeof(cx<R>) / 8);
+  const long long rows = P / d.S;  // P = O L S: rows of S elements per array
+  CUtensorMap map;
+  const cuuint64_t dims[2] = {(cuuint64_t)(d.S * W), (cuuint64_t)(rows * nbb)};
+  const cuuint64_t strides[1] = {(cuuint64_t)(d.S * sizeof(cx<R>))};
+  const cuuint32_t box[2] = {(cuuint32_t)(kTmaLines * W), (cuuint32_t)d.L};
+  const cuuint32_t es[2] = {1, 1};
+  const CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, static_cast<void*>(data), dims, strides, box, es,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  PGB_CHECK(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed for an FFT pass (code " + std::to_string((int)r) + ")");
+  const long long nsb = d.S / kTmaLines, ntiles = nbb * d.O * nsb;
+#define PGB_TMA(A_, B_)                                                 \
+  if (d.fa == A_ && d.fb == B_) {                                       \
+    launch_tma_ab<R, A_, B_>(map, d, nsb, ntiles, rows, s, sign);        \
+    return;                                                             \
+  }
+  PGB_TMA(8, 8) PGB_TMA(4, 8) PGB_TMA(8, 4) PGB_TMA(4, 4) PGB_TMA(2, 8) PGB_TMA(8, 2) PGB_TMA(3, 8) PGB_TMA(8, 3)
+  PGB_TMA(2, 4) PGB_TMA(4, 2) PGB_TMA(3, 4) PGB_TMA(4, 3)
+#undef PGB_TMA
+  throw Error("no TMA FFT kernel for this line length");
+}
+
+bool tma_pair(int a, int b) {
+  const int ok[][2] = {{8, 8}, {4, 8}, {8, 4}, {4, 4}, {2, 8}, {8, 2}, {3, 8}, {8, 3}, {2, 4}, {4, 2}, {3, 4}, {4, 3}};
+  for (const auto& x : ok)
+    if (x[0] == a && x[1] == b) return true;
+  return false;
 }
 
 template <typename R>
@@ -976,6 +1241,13 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes, const PlanTune* tun
       }
     }
   }
+  // strided two-level passes staged by TMA (opt-in)
+  if (tma_pass_enabled()) {
+    for (auto* v : {&fwd_, &bwd_, &fwd_space_, &bwd_space_})
+      for (PassDesc& p : *v)
+        if (p.fa && !p.xy && !p.plane && !p.lp && p.S > 1 && p.S % kTmaLines == 0 && tma_pair(p.fa, p.fb))
+          p.tma = 1;
+  }
   // device tables
   std::vector<int> h;
   for (int a = 0; a < 4; ++a) {
@@ -1027,6 +1299,7 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
         fft_plane_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
       }
       else if (d.xy) launch_xy<R>(d, grid, s, data + (long long)b0 * P_, P_, sign);
+      else if (d.tma) launch_tma<R>(d, nbb, s, data + (long long)b0 * P_, P_, sign);
       else if (d.lp) launch_long<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
       else if (d.fa) launch_fast<R>(d, grid, smem, s, data + (long long)b0 * P_, P_, sign);
       else fft_pass_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
@@ -1067,6 +1340,13 @@ template void FFT4D::forward_space<dfl>(cdf*, int, cudaStream_t) const;
 template void FFT4D::backward_space<dfl>(cdf*, int, cudaStream_t) const;
 
 void fft_profile_enable(bool on) { g_prof = on; }
+
+void fft_raise_pending() {
+  if (g_tma_flag_h && *g_tma_flag_h) {
+    *g_tma_flag_h = 0;
+    throw Error("an FFT pass gave up waiting for its TMA copies (bounded wait ran out)");
+  }
+}
 
 void fft_profile_collect(double* launches, double* ms, double* bytes) {
   double n = 0, t = 0, b = 0;

@@ -65,6 +65,9 @@ struct PassDesc {
   // x-y plane pass: both axes of each square (x, y) plane of side L = fa fb
   // in one kernel (fft_xy_kernel); O = number of planes
   int xy;
+  // strided two-level pass staged by TMA (fft2_tma_kernel): tiles of
+  // kTmaLines adjacent lines, S a multiple of kTmaLines
+  int tma;
 };
 
 // Per-axis overrides of the plan's heuristics; 0 keeps the heuristic.

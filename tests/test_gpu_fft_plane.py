@@ -1,7 +1,8 @@
 """GPU parity of the opt-in FFT variants through chi0 and the FLEX loop,
 against the FP64 oracle: the plane pass (PYRPA_GB_FFT_PLANE=1: x and y of
 each (x, y) plane in one kernel), the long pass (PYRPA_GB_FFT_LONG=1: a
-four-step axis in one kernel) and autotuned plans (PYRPA_GB_FFT_TUNE=1).  Mesh shapes here are used by no other test, so their FFT plans are
+four-step axis in one kernel), autotuned plans (PYRPA_GB_FFT_TUNE=1) and the
+TMA-staged strided passes (PYRPA_GB_FFT_TMA=1).  Mesh shapes here are used by no other test, so their FFT plans are
 built while the switch is on; it is cleared right after, so that plans made
 later take the default passes.
 """
@@ -71,6 +72,17 @@ LONG = [(2, 6, 10, 1, 128, False), (1, 10, 6, 1, 512, False), (1, 6, 10, 1, 2048
 @pytest.mark.parametrize("Norb,Nx,Ny,Nz,Nw,fp32", LONG)
 def test_long_pass_matches_oracle(F, Norb, Nx, Ny, Nz, Nw, fp32):
     _check(F, "PYRPA_GB_FFT_LONG", Norb, Nx, Ny, Nz, Nw, fp32)
+
+
+# (Norb, Nx, Ny, Nz, Nw, FP32 run): strides that are multiples of 32 lines:
+# the Matsubara four-step passes of 4096 = 64 x 64 and 1024 = 32 x 32 points,
+# a 512-point axis in FP32, and the z pass of an 8 x 4 x 8 mesh
+TMA = [(1, 8, 8, 1, 2048, False), (2, 4, 8, 1, 512, False), (1, 16, 16, 1, 256, True), (1, 8, 4, 8, 64, False)]
+
+
+@pytest.mark.parametrize("Norb,Nx,Ny,Nz,Nw,fp32", TMA)
+def test_tma_pass_matches_oracle(F, Norb, Nx, Ny, Nz, Nw, fp32):
+    _check(F, "PYRPA_GB_FFT_TMA", Norb, Nx, Ny, Nz, Nw, fp32)
 
 
 def _check(F, switch, Norb, Nx, Ny, Nz, Nw, fp32):
