@@ -436,21 +436,26 @@ bool mix_diis_reset() {
   return !(s && std::string(s) == "keep");
 }
 
-// The judging phase of the mixed schedule.  Its DIIS history starts fresh
-// (PYRPA_GB_JUDGE_DIIS=keep carries the middle phase's over): the middle
-// phase's iterates come from the FP32 vertex, whose fixed point differs from
-// the FP64 one near the magnetic instability, and an extrapolation over them
-// passes eps with that bias still in Sigma.  PYRPA_GB_JUDGE_MIN is the least
-// number of judging iterations, PYRPA_GB_JUDGE_EPS_FACTOR scales eps for the
-// judging phase's convergence test (<= 1).
+// The judging phase of the mixed schedule.  The middle phase's iterates come
+// from an FP32 vertex (double-float for its lowest frequencies, mid_df_nu),
+// whose fixed point differs from the FP64 one: on c2 by 1.7e-6 of max|Sigma|,
+// mostly at high Matsubara frequencies.  The judging phase keeps the middle
+// phase's DIIS history (PYRPA_GB_JUDGE_DIIS=fresh starts a new one, which
+// removes the bias through about five more judging iterations), and after
+// convergence takes kJudgePolish full steps of the judging map without DIIS
+// (PYRPA_GB_JUDGE_POLISH), each of which contracts what is left of the bias.
+// PYRPA_GB_JUDGE_MIN is the least number of judging iterations,
+// PYRPA_GB_JUDGE_EPS_FACTOR scales eps for the judging test (<= 1).
 struct JudgeRule {
-  bool fresh = true;
+  bool fresh = false;
   int min_iterations = 1;
   double eps_factor = 1.0;
+  int polish = kJudgePolish;
 };
 JudgeRule judge_rule() {
   JudgeRule r;
-  if (const char* s = std::getenv("PYRPA_GB_JUDGE_DIIS")) r.fresh = std::string(s) != "keep";
+  if (const char* s = std::getenv("PYRPA_GB_JUDGE_DIIS")) r.fresh = std::string(s) == "fresh";
+  if (const char* s = std::getenv("PYRPA_GB_JUDGE_POLISH")) r.polish = std::max(0, std::atoi(s));
   if (const char* s = std::getenv("PYRPA_GB_JUDGE_MIN")) r.min_iterations = std::max(1, std::atoi(s));
   if (const char* s = std::getenv("PYRPA_GB_JUDGE_EPS_FACTOR")) r.eps_factor = std::min(1.0, std::atof(s));
   return r;
@@ -744,6 +749,21 @@ void mkself_core(Inputs& in, const FlexParams& a, double2* sig_out, double* mu_o
     PGB_CHECK(dyson(G.p, sig.p, H.p, mu, a.temp, Nk, Nw, Norb), "singular G^-1 in the Dyson step");
     PGB_CUDA(cudaMemcpyAsync(sig0.p, sig.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     g_stats.t_dyson += tm.stop();
+  }
+  if (prec == kPrecMixed && phase == 2 && esterr < a.eps) {
+    // full steps of the judging map from the converged Sigma, without DIIS
+    for (int k = 0; k < judge_r.polish; ++k) {
+      tm.start();
+      renew_mu();
+      g_stats.t_mu += tm.stop();
+      tm.start();
+      PGB_CHECK(dyson(G.p, sig.p, H.p, mu, a.temp, Nk, Nw, Norb), "singular G^-1 in the Dyson step");
+      g_stats.t_dyson += tm.stop();
+      maxchi0s = flex_bulk(in, a, G.p, mu, prec_of(2), bufs, sig.p);
+      if (a.sub_sigma > 0) hf_subtract(sig.p, Nk, Nw, Norb, (int)a.sub_sigma);
+      g_stats.stoner = maxchi0s;
+      ++g_stats.judge_polish;
+    }
   }
   if (maxchi0s >= 1.0) {
     log("[FLEX] WARNING: Stoner factor >= 1 at the final iteration:\n");

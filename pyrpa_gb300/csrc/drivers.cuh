@@ -136,6 +136,7 @@ struct LastStats {
   // Arnoldi cycles of the pass that produced it (restarts + 1)
   double ritz_residual = 0;
   int arnoldi_cycles = 0;
+  int judge_polish = 0;  // mixed schedule: full judging steps taken after convergence
 };
 
 // bulk type of each stage of a FLEX iteration: 32 FP32, 64 FP64, 48 double-float
@@ -149,7 +150,8 @@ constexpr int kPrecDF = 48;  // double-float chi0 and Sigma convolutions, FP64 e
 constexpr double kMixSwitch = 2.0e-3;  // residual at which the mixed schedule leaves FP32
 constexpr int kMixStall = 6;           // or after this many FP32 iterations without a new minimum
 constexpr double kMixStallFrom = 0.1;  //   counted once the residual has been below this
-constexpr int kMidDfNu = 0;            // middle phase: bosonic frequencies with a double-float vertex
+constexpr int kMidDfNu = 4;            // middle phase: bosonic frequencies with a double-float vertex
+constexpr int kJudgePolish = 1;        // full judging steps after convergence (mixed schedule)
 
 // the reference's irreducible TRS mesh (generate_irr_kpoint_inv): kmap and
 // invk (3 per full point), returns Nk
