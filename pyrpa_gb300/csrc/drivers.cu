@@ -441,9 +441,12 @@ bool mix_diis_reset() {
 // whose fixed point differs from the FP64 one: on c2 by 1.7e-6 of max|Sigma|,
 // mostly at high Matsubara frequencies.  The judging phase keeps the middle
 // phase's DIIS history (PYRPA_GB_JUDGE_DIIS=fresh starts a new one, which
-// removes the bias through about five more judging iterations), and after
-// convergence takes kJudgePolish full steps of the judging map without DIIS
-// (PYRPA_GB_JUDGE_POLISH), each of which contracts what is left of the bias.
+// removes the bias through about five more judging iterations).
+// PYRPA_GB_JUDGE_POLISH takes that many full steps of the judging map without
+// DIIS after convergence; on c2 one step cut the Sigma bias to 1.6e-7 but
+// moved lambda from 8.8e-8 to 4.7e-7 of the FP64 value, and a second made both
+// worse (undamped steps are not contractive near the instability), so the
+// default is none.
 // PYRPA_GB_JUDGE_MIN is the least number of judging iterations,
 // PYRPA_GB_JUDGE_EPS_FACTOR scales eps for the judging test (<= 1).
 struct JudgeRule {

@@ -151,7 +151,7 @@ constexpr double kMixSwitch = 2.0e-3;  // residual at which the mixed schedule l
 constexpr int kMixStall = 6;           // or after this many FP32 iterations without a new minimum
 constexpr double kMixStallFrom = 0.1;  //   counted once the residual has been below this
 constexpr int kMidDfNu = 4;            // middle phase: bosonic frequencies with a double-float vertex
-constexpr int kJudgePolish = 1;        // full judging steps after convergence (mixed schedule)
+constexpr int kJudgePolish = 0;        // full judging steps after convergence (mixed schedule)
 
 // the reference's irreducible TRS mesh (generate_irr_kpoint_inv): kmap and
 // invk (3 per full point), returns Nk

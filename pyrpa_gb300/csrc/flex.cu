@@ -1232,21 +1232,24 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
   constexpr int T = W;
   constexpr int TP = T + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
+  // Si, Ci and S+C in shared memory; S and C (the V_Delta modes' constant
+  // parts, read once per row) from global memory through the read-only cache
   R* cs = reinterpret_cast<R*>(smraw);
-  constexpr size_t cs_bytes = (5 * N * N * sizeof(R) + 15) / 16 * 16;
+  constexpr size_t cs_bytes = (3 * N * N * sizeof(R) + 15) / 16 * 16;
   cx<R>* tile = reinterpret_cast<cx<R>*>(smraw + cs_bytes);  // [N*N][TP]
-  cx<R>* vb = tile + (size_t)N * N * TP;                      // [W][N][32]
-  int* pv = reinterpret_cast<int*>(vb + (size_t)W * N * 32);  // [W][N+1]
+  cx<R>* vb = tile + (size_t)N * N * TP;                      // [W][N][N], row j of lane i at j * N + i
+  int* pv = reinterpret_cast<int*>(vb + (size_t)W * N * N);   // [W][N+1]
   int* mp = pv + W * (N + 1);                                 // [W][32]
-  for (int e = threadIdx.x; e < 5 * N * N; e += blockDim.x) cs[e] = consts[e];
+  for (int e = threadIdx.x; e < 3 * N * N; e += blockDim.x) cs[e] = consts[e];
   const R* Si = cs;
   const R* Ci = cs + N * N;
   const R* SC = cs + 2 * N * N;
-  const R* Sm = cs + 3 * N * N;
-  const R* Cm = cs + 4 * N * N;
+  const R* Sm = consts + 3 * N * N;
+  const R* Cm = consts + 4 * N * N;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = lane < N ? lane : 0;
-  cx<R>* vw = vb + (size_t)w * N * 32;
+  const bool row = lane < N;
+  cx<R>* vw = vb + (size_t)w * N * N;
   const R c1 = mode == 2 ? (R)-0.5 : (R)1.5;
   const R c2 = mode == 0 ? (R)-0.5 : (R)0.5;
   for (long long m0 = (long long)blockIdx.x * T; m0 < nmat; m0 += (long long)gridDim.x * T) {
@@ -1263,18 +1266,22 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
 #pragma unroll
       for (int j = 0; j < N; ++j) a[j] = cmk<R>(Si[i * N + j], (R)0) - tile[(i + N * j) * TP + t];
       bool ok = warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+      if (row) {
 #pragma unroll
-      for (int j = 0; j < N; ++j) {
-        R base = 0;
-        if (mode == 1) base = -Sm[i * N + j];
-        else if (mode == 2) base = Sm[i * N + j] - Cm[i * N + j];
-        vw[j * 32 + lane] = cmk<R>(base, (R)0) + c1 * a[j];
+        for (int j = 0; j < N; ++j) {
+          R base = 0;
+          if (mode == 1) base = -Sm[i * N + j];
+          else if (mode == 2) base = Sm[i * N + j] - Cm[i * N + j];
+          vw[j * N + lane] = cmk<R>(base, (R)0) + c1 * a[j];
+        }
       }
 #pragma unroll
       for (int j = 0; j < N; ++j) a[j] = cmk<R>(Ci[i * N + j], (R)0) + tile[(i + N * j) * TP + t];
       ok &= warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+      if (row) {
 #pragma unroll
-      for (int j = 0; j < N; ++j) vw[j * 32 + lane] += c2 * a[j];
+        for (int j = 0; j < N; ++j) vw[j * N + lane] += c2 * a[j];
+      }
       if (mode == 0) {
         // -0.25 (S+C) X (S+C): row i of X (S+C) into the tile slot, then (S+C) times it
 #pragma unroll
@@ -1299,14 +1306,16 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
 #pragma unroll
           for (int j = 0; j < N; ++j) a[j] += sk * tile[(k + N * j) * TP + t];
         }
+        if (row) {
 #pragma unroll
-        for (int j = 0; j < N; ++j) vw[j * 32 + lane] += a[j];
+          for (int j = 0; j < N; ++j) vw[j * N + lane] += a[j];
+        }
       }
       if (!ok && lane == 0) atomicExch(&g_err_dev, 3);
       __syncwarp();
       if (lane < N) {
 #pragma unroll
-        for (int j = 0; j < N; ++j) tile[(i + N * j) * TP + t] = vw[j * 32 + lane];
+        for (int j = 0; j < N; ++j) tile[(i + N * j) * TP + t] = vw[j * N + lane];
       }
       __syncwarp();
     }
@@ -1319,7 +1328,7 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
 }
 
 template <typename R, int N, int W> size_t vertex_vs_smem() {
-  return (sizeof(R) * 5 * N * N + 15) / 16 * 16 + sizeof(cx<R>) * ((size_t)N * N * (W + 1) + (size_t)W * N * 32) +
+  return (sizeof(R) * 3 * N * N + 15) / 16 * 16 + sizeof(cx<R>) * ((size_t)N * N * (W + 1) + (size_t)W * N * N) +
          sizeof(int) * (W * (N + 1) + W * 32);
 }
 
@@ -1378,8 +1387,10 @@ bool vertex_reg_launch(cx<R>* chi, long long nmat, long long estride, const R* d
 template <typename R, int N>
 bool vertex_vs_launch(cx<R>* chi, long long nmat, long long estride, const R* dconsts, int mode) {
   // FP32: 8 warps a CTA held to 128 registers (no spills), two CTAs and 16
-  // warps per SM against 12 with 168 registers; 8-byte types keep 6 warps
-  constexpr int warps = sizeof(R) == 4 ? 8 : 6;
+  // warps per SM against 12 with 168 registers.  8-byte types: 4 warps at up
+  // to 255 registers, so that two CTAs (8 warps) fit an SM in registers and
+  // in shared memory (about 105 KB each for N = 25)
+  constexpr int warps = sizeof(R) == 4 ? 8 : 4;
   const size_t smem = vertex_vs_smem<R, N, warps>();
   static bool attr = false;
   if (!attr) {
