@@ -15,6 +15,9 @@ single 10-step pass stops 20% short of the leading eigenvalue on this model.
   plain_fp64   after the timed steps, the same model solved once in plain FP64
                from G0 (no warm start): the metric's denominator, with the
                lambda, Sigma and mu differences of the fast form from it
+  strict_judging  then the fast form once more with a fresh DIIS history in
+               its judging phase, which also removes the middle phase's Sigma
+               bias: its time and its differences from plain FP64
   roofline     the FFT passes (fft2_kernel<R, A, B>; every pass of the 64x64x4096
                transforms), the kernel that moves the most bytes, timed live per
                launch with CUDA events during the timed steps
@@ -139,6 +142,8 @@ def parse():
                         "(0: the reference's single fixed-size pass)")
     p.add_argument("--no-fp64", action="store_true",
                    help="skip the plain FP64 cold-start solve after the timed steps (the metric's denominator)")
+    p.add_argument("--no-strict", action="store_true",
+                   help="skip the fast form with a fresh DIIS history in the judging phase after the timed steps")
     p.add_argument("--flex-iters", type=int, default=0, help="reference arm: FLEX iterations to scale with")
     p.add_argument("--applies", type=int, default=0, help="reference arm: Eliashberg applications to scale with")
     return p.parse_args()
@@ -517,6 +522,7 @@ def main():
     solve_s = value - stats["t_warm_ms"] / 1e3
     ritz = [float(x) for x in F.last_ritz(4)]
     fp64 = None if a.no_fp64 else plain_fp64_comparison(F, solve_args=(m, call), res=res)
+    strict = None if (a.no_strict or not fp64 or a.precision != "mixed") else strict_form(F, (m, call), fp64)
     cpu_counts = ((fp64["flex_iterations"], fp64["eliashberg_applications"]) if fp64
                   else PLAIN_FP64_COUNTS[a.config])
     cpu_v, cores, cpu_sample = cpu_reference_estimate(c, tail, *cpu_counts)
@@ -557,10 +563,35 @@ def main():
         "stages_ms": {k: v for k, v in stats.items() if k.startswith("t_")},
     }
     if fp64:
+        fp64.pop("_lambda", None)
+        fp64.pop("_sigma", None)
         line["plain_fp64"] = fp64
         line["speedup_vs_plain_fp64"] = fp64["seconds"] / value
+    if strict:
+        line["strict_judging"] = strict
     print(json.dumps(line), flush=True)
     return 0
+
+
+def strict_form(F, solve_args, fp64) -> dict:
+    """The fast form with a fresh DIIS history in the judging phase
+    (PYRPA_GB_JUDGE_DIIS=fresh), solved once: it removes the middle phase's
+    FP32-vertex bias from Sigma at the cost of more judging iterations.  Its
+    device seconds, iterations and lambda / Sigma differences from the plain
+    FP64 solve."""
+    m, call = solve_args
+    os.environ["PYRPA_GB_JUDGE_DIIS"] = "fresh"
+    try:
+        r = F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
+                          m["init"], m["plist"], **call)
+    finally:
+        os.environ.pop("PYRPA_GB_JUDGE_DIIS", None)
+    st = F.last_stats()
+    ref_lam, ref_sig = fp64.pop("_lambda"), fp64.pop("_sigma")
+    return {"seconds": r["compute_ms"] / 1e3, "flex_iterations": int(st["iterations"]),
+            "speedup_vs_plain_fp64": fp64["seconds"] / (r["compute_ms"] / 1e3), "lambda": r["lam"],
+            "lambda_rel_diff": abs(r["lam"] - ref_lam) / abs(ref_lam),
+            "sigma_max_rel_diff": float(np.abs(r["sigmak"] - ref_sig).max() / np.abs(ref_sig).max())}
 
 
 def plain_fp64_comparison(F, solve_args, res) -> dict:
@@ -581,7 +612,7 @@ def plain_fp64_comparison(F, solve_args, res) -> dict:
             "ritz_residual": st["ritz_residual"],
             "lambda_rel_diff": abs(res["lam"] - ref["lam"]) / abs(ref["lam"]),
             "sigma_max_rel_diff": float(np.abs(res["sigmak"] - ref["sigmak"]).max() / np.abs(ref["sigmak"]).max()),
-            "mu_diff": abs(res["mu"] - ref["mu"])}
+            "mu_diff": abs(res["mu"] - ref["mu"]), "_lambda": ref["lam"], "_sigma": ref["sigmak"]}
 
 
 if __name__ == "__main__":
