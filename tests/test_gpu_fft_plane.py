@@ -1,10 +1,12 @@
-"""GPU parity of the opt-in FFT variants through chi0 and the FLEX loop,
+"""GPU parity of the FFT pass variants through chi0 and the FLEX loop,
 against the FP64 oracle: the plane pass (PYRPA_GB_FFT_PLANE=1: x and y of
 each (x, y) plane in one kernel), the long pass (PYRPA_GB_FFT_LONG=1: a
 four-step axis in one kernel), autotuned plans (PYRPA_GB_FFT_TUNE=1) and the
-TMA-staged strided passes (PYRPA_GB_FFT_TMA=1).  Mesh shapes here are used by no other test, so their FFT plans are
-built while the switch is on; it is cleared right after, so that plans made
-later take the default passes.
+TMA-staged strided passes.  TMA staging is on by default for FP32 (8-byte)
+elements; PYRPA_GB_FFT_TMA=1 turns it on for 16-byte (FP64, double-float)
+elements too, and the tests here cover both.  Mesh shapes here are used by
+no other test, so their FFT plans are built while the switch is on; it is
+cleared right after, so that plans made later take the default passes.
 """
 import os
 
