@@ -163,14 +163,27 @@ void pyrpa_gb_set_verbose(const int64_t* level);
  * Ritz residual |A x - lambda x| / |lambda| = |h_{m+1,m} y_m| / |lambda| is
  * below tol.  Also PYRPA_GB_ARNOLDI_TOL. */
 void pyrpa_gb_set_arnoldi_tol(const double* tol);
-/* message of the last failure (NUL-terminated, at most len bytes) and its
- * code: 0 none, 1 a failure of the library or the GPU, 2 an input the caller
- * has to fix (the Python wrappers raise ValueError for 2, RuntimeError for 1) */
+/* *on != 0 gives the calling host thread a context of its own: its own CUDA
+ * stream, device error flags, launch counter, last error and last
+ * statistics, with the process context's settings (precision, verbosity,
+ * Arnoldi tolerance) copied at that moment; later settings calls from the
+ * thread change only its context.  Independent problems solved from several
+ * such threads overlap on the GPU (the parameter sweep packs its instances
+ * this way).  *on == 0 waits for the thread's stream and hands the context
+ * back for reuse.  At most 63 thread contexts exist at once.  No
+ * counterpart in the reference, which runs one problem per process. */
+void pyrpa_gb_set_thread_stream(const int64_t* on);
+/* message of the last failure in the calling thread (NUL-terminated, at
+ * most len bytes) and its code: 0 none, 1 a failure of the library or the
+ * GPU, 2 an input the caller has to fix (the Python wrappers raise
+ * ValueError for 2, RuntimeError for 1) */
 void pyrpa_gb_last_error(char* buf, const int64_t* len, int64_t* code);
 void pyrpa_gb_clear_error(void);
-/* kernels this process has launched (all engine kernels, FFT passes included) */
+/* kernels launched through the calling thread's context (the process
+ * context unless pyrpa_gb_set_thread_stream gave it one; all engine kernels,
+ * FFT passes included) */
 void pyrpa_gb_kernel_launches(int64_t* n);
-/* statistics of the last mkself / lin_eliash: iterations, esterr, Stoner, mu, lambda,
+/* statistics of the last mkself / lin_eliash called from this thread: iterations, esterr, Stoner, mu, lambda,
  * Eliashberg applications, then device milliseconds of chi0, vertex, Sigma, DIIS,
  * mu, Dyson, Eliashberg applications, then the FLEX iterations run on FP32 bulk,
  * the FLEX iterations of a coarse-mesh warm start and its device milliseconds,

@@ -27,13 +27,22 @@
 
 namespace pgb {
 
-Context& ctx() {
+static Context& process_context() {
   static Context c;
   return c;
 }
+// the calling thread's own context, if it asked for one
+static thread_local Context* t_context = nullptr;
+// thread contexts no thread holds, for reuse (streams and flag slots are kept)
+static std::mutex g_thread_ctx_mu;
+static std::vector<Context*> g_thread_ctx_free;
+static int g_thread_ctx_made = 0;
+
+Context& ctx() { return t_context ? *t_context : process_context(); }
 
 void ensure_context() {
-  Context& c = ctx();
+  if (t_context) return;  // thread contexts are made ready
+  Context& c = process_context();
   if (c.ready) return;
   int n = 0;
   cudaError_t e = cudaGetDeviceCount(&n);
@@ -56,7 +65,47 @@ void ensure_context() {
   }
   if (const char* s = std::getenv("PYRPA_GB_VERBOSE")) c.verbose = std::atoi(s);
   if (const char* s = std::getenv("PYRPA_GB_ARNOLDI_TOL")) c.arnoldi_tol = std::atof(s);
+  c.err = err_slot_address(0);
   c.ready = true;
+}
+
+// Gives the calling thread a context of its own (on != 0) or hands it back
+// (on == 0).  The thread context copies the process context's settings, and
+// later settings calls from this thread change only it.
+void set_thread_context(bool on) {
+  if (on) {
+    if (t_context) return;
+    ensure_context();
+    const Context& pc = process_context();
+    Context* c = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(g_thread_ctx_mu);
+      if (!g_thread_ctx_free.empty()) {
+        c = g_thread_ctx_free.back();
+        g_thread_ctx_free.pop_back();
+      } else {
+        if (g_thread_ctx_made + 1 >= kErrSlots)
+          throw Error("more than " + std::to_string(kErrSlots - 1) + " thread contexts at once");
+        c = new Context();
+        c->err = err_slot_address(++g_thread_ctx_made);
+        PGB_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+      }
+    }
+    c->device = pc.device;
+    c->num_sms = pc.num_sms;
+    c->precision = pc.precision;
+    c->verbose = pc.verbose;
+    c->arnoldi_tol = pc.arnoldi_tol;
+    c->kernel_launches = 0;
+    c->ready = true;
+    t_context = c;
+  } else {
+    if (!t_context) return;
+    PGB_CUDA(cudaStreamSynchronize(t_context->stream));
+    std::lock_guard<std::mutex> lk(g_thread_ctx_mu);
+    g_thread_ctx_free.push_back(t_context);
+    t_context = nullptr;
+  }
 }
 
 }  // namespace pgb
@@ -65,12 +114,11 @@ using namespace pgb;
 
 namespace {
 
-std::mutex g_err_mu;
-std::string g_last_error;
-int64_t g_last_code = 0;
+// the last failure of an entry point called from this thread
+thread_local std::string g_last_error;
+thread_local int64_t g_last_code = 0;
 
 void report(const char* fn, const char* what, int64_t code = 1) {
-  std::lock_guard<std::mutex> lk(g_err_mu);
   g_last_error = std::string(fn) + ": " + what;
   g_last_code = code;
   fprintf(stderr, "pyrpa_gb300 error in %s: %s\n", fn, what);
@@ -521,7 +569,6 @@ void pyrpa_gb_set_arnoldi_tol(const double* tol) {
   ABI_CATCH("pyrpa_gb_set_arnoldi_tol", (void)0)
 }
 void pyrpa_gb_last_error(char* buf, const int64_t* len, int64_t* code) {
-  std::lock_guard<std::mutex> lk(g_err_mu);
   if (buf && len && *len > 0) {
     const size_t n = std::min<size_t>((size_t)*len - 1, g_last_error.size());
     memcpy(buf, g_last_error.data(), n);
@@ -530,9 +577,11 @@ void pyrpa_gb_last_error(char* buf, const int64_t* len, int64_t* code) {
   if (code) *code = g_last_code;
 }
 void pyrpa_gb_clear_error() {
-  std::lock_guard<std::mutex> lk(g_err_mu);
   g_last_error.clear();
   g_last_code = 0;
+}
+void pyrpa_gb_set_thread_stream(const int64_t* on) {
+  ABI_TRY set_thread_context(*on != 0); ABI_CATCH("pyrpa_gb_set_thread_stream", (void)0)
 }
 void pyrpa_gb_kernel_launches(int64_t* n) { *n = ctx().kernel_launches; }
 void pyrpa_gb_last_stats(double* out) {

@@ -203,6 +203,18 @@ struct BadInput : Error {
       throw ::pgb::Error(std::string(#call) + ": " + cudaGetErrorString(e_));        \
   } while (0)
 
+// Raises a kernel's dynamic shared memory limit once per process (a
+// function-local static, so the first call is thread-safe).  KERNEL goes in
+// parentheses when it has template arguments.
+#define PGB_SMEM_LIMIT_ONCE(KERNEL, BYTES)                                                               \
+  do {                                                                                                   \
+    static const bool pgb_smem_set_ = [&] {                                                              \
+      PGB_CUDA(cudaFuncSetAttribute(KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(BYTES))); \
+      return true;                                                                                       \
+    }();                                                                                                 \
+    (void)pgb_smem_set_;                                                                                 \
+  } while (0)
+
 #define PGB_CHECK(cond, msg)                     \
   do {                                           \
     if (!(cond)) throw ::pgb::Error(msg);        \
@@ -237,9 +249,13 @@ inline unsigned nblocks(long long n, int threads) {
 }
 
 // -------------------------------------------------------------- context --
-// One CUDA stream per process; every entry point of the library runs on it and
-// synchronizes it before returning (the C ABI is synchronous like the
-// reference's Fortran subroutines).
+// One CUDA stream per context; every entry point of the library runs on its
+// caller's context and synchronizes that stream before returning (the C ABI
+// is synchronous like the reference's Fortran subroutines).  The process has
+// one context; a host thread that calls pyrpa_gb_set_thread_stream(1) gets a
+// context of its own (own stream, device error flags, launch counter and
+// settings copied from the process context), so that several threads can
+// solve independent problems at once and their kernels overlap on the GPU.
 struct Context {
   cudaStream_t stream = nullptr;
   int device = 0;
@@ -252,9 +268,20 @@ struct Context {
   double arnoldi_tol = 0.0;
   // bumped by the entry points, some of which run on callers' own threads
   std::atomic<long long> kernel_launches{0};
+  // this context's slot of the device error flags that kernels raise
+  // (singular matrices, unconverged eigenvalue iterations)
+  int* err = nullptr;
+  // this context's timeout flag of the TMA passes, in mapped pinned host
+  // memory (made on first use)
+  volatile int* tma_flag_h = nullptr;
+  int* tma_flag_d = nullptr;
 };
 Context& ctx();
 void ensure_context();
+// device error flag slots: slot 0 is the process context's, the others go
+// to thread contexts
+constexpr int kErrSlots = 64;
+int* err_slot_address(int slot);
 
 // Device allocation through the stream-ordered pool (memory stays cached in
 // the pool between calls, so repeated calls of one shape do not re-map HBM).

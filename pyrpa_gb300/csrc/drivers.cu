@@ -20,7 +20,8 @@ namespace pgb {
 
 namespace {
 
-LastStats g_stats;
+// the statistics of the last solve called from this thread
+thread_local LastStats g_stats;
 
 struct Timer {
   cudaEvent_t a, b;

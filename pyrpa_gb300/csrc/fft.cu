@@ -332,12 +332,7 @@ __global__ void __launch_bounds__(256) fft_long_kernel(cx<R>* data, long long P,
 
 template <typename R, int G1, int G2>
 void launch_long_one(const PassDesc& d, dim3 grid, size_t smem, cudaStream_t s, cx<R>* data, long long P, int sign) {
-  static bool attr = false;
-  if (!attr) {
-    PGB_CUDA(cudaFuncSetAttribute(fft_long_kernel<R, G1, G2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)kLongSmem));
-    attr = true;
-  }
+  PGB_SMEM_LIMIT_ONCE((fft_long_kernel<R, G1, G2>), kLongSmem);
   fft_long_kernel<R, G1, G2><<<grid, 256, smem, s>>>(data, P, d, sign);
 }
 
@@ -806,20 +801,20 @@ PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
   return fn;
 }
 
-// the timeout flag of the TMA passes, in mapped pinned host memory
-volatile int* g_tma_flag_h = nullptr;
-int* g_tma_flag_d = nullptr;
+// the current context's timeout flag of the TMA passes, in mapped pinned
+// host memory
 int* tma_flag() {
-  if (!g_tma_flag_h) {
+  Context& c = ctx();
+  if (!c.tma_flag_h) {
     void* h = nullptr;
     PGB_CUDA(cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped));
     *static_cast<volatile int*>(h) = 0;
     void* dptr = nullptr;
     PGB_CUDA(cudaHostGetDevicePointer(&dptr, h, 0));
-    g_tma_flag_d = static_cast<int*>(dptr);
-    g_tma_flag_h = static_cast<volatile int*>(h);
+    c.tma_flag_d = static_cast<int*>(dptr);
+    c.tma_flag_h = static_cast<volatile int*>(h);
   }
-  return g_tma_flag_d;
+  return c.tma_flag_d;
 }
 
 // TMA-staged strided passes: on for 8-byte elements (c2's FP32 4-D transform
@@ -836,12 +831,12 @@ void launch_tma_ab(const CUtensorMap& map, const PassDesc& d, long long nsb, lon
                    cudaStream_t s, int sign) {
   constexpr int L = A * B;
   const size_t smem = (size_t)3 * L * kTmaLines * sizeof(cx<R>) + 2 * sizeof(uint64_t);
-  static int per_sm = 0;
-  if (!per_sm) {
+  static const int per_sm = [&] {
+    int n = 0;
     PGB_CUDA(cudaFuncSetAttribute(fft2_tma_kernel<R, A, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fft2_tma_kernel<R, A, B>, 256, smem));
-    per_sm = std::max(1, per_sm);
-  }
+    PGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fft2_tma_kernel<R, A, B>, 256, smem));
+    return std::max(1, n);
+  }();
   const long long grid = std::max(1LL, std::min<long long>(ntiles, (long long)ctx().num_sms * per_sm));
   fft2_tma_kernel<R, A, B><<<(unsigned)grid, 256, smem, s>>>(map, d, nsb, ntiles, rows, sign, tma_flag());
 }
@@ -885,12 +880,7 @@ void launch_xy(const PassDesc& d, dim3 grid, cudaStream_t s, cx<R>* data, long l
   const size_t smem = (size_t)d.L * (d.L + 1) * sizeof(cx<R>);
 #define PGB_XY(A_, B_)                                                                              \
   if (d.fa == A_ && d.fb == B_) {                                                                   \
-    static bool attr = false;                                                                       \
-    if (!attr) {                                                                                    \
-      PGB_CUDA(cudaFuncSetAttribute(fft_xy_kernel<R, A_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                    (int)smem));                                                     \
-      attr = true;                                                                                  \
-    }                                                                                               \
+    PGB_SMEM_LIMIT_ONCE((fft_xy_kernel<R, A_, B_>), smem);                                          \
     fft_xy_kernel<R, A_, B_><<<grid, 256, smem, s>>>(data, P, d, sign);                             \
     return;                                                                                         \
   }
@@ -1000,6 +990,9 @@ const double2* twiddle_table(int L) {
   cdf* dd = nullptr;
   PGB_CUDA(cudaMalloc(&dd, sizeof(cdf) * L));
   PGB_CUDA(cudaMemcpy(dd, hd.data(), sizeof(cdf) * L, cudaMemcpyHostToDevice));
+  // a copy from pageable memory may still be in flight when cudaMemcpy
+  // returns, and the tables are read from every thread's stream
+  PGB_CUDA(cudaDeviceSynchronize());
   g_tables_d[L] = dd;
   return d;
 }
@@ -1263,17 +1256,13 @@ FFT4D::FFT4D(int nx, int ny, int nz, int nt, int elem_bytes, const PlanTune* tun
   }
   PGB_CUDA(cudaMalloc(&d_tables_, sizeof(int) * h.size()));
   PGB_CUDA(cudaMemcpy(d_tables_, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+  PGB_CUDA(cudaDeviceSynchronize());  // complete before any thread's stream reads them
 }
 
 template <typename R>
 void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int sign,
                 cudaStream_t s) const {
-  static bool attr_set = false;
-  if (!attr_set) {
-    PGB_CUDA(cudaFuncSetAttribute(fft_pass_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  96 * 1024));
-    attr_set = true;
-  }
+  PGB_SMEM_LIMIT_ONCE(fft_pass_kernel<R>, 96 * 1024);
   for (const PassDesc& d : passes) {
     const long long tiles = (d.plane || d.xy) ? d.O
                             : d.lp ? d.O * ((d.S + d.B - 1) / d.B)
@@ -1293,12 +1282,7 @@ void FFT4D::run(const std::vector<PassDesc>& passes, cx<R>* data, int nb, int si
         PGB_CUDA(cudaEventRecord(pe.a, s));
       }
       if (d.plane) {
-        static bool plane_attr_set = false;
-        if (!plane_attr_set) {
-          PGB_CUDA(cudaFuncSetAttribute(fft_plane_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)(2 * kMaxPlaneSide * (kMaxPlaneSide + 1) * sizeof(cx<R>))));
-          plane_attr_set = true;
-        }
+        PGB_SMEM_LIMIT_ONCE(fft_plane_kernel<R>, 2 * kMaxPlaneSide * (kMaxPlaneSide + 1) * sizeof(cx<R>));
         fft_plane_kernel<R><<<grid, 256, smem, s>>>(data + (long long)b0 * P_, P_, d, sign);
       }
       else if (d.xy) launch_xy<R>(d, grid, s, data + (long long)b0 * P_, P_, sign);
@@ -1345,8 +1329,9 @@ template void FFT4D::backward_space<dfl>(cdf*, int, cudaStream_t) const;
 void fft_profile_enable(bool on) { g_prof = on; }
 
 void fft_raise_pending() {
-  if (g_tma_flag_h && *g_tma_flag_h) {
-    *g_tma_flag_h = 0;
+  Context& c = ctx();
+  if (c.tma_flag_h && *c.tma_flag_h) {
+    *c.tma_flag_h = 0;
     throw Error("an FFT pass gave up waiting for its TMA copies (bounded wait ran out)");
   }
 }

@@ -28,15 +28,25 @@ template <typename T> __device__ __forceinline__ T thresh(T v) {
   return v;
 }
 
-__device__ int g_err_dev = 0;
+// Device error flags, one slot per context: a kernel that finds a singular
+// matrix or an unconverged eigenvalue iteration writes its code to the slot
+// its launch was given (ctx().err), and the host reads it after the stage
+__device__ int g_err_slots[kErrSlots];
 
-void reset_err() {
-  int z = 0;
-  PGB_CUDA(cudaMemcpyToSymbolAsync(g_err_dev, &z, sizeof(int), 0, cudaMemcpyHostToDevice, ctx().stream));
+}  // namespace
+
+int* err_slot_address(int slot) {
+  void* p = nullptr;
+  PGB_CUDA(cudaGetSymbolAddress(&p, g_err_slots));
+  return static_cast<int*>(p) + slot;
 }
+
+namespace {
+
+void reset_err() { PGB_CUDA(cudaMemsetAsync(ctx().err, 0, sizeof(int), ctx().stream)); }
 int fetch_err() {
   int e = 0;
-  PGB_CUDA(cudaMemcpyFromSymbolAsync(&e, g_err_dev, sizeof(int), 0, cudaMemcpyDeviceToHost, ctx().stream));
+  PGB_CUDA(cudaMemcpyAsync(&e, ctx().err, sizeof(int), cudaMemcpyDeviceToHost, ctx().stream));
   sync();
   return e;
 }
@@ -271,7 +281,7 @@ void green0(double2* G, const double* eig, const double2* uni, double mu, double
 }
 
 __global__ void k_dyson(double2* G, const double2* sig, const double2* hamk, double mu, double temp,
-                        int Nk, int Nw, int No, int invert) {
+                        int Nk, int Nw, int No, int invert, int* err) {
   const long long K = (long long)Nk * Nw;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -284,7 +294,7 @@ __global__ void k_dyson(double2* G, const double2* sig, const double2* hamk, dou
         if (l == m) v += iw;
         A[m * No + l] = v;
       }
-    if (invert && !inv_small(A, No)) atomicExch(&g_err_dev, 1);
+    if (invert && !inv_small(A, No)) atomicExch(err, 1);
     for (int l = 0; l < No; ++l)
       for (int m = 0; m < No; ++m) G[fidx(k, j, m, l, Nk, Nw, No)] = A[m * No + l];
   }
@@ -294,7 +304,7 @@ bool dyson(double2* G, const double2* sig, const double2* hamk, double mu, doubl
            int Norb) {
   reset_err();
   const long long K = (long long)Nk * Nw;
-  k_dyson<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, sig, hamk, mu, temp, Nk, Nw, Norb, 1);
+  k_dyson<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, sig, hamk, mu, temp, Nk, Nw, Norb, 1, ctx().err);
   count_launch("dyson");
   return fetch_err() == 0;
 }
@@ -302,17 +312,17 @@ bool dyson(double2* G, const double2* sig, const double2* hamk, double mu, doubl
 void green_inv_only(double2* G, const double2* sig, const double2* hamk, double mu, double temp, int Nk,
                     int Nw, int Norb) {
   const long long K = (long long)Nk * Nw;
-  k_dyson<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, sig, hamk, mu, temp, Nk, Nw, Norb, 0);
+  k_dyson<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, sig, hamk, mu, temp, Nk, Nw, Norb, 0, ctx().err);
   count_launch("green_inv");
 }
 
-__global__ void k_invert_blocks(double2* G, long long nmat, int No, long long smat, long long sel) {
+__global__ void k_invert_blocks(double2* G, long long nmat, int No, long long smat, long long sel, int* err) {
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nmat;
        t += (long long)gridDim.x * blockDim.x) {
     double2 A[kMaxOrb * kMaxOrb];
     for (int l = 0; l < No; ++l)
       for (int m = 0; m < No; ++m) A[m * No + l] = G[t * smat + sel * (m + No * l)];
-    if (!inv_small(A, No)) atomicExch(&g_err_dev, 1);
+    if (!inv_small(A, No)) atomicExch(err, 1);
     for (int l = 0; l < No; ++l)
       for (int m = 0; m < No; ++m) G[t * smat + sel * (m + No * l)] = A[m * No + l];
   }
@@ -321,7 +331,7 @@ __global__ void k_invert_blocks(double2* G, long long nmat, int No, long long sm
 bool invert_blocks(double2* G, long long nmat, int Norb, long long stride_mat, long long stride_el) {
   reset_err();
   k_invert_blocks<<<grid_1d(nmat, 128, 65536), 128, 0, ctx().stream>>>(G, nmat, Norb, stride_mat,
-                                                                         stride_el);
+                                                                         stride_el, ctx().err);
   count_launch("invert_blocks");
   return fetch_err() == 0;
 }
@@ -711,6 +721,8 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
         e = new DBuf<double2>(g.Nw);
         k_sawc<<<grid_1d(g.Nw, 128), 128, 0, st>>>(e->p, g.Nw, (int)g.M, temp);
         count_launch("sawc");
+        // complete before another thread's stream reads the cached entry
+        PGB_CUDA(cudaStreamSynchronize(st));
       }
       sawc64 = e->p;
     }
@@ -780,7 +792,7 @@ template <> constexpr float kEpsOf<float> = 1.1920929e-7f;
 // type, float for an FP32 chi0 in the fast schedule (stoner() decides)
 template <typename R, typename T>
 __global__ void __launch_bounds__(32 * kStonerWarps) k_stoner(double* out, const cx<R>* chi, const double* S,
-                                                              const double* C, int Nk, int Nw, int n) {
+                                                              const double* C, int Nk, int Nw, int n, int* err) {
   using cT = cx<T>;
   extern __shared__ __align__(16) unsigned char sm_st[];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -905,7 +917,7 @@ __global__ void __launch_bounds__(32 * kStonerWarps) k_stoner(double* out, const
     __syncwarp();
   }
   if (lane == 0) {
-    if (failed) atomicExch(&g_err_dev, 2);
+    if (failed) atomicExch(err, 2);
     out[t] = best;
   }
 }
@@ -916,13 +928,10 @@ bool stoner_launch(const Geom& g, const cx<R>* chi, const double* S, const doubl
   reset_err();
   DBuf<double> out(2 * (size_t)g.Nk);
   const size_t smem = (size_t)kStonerWarps * ((size_t)g.Nchi * (g.Nchi + 1) + 64) * sizeof(cx<T>);
-  static bool attr = false;
-  if (!attr) {
-    PGB_CUDA(cudaFuncSetAttribute(k_stoner<R, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(96 * 1024)));
-    attr = true;
-  }
+  PGB_SMEM_LIMIT_ONCE((k_stoner<R, T>), 96 * 1024);
   const unsigned blocks = (unsigned)((2LL * g.Nk + kStonerWarps - 1) / kStonerWarps);
-  k_stoner<R, T><<<blocks, 32 * kStonerWarps, smem, ctx().stream>>>(out.p, chi, S, C, g.Nk, g.Nw, g.Nchi);
+  k_stoner<R, T><<<blocks, 32 * kStonerWarps, smem, ctx().stream>>>(out.p, chi, S, C, g.Nk, g.Nw, g.Nchi,
+                                                                     ctx().err);
   count_launch("stoner");
   h.resize(2 * (size_t)g.Nk);
   out.download(h.data(), h.size());
@@ -972,7 +981,7 @@ void ckchi_print_soc(const Geom& g, double v, int q) {  // fchi0withsoc.f90:189-
 // ================================================================ vertex ==
 template <typename R>
 __global__ void k_vertex(cx<R>* chi, long long nmat, long long mstride, long long estride, int n,
-                         const double* S, const double* C, int mode, int warps) {
+                         const double* S, const double* C, int mode, int warps, int* err) {
   extern __shared__ __align__(16) unsigned char sm[];
   double* sS = reinterpret_cast<double*>(sm);
   double* sC = sS + n * n;
@@ -1041,7 +1050,7 @@ __global__ void k_vertex(cx<R>* chi, long long nmat, long long mstride, long lon
       __syncwarp();
       ok &= wsolve<R>(T, X, n, ld);
     }
-    if (!ok && lane == 0) atomicExch(&g_err_dev, 3);
+    if (!ok && lane == 0) atomicExch(err, 3);
     for (int e = lane; e < n * n; e += 32) base[estride * e] = X[(e % n) * ld + e / n];
     __syncwarp();
   }
@@ -1128,12 +1137,127 @@ __device__ __forceinline__ bool warp_inverse(cx<R> (&a)[N], int* piv, int* map) 
   return ok;
 }
 
+// Pivot magnitude |Re| + |Im| as a float, for the pivot key of
+// warp_inverse_rot (double-float: the high words)
+__device__ __forceinline__ float pivot_mag(float2 a) { return fabsf(a.x) + fabsf(a.y); }
+__device__ __forceinline__ float pivot_mag(double2 a) { return (float)(fabs(a.x) + fabs(a.y)); }
+__device__ __forceinline__ float pivot_mag(cdf a) { return fabsf(a.x.hi) + fabsf(a.y.hi); }
+
+// Shared pivot row of warp_inverse_rot.  FP32 entries are stored one place
+// up (slot s at index s + 1), so that slots 1..N-1 pair into aligned 16-byte
+// words: one store per two entries for the pivot lane, one broadcast load
+// per two entries for the others.  16-byte entries are stored at index s.
+template <typename C> __host__ __device__ constexpr int prow_len(int n) { return sizeof(C) == 8 ? ((n + 2) & ~1) : n; }
+
+template <int N> __device__ __forceinline__ void prow_put(float2* d, const float2 (&a)[N]) {
+  float4* d4 = reinterpret_cast<float4*>(d);
+  d[1] = a[0];
+#pragma unroll
+  for (int s = 1; s < N; s += 2) {
+    if (s + 1 < N) d4[(s + 1) >> 1] = make_float4(a[s].x, a[s].y, a[s + 1].x, a[s + 1].y);
+    else d[s + 1] = a[s];
+  }
+}
+template <typename C, int N> __device__ __forceinline__ void prow_put(C* d, const C (&a)[N]) {
+#pragma unroll
+  for (int s = 0; s < N; ++s) d[s] = a[s];
+}
+__device__ __forceinline__ float2 prow_pivot(const float2* d) { return d[1]; }
+template <typename C> __device__ __forceinline__ C prow_pivot(const C* d) { return d[0]; }
+
+// Gauss-Jordan inverse of the warp's matrix (lane = row, N complex entries
+// in registers), arranged so that a step is little more than its complex
+// FMAs:
+//  * the column being eliminated always sits in register slot 0: a step
+//    writes its update of slot s into slot s - 1 and the new column into
+//    slot N - 1, so no register is ever indexed by the step number, and after
+//    N steps the slots are back in order;
+//  * the pivot row of a step is not divided by its pivot: it stays as it is
+//    and its entry of the eliminated column becomes 1.  Row r of the inverse
+//    is then the register row times 1 / (its pivot), which is returned in
+//    `scale` for the caller to fold into its write.  The other rows are
+//    eliminated with f = -a_k / p as in the textbook form, so every row
+//    equals the textbook row times a constant, and the pivot choices are
+//    the same;
+//  * the pivot row reaches the other lanes through shared memory (a
+//    double buffer `prow` of 2 x prow_len entries per warp) instead of two
+//    shuffles per entry;
+//  * the pivot is the candidate row with the largest |Re| + |Im|, taken by one
+//    redux.sync over a key of the magnitude's top 27 bits and the row label
+//    (the lowest label among equal keys; magnitudes within 2^-18 of each
+//    other count as equal).
+// Row interchanges relabel lanes (the lane holds logical row `label`), and
+// column interchanges are not undone in registers: on return pos[c] (per
+// warp, shared) is the column of the inverse that register slot c holds, for
+// rows with lane < N.  piv[] (N ints, shared) is scratch.
+template <typename R, int N>
+__device__ __forceinline__ bool warp_inverse_rot(cx<R> (&a)[N], cx<R>* prow, int* piv, int* pos, int& label,
+                                                 cx<R>& scale) {
+  constexpr int PL = prow_len<cx<R>>(N);
+  const int lane = threadIdx.x & 31;
+  label = lane;
+  scale = cmk<R>((R)0, (R)0);
+  bool ok = true;
+#pragma unroll 1
+  for (int k = 0; k < N; ++k) {
+    const cx<R> ak = a[0];
+    unsigned key = 0u;
+    if (lane < N && label >= k) key = (__float_as_uint(pivot_mag(ak)) & ~31u) | (unsigned)(31 - label);
+    const unsigned best = __reduce_max_sync(0xffffffffu, key);
+    const int plabel = 31 - (int)(best & 31u);
+    if (!(__uint_as_float(best & ~31u) > 0.f)) ok = false;
+    const bool is_piv = (label == plabel);
+    if (label == k) label = plabel;
+    else if (is_piv) label = k;
+    if (lane == 0) piv[k] = plabel;
+    cx<R>* buf = prow + (k & 1) * PL;
+    if (is_piv) prow_put(buf, a);
+    __syncwarp();
+    const cx<R> p = prow_pivot(buf);
+    const cx<R> ip = ok ? cdiv(cmk<R>((R)1, (R)0), p) : cmk<R>((R)0, (R)0);
+    if (is_piv) scale = ip;
+    const cx<R> f = is_piv ? cmk<R>((R)0, (R)0) : -(ak * ip);
+    if constexpr (sizeof(cx<R>) == 8) {
+      const float4* b4 = reinterpret_cast<const float4*>(buf);
+#pragma unroll
+      for (int s = 1; s < N; s += 2) {
+        const float4 q = b4[(s + 1) >> 1];
+        a[s - 1] = cmk<R>(mad(f.x, q.x, mad(-f.y, q.y, a[s].x)), mad(f.x, q.y, mad(f.y, q.x, a[s].y)));
+        if (s + 1 < N)
+          a[s] = cmk<R>(mad(f.x, q.z, mad(-f.y, q.w, a[s + 1].x)), mad(f.x, q.w, mad(f.y, q.z, a[s + 1].y)));
+      }
+    } else {
+#pragma unroll
+      for (int s = 1; s < N; ++s) {
+        const cx<R> q = buf[s];
+        a[s - 1] = cmk<R>(mad(f.x, q.x, mad(-f.y, q.y, a[s].x)), mad(f.x, q.y, mad(f.y, q.x, a[s].y)));
+      }
+    }
+    a[N - 1] = is_piv ? cmk<R>((R)1, (R)0) : f;
+  }
+  // the column interchanges, in reverse order, applied to the position of
+  // register slot `lane`
+  __syncwarp();
+  if (lane < N) {
+    int c = lane;
+#pragma unroll 1
+    for (int k = N - 1; k >= 0; --k) {
+      const int p = piv[k];
+      if (c == k) c = p;
+      else if (c == p) c = k;
+    }
+    pos[lane] = c;
+  }
+  __syncwarp();
+  return ok;
+}
+
 // Matrices of consecutive (q,iv) are staged through shared memory in tiles of
 // 2W: the loads and stores of the Fortran (Nk,Nw,Nchi,Nchi) layout are then
 // runs of 2W consecutive elements instead of one element per cache sector.
 template <typename R, int N, int W>
 __global__ void __launch_bounds__(32 * W) k_vertex_reg(cx<R>* chi, long long nmat, long long estride,
-                                                       const R* consts, int mode) {
+                                                       const R* consts, int mode, int* err) {
   constexpr int T = 2 * W;          // matrices per tile
   constexpr int TP = T + 1;         // padded tile row
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -1204,7 +1328,7 @@ __global__ void __launch_bounds__(32 * W) k_vertex_reg(cx<R>* chi, long long nma
           for (int j = 0; j < N; ++j) v[j] += sk * tbw[k * N + j];
         }
       }
-      if (!ok && lane == 0) atomicExch(&g_err_dev, 3);
+      if (!ok && lane == 0) atomicExch(err, 3);
       __syncwarp();
       if (lane < N) {
 #pragma unroll
@@ -1224,22 +1348,26 @@ __global__ void __launch_bounds__(32 * W) k_vertex_reg(cx<R>* chi, long long nma
 // the working matrix (N complex values) is the only per-lane register array,
 // so N = 25 fits in FP64.  One matrix per warp per tile.  The tile slot of a
 // matrix holds X until both inversions are done, then X(S+C) as the scratch
-// of the sandwich term, then the result.
+// of the sandwich term, then the result.  The inversions are
+// warp_inverse_rot's: each lane writes its register row, times the row's
+// scale, to the accumulator at the row's label and the slots' columns.
 template <typename R, int N, int W>
 __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(cx<R>* chi, long long nmat,
                                                                                  long long estride,
-                                                      const R* consts, int mode) {
+                                                      const R* consts, int mode, int* err) {
   constexpr int T = W;
   constexpr int TP = T + 1;
+  constexpr int PL = prow_len<cx<R>>(N);
   extern __shared__ __align__(16) unsigned char smraw[];
   // Si, Ci and S+C in shared memory; S and C (the V_Delta modes' constant
-  // parts, read once per row) from global memory through the read-only cache
+  // parts) from global memory through the read-only cache
   R* cs = reinterpret_cast<R*>(smraw);
   constexpr size_t cs_bytes = (3 * N * N * sizeof(R) + 15) / 16 * 16;
-  cx<R>* tile = reinterpret_cast<cx<R>*>(smraw + cs_bytes);  // [N*N][TP]
-  cx<R>* vb = tile + (size_t)N * N * TP;                      // [W][N][N], row j of lane i at j * N + i
+  cx<R>* prow = reinterpret_cast<cx<R>*>(smraw + cs_bytes);  // [W][2][PL] pivot rows
+  cx<R>* tile = prow + (size_t)W * 2 * PL;                    // [N*N][TP]
+  cx<R>* vb = tile + (size_t)N * N * TP;                      // [W][N][N], entry (r, c) at c * N + r
   int* pv = reinterpret_cast<int*>(vb + (size_t)W * N * N);   // [W][N+1]
-  int* mp = pv + W * (N + 1);                                 // [W][32]
+  int* ps = pv + W * (N + 1);                                 // [W][32]
   for (int e = threadIdx.x; e < 3 * N * N; e += blockDim.x) cs[e] = consts[e];
   const R* Si = cs;
   const R* Ci = cs + N * N;
@@ -1250,6 +1378,9 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
   const int i = lane < N ? lane : 0;
   const bool row = lane < N;
   cx<R>* vw = vb + (size_t)w * N * N;
+  cx<R>* pw = prow + (size_t)w * 2 * PL;
+  int* pvw = pv + w * (N + 1);
+  int* psw = ps + w * 32;
   const R c1 = mode == 2 ? (R)-0.5 : (R)1.5;
   const R c2 = mode == 0 ? (R)-0.5 : (R)0.5;
   for (long long m0 = (long long)blockIdx.x * T; m0 < nmat; m0 += (long long)gridDim.x * T) {
@@ -1263,24 +1394,33 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
     const int t = w;
     if (t < nt) {
       cx<R> a[N];
+      int lab;
+      cx<R> sc;
 #pragma unroll
       for (int j = 0; j < N; ++j) a[j] = cmk<R>(Si[i * N + j], (R)0) - tile[(i + N * j) * TP + t];
-      bool ok = warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+      bool ok = warp_inverse_rot<R, N>(a, pw, pvw, psw, lab, sc);
       if (row) {
+        const cx<R> s1 = c1 * sc;
 #pragma unroll
         for (int j = 0; j < N; ++j) {
+          const int c = psw[j];
           R base = 0;
-          if (mode == 1) base = -Sm[i * N + j];
-          else if (mode == 2) base = Sm[i * N + j] - Cm[i * N + j];
-          vw[j * N + lane] = cmk<R>(base, (R)0) + c1 * a[j];
+          if (mode == 1) base = -Sm[lab * N + c];
+          else if (mode == 2) base = Sm[lab * N + c] - Cm[lab * N + c];
+          vw[c * N + lab] = cmk<R>(base, (R)0) + s1 * a[j];
         }
       }
+      __syncwarp();
 #pragma unroll
       for (int j = 0; j < N; ++j) a[j] = cmk<R>(Ci[i * N + j], (R)0) + tile[(i + N * j) * TP + t];
-      ok &= warp_inverse<R, N>(a, pv + w * (N + 1), mp + w * 32);
+      ok &= warp_inverse_rot<R, N>(a, pw, pvw, psw, lab, sc);
       if (row) {
+        const cx<R> s2 = c2 * sc;
 #pragma unroll
-        for (int j = 0; j < N; ++j) vw[j * N + lane] += c2 * a[j];
+        for (int j = 0; j < N; ++j) {
+          const int c = psw[j];
+          vw[c * N + lab] += s2 * a[j];
+        }
       }
       if (mode == 0) {
         // -0.25 (S+C) X (S+C): row i of X (S+C) into the tile slot, then (S+C) times it
@@ -1311,7 +1451,7 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
           for (int j = 0; j < N; ++j) vw[j * N + lane] += a[j];
         }
       }
-      if (!ok && lane == 0) atomicExch(&g_err_dev, 3);
+      if (!ok && lane == 0) atomicExch(err, 3);
       __syncwarp();
       if (lane < N) {
 #pragma unroll
@@ -1328,8 +1468,8 @@ __global__ void __launch_bounds__(32 * W, (sizeof(R) == 4 ? 2 : 1)) k_vertex_vs(
 }
 
 template <typename R, int N, int W> size_t vertex_vs_smem() {
-  return (sizeof(R) * 3 * N * N + 15) / 16 * 16 + sizeof(cx<R>) * ((size_t)N * N * (W + 1) + (size_t)W * N * N) +
-         sizeof(int) * (W * (N + 1) + W * 32);
+  return (sizeof(R) * 3 * N * N + 15) / 16 * 16 + sizeof(cx<R>) * (size_t)W * 2 * prow_len<cx<R>>(N) +
+         sizeof(cx<R>) * ((size_t)N * N * (W + 1) + (size_t)W * N * N) + sizeof(int) * (W * (N + 1) + W * 32);
 }
 
 template <typename R, int N, int W> size_t vertex_reg_smem() {
@@ -1370,16 +1510,11 @@ template <typename R, int N>
 bool vertex_reg_launch(cx<R>* chi, long long nmat, long long estride, const R* dconsts, int mode) {
   constexpr int warps = (N >= 16) ? 4 : 8;
   const size_t smem = vertex_reg_smem<R, N, warps>();
-  static bool attr = false;
-  if (!attr) {
-    PGB_CUDA(cudaFuncSetAttribute(k_vertex_reg<R, N, warps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-    attr = true;
-  }
+  PGB_SMEM_LIMIT_ONCE((k_vertex_reg<R, N, warps>), smem);
   const long long tiles = (nmat + 2 * warps - 1) / (2 * warps);
   const long long blocks = std::min<long long>(tiles, (long long)ctx().num_sms * 8);
   k_vertex_reg<R, N, warps><<<(unsigned)std::max(1LL, blocks), 32 * warps, smem, ctx().stream>>>(
-      chi, nmat, estride, dconsts, mode);
+      chi, nmat, estride, dconsts, mode, ctx().err);
   count_launch("vertex_reg");
   return true;
 }
@@ -1392,15 +1527,11 @@ bool vertex_vs_launch(cx<R>* chi, long long nmat, long long estride, const R* dc
   // in shared memory (about 105 KB each for N = 25)
   constexpr int warps = sizeof(R) == 4 ? 8 : 4;
   const size_t smem = vertex_vs_smem<R, N, warps>();
-  static bool attr = false;
-  if (!attr) {
-    PGB_CUDA(cudaFuncSetAttribute(k_vertex_vs<R, N, warps>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = true;
-  }
+  PGB_SMEM_LIMIT_ONCE((k_vertex_vs<R, N, warps>), smem);
   const long long tiles = (nmat + warps - 1) / warps;
   const long long blocks = std::min<long long>(tiles, (long long)ctx().num_sms * 8);
   k_vertex_vs<R, N, warps><<<(unsigned)std::max(1LL, blocks), 32 * warps, smem, ctx().stream>>>(chi, nmat, estride,
-                                                                                                dconsts, mode);
+                                                                                                dconsts, mode, ctx().err);
   count_launch("vertex_vs");
   return true;
 }
@@ -1484,15 +1615,11 @@ bool vertex(cx<R>* chi, long long nmat, long long stride, int Nchi, const double
   const size_t per_warp = (size_t)4 * n * n * sizeof(cx<R>);
   int warps = (int)std::max<size_t>(1, std::min<size_t>(8, (200 * 1024 - head) / per_warp));
   const size_t smem = head + warps * per_warp;
-  static bool attr[2] = {false, false};
-  if (!attr[sizeof(R) == 8]) {
-    PGB_CUDA(cudaFuncSetAttribute(k_vertex<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
-    attr[sizeof(R) == 8] = true;
-  }
+  PGB_SMEM_LIMIT_ONCE(k_vertex<R>, 210 * 1024);
   reset_err();
   const long long blocks = std::min<long long>((nmat + warps - 1) / warps, (long long)ctx().num_sms * 16);
   k_vertex<R><<<(unsigned)std::max(1LL, blocks), 32 * warps, smem, ctx().stream>>>(chi, nmat, mstride, estride,
-                                                                                     n, S, C, mode, warps);
+                                                                                     n, S, C, mode, warps, ctx().err);
   count_launch("vertex");
   return fetch_err() == 0;
   }
@@ -1827,7 +1954,7 @@ void combine_sc(double2* gg, double2* ff, long long n) {
 // each) and an N x 32 accumulation block, one column per lane.
 template <int N, int W>
 __global__ void __launch_bounds__(32 * W) k_vertex_sc(double2* XS, double2* XC, long long K, const double* S,
-                                                      const double* C, int singlet) {
+                                                      const double* C, int singlet, int* err) {
   extern __shared__ __align__(16) unsigned char smsc[];
   double* sS = reinterpret_cast<double*>(smsc);  // row-major S, C
   double* sC = sS + N * N;
@@ -1889,7 +2016,7 @@ __global__ void __launch_bounds__(32 * W) k_vertex_sc(double2* XS, double2* XC, 
         for (int j = 0; j < N; ++j) Mm[i * N + j] = Rb[j * 32 + lane];  // chi_s or chi_c
       __syncwarp();
     }
-    if (!ok && lane == 0) atomicExch(&g_err_dev, 5);
+    if (!ok && lane == 0) atomicExch(err, 5);
     // V_sigma row i
     for (int j = 0; j < N; ++j) {
       double2 s = mkc(1.5 * sS[i * N + j] - 0.5 * sC[i * N + j], 0.0);
@@ -1915,7 +2042,8 @@ bool vertex_sc(double2* XS, double2* XC, long long K, int Nchi, const double* S,
                         (size_t)W * (3 * n * n + 32 * n) * sizeof(double2) + sizeof(int) * (W * (n + 1) + W * 32);
     PGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = std::min<long long>((K + W - 1) / W, (long long)ctx().num_sms * 16);
-    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(XS, XC, K, S, C, singlet ? 1 : 0);
+    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(XS, XC, K, S, C, singlet ? 1 : 0,
+                                                                             ctx().err);
   };
   reset_err();
   switch (Nchi) {
@@ -2389,7 +2517,7 @@ double filling(const double2* eig_g, const double* eig, int Nk, int Nw, int Norb
   return (s.y + 2.0 * temp * s.x) / (double)Nk;
 }
 
-__global__ void k_eig_gkinv(double2* eg, const double2* hamk, const double2* sig, int Nk, int Nw, int No) {
+__global__ void k_eig_gkinv(double2* eg, const double2* hamk, const double2* sig, int Nk, int Nw, int No, int* err) {
   const long long K = (long long)Nk * Nw;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -2398,7 +2526,7 @@ __global__ void k_eig_gkinv(double2* eg, const double2* hamk, const double2* sig
     for (int l = 0; l < No; ++l)
       for (int m = 0; m < No; ++m)
         A[m * No + l] = hamk[m + No * (l + (long long)No * k)] + sig[fidx(k, j, m, l, Nk, Nw, No)];
-    if (eigvals_general(A, No, w) < 0) atomicExch(&g_err_dev, 4);
+    if (eigvals_general(A, No, w) < 0) atomicExch(err, 4);
     for (int n = 0; n < No; ++n) eg[n + (long long)No * idx] = w[n];
   }
 }
@@ -2560,7 +2688,7 @@ double filling_cp(const double2* cp, const double* eig, int Nk, int Nw, int Norb
 bool eig_gkinv(double2* eig_g, const double2* hamk, const double2* sig, int Nk, int Nw, int Norb) {
   reset_err();
   const long long K = (long long)Nk * Nw;
-  k_eig_gkinv<<<grid_1d(K, 64, 1 << 20), 64, 0, ctx().stream>>>(eig_g, hamk, sig, Nk, Nw, Norb);
+  k_eig_gkinv<<<grid_1d(K, 64, 1 << 20), 64, 0, ctx().stream>>>(eig_g, hamk, sig, Nk, Nw, Norb, ctx().err);
   count_launch("eig_gkinv");
   return fetch_err() == 0;
 }
@@ -2876,7 +3004,7 @@ namespace {
 // V_sigma / V_Delta = -V + V (I + X V)^-1 X V = -V (I + X V)^-1 per (q, iw),
 // in place; one warp per matrix, row i on lane i (fUJ.f90:367-399)
 template <int N, int W>
-__global__ void __launch_bounds__(32 * W) k_vertex_soc(double2* chi, long long K, const double* V) {
+__global__ void __launch_bounds__(32 * W) k_vertex_soc(double2* chi, long long K, const double* V, int* err) {
   extern __shared__ __align__(16) unsigned char smv[];
   double* sV = reinterpret_cast<double*>(smv);  // row-major V
   double2* base = reinterpret_cast<double2*>(smv + ((N * N * sizeof(double) + 15) / 16) * 16);
@@ -2908,14 +3036,14 @@ __global__ void __launch_bounds__(32 * W) k_vertex_soc(double2* chi, long long K
       if (lane < N) chi[q + K * (i + N * j)] = -s;
     }
     __syncwarp();
-    if (!ok && lane == 0) atomicExch(&g_err_dev, 6);
+    if (!ok && lane == 0) atomicExch(err, 6);
   }
 }
 
 // Y = (I + chi0(q,0) V)^-1 chi0(q,0) per irreducible q (fchi0withsoc.f90:297-304)
 template <int N, int W>
 __global__ void __launch_bounds__(32 * W) k_rpa0_soc(double2* Y, const double2* chi, int Nk, long long K,
-                                                     const double* V) {
+                                                     const double* V, int* err) {
   extern __shared__ __align__(16) unsigned char smr[];
   double* sV = reinterpret_cast<double*>(smr);
   int* ints = reinterpret_cast<int*>(smr + ((N * N * sizeof(double) + 15) / 16) * 16);
@@ -2941,7 +3069,7 @@ __global__ void __launch_bounds__(32 * W) k_rpa0_soc(double2* Y, const double2* 
       for (int c = 0; c < N; ++c) s += pick<double, N>(a, c) * chi[q + K * (c + N * j)];
       if (lane < N) Y[q + (long long)Nk * (i + N * j)] = s;
     }
-    if (!ok && lane == 0) atomicExch(&g_err_dev, 7);
+    if (!ok && lane == 0) atomicExch(err, 7);
   }
 }
 
@@ -3160,7 +3288,7 @@ bool vertex_soc(double2* chi, long long K, int Nchi, const double* V) {
                         sizeof(int) * (W * (n + 1) + W * 32);
     PGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long blocks = std::min<long long>((K + W - 1) / W, (long long)ctx().num_sms * 16);
-    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(chi, K, V);
+    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(chi, K, V, ctx().err);
   };
   reset_err();
   switch (Nchi) {
@@ -3181,7 +3309,7 @@ void chis_chic_soc(double2* chic, double2* chiszz, double2* chispm, const double
   auto launch = [&](auto kernel, int n) {
     const size_t smem = ((size_t)n * n * sizeof(double) + 15) / 16 * 16 + sizeof(int) * (W * (n + 1) + W * 32);
     const long long blocks = std::min<long long>((Nk + W - 1) / W, (long long)ctx().num_sms * 16);
-    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(Y.p, chi, Nk, K, V);
+    kernel<<<(unsigned)std::max(1LL, blocks), 32 * W, smem, ctx().stream>>>(Y.p, chi, Nk, K, V, ctx().err);
   };
   reset_err();
   switch (Nchi) {
@@ -3396,7 +3524,7 @@ __global__ void k_bubble_rf(double2* out, const double2* uni, const double* eig,
 // (fchi.f90:289-314); one warp per q
 template <int N>
 __global__ void k_rpa_trace(double2* trs, double2* tr0, const double2* chi, const double* S, const int* dmask,
-                            int Nq) {
+                            int Nq, int* err) {
   __shared__ int piv[4][N + 1], map[4][32];
   __shared__ double sS[N * N];
   for (int e = threadIdx.x; e < N * N; e += blockDim.x) sS[(e % N) * N + e / N] = S[e];
@@ -3430,7 +3558,7 @@ __global__ void k_rpa_trace(double2* trs, double2* tr0, const double2* chi, cons
     if (lane == 0) {
       trs[q] = s_s;
       tr0[q] = s_0;
-      if (!ok) atomicExch(&g_err_dev, 8);
+      if (!ok) atomicExch(err, 8);
     }
   }
 }
@@ -3519,11 +3647,11 @@ void rpa_trace(double2* trs, double2* tr0, const double2* chi, const double* S, 
   reset_err();
   const unsigned blocks = (unsigned)std::min<long long>((Nq + 3) / 4, 65535LL);
   switch (Nchi) {
-    case 1: k_rpa_trace<1><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
-    case 4: k_rpa_trace<4><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
-    case 9: k_rpa_trace<9><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
-    case 16: k_rpa_trace<16><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
-    case 25: k_rpa_trace<25><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq); break;
+    case 1: k_rpa_trace<1><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq, ctx().err); break;
+    case 4: k_rpa_trace<4><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq, ctx().err); break;
+    case 9: k_rpa_trace<9><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq, ctx().err); break;
+    case 16: k_rpa_trace<16><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq, ctx().err); break;
+    case 25: k_rpa_trace<25><<<blocks, 128, 0, ctx().stream>>>(trs, tr0, chi, S, dmask, Nq, ctx().err); break;
     default: throw Error("chiq_map supports Nchi = Norb^2 with Norb <= 5");
   }
   count_launch("rpa_trace");

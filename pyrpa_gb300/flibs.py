@@ -115,6 +115,7 @@ _SIGNATURES = {
     "pyrpa_gb_get_precision": [_pi],
     "pyrpa_gb_set_verbose": [_pi],
     "pyrpa_gb_set_arnoldi_tol": [_pd],
+    "pyrpa_gb_set_thread_stream": [_pi],
     "pyrpa_gb_last_error": [POINTER(c_char), _pi, _pi],
     "pyrpa_gb_clear_error": [],
     "pyrpa_gb_kernel_launches": [_pi],
@@ -240,6 +241,14 @@ def set_arnoldi_tol(tol: float) -> None:
     restarts the pass that gives lambda until the Ritz residual over |lambda|
     is below tol (last_stats()["ritz_residual"], ["arnoldi_cycles"])."""
     _call("pyrpa_gb_set_arnoldi_tol", dbl(tol))
+
+
+def set_thread_stream(on: bool) -> None:
+    """Gives the calling thread its own engine context (CUDA stream, error
+    flags, last error and statistics; settings copied from the process
+    context) so that solves from several threads overlap on the GPU; False
+    hands it back."""
+    _call("pyrpa_gb_set_thread_stream", i64(1 if on else 0))
 
 
 def fft_profile(on: bool) -> None:

@@ -58,3 +58,45 @@ def test_run_records_failures_and_keeps_the_draw_order(monkeypatch):
     assert [r["index"] for r in res] == list(range(6))
     assert "error" in res[2] and "Dyson" in res[2]["error"]
     assert all("error" not in r for i, r in enumerate(res) if i != 2)
+
+
+def test_run_packed_solves_each_instance_once_within_the_budget(monkeypatch):
+    """run_packed() gives every worker thread its own context, solves each
+    instance exactly once, keeps the estimated footprint in flight within the
+    budget (an instance above it runs alone), records failures and returns
+    the results in draw order."""
+    import threading
+    import time
+
+    from pyrpa_gb300 import flibs
+    lock = threading.Lock()
+    seen, live, peaks, ctx_calls = [], [], [], []
+
+    def fake_solve(inst, eps=1e-4, scf_loop=300):
+        b = S.device_bytes(inst)
+        with lock:
+            seen.append(inst.index)
+            live.append(b)
+            peaks.append((sum(live), len(live), b))
+        time.sleep(0.002)
+        with lock:
+            live.remove(b)
+        if inst.index == 4:
+            raise RuntimeError("zgesv failed in V_sigma")
+        return dict(index=inst.index, iterations=5)
+
+    monkeypatch.setattr(S, "solve", fake_solve)
+    monkeypatch.setattr(flibs, "load_library", lambda *a, **k: None)
+    monkeypatch.setattr(flibs, "set_verbose", lambda v: None)
+    monkeypatch.setattr(flibs, "set_precision", lambda v: None)
+    monkeypatch.setattr(flibs, "set_thread_stream", lambda on: ctx_calls.append(bool(on)))
+    insts = S.draw(24, seed=2)
+    budget = 2.0 * sorted(S.device_bytes(x) for x in insts)[len(insts) // 2]
+    res = S.run_packed(insts, workers=4, precision=3264, budget_bytes=budget)
+    assert sorted(seen) == list(range(24))
+    assert [r["index"] for r in res] == list(range(24))
+    assert "error" in res[4] and "zgesv" in res[4]["error"]
+    for total, n, b in peaks:
+        assert n == 1 or total <= budget * (1 + 1e-12)
+    assert ctx_calls.count(True) == 4 and ctx_calls.count(False) == 4
+    assert S.run_packed.peak_bytes <= max(budget, max(S.device_bytes(x) for x in insts))
