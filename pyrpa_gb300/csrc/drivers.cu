@@ -11,6 +11,7 @@
 #include <string>
 #include <type_traits>
 #include <fstream>
+#include <memory>
 #include <vector>
 
 #include "drivers.cuh"
@@ -807,9 +808,13 @@ void run_mkself(const MkselfArgs& a, int prec) {
 // the shift -lambda_- and that Ritz vector deflated.  apply_op/inner/norm/init
 // define the operator and the inner product of the caller's vector space of n
 // elements; the normalized Ritz vector goes to delta_out, lambda is returned.
-template <class Apply, class Inner, class Norm, class Init>
+// With a restart tolerance set, refine(residual / |lambda|) is asked after
+// every cycle whether the operator has just been replaced by a more precise
+// one (true: the pass restarts on it from the current Ritz vector, whatever
+// the residual).
+template <class Apply, class Inner, class Norm, class Init, class Refine>
 double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm norm, Init init_vec,
-                        double2* delta_out) {
+                        double2* delta_out, Refine refine) {
   cudaStream_t st = ctx().stream;
   double lambda_out = 0.0;
   DBuf<double2> w(KE);
@@ -874,7 +879,9 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
                       std::vector<double2>& ev, int& imax, double res) {
     int cycles = 1;
     double lam = ev[imax].x - shift;
-    while (tol > 0.0 && res > tol * std::fabs(lam) && cycles < kMaxCycles) {
+    while (tol > 0.0 && cycles < kMaxCycles) {
+      const bool switched = refine(res / std::max(std::fabs(lam), 1e-300));
+      if (!switched && res <= tol * std::fabs(lam)) break;
       PGB_CUDA(cudaMemcpyAsync(V[0].p, D.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
       arnoldi(shift, defl, Hm, m_act);
       ev = ritz_values(Hm, m_act);
@@ -919,6 +926,7 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
     if (g_stats.arnoldi_cycles > 1) keep_ritz(ev, 0.0);
     log("  eliash   =%12.6f\n", lambda_out);
   } else {
+    refine(0.0);  // pass 2 runs on the final operator from its first step
     DBuf<double2> delta1(KE);
     ritz(delta1.p, Hm, m_act, ev[imin]);
     const double shift = -lambda1;
@@ -950,6 +958,19 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   PGB_CUDA(cudaMemcpyAsync(delta_out, D.p, KE * sizeof(double2), cudaMemcpyDeviceToDevice, st));
   sync();
   return lambda_out;
+}
+
+template <class Apply, class Inner, class Norm, class Init>
+double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm norm, Init init_vec,
+                        double2* delta_out) {
+  return arnoldi_two_pass(m, KE, apply_op, inner, norm, init_vec, delta_out, [](double) { return false; });
+}
+
+// FP32 start of the double-float Eliashberg stage of the mixed schedule
+// (PYRPA_GB_ELIASH_FP32=0 turns it off)
+bool eliash_fp32_start() {
+  const char* e = std::getenv("PYRPA_GB_ELIASH_FP32");
+  return !(e && std::string(e) == "0");
 }
 
 // V_Delta in the bulk type of the Eliashberg stage; for double-float the
@@ -1005,12 +1026,39 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
   DeltaKernelCache<R> cache;
   DBuf<double2> F(KE);
   Timer ta;
+  // Mixed schedule with a restarted Arnoldi: the first cycles (at most
+  // kEliashFp32Cycles, until the Ritz residual is below kEliashFp32Tol of
+  // lambda) apply an FP32 copy of the double-float operator, which costs a
+  // fraction of a double-float application; the pass then restarts from
+  // their Ritz vector on the double-float operator and converges there, so
+  // lambda and the gap come from double-float cycles only.  The FP32 V_Delta
+  // and its transforms are freed before the double-float transforms are made.
+  std::unique_ptr<DBuf<cx<float>>> chi32;
+  std::unique_ptr<DeltaKernelCache<float>> cache32;
+  int fp32_cycles = 0;
+  if constexpr (std::is_same<R, dfl>::value) {
+    if (ctx().precision == kPrecMixed && ctx().arnoldi_tol > 0.0 && a.arnoldi_m > 0 && eliash_fp32_start()) {
+      chi32 = std::make_unique<DBuf<cx<float>>>((size_t)KC);
+      convert<float, dfl>(chi32->p, chi, KC);
+      cache32 = std::make_unique<DeltaKernelCache<float>>();
+    }
+  }
   auto apply_op = [&](double2* out, const double2* v) {
     ta.start();
     mkfk(F.p, G, v, K, Norb);
-    mkdelta<R>(g, p, F.p, chi, S.p, C.p, prt, singlet, scale, out, &cache);
+    if (chi32) mkdelta<float>(g, p, F.p, chi32->p, S.p, C.p, prt, singlet, scale, out, cache32.get());
+    else mkdelta<R>(g, p, F.p, chi, S.p, C.p, prt, singlet, scale, out, &cache);
     g_stats.t_apply += ta.stop();
     g_stats.applies += 1;
+  };
+  auto refine = [&](double rel) {
+    if (!chi32) return false;
+    ++fp32_cycles;
+    if (rel > kEliashFp32Tol && fp32_cycles < kEliashFp32Cycles) return false;
+    log("  FP32 Arnoldi cycles: %d (residual %9.2e), continuing in double-float\n", fp32_cycles, rel);
+    cache32.reset();
+    chi32.reset();
+    return true;
   };
   auto inner = [&](const double2* u, const double2* v) {
     double2 s = inner_w(u, v, g.kweight.p, Nk, KE);
@@ -1026,7 +1074,8 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
   double lambda_out = 0.0;
   const int m = (int)a.arnoldi_m;
   if (m > 0) {
-    lambda_out = arnoldi_two_pass(m, KE, apply_op, inner, norm, init_vec, delta_out);
+    lambda_out = arnoldi_two_pass(m, KE, apply_op, inner, norm, init_vec, delta_out, refine);
+    PGB_CHECK(!chi32, "the FP32 Arnoldi cycles did not hand over to double-float");
   } else {
     // shifted power method with deflation (feliash.f90:66-140)
     DBuf<double2> D(KE), nd(KE), d1(KE), tmp(KE);

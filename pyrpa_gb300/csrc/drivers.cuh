@@ -152,6 +152,11 @@ constexpr int kMixStall = 6;           // or after this many FP32 iterations wit
 constexpr double kMixStallFrom = 0.1;  //   counted once the residual has been below this
 constexpr int kMidDfNu = 4;            // middle phase: bosonic frequencies with a double-float vertex
 constexpr int kJudgePolish = 0;        // full judging steps after convergence (mixed schedule)
+// mixed schedule, restarted Arnoldi of the double-float Eliashberg stage: its
+// first cycles run on an FP32 copy of the operator, at most this many, until
+// the Ritz residual over lambda is below kEliashFp32Tol
+constexpr int kEliashFp32Cycles = 2;
+constexpr double kEliashFp32Tol = 1.0e-5;
 
 // the reference's irreducible TRS mesh (generate_irr_kpoint_inv): kmap and
 // invk (3 per full point), returns Nk
