@@ -966,11 +966,13 @@ double arnoldi_two_pass(int m, long long KE, Apply apply_op, Inner inner, Norm n
   return arnoldi_two_pass(m, KE, apply_op, inner, norm, init_vec, delta_out, [](double) { return false; });
 }
 
-// FP32 start of the double-float Eliashberg stage of the mixed schedule
-// (PYRPA_GB_ELIASH_FP32=0 turns it off)
-bool eliash_fp32_start() {
+// FP32 start of the double-float Eliashberg stage of the mixed schedule:
+// PYRPA_GB_ELIASH_FP32=n runs at most n FP32 cycles (off by default: on c2
+// an FP32 application costs about half a double-float one, and two FP32
+// cycles plus one double-float cycle took longer than two double-float ones)
+int eliash_fp32_cycles() {
   const char* e = std::getenv("PYRPA_GB_ELIASH_FP32");
-  return !(e && std::string(e) == "0");
+  return e ? std::max(0, std::atoi(e)) : kEliashFp32Cycles;
 }
 
 // V_Delta in the bulk type of the Eliashberg stage; for double-float the
@@ -1036,8 +1038,9 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
   std::unique_ptr<DBuf<cx<float>>> chi32;
   std::unique_ptr<DeltaKernelCache<float>> cache32;
   int fp32_cycles = 0;
+  const int fp32_cap = eliash_fp32_cycles();
   if constexpr (std::is_same<R, dfl>::value) {
-    if (ctx().precision == kPrecMixed && ctx().arnoldi_tol > 0.0 && a.arnoldi_m > 0 && eliash_fp32_start()) {
+    if (ctx().precision == kPrecMixed && ctx().arnoldi_tol > 0.0 && a.arnoldi_m > 0 && fp32_cap > 0) {
       chi32 = std::make_unique<DBuf<cx<float>>>((size_t)KC);
       convert<float, dfl>(chi32->p, chi, KC);
       cache32 = std::make_unique<DeltaKernelCache<float>>();
@@ -1054,7 +1057,7 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
   auto refine = [&](double rel) {
     if (!chi32) return false;
     ++fp32_cycles;
-    if (rel > kEliashFp32Tol && fp32_cycles < kEliashFp32Cycles) return false;
+    if (rel > kEliashFp32Tol && fp32_cycles < fp32_cap) return false;
     log("  FP32 Arnoldi cycles: %d (residual %9.2e), continuing in double-float\n", fp32_cycles, rel);
     cache32.reset();
     chi32.reset();

@@ -153,9 +153,10 @@ constexpr double kMixStallFrom = 0.1;  //   counted once the residual has been b
 constexpr int kMidDfNu = 4;            // middle phase: bosonic frequencies with a double-float vertex
 constexpr int kJudgePolish = 0;        // full judging steps after convergence (mixed schedule)
 // mixed schedule, restarted Arnoldi of the double-float Eliashberg stage: its
-// first cycles run on an FP32 copy of the operator, at most this many, until
-// the Ritz residual over lambda is below kEliashFp32Tol
-constexpr int kEliashFp32Cycles = 2;
+// first cycles may run on an FP32 copy of the operator, at most this many
+// (PYRPA_GB_ELIASH_FP32 sets it; 0, the default, runs every cycle in
+// double-float), until the Ritz residual over lambda is below kEliashFp32Tol
+constexpr int kEliashFp32Cycles = 0;
 constexpr double kEliashFp32Tol = 1.0e-5;
 
 // the reference's irreducible TRS mesh (generate_irr_kpoint_inv): kmap and

@@ -42,6 +42,29 @@ template <> __device__ __forceinline__ cdf twid<dfl>(const cdf* tab, int t, int 
   return mkc(dfl(v.x, v.y), sign < 0 ? dfl(v.z, v.w) : dfl(-v.z, -v.w));
 }
 
+// Butterfly sums.  For float and double the plain sum.  For double-float the
+// sum of the high words by two-sum plus the low words, without the final
+// renormalization (8 flops instead of Dekker's 11): the radix-4 and radix-8
+// butterflies chain two or three of these and renormalize their outputs
+// once (bnorm).  Within a butterfly the low word stays a few units in the
+// last place of the high word, so the normwise error stays a few 2^-47
+// (|a| + |b|), as for the renormalized sum.
+__device__ __forceinline__ float2 badd(float2 a, float2 b) { return a + b; }
+__device__ __forceinline__ float2 bsub(float2 a, float2 b) { return a - b; }
+__device__ __forceinline__ float2 bnorm(float2 a) { return a; }
+__device__ __forceinline__ double2 badd(double2 a, double2 b) { return a + b; }
+__device__ __forceinline__ double2 bsub(double2 a, double2 b) { return a - b; }
+__device__ __forceinline__ double2 bnorm(double2 a) { return a; }
+__device__ __forceinline__ dfl lazy_add(dfl a, dfl b) {
+  const dfl s = two_sum(a.hi, b.hi);
+  return dfl(s.hi, s.lo + (a.lo + b.lo));
+}
+__device__ __forceinline__ cdf badd(cdf a, cdf b) { return mkc(lazy_add(a.x, b.x), lazy_add(a.y, b.y)); }
+__device__ __forceinline__ cdf bsub(cdf a, cdf b) { return mkc(lazy_add(a.x, -b.x), lazy_add(a.y, -b.y)); }
+__device__ __forceinline__ cdf bnorm(cdf a) {
+  return mkc(fast_two_sum(a.x.hi, a.x.lo), fast_two_sum(a.y.hi, a.y.lo));
+}
+
 template <typename R, int RAD> struct Dft {
   // generic radix: direct O(RAD^2) evaluation with roots from the line table
   __device__ static void run(cx<R>* v, int sign, const cx<R>* tab, int L) {
@@ -68,13 +91,19 @@ template <typename R> struct Dft<R, 2> {
 };
 
 template <typename R> struct Dft<R, 4> {
+  // outputs left unrenormalized (the radix-8 butterfly goes on with them)
+  __device__ static void run_lazy(cx<R>* v, int sign) {
+    cx<R> a0 = badd(v[0], v[2]), a1 = bsub(v[0], v[2]), a2 = badd(v[1], v[3]);
+    cx<R> a3 = muli(bsub(v[1], v[3]), (R)sign);
+    v[0] = badd(a0, a2);
+    v[1] = badd(a1, a3);
+    v[2] = bsub(a0, a2);
+    v[3] = bsub(a1, a3);
+  }
   __device__ static void run(cx<R>* v, int sign, const cx<R>*, int) {
-    cx<R> a0 = v[0] + v[2], a1 = v[0] - v[2], a2 = v[1] + v[3];
-    cx<R> a3 = muli(v[1] - v[3], (R)sign);
-    v[0] = a0 + a2;
-    v[1] = a1 + a3;
-    v[2] = a0 - a2;
-    v[3] = a1 - a3;
+    run_lazy(v, sign);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = bnorm(v[k]);
   }
 };
 
@@ -112,19 +141,29 @@ template <typename R> struct Dft<R, 8> {
     const R h = (R)0.70710678118654752440084436210485;
     cx<R> e[4] = {v[0], v[2], v[4], v[6]};
     cx<R> o[4] = {v[1], v[3], v[5], v[7]};
-    Dft<R, 4>::run(e, sign, t, L);
-    Dft<R, 4>::run(o, sign, t, L);
+    Dft<R, 4>::run_lazy(e, sign);
+    Dft<R, 4>::run_lazy(o, sign);
     const R s = (R)sign;
-    cx<R> w1 = cmk<R>(h, s * h), w3 = cmk<R>(-h, s * h);
-    cx<R> o1 = o[1] * w1, o2 = muli(o[2], s), o3 = o[3] * w3;
-    v[0] = e[0] + o[0];
-    v[4] = e[0] - o[0];
-    v[1] = e[1] + o1;
-    v[5] = e[1] - o1;
-    v[2] = e[2] + o2;
-    v[6] = e[2] - o2;
-    v[3] = e[3] + o3;
-    v[7] = e[3] - o3;
+    // o1 = o[1] (h + i s h), o3 = o[3] (-h + i s h): a sum and a difference
+    // times h instead of a full complex product (fewer double-word operations)
+    const cx<R> a1 = o[1], a3 = o[3];
+    cx<R> o1, o3;
+    if (sign > 0) {
+      o1 = h * cmk<R>(a1.x - a1.y, a1.x + a1.y);
+      o3 = h * cmk<R>(-(a3.x + a3.y), a3.x - a3.y);
+    } else {
+      o1 = h * cmk<R>(a1.x + a1.y, a1.y - a1.x);
+      o3 = h * cmk<R>(a3.y - a3.x, -(a3.x + a3.y));
+    }
+    const cx<R> o2 = muli(o[2], s);
+    v[0] = bnorm(badd(e[0], o[0]));
+    v[4] = bnorm(bsub(e[0], o[0]));
+    v[1] = bnorm(badd(e[1], o1));
+    v[5] = bnorm(bsub(e[1], o1));
+    v[2] = bnorm(badd(e[2], o2));
+    v[6] = bnorm(bsub(e[2], o2));
+    v[3] = bnorm(badd(e[3], o3));
+    v[7] = bnorm(bsub(e[3], o3));
   }
 };
 

@@ -43,7 +43,11 @@ int* err_slot_address(int slot) {
 
 namespace {
 
-void reset_err() { PGB_CUDA(cudaMemsetAsync(ctx().err, 0, sizeof(int), ctx().stream)); }
+// every launch of a flag-raising kernel follows a reset_err on its context
+void reset_err() {
+  PGB_CHECK(ctx().err != nullptr, "the engine context is not set up (no device error flag)");
+  PGB_CUDA(cudaMemsetAsync(ctx().err, 0, sizeof(int), ctx().stream));
+}
 int fetch_err() {
   int e = 0;
   PGB_CUDA(cudaMemcpyAsync(&e, ctx().err, sizeof(int), cudaMemcpyDeviceToHost, ctx().stream));

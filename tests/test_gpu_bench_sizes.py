@@ -172,19 +172,19 @@ def test_c1_fused_solve_against_oracle(F, c1, form):
 
 
 def test_c1_fused_fp32_arnoldi_start(F, c1, monkeypatch):
-    """The mixed fused solve with a restarted Arnoldi starts its Eliashberg
-    stage with FP32 cycles (an FP32 copy of V_Delta and FP32 transforms),
-    then restarts from their Ritz vector in double-float.  lambda and the gap
-    equal those of the all-double-float stage (PYRPA_GB_ELIASH_FP32=0) to the
-    Krylov tolerance, both Ritz residuals meet it, and lambda stays within
-    1e-6 of the oracle's."""
+    """With PYRPA_GB_ELIASH_FP32=n the mixed fused solve with a restarted
+    Arnoldi starts its Eliashberg stage with up to n FP32 cycles (an FP32
+    copy of V_Delta and FP32 transforms), then restarts from their Ritz
+    vector in double-float.  lambda and the gap equal those of the
+    all-double-float stage (the default, 0) to the Krylov tolerance, both
+    Ritz residuals meet it, and lambda stays within 1e-6 of the oracle's."""
     o = c1_oracle(c1, True)
     m = c1
     out = {}
     F.set_precision(F.MIXED)
     F.set_arnoldi_tol(1e-9)
     try:
-        for flag in ("1", "0"):
+        for flag in ("2", "0"):
             monkeypatch.setenv("PYRPA_GB_ELIASH_FP32", flag)
             r = F.flex_eliash(m["S"], m["C"], m["kmap"], m["invk"], m["olist"], m["hamk"], m["eig"], m["uni"],
                               o["init"], np.ones(1), m["mu"], m["fill"], m["temp"], m["Nw"], m["Nx"], m["Ny"], m["Nz"],
@@ -193,7 +193,7 @@ def test_c1_fused_fp32_arnoldi_start(F, c1, monkeypatch):
     finally:
         F.set_arnoldi_tol(0.0)
         F.set_precision(64)
-    (r1, s1), (r0, s0) = out["1"], out["0"]
+    (r1, s1), (r0, s0) = out["2"], out["0"]
     assert s1["ritz_residual"] <= 1e-9 and s0["ritz_residual"] <= 1e-9
     if r1["lam"] >= 0.1:  # pass 1 gives lambda: its FP32 cycles end in a restart
         assert s1["arnoldi_cycles"] >= 2
