@@ -173,6 +173,26 @@ __host__ __device__ __forceinline__ cdf cdiv(cdf a, cdf b) {  // same scaling as
   const dfl ax = a.x / s, ay = a.y / s;
   return mkc((ax * bx + ay * by) / d, (ay * bx - ax * by) / d);
 }
+// 1 / b as conj(b) / |b|^2: one real division instead of cdiv's six, for
+// |b|^2 well inside the type's range (else cdiv's scaled form)
+__host__ __device__ __forceinline__ float2 crecip(float2 b) {
+  const float d = fmaf(b.x, b.x, b.y * b.y);
+  if (!(d > 1e-30f && d < 1e30f)) return cdiv(mkc(1.f, 0.f), b);
+  const float r = 1.0f / d;
+  return mkc(b.x * r, -b.y * r);
+}
+__host__ __device__ __forceinline__ double2 crecip(double2 b) {
+  const double d = fma(b.x, b.x, b.y * b.y);
+  if (!(d > 1e-280 && d < 1e280)) return cdiv(mkc(1.0, 0.0), b);
+  const double r = 1.0 / d;
+  return mkc(b.x * r, -b.y * r);
+}
+__host__ __device__ __forceinline__ cdf crecip(cdf b) {
+  const dfl d = b.x * b.x + b.y * b.y;
+  if (!(d.hi > 1e-30f && d.hi < 1e30f)) return cdiv(mkc(dfl(1.f), dfl(0.f)), b);
+  const dfl r = dfl(1.f) / d;
+  return mkc(b.x * r, -(b.y * r));
+}
 #ifdef __CUDACC__
 __device__ __forceinline__ float shfl_idx(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 __device__ __forceinline__ double shfl_idx(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }

@@ -1218,7 +1218,7 @@ __device__ __forceinline__ bool warp_inverse_rot(cx<R> (&a)[N], cx<R>* prow, int
     if (is_piv) prow_put(buf, a);
     __syncwarp();
     const cx<R> p = prow_pivot(buf);
-    const cx<R> ip = ok ? cdiv(cmk<R>((R)1, (R)0), p) : cmk<R>((R)0, (R)0);
+    const cx<R> ip = ok ? crecip(p) : cmk<R>((R)0, (R)0);
     if (is_piv) scale = ip;
     const cx<R> f = is_piv ? cmk<R>((R)0, (R)0) : -(ak * ip);
     if constexpr (sizeof(cx<R>) == 8) {

@@ -339,7 +339,11 @@ def test_lin_eliash_ritz_values_match_oracle(F, name, gap_sym):
     assert abs(got[0] - lamo) < 1e-8 * max(1.0, abs(lamo))
     stable = np.abs(ref[:n] - ref_p[:n]) < 1e-7
     assert stable.sum() >= 2
-    assert np.allclose(got[stable], ref[:n][stable], rtol=1e-6, atol=1e-9), (got, ref[:n])
+    # a stable value is one the oracle keeps to 1e-7 under the perturbation;
+    # the engine's own rounding (FFT order, GPU sums) is such a perturbation,
+    # so stable values agree to that threshold (the second Ritz value of the
+    # two-orbital case moves by up to 1e-8 under 1e-13 relative changes of G)
+    assert np.allclose(got[stable], ref[:n][stable], rtol=1e-6, atol=1e-7), (got, ref[:n], ref_p[:n])
     assert np.all(np.diff(got) <= 0)
 
 
