@@ -258,7 +258,32 @@ void build_pairs_soc(Pairs& p, Geom& g, const int64_t* olist, int Norb, int Nchi
 }
 
 // =============================================================== green ==
-__global__ void k_green0(double2* G, const double* eig, const double2* uni, double mu, double temp,
+// Band projectors C(k)_{ml,n} = U_mn(k) conj(U_ln(k)) at cf[((k No + l) No + m) No + n]
+// (element e = m + No l), used by G0 and the tail's tau reference; they do
+// not depend on the frequency or the imaginary time
+__global__ void k_band_proj(double2* cf, const double2* uni, int Nk, int No) {
+  const long long N = (long long)Nk * No * No * No;
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(idx % No);
+    const long long r = idx / No;
+    const int e = (int)(r % (No * No));
+    const int k = (int)(r / (No * No));
+    const int m = e % No, l = e / No;
+    const double2* U = uni + (long long)No * No * k;
+    cf[idx] = U[m + No * n] * conj(U[l + No * n]);
+  }
+}
+
+void band_projectors(double2* cf, const double2* uni, int Nk, int Norb) {
+  const long long N = (long long)Nk * Norb * Norb * Norb;
+  k_band_proj<<<grid_1d(N, 256, 65536), 256, 0, ctx().stream>>>(cf, uni, Nk, Norb);
+  count_launch("band_proj");
+}
+
+// G0_ml(k, i w_j) = sum_n C(k)_{ml,n} / (i w_j + mu - e_n(k)) (fself.f90:1-41),
+// one reciprocal per band and (k, j)
+__global__ void k_green0(double2* G, const double* eig, const double2* cf, double mu, double temp,
                          int Nk, int Nw, int No) {
   const long long K = (long long)Nk * Nw;
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
@@ -266,12 +291,13 @@ __global__ void k_green0(double2* G, const double* eig, const double2* uni, doub
     const int k = (int)(idx % Nk), j = (int)(idx / Nk);
     const double2 iw = mkc(mu, (2.0 * j + 1.0) * kPi * temp);
     double2 den[kMaxOrb];
-    for (int n = 0; n < No; ++n) den[n] = cdiv(mkc(1.0, 0.0), iw - mkc(eig[n + (long long)No * k], 0.0));
-    const double2* U = uni + (long long)No * No * k;
+    for (int n = 0; n < No; ++n) den[n] = crecip(iw - mkc(eig[n + (long long)No * k], 0.0));
+    const double2* C = cf + (long long)No * No * No * k;
     for (int l = 0; l < No; ++l)
       for (int m = 0; m < No; ++m) {
+        const double2* c = C + (long long)(m + No * l) * No;
         double2 acc = mkc(0.0, 0.0);
-        for (int n = 0; n < No; ++n) acc += U[m + No * n] * conj(U[l + No * n]) * den[n];
+        for (int n = 0; n < No; ++n) acc += c[n] * den[n];
         G[fidx(k, j, m, l, Nk, Nw, No)] = acc;
       }
   }
@@ -280,7 +306,9 @@ __global__ void k_green0(double2* G, const double* eig, const double2* uni, doub
 void green0(double2* G, const double* eig, const double2* uni, double mu, double temp, int Nk, int Nw,
             int Norb) {
   const long long K = (long long)Nk * Nw;
-  k_green0<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, eig, uni, mu, temp, Nk, Nw, Norb);
+  DBuf<double2> cf((size_t)Nk * Norb * Norb * Norb);
+  band_projectors(cf.p, uni, Nk, Norb);
+  k_green0<<<grid_1d(K, 128, 65536), 128, 0, ctx().stream>>>(G, eig, cf.p, mu, temp, Nk, Nw, Norb);
   count_launch("green0");
 }
 
@@ -340,6 +368,33 @@ bool invert_blocks(double2* G, long long nmat, int Norb, long long stride_mat, l
   return fetch_err() == 0;
 }
 
+// ====================================================== mesh x time grids ==
+// Kernels over a padded array of P = Nkall x M points (mesh point r fastest)
+// give each thread one mesh point r and up to kTauChunk consecutive slices t
+// (blocks of 256 threads: the mesh in blocks, then the slices in chunks).
+// The mesh index is split once per thread in 32-bit arithmetic, and the
+// per-point tables (grid_irr, grid_flag, reversed indices) are read once;
+// a grid-stride loop over P would split every element's index with 64-bit
+// divisions, which on GB300 cost far more than the element's own loads.
+constexpr int kTauChunk = 8;
+
+dim3 mesh_tau_grid(long long Nkall, long long M, unsigned ny) {
+  const long long nrb = (Nkall + 255) / 256, nch = (M + kTauChunk - 1) / kTauChunk;
+  return dim3((unsigned)(nrb * nch), ny);
+}
+
+struct MeshTau {
+  int r, t0, t1;
+};
+__device__ __forceinline__ bool mesh_tau(long long Nkall, long long M, MeshTau& q) {
+  const unsigned nrb = (unsigned)((Nkall + 255) / 256);
+  const unsigned rb = blockIdx.x % nrb, tc = blockIdx.x / nrb;
+  q.r = (int)(rb * 256u + threadIdx.x);
+  q.t0 = (int)tc * kTauChunk;
+  q.t1 = min((int)M, q.t0 + kTauChunk);
+  return q.r < Nkall;
+}
+
 // ========================================================== padded grids ==
 // Full-grid padded Green function of element e=(a,b) (fchi.f90:563-583):
 // slot n<Nw: G_ab(k,iw_n) (at -k: G_ba), slot 2Nw-1-j: conj G_ba(k,iw_j)
@@ -353,11 +408,12 @@ __global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, cons
   const int ia = sm.inv[a], ib = sm.inv[b];
   const double sg = (double)(sm.sgn[a] * sm.sgn[b]);
   cx<R>* o = out + (long long)blockIdx.y * P;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long gi = idx % Nkall;
-    const int n = (int)(idx / Nkall);
-    const int k = grid_irr[gi], fl = grid_flag[gi];
+  MeshTau q;
+  if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
+  const long long gi = q.r;
+  const int k = grid_irr[gi], fl = grid_flag[gi];
+  for (int n = q.t0; n < q.t1; ++n) {
+    const long long idx = gi + Nkall * n;
     double2 v;
     if (n < Nw) {
       v = fl ? sg * G[fidx(k, n, ib, ia, Nk, Nw, No)] : G[fidx(k, n, a, b, Nk, Nw, No)];
@@ -385,11 +441,12 @@ __global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, 
   if (threadIdx.x == 0) s_stat = (R)t.stat;
   __syncthreads();
   const R stat = s_stat;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long gi = idx % Nkall;
-    const int n = (int)(idx / Nkall);
-    const int k = grid_irr[gi], fl = grid_flag[gi];
+  MeshTau q;
+  if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
+  const long long gi = q.r;
+  const int k = grid_irr[gi], fl = grid_flag[gi];
+  for (int n = q.t0; n < q.t1; ++n) {
+    const long long idx = gi + Nkall * n;
     cx<R> v;
     if (n < Nw) {
       v = fl ? V[fidx(k, n, t.l, t.m, Nk, Nw, Nchi)] : V[fidx(k, n, t.m, t.l, Nk, Nw, Nchi)];
@@ -413,11 +470,12 @@ __global__ void k_pad_anomalous(cx<R>* out, const double2* F, const int* grid_ir
   const int a = e % No, b = e / No;
   const double pp = prt[a] * prt[b];
   cx<R>* o = out + (long long)e * P;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long gi = idx % Nkall;
-    const int n = (int)(idx / Nkall);
-    const int k = grid_irr[gi], fl = grid_flag[gi];
+  MeshTau q;
+  if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
+  const long long gi = q.r;
+  const int k = grid_irr[gi], fl = grid_flag[gi];
+  for (int n = q.t0; n < q.t1; ++n) {
+    const long long idx = gi + Nkall * n;
     double2 v;
     if (n < Nw) {
       v = F[fidx(k, n, a, b, Nk, Nw, No)];
@@ -438,8 +496,7 @@ void pad_green_all(const Geom& g, const double2* G, cx<R>* out) {
   for (int e = 0; e < No2; ++e) h[e] = e;
   DBuf<int> d(No2);
   d.upload(h.data(), No2);
-  dim3 grid(grid_1d(g.P, 256, 4096), No2);
-  k_pad_green<R><<<grid, 256, 0, ctx().stream>>>(out, G, d.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk,
+  k_pad_green<R><<<mesh_tau_grid(g.Nkall, g.M, No2), 256, 0, ctx().stream>>>(out, G, d.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk,
                                                   g.Nw, g.Norb, g.P, g.spin);
   count_launch("pad_green");
 }
@@ -468,14 +525,15 @@ __global__ void k_chi0_product(cx<R>* out, const cx<R>* F, const cx<R>* F0, cons
   const cx<R>* a13 = F + (long long)pr.e13 * P;
   const cx<R>* b42 = F + (long long)pr.e42 * P;
   cx<R>* o = out + (long long)blockIdx.y * P;
-  const long long Nxy = (long long)Nx * Ny, Nkall = Nxy * Nz;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long r = idx % Nkall;
-    const int t = (int)(idx / Nkall);
-    const int x = (int)(r % Nx), y = (int)((r / Nx) % Ny), z = (int)(r / Nxy);
-    const long long rr = rx[x] + Nx * (ry[y] + (long long)Ny * rz[z]);
-    const long long ir = rr + Nkall * rt[t];
+  const int Nxy = Nx * Ny, Nkall = Nxy * Nz;
+  MeshTau q;
+  if (!mesh_tau(Nkall, M, q)) return;
+  const int r = q.r;
+  const int x = r % Nx, y = (r / Nx) % Ny, z = r / Nxy;
+  const long long rr = rx[x] + (long long)Nx * (ry[y] + (long long)Ny * rz[z]);
+  for (int t = q.t0; t < q.t1; ++t) {
+    const long long idx = r + (long long)Nkall * t;
+    const long long ir = rr + (long long)Nkall * rt[t];
     cx<R> v = -(a13[idx] * b42[ir]);
     if (F0) {
       // The reference conjugates a self-partner pair after each of its three
@@ -508,11 +566,12 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
   }
   __syncthreads();
   const cx<R> J = sJ[0], dJ = sJ[1];
-  const long long K = (long long)Nk * Nw;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
-    cx<R> v = t[irr_grid[k] + Nkall * j];
+  MeshTau q;  // here: one irreducible k, a chunk of frequencies j
+  if (!mesh_tau(Nk, Nw, q)) return;
+  const int k = q.r;
+  const long long gk = irr_grid[k];
+  for (int j = q.t0; j < q.t1; ++j) {
+    cx<R> v = t[gk + Nkall * j];
     if (sawc) v += J * sawc[j];
     if (pr.self) v = pr.pneg ? -conj(v) : conj(v);
     if (abs_below(v.x, kThresh)) v.x = 0;
@@ -521,7 +580,7 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
     if (!pr.self) chi[fidx(k, j, pr.m2, pr.l2, Nk, Nw, Nchi)] = pr.pneg ? -conj(v) : conj(v);
     if (pr.has_d) {
       const long long M = 2LL * Nw;
-      cx<R> d = conj(t[irr_grid[k] + Nkall * ((M - j) % M)]);
+      cx<R> d = conj(t[gk + Nkall * ((M - j) % M)]);
       if (sawc) d += dJ * sawc[j];
       if (abs_below(d.x, kThresh)) d.x = 0;
       if (abs_below(d.y, kThresh)) d.y = 0;
@@ -533,7 +592,8 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
 
 // tau kernels of the analytic reference bubble (fchi.f90:703-729), laid out
 // [(s*Norb + n)*Nk + k]
-__global__ void k_gpm(double* gp, double* gm, double* ff, const double* eig, double mu, double temp,
+template <typename T>
+__global__ void k_gpm(T* gp, T* gm, double* ff, const double* eig, double mu, double temp,
                       int Nk, int No, int M) {
   const long long N = (long long)Nk * No * M;
   const double beta = 1.0 / temp, dtau = beta / M;
@@ -556,31 +616,35 @@ __global__ void k_gpm(double* gp, double* gm, double* ff, const double* eig, dou
       q = exp(xi * tau) / d;
       if (s == 0) ff[n + (long long)No * k] = 1.0 / d;
     }
-    gp[idx] = p;
-    gm[idx] = q;
+    gp[idx] = (T)p;
+    gm[idx] = (T)q;
   }
 }
 
-// A_ab(g,s) = sum_n U_an U*_bn gp (conjugated coefficient at -k), same for B with gm
-template <typename R>
-__global__ void k_ref_tau(cx<R>* A, cx<R>* B, const double* gp, const double* gm, const double2* uni,
+// A_ab(g,s) = sum_n U_an U*_bn gp (conjugated at -k), same for B with gm, from
+// the band projectors; in FP32 for an FP32 chi0, in FP64 otherwise (T)
+template <typename R, typename T>
+__global__ void k_ref_tau(cx<R>* A, cx<R>* B, const T* gp, const T* gm, const cx<T>* cf,
                           const int* grid_irr, const int* grid_flag, long long Nkall, int Nk, int No,
                           int M, long long P) {
   const int e = blockIdx.y;
-  const int a = e % No, b = e / No;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long gi = idx % Nkall;
-    const int s = (int)(idx / Nkall);
-    const int k = grid_irr[gi], fl = grid_flag[gi];
-    const double2* U = uni + (long long)No * No * k;
-    double2 sa = mkc(0.0, 0.0), sb = mkc(0.0, 0.0);
+  MeshTau q;
+  if (!mesh_tau(Nkall, M, q)) return;
+  const long long gi = q.r;
+  const int k = grid_irr[gi], fl = grid_flag[gi];
+  const cx<T>* c = cf + ((long long)k * No * No + e) * No;
+  for (int s = q.t0; s < q.t1; ++s) {
+    const long long idx = gi + Nkall * s;
+    cx<T> sa = cmk<T>((T)0, (T)0), sb = cmk<T>((T)0, (T)0);
     for (int n = 0; n < No; ++n) {
-      double2 c = U[a + No * n] * conj(U[b + No * n]);
-      if (fl) c = conj(c);
       const long long gidx = ((long long)s * No + n) * Nk + k;
-      sa += gp[gidx] * c;
-      sb += gm[gidx] * c;
+      const cx<T> cn = c[n];
+      sa += gp[gidx] * cn;
+      sb += gm[gidx] * cn;
+    }
+    if (fl) {
+      sa = conj(sa);
+      sb = conj(sb);
     }
     A[(long long)e * P + idx] = cmk<R>((R)sa.x, (R)sa.y);
     B[(long long)e * P + idx] = cmk<R>((R)sb.x, (R)sb.y);
@@ -684,15 +748,30 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
     pad_green_all<R>(g, G0.p, F0.p);
     G0.release();
     fft.forward<R>(F0.p, No2, st);
-    DBuf<double> gp((size_t)g.Nk * g.Norb * g.M), gm((size_t)g.Nk * g.Norb * g.M), ff((size_t)g.Nk * g.Norb);
-    k_gpm<<<grid_1d((long long)g.Nk * g.Norb * g.M, 256, 65536), 256, 0, st>>>(
+    // the tau reference in FP32 for an FP32 chi0 (its rounding is below the
+    // FP32 transforms'), in FP64 for the wider types
+    using T = typename std::conditional<std::is_same<R, float>::value, float, double>::type;
+    DBuf<T> gp((size_t)g.Nk * g.Norb * g.M), gm((size_t)g.Nk * g.Norb * g.M);
+    DBuf<double> ff((size_t)g.Nk * g.Norb);
+    k_gpm<T><<<grid_1d((long long)g.Nk * g.Norb * g.M, 256, 65536), 256, 0, st>>>(
         gp.p, gm.p, ff.p, tail->eig, tail->mu, temp, g.Nk, g.Norb, (int)g.M);
     count_launch("gpm");
+    const size_t ncf = (size_t)g.Nk * g.Norb * No2;
+    DBuf<double2> cf64(ncf);
+    band_projectors(cf64.p, tail->uni, g.Nk, g.Norb);
+    DBuf<cx<float>> cf32;
+    const cx<T>* cf = nullptr;
+    if constexpr (std::is_same<T, float>::value) {
+      cf32.alloc(ncf);
+      convert<float, double>(cf32.p, cf64.p, (long long)ncf);
+      cf = cf32.p;
+    } else {
+      cf = cf64.p;
+    }
     A.alloc((size_t)No2 * g.P);
     B.alloc((size_t)No2 * g.P);
-    dim3 gr(grid_1d(g.P, 256, 4096), No2);
-    k_ref_tau<R><<<gr, 256, 0, st>>>(A.p, B.p, gp.p, gm.p, tail->uni, g.grid_irr.p, g.grid_flag.p, g.Nkall,
-                                      g.Nk, g.Norb, (int)g.M, g.P);
+    k_ref_tau<R, T><<<mesh_tau_grid(g.Nkall, g.M, No2), 256, 0, st>>>(A.p, B.p, gp.p, gm.p, cf, g.grid_irr.p, g.grid_flag.p, g.Nkall,
+                                         g.Nk, g.Norb, (int)g.M, g.P);
     count_launch("ref_tau");
     fft.forward_space<R>(A.p, No2, st);
     fft.forward_space<R>(B.p, No2, st);
@@ -753,15 +832,13 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
   const double sr = 1.0 / (temp * (double)g.Nkall) / (double)g.P;
   for (long long c0 = 0; c0 < (long long)hp.size(); c0 += ch) {
     const int nc = (int)std::min<long long>(ch, (long long)hp.size() - c0);
-    dim3 gr(grid_1d(g.P, 256, 4096), nc);
-    k_chi0_product<R><<<gr, 256, 0, st>>>(T.p, F.p, tail ? F0.p : nullptr, tail ? A.p : nullptr,
+    k_chi0_product<R><<<mesh_tau_grid(g.Nkall, g.M, nc), 256, 0, st>>>(T.p, F.p, tail ? F0.p : nullptr, tail ? A.p : nullptr,
                                           tail ? B.p : nullptr, dp.p + c0, g.P, g.Nx, g.Ny, g.Nz, (int)g.M,
                                           fft.d_rev(0), fft.d_rev(1), fft.d_rev(2), fft.d_rev(3),
                                           fft.d_logical(3), (R)sc, (R)sr);
     count_launch("chi0_product");
     fft.backward<R>(T.p, nc, st);
-    dim3 gs(grid_1d(g.K, 256, 4096), nc);
-    k_chi0_scatter<R><<<gs, 256, 0, st>>>(chi, T.p, dp.p + c0, g.irr_grid.p, tail ? sawc.p : nullptr,
+    k_chi0_scatter<R><<<mesh_tau_grid(g.Nk, g.Nw, nc), 256, 0, st>>>(chi, T.p, dp.p + c0, g.irr_grid.p, tail ? sawc.p : nullptr,
                                           g.Nkall, g.Nk, g.Nw, g.Nchi, g.P);
     count_launch("chi0_scatter");
   }
@@ -1923,12 +2000,12 @@ void chi0_ff(const Geom& g, const Pairs& p, const double2* F, const std::vector<
                                                                       g.Nkall, g.Nk, g.Nw, g.Norb, g.P);
     count_launch("pad_ff");
     fft.forward<R>(A.p, 2 * nc, st);
-    k_chi0_product<R><<<dim3(grid_1d(g.P, 256, 4096), nc), 256, 0, st>>>(
+    k_chi0_product<R><<<mesh_tau_grid(g.Nkall, g.M, nc), 256, 0, st>>>(
         T.p, A.p, nullptr, nullptr, nullptr, dc.p, g.P, g.Nx, g.Ny, g.Nz, (int)g.M, fft.d_rev(0), fft.d_rev(1),
         fft.d_rev(2), fft.d_rev(3), fft.d_logical(3), (R)sc, (R)0);
     count_launch("chi0_product");
     fft.backward<R>(T.p, nc, st);
-    k_chi0_scatter<R><<<dim3(grid_1d(g.K, 256, 4096), nc), 256, 0, st>>>(chi, T.p, dc.p, g.irr_grid.p, nullptr,
+    k_chi0_scatter<R><<<mesh_tau_grid(g.Nk, g.Nw, nc), 256, 0, st>>>(chi, T.p, dc.p, g.irr_grid.p, nullptr,
                                                                         g.Nkall, g.Nk, g.Nw, g.Nchi, g.P);
     count_launch("chi0_scatter");
     sync();
@@ -2224,11 +2301,13 @@ template <typename R> constexpr int elem_kind() { return sizeof(cx<R>) == 8 ? 0 
 
 __global__ void k_scatter_out(double2* dst, const void* tmp, int kind, const int* irr_grid, long long Nkall,
                               int Nk, int Nw, double scale, int do_thresh) {
-  const long long K = (long long)Nk * Nw;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(idx % Nk), j = (int)(idx / Nk);
-    const long long src = irr_grid[k] + Nkall * j;
+  MeshTau q;  // one irreducible k, a chunk of frequencies j
+  if (!mesh_tau(Nk, Nw, q)) return;
+  const int k = q.r;
+  const long long gk = irr_grid[k];
+  for (int j = q.t0; j < q.t1; ++j) {
+    const long long idx = k + (long long)Nk * j;
+    const long long src = gk + Nkall * j;
     double2 v = kind == 1 ? ((const double2*)tmp)[src]
                           : (kind == 0 ? ccast<double>(((const float2*)tmp)[src]) : ccast<double>(((const cdf*)tmp)[src]));
     v = scale * v;
@@ -2274,11 +2353,13 @@ __global__ void k_contract_mirror(cx<R>* T0, cx<R>* T1, const cx<R>* W, const cx
   if (threadIdx.x == 0) s_nk = (R)(double)Nkall;
   __syncthreads();
   const R nk = s_nk;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < P;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const long long s = idx % Nkall, pt = idx / Nkall;
-    const int px = (int)(s % Nx), py = (int)((s / Nx) % Ny), pz = (int)(s / ((long long)Nx * Ny));
-    const long long s_m = rev_x[px] + (long long)Nx * (rev_y[py] + (long long)Ny * rev_z[pz]);
+  MeshTau q;
+  if (!mesh_tau(Nkall, P / Nkall, q)) return;
+  const int s = q.r;
+  const int px = s % Nx, py = (s / Nx) % Ny, pz = s / (Nx * Ny);
+  const long long s_m = rev_x[px] + (long long)Nx * (rev_y[py] + (long long)Ny * rev_z[pz]);
+  for (int pt = q.t0; pt < q.t1; ++pt) {
+    const long long idx = s + Nkall * pt;
     const long long idx_m = s_m + Nkall * pt;
     const R sgn = (log_t[pt] & 1) ? (R)-1 : (R)1;
     cx<R> a0 = cmk<R>(0, 0), a1 = cmk<R>(0, 0);
@@ -2353,8 +2434,7 @@ void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, cons
     for (int t = 0; t < nt; ++t) ht[t] = BosonTerm{gr.terms[t].m, gr.terms[t].l, stat(gr.terms[t].m, gr.terms[t].l)};
     dterms.upload(ht.data(), nt);
     mterms.upload(gr.terms.data(), nt);
-    dim3 grd(grid_1d(g.P, 256, 4096), nt);
-    k_pad_boson<R><<<grd, 256, 0, st>>>(W.p, V, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, Nchi,
+    k_pad_boson<R><<<mesh_tau_grid(g.Nkall, g.M, nt), 256, 0, st>>>(W.p, V, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, Nchi,
                                          g.P);
     count_launch("pad_boson");
     fft.forward<R>(W.p, nt, st);
@@ -2363,16 +2443,16 @@ void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, cons
                                               Nchi);
     count_launch("mirror_delta0");
     fft3.forward<R>(Dm.p, nt, st);
-    k_contract_mirror<R><<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(
+    k_contract_mirror<R><<<mesh_tau_grid(g.Nkall, g.M, 1), 256, 0, st>>>(
         T.p, two ? T.p + g.P : nullptr, W.p, F.p, Dm.p, mterms.p, nt, g.P, g.Nkall, g.Nx, g.Ny, fft.d_rev(0),
         fft.d_rev(1), fft.d_rev(2), fft.d_logical(3));
     count_launch("contract_mirror");
     fft.backward<R>(T.p, two ? 2 : 1, st);
-    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.e * g.K, T.p, elem_kind<R>(),
+    k_scatter_out<<<mesh_tau_grid(g.Nk, g.Nw, 1), 256, 0, st>>>(sig + (size_t)gr.e * g.K, T.p, elem_kind<R>(),
                                                              g.irr_grid.p, g.Nkall, g.Nk, g.Nw, scale, 1);
     count_launch("scatter_sigma");
     if (two) {
-      k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(sig + (size_t)gr.et * g.K, T.p + g.P, elem_kind<R>(),
+      k_scatter_out<<<mesh_tau_grid(g.Nk, g.Nw, 1), 256, 0, st>>>(sig + (size_t)gr.et * g.K, T.p + g.P, elem_kind<R>(),
                                                                g.irr_grid.p, g.Nkall, g.Nk, g.Nw, scale, 1);
       count_launch("scatter_sigma");
     }
@@ -2645,7 +2725,8 @@ __global__ void k_filling_cp(double2* part, const double2* cp, const double* eig
       dp = dp * z + p;
       p = p * z + cp[d + (long long)N * idx];
     }
-    double s = cdiv(dp, p).x;
+    const double2 ip = crecip(p);  // Re(p'/p) with one division
+    double s = dp.x * ip.x - dp.y * ip.y;
 #pragma unroll
     for (int n = 0; n < N; ++n) {
       const double x = mu - eig[n + (long long)N * k];
@@ -2753,8 +2834,7 @@ void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, c
   const int No2 = g.Norb * g.Norb;
   const double sgn = singlet ? 1.0 : -1.0, dprt = singlet ? 1.0 : -1.0;
   DBuf<cx<R>> FF((size_t)No2 * g.P);
-  dim3 gp(grid_1d(g.P, 256, 4096), No2);
-  k_pad_anomalous<R><<<gp, 256, 0, st>>>(FF.p, F, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, g.Norb, g.P,
+  k_pad_anomalous<R><<<mesh_tau_grid(g.Nkall, g.M, No2), 256, 0, st>>>(FF.p, F, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, g.Norb, g.P,
                                           prt, sgn, dprt);
   count_launch("pad_anomalous");
   fft.forward<R>(FF.p, No2, st);
@@ -2793,8 +2873,7 @@ void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, c
         std::vector<int> hef;
         terms_of(e, ht, hef);
         dterms.upload(ht.data(), ht.size());
-        dim3 gr(grid_1d(g.P, 256, 4096), (unsigned)ht.size());
-        k_pad_boson<R><<<gr, 256, 0, st>>>(cache->W.p + off * g.P, Vd, dterms.p, g.grid_irr.p, g.grid_flag.p,
+        k_pad_boson<R><<<mesh_tau_grid(g.Nkall, g.M, (unsigned)ht.size()), 256, 0, st>>>(cache->W.p + off * g.P, Vd, dterms.p, g.grid_irr.p, g.grid_flag.p,
                                             g.Nkall, g.Nk, g.Nw, g.Nchi, g.P);
         count_launch("pad_vdelta");
         fft.forward<R>(cache->W.p + off * g.P, (int)ht.size(), st);
@@ -2819,8 +2898,7 @@ void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, c
       Wp = cache->W.p + cache->offset[e] * g.P;
     } else {
       dterms.upload(ht.data(), nt);
-      dim3 gr(grid_1d(g.P, 256, 4096), nt);
-      k_pad_boson<R><<<gr, 256, 0, st>>>(W.p, Vd, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw,
+      k_pad_boson<R><<<mesh_tau_grid(g.Nkall, g.M, nt), 256, 0, st>>>(W.p, Vd, dterms.p, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw,
                                           g.Nchi, g.P);
       count_launch("pad_vdelta");
       fft.forward<R>(W.p, nt, st);
@@ -2829,7 +2907,7 @@ void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, c
     k_contract<R><<<grid_1d(g.P, 256, 65536), 256, 0, st>>>(T.p, Wp, FF.p, def.p, nt, g.P);
     count_launch("contract");
     fft.backward<R>(T.p, 1, st);
-    k_scatter_out<<<grid_1d(g.K, 256, 65536), 256, 0, st>>>(out + (size_t)e * g.K, T.p, elem_kind<R>(), g.irr_grid.p,
+    k_scatter_out<<<mesh_tau_grid(g.Nk, g.Nw, 1), 256, 0, st>>>(out + (size_t)e * g.K, T.p, elem_kind<R>(), g.irr_grid.p,
                                                              g.Nkall, g.Nk, g.Nw, scale, 0);
     count_launch("scatter_delta");
     sync();
