@@ -378,21 +378,31 @@ bool invert_blocks(double2* G, long long nmat, int Norb, long long stride_mat, l
 // divisions, which on GB300 cost far more than the element's own loads.
 constexpr int kTauChunk = 8;
 
-dim3 mesh_tau_grid(long long Nkall, long long M, unsigned ny) {
-  const long long nrb = (Nkall + 255) / 256, nch = (M + kTauChunk - 1) / kTauChunk;
+dim3 mesh_tau_grid(long long Nkall, long long M, unsigned ny, int chunk = kTauChunk) {
+  const long long nrb = (Nkall + 255) / 256, nch = (M + chunk - 1) / chunk;
   return dim3((unsigned)(nrb * nch), ny);
 }
 
 struct MeshTau {
   int r, t0, t1;
 };
-__device__ __forceinline__ bool mesh_tau(long long Nkall, long long M, MeshTau& q) {
+__device__ __forceinline__ bool mesh_tau(long long Nkall, long long M, MeshTau& q, int chunk = kTauChunk) {
   const unsigned nrb = (unsigned)((Nkall + 255) / 256);
   const unsigned rb = blockIdx.x % nrb, tc = blockIdx.x / nrb;
   q.r = (int)(rb * 256u + threadIdx.x);
-  q.t0 = (int)tc * kTauChunk;
-  q.t1 = min((int)M, q.t0 + kTauChunk);
+  q.t0 = (int)tc * chunk;
+  q.t1 = min((int)M, q.t0 + chunk);
   return q.r < Nkall;
+}
+// body(t) for the thread's slices; a full chunk is unrolled so that its
+// slices' loads are in flight together
+template <class Body> __device__ __forceinline__ void for_tau(const MeshTau& q, Body&& body) {
+  if (q.t1 - q.t0 == kTauChunk) {
+#pragma unroll
+    for (int u = 0; u < kTauChunk; ++u) body(q.t0 + u);
+  } else {
+    for (int t = q.t0; t < q.t1; ++t) body(t);
+  }
 }
 
 // ========================================================== padded grids ==
@@ -412,7 +422,7 @@ __global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, cons
   if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
   const long long gi = q.r;
   const int k = grid_irr[gi], fl = grid_flag[gi];
-  for (int n = q.t0; n < q.t1; ++n) {
+  for_tau(q, [&](int n) {
     const long long idx = gi + Nkall * n;
     double2 v;
     if (n < Nw) {
@@ -422,7 +432,7 @@ __global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, cons
       v = fl ? sg * conj(G[fidx(k, j, ia, ib, Nk, Nw, No)]) : conj(G[fidx(k, j, b, a, Nk, Nw, No)]);
     }
     o[idx] = cmk<R>((R)v.x, (R)v.y);
-  }
+  });
 }
 
 // Padded bosonic array of pair (m,l) (fself.f90:201-223, feliash.f90:538-560):
@@ -445,7 +455,7 @@ __global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, 
   if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
   const long long gi = q.r;
   const int k = grid_irr[gi], fl = grid_flag[gi];
-  for (int n = q.t0; n < q.t1; ++n) {
+  for_tau(q, [&](int n) {
     const long long idx = gi + Nkall * n;
     cx<R> v;
     if (n < Nw) {
@@ -457,7 +467,7 @@ __global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, 
       v = conj(fl ? V[fidx(k, j, t.m, t.l, Nk, Nw, Nchi)] : V[fidx(k, j, t.l, t.m, Nk, Nw, Nchi)]);
     }
     o[idx] = v;
-  }
+  });
 }
 
 // Padded anomalous function of element (a,b) with the parity rules of
@@ -531,7 +541,7 @@ __global__ void k_chi0_product(cx<R>* out, const cx<R>* F, const cx<R>* F0, cons
   const int r = q.r;
   const int x = r % Nx, y = (r / Nx) % Ny, z = r / Nxy;
   const long long rr = rx[x] + (long long)Nx * (ry[y] + (long long)Ny * rz[z]);
-  for (int t = q.t0; t < q.t1; ++t) {
+  for_tau(q, [&](int t) {
     const long long idx = r + (long long)Nkall * t;
     const long long ir = rr + (long long)Nkall * rt[t];
     cx<R> v = -(a13[idx] * b42[ir]);
@@ -549,7 +559,7 @@ __global__ void k_chi0_product(cx<R>* out, const cx<R>* F, const cx<R>* F0, cons
       v -= sr * (A[(long long)pr.e13 * P + r + Nkall * s] * B[(long long)pr.e42 * P + rr + Nkall * s]);
     }
     o[idx] = v;
-  }
+  });
 }
 
 template <typename R>
@@ -595,15 +605,29 @@ __global__ void k_chi0_scatter(cx<R>* chi, const cx<R>* tmp, const ChiDev* pairs
 template <typename T>
 __global__ void k_gpm(T* gp, T* gm, double* ff, const double* eig, double mu, double temp,
                       int Nk, int No, int M) {
-  const long long N = (long long)Nk * No * M;
   const double beta = 1.0 / temp, dtau = beta / M;
-  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < N;
-       idx += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(idx % Nk);
-    const int n = (int)((idx / Nk) % No);
-    const int s = (int)(idx / ((long long)Nk * No));
-    const double xi = eig[n + (long long)No * k] - mu;
+  const int Nkn = Nk * No;
+  MeshTau mt;  // here: one (n, k) pair, a chunk of tau slices s
+  if (!mesh_tau(Nkn, M, mt)) return;
+  const int k = mt.r % Nk, n = mt.r / Nk;
+  const double xi = eig[n + (long long)No * k] - mu;
+  for (int s = mt.t0; s < mt.t1; ++s) {
+    const long long idx = mt.r + (long long)Nkn * s;
     const double tau = s * dtau;
+    if constexpr (std::is_same<T, float>::value) {
+      // FP32 kernels for an FP32 chi0: the exponents in FP64, the
+      // exponentials in FP32 (their FP64 forms run at 1/64 of the rate)
+      const float e = expf((float)(-beta * fabs(xi)));
+      const float rd = 1.0f / (1.0f + e);
+      const float lo = expf((float)(-fabs(xi) * tau)), hi = expf((float)(-fabs(xi) * (beta - tau)));
+      gp[idx] = xi >= 0 ? -lo * rd : -hi * rd;
+      gm[idx] = xi >= 0 ? hi * rd : lo * rd;
+      if (s == 0) {
+        const double d = 1.0 + exp(-beta * fabs(xi));
+        ff[n + (long long)No * k] = xi >= 0 ? exp(-beta * xi) / d : 1.0 / d;
+      }
+      continue;
+    }
     double p, q;
     if (xi >= 0) {
       const double d = 1.0 + exp(-beta * xi);
@@ -753,7 +777,7 @@ void chi0(const Geom& g, const Pairs& p, const double2* G, double temp, const Ta
     using T = typename std::conditional<std::is_same<R, float>::value, float, double>::type;
     DBuf<T> gp((size_t)g.Nk * g.Norb * g.M), gm((size_t)g.Nk * g.Norb * g.M);
     DBuf<double> ff((size_t)g.Nk * g.Norb);
-    k_gpm<T><<<grid_1d((long long)g.Nk * g.Norb * g.M, 256, 65536), 256, 0, st>>>(
+    k_gpm<T><<<mesh_tau_grid((long long)g.Nk * g.Norb, g.M, 1), 256, 0, st>>>(
         gp.p, gm.p, ff.p, tail->eig, tail->mu, temp, g.Nk, g.Norb, (int)g.M);
     count_launch("gpm");
     const size_t ncf = (size_t)g.Nk * g.Norb * No2;
@@ -2353,8 +2377,8 @@ __global__ void k_contract_mirror(cx<R>* T0, cx<R>* T1, const cx<R>* W, const cx
   if (threadIdx.x == 0) s_nk = (R)(double)Nkall;
   __syncthreads();
   const R nk = s_nk;
-  MeshTau q;
-  if (!mesh_tau(Nkall, P / Nkall, q)) return;
+  MeshTau q;  // one slice per thread: the term loop below already streams many arrays
+  if (!mesh_tau(Nkall, P / Nkall, q, 1)) return;
   const int s = q.r;
   const int px = s % Nx, py = (s / Nx) % Ny, pz = s / (Nx * Ny);
   const long long s_m = rev_x[px] + (long long)Nx * (rev_y[py] + (long long)Ny * rev_z[pz]);
@@ -2443,7 +2467,7 @@ void sigma(const Geom& g, const Pairs& p, const double2* G, const cx<R>* V, cons
                                               Nchi);
     count_launch("mirror_delta0");
     fft3.forward<R>(Dm.p, nt, st);
-    k_contract_mirror<R><<<mesh_tau_grid(g.Nkall, g.M, 1), 256, 0, st>>>(
+    k_contract_mirror<R><<<mesh_tau_grid(g.Nkall, g.M, 1, 1), 256, 0, st>>>(
         T.p, two ? T.p + g.P : nullptr, W.p, F.p, Dm.p, mterms.p, nt, g.P, g.Nkall, g.Nx, g.Ny, fft.d_rev(0),
         fft.d_rev(1), fft.d_rev(2), fft.d_logical(3));
     count_launch("contract_mirror");
