@@ -2751,11 +2751,23 @@ __global__ void k_filling_cp(double2* part, const double2* cp, const double* eig
     }
     const double2 ip = crecip(p);  // Re(p'/p) with one division
     double s = dp.x * ip.x - dp.y * ip.y;
+    // sum_n x_n / (x_n^2 + w^2) with one division: 1/d_n = (prod_{m != n} d_m) / prod_m d_m
+    // from prefix and suffix products (each d_n >= w^2 >= (pi T)^2, at most a few hundred)
+    double x[N], d[N], pre[N + 1];
+    pre[0] = 1.0;
 #pragma unroll
     for (int n = 0; n < N; ++n) {
-      const double x = mu - eig[n + (long long)N * k];
-      s -= x / (x * x + w * w);
-      if (j == 0) acc.y += 0.5 * (1.0 - tanh(-0.5 * x / temp));
+      x[n] = mu - eig[n + (long long)N * k];
+      d[n] = fma(x[n], x[n], w * w);
+      pre[n + 1] = pre[n] * d[n];
+    }
+    const double rall = 1.0 / pre[N];
+    double suf = 1.0;
+#pragma unroll
+    for (int n = N - 1; n >= 0; --n) {
+      s -= x[n] * (pre[n] * suf * rall);
+      suf *= d[n];
+      if (j == 0) acc.y += 0.5 * (1.0 - tanh(-0.5 * x[n] / temp));
     }
     acc.x += s;
   }
