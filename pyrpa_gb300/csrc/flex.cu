@@ -394,16 +394,6 @@ __device__ __forceinline__ bool mesh_tau(long long Nkall, long long M, MeshTau& 
   q.t1 = min((int)M, q.t0 + chunk);
   return q.r < Nkall;
 }
-// body(t) for the thread's slices; a full chunk is unrolled so that its
-// slices' loads are in flight together
-template <class Body> __device__ __forceinline__ void for_tau(const MeshTau& q, Body&& body) {
-  if (q.t1 - q.t0 == kTauChunk) {
-#pragma unroll
-    for (int u = 0; u < kTauChunk; ++u) body(q.t0 + u);
-  } else {
-    for (int t = q.t0; t < q.t1; ++t) body(t);
-  }
-}
 
 // ========================================================== padded grids ==
 // Full-grid padded Green function of element e=(a,b) (fchi.f90:563-583):
@@ -422,7 +412,7 @@ __global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, cons
   if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
   const long long gi = q.r;
   const int k = grid_irr[gi], fl = grid_flag[gi];
-  for_tau(q, [&](int n) {
+  for (int n = q.t0; n < q.t1; ++n) {
     const long long idx = gi + Nkall * n;
     double2 v;
     if (n < Nw) {
@@ -432,7 +422,7 @@ __global__ void k_pad_green(cx<R>* out, const double2* G, const int* elems, cons
       v = fl ? sg * conj(G[fidx(k, j, ia, ib, Nk, Nw, No)]) : conj(G[fidx(k, j, b, a, Nk, Nw, No)]);
     }
     o[idx] = cmk<R>((R)v.x, (R)v.y);
-  });
+  }
 }
 
 // Padded bosonic array of pair (m,l) (fself.f90:201-223, feliash.f90:538-560):
@@ -455,7 +445,7 @@ __global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, 
   if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
   const long long gi = q.r;
   const int k = grid_irr[gi], fl = grid_flag[gi];
-  for_tau(q, [&](int n) {
+  for (int n = q.t0; n < q.t1; ++n) {
     const long long idx = gi + Nkall * n;
     cx<R> v;
     if (n < Nw) {
@@ -467,7 +457,7 @@ __global__ void k_pad_boson(cx<R>* out, const cx<R>* V, const BosonTerm* terms, 
       v = conj(fl ? V[fidx(k, j, t.m, t.l, Nk, Nw, Nchi)] : V[fidx(k, j, t.l, t.m, Nk, Nw, Nchi)]);
     }
     o[idx] = v;
-  });
+  }
 }
 
 // Padded anomalous function of element (a,b) with the parity rules of
@@ -541,7 +531,7 @@ __global__ void k_chi0_product(cx<R>* out, const cx<R>* F, const cx<R>* F0, cons
   const int r = q.r;
   const int x = r % Nx, y = (r / Nx) % Ny, z = r / Nxy;
   const long long rr = rx[x] + (long long)Nx * (ry[y] + (long long)Ny * rz[z]);
-  for_tau(q, [&](int t) {
+  for (int t = q.t0; t < q.t1; ++t) {
     const long long idx = r + (long long)Nkall * t;
     const long long ir = rr + (long long)Nkall * rt[t];
     cx<R> v = -(a13[idx] * b42[ir]);
@@ -559,7 +549,7 @@ __global__ void k_chi0_product(cx<R>* out, const cx<R>* F, const cx<R>* F0, cons
       v -= sr * (A[(long long)pr.e13 * P + r + Nkall * s] * B[(long long)pr.e42 * P + rr + Nkall * s]);
     }
     o[idx] = v;
-  });
+  }
 }
 
 template <typename R>
