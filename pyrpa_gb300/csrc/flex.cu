@@ -2310,6 +2310,25 @@ __global__ void k_contract(cx<R>* out, const cx<R>* W, const cx<R>* F, const int
   }
 }
 
+// All outputs of mkdelta in one launch, from the cached transforms: block x
+// is the output (fastest, so the outputs of one index tile run together
+// and share the F tiles in L2), blocks y stride over index tiles.  Output o
+// sums its terms tb[o] .. tb[o+1]-1 in the order k_contract does:
+// T_o = sum_t W_t F_{ef[t]}.
+template <typename R>
+__global__ void k_contract_all(cx<R>* out, const cx<R>* W, const cx<R>* F, const int* ef, const int* tb,
+                               long long P) {
+  const int o = blockIdx.x;
+  const int t0 = tb[o], t1 = tb[o + 1];
+  cx<R>* dst = out + (long long)o * P;
+  for (long long idx = (long long)blockIdx.y * blockDim.x + threadIdx.x; idx < P;
+       idx += (long long)gridDim.y * blockDim.x) {
+    cx<R> acc = cmk<R>(0, 0);
+    for (int t = t0; t < t1; ++t) acc += W[(long long)t * P + idx] * F[(long long)ef[t] * P + idx];
+    dst[idx] = acc;
+  }
+}
+
 // element type of an untyped work array: 0 float2, 1 double2, 2 double-float
 template <typename R> constexpr int elem_kind() { return sizeof(cx<R>) == 8 ? 0 : (sizeof(R) == 8 && sizeof(cx<R>) == 16 && !std::is_same<R, dfl>::value ? 1 : 2); }
 
@@ -2909,9 +2928,49 @@ void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, c
     }
   }
   const bool use_cache = cache && cache->W.p;
+  PGB_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)g.K * No2, st));
+  if (use_cache) {
+    // every output in one contraction launch and one batched backward
+    // transform, when their transforms fit beside the cache
+    if (cache->out_elems.empty()) {
+      std::vector<int> hef, htb(1, 0);
+      for (int e = 0; e < No2; ++e) {
+        if (p.delta[e].empty()) continue;
+        std::vector<BosonTerm> ht;
+        std::vector<int> he;
+        terms_of(e, ht, he);
+        hef.insert(hef.end(), he.begin(), he.end());
+        htb.push_back((int)hef.size());
+        cache->out_elems.push_back(e);
+      }
+      cache->ef.alloc(std::max<size_t>(1, hef.size()));
+      cache->ef.upload(hef.data(), hef.size());
+      cache->tb.alloc(htb.size());
+      cache->tb.upload(htb.data(), htb.size());
+      sync();
+    }
+    const int ne = (int)cache->out_elems.size();
+    if (ne > 0 && (size_t)ne * g.P * sizeof(cx<R>) < device_bytes_available() * 0.7) {
+      DBuf<cx<R>> TA((size_t)ne * g.P);
+      const unsigned tiles = (unsigned)std::min<long long>((g.P + 255) / 256, 65535);
+      k_contract_all<R><<<dim3((unsigned)ne, tiles), 256, 0, st>>>(TA.p, cache->W.p, FF.p, cache->ef.p,
+                                                                  cache->tb.p, g.P);
+      count_launch("contract_all");
+      fft.backward<R>(TA.p, ne, st);
+      for (int o = 0; o < ne; ++o) {
+        const int e = cache->out_elems[o];
+        k_scatter_out<<<mesh_tau_grid(g.Nk, g.Nw, 1), 256, 0, st>>>(out + (size_t)e * g.K, TA.p + (size_t)o * g.P,
+                                                                   elem_kind<R>(), g.irr_grid.p, g.Nkall, g.Nk,
+                                                                   g.Nw, scale, 0);
+        count_launch("scatter_delta");
+      }
+      sync();
+      hermitize(out, g.K, g.Norb);
+      return;
+    }
+  }
   DBuf<cx<R>> W, T(g.P);
   if (!use_cache) W.alloc(std::max<size_t>(1, maxt) * g.P);
-  PGB_CUDA(cudaMemsetAsync(out, 0, sizeof(double2) * (size_t)g.K * No2, st));
   for (int e = 0; e < No2; ++e) {
     if (p.delta[e].empty()) continue;
     std::vector<BosonTerm> ht;

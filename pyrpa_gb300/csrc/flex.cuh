@@ -132,6 +132,10 @@ template <typename R> struct DeltaKernelCache {
   bool built = false;
   DBuf<cx<R>> W;
   std::vector<long long> offset;  // first term of each output element
+  // the one-launch contraction: outputs with terms, their terms' F element
+  // and the first term of each (device)
+  std::vector<int> out_elems;
+  DBuf<int> ef, tb;
 };
 template <typename R>
 void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, const double* S,
