@@ -1046,11 +1046,36 @@ double eliash_core(Inputs& in, cx<R>* chi, const double2* G, const double* init,
       cache32 = std::make_unique<DeltaKernelCache<float>>();
     }
   }
+  // Double-float stage: F = -G Delta G^H in double-float too, from a
+  // double-float copy of G (PYRPA_GB_MKFK_DF=0 keeps the FP64 product)
+  std::unique_ptr<DBuf<cdf>> Gdf, Fdf;
+  if constexpr (std::is_same<R, dfl>::value) {
+    const char* e = std::getenv("PYRPA_GB_MKFK_DF");
+    std::vector<double> hprt(Norb);
+    PGB_CUDA(cudaMemcpyAsync(hprt.data(), prt, sizeof(double) * Norb, cudaMemcpyDeviceToHost, st));
+    sync();
+    bool signs = true;
+    for (double x : hprt) signs = signs && (x == 1.0 || x == -1.0);
+    if (!(e && std::string(e) == "0") && signs && Norb <= 5) {
+      Gdf = std::make_unique<DBuf<cdf>>((size_t)KE);
+      Fdf = std::make_unique<DBuf<cdf>>((size_t)KE);
+      convert<dfl, double>(Gdf->p, G, KE);
+    }
+  }
   auto apply_op = [&](double2* out, const double2* v) {
     ta.start();
-    mkfk(F.p, G, v, K, Norb);
-    if (chi32) mkdelta<float>(g, p, F.p, chi32->p, S.p, C.p, prt, singlet, scale, out, cache32.get());
-    else mkdelta<R>(g, p, F.p, chi, S.p, C.p, prt, singlet, scale, out, &cache);
+    if (chi32) {
+      mkfk(F.p, G, v, K, Norb);
+      mkdelta<float>(g, p, F.p, chi32->p, S.p, C.p, prt, singlet, scale, out, cache32.get());
+    } else if (Fdf) {
+      if constexpr (std::is_same<R, dfl>::value) {
+        PGB_CHECK(mkfk_df(Fdf->p, Gdf->p, v, K, Norb), "no double-float mkfk for this orbital count");
+        mkdelta<R>(g, p, nullptr, chi, S.p, C.p, prt, singlet, scale, out, &cache, Fdf->p);
+      }
+    } else {
+      mkfk(F.p, G, v, K, Norb);
+      mkdelta<R>(g, p, F.p, chi, S.p, C.p, prt, singlet, scale, out, &cache);
+    }
     g_stats.t_apply += ta.stop();
     g_stats.applies += 1;
   };

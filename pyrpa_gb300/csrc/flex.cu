@@ -489,6 +489,42 @@ __global__ void k_pad_anomalous(cx<R>* out, const double2* F, const int* grid_ir
   }
 }
 
+// The same padding from an anomalous function already in the bulk type
+// (the double-float F of the mixed Eliashberg stage).  The parity factors
+// are signs (prt = +-1, checked by the caller), applied as sign changes.
+template <typename R>
+__global__ void k_pad_anomalous_bulk(cx<R>* out, const cx<R>* F, const int* grid_irr, const int* grid_flag,
+                                     long long Nkall, int Nk, int Nw, int No, long long P, const double* prt,
+                                     double sgn, double dprt) {
+  const int e = blockIdx.y;
+  const int a = e % No, b = e / No;
+  const double pp = prt[a] * prt[b];
+  const bool neg_fl = pp * dprt < 0, neg_mirror = sgn * dprt * pp < 0, neg_sgn = sgn < 0;
+  cx<R>* o = out + (long long)e * P;
+  MeshTau q;
+  if (!mesh_tau(Nkall, 2LL * Nw, q)) return;
+  const long long gi = q.r;
+  const int k = grid_irr[gi], fl = grid_flag[gi];
+  for (int n = q.t0; n < q.t1; ++n) {
+    const long long idx = gi + Nkall * n;
+    cx<R> v;
+    if (n < Nw) {
+      v = F[fidx(k, n, a, b, Nk, Nw, No)];
+      if (fl && neg_fl) v = -v;
+    } else {
+      const int j = 2 * Nw - 1 - n;
+      if (!fl) {
+        v = conj(F[fidx(k, j, a, b, Nk, Nw, No)]);
+        if (neg_mirror) v = -v;
+      } else {
+        v = F[fidx(k, j, b, a, Nk, Nw, No)];
+        if (neg_sgn) v = -v;
+      }
+    }
+    o[idx] = v;
+  }
+}
+
 template <typename R>
 void pad_green_all(const Geom& g, const double2* G, cx<R>* out) {
   const int No2 = g.Norb * g.Norb;
@@ -2857,6 +2893,59 @@ void mkfk(double2* F, const double2* G, const double2* D, long long K, int Norb)
   count_launch("mkfk");
 }
 
+// F = -(G Delta) G^H in double-float for the double-float Eliashberg stage:
+// G already in double-float, Delta (the FP64 Arnoldi vector) converted once
+// per element; the products run on the FP32 pipe instead of the FP64 one
+template <int N>
+__global__ void k_mkfk_df(cdf* F, const cdf* G, const double2* D, long long K) {
+  for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
+       idx += (long long)gridDim.x * blockDim.x) {
+    cdf d[N * N];
+#pragma unroll
+    for (int b = 0; b < N; ++b)
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+        const double2 v = D[idx + K * (a + N * b)];
+        d[a * N + b] = mkc(dfl(v.x), dfl(v.y));
+      }
+#pragma unroll 1
+    for (int a = 0; a < N; ++a) {
+      cdf t[N];
+#pragma unroll
+      for (int b = 0; b < N; ++b) {
+        cdf acc = mkc(dfl(0.f), dfl(0.f));
+#pragma unroll
+        for (int c = 0; c < N; ++c) acc += G[idx + K * (a + N * c)] * d[c * N + b];
+        t[b] = acc;
+      }
+      for (int b = 0; b <= a; ++b) {
+        cdf acc = mkc(dfl(0.f), dfl(0.f));
+#pragma unroll
+        for (int c = 0; c < N; ++c) acc += t[c] * conj(G[idx + K * (b + N * c)]);
+        acc = -acc;
+        if (a == b) acc.y = dfl(0.f);
+        F[idx + K * (a + N * b)] = acc;
+        if (a != b) F[idx + K * (b + N * a)] = conj(acc);
+      }
+    }
+  }
+}
+
+// false: no double-float kernel for this orbital count (the caller uses mkfk)
+bool mkfk_df(cdf* F, const cdf* G, const double2* D, long long K, int Norb) {
+  const unsigned grid = grid_1d(K, 128, 65536);
+  switch (Norb) {
+    case 1: k_mkfk_df<1><<<grid, 128, 0, ctx().stream>>>(F, G, D, K); break;
+    case 2: k_mkfk_df<2><<<grid, 128, 0, ctx().stream>>>(F, G, D, K); break;
+    case 3: k_mkfk_df<3><<<grid, 128, 0, ctx().stream>>>(F, G, D, K); break;
+    case 4: k_mkfk_df<4><<<grid, 128, 0, ctx().stream>>>(F, G, D, K); break;
+    case 5: k_mkfk_df<5><<<grid, 128, 0, ctx().stream>>>(F, G, D, K); break;
+    default: return false;
+  }
+  count_launch("mkfk_df");
+  return true;
+}
+
 __global__ void k_hermitize(double2* D, long long K, int No) {
   for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < K;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -2873,14 +2962,20 @@ void hermitize(double2* D, long long K, int Norb) {
 
 template <typename R>
 void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, const double* S, const double* C,
-             const double* prt, bool singlet, double scale, double2* out, DeltaKernelCache<R>* cache) {
+             const double* prt, bool singlet, double scale, double2* out, DeltaKernelCache<R>* cache,
+             const cx<R>* Fbulk) {
   cudaStream_t st = ctx().stream;
   const FFT4D& fft = fft_plan(g.Nx, g.Ny, g.Nz, (int)g.M, (int)sizeof(cx<R>));
   const int No2 = g.Norb * g.Norb;
   const double sgn = singlet ? 1.0 : -1.0, dprt = singlet ? 1.0 : -1.0;
   DBuf<cx<R>> FF((size_t)No2 * g.P);
-  k_pad_anomalous<R><<<mesh_tau_grid(g.Nkall, g.M, No2), 256, 0, st>>>(FF.p, F, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, g.Norb, g.P,
-                                          prt, sgn, dprt);
+  if (Fbulk) {
+    k_pad_anomalous_bulk<R><<<mesh_tau_grid(g.Nkall, g.M, No2), 256, 0, st>>>(
+        FF.p, Fbulk, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, g.Norb, g.P, prt, sgn, dprt);
+  } else {
+    k_pad_anomalous<R><<<mesh_tau_grid(g.Nkall, g.M, No2), 256, 0, st>>>(
+        FF.p, F, g.grid_irr.p, g.grid_flag.p, g.Nkall, g.Nk, g.Nw, g.Norb, g.P, prt, sgn, dprt);
+  }
   count_launch("pad_anomalous");
   fft.forward<R>(FF.p, No2, st);
   std::vector<double> hS(g.Nchi * g.Nchi), hC(g.Nchi * g.Nchi);
@@ -3117,7 +3212,8 @@ template void convert<double, float>(double2*, const float2*, long long);
   template void sigma<R>(const Geom&, const Pairs&, const double2*, const cx<R>*, const double*,           \
                          const double*, double, double2*);                                                 \
   template void mkdelta<R>(const Geom&, const Pairs&, const double2*, const cx<R>*, const double*,         \
-                           const double*, const double*, bool, double, double2*, DeltaKernelCache<R>*);    \
+                           const double*, const double*, bool, double, double2*, DeltaKernelCache<R>*,     \
+                           const cx<R>*);                                                                  \
   template void widen<R>(double2*, const cx<R>*, long long);                                               \
   template void narrow<R>(cx<R>*, const double2*, long long);
 PGB_INST(float)
@@ -3131,7 +3227,7 @@ template void sigma<dfl>(const Geom&, const Pairs&, const double2*, const cx<dfl
 template void widen<dfl>(double2*, const cx<dfl>*, long long);
 template void narrow<dfl>(cx<dfl>*, const double2*, long long);
 template void mkdelta<dfl>(const Geom&, const Pairs&, const double2*, const cx<dfl>*, const double*, const double*,
-                           const double*, bool, double, double2*, DeltaKernelCache<dfl>*);
+                           const double*, bool, double, double2*, DeltaKernelCache<dfl>*, const cx<dfl>*);
 template bool vertex<dfl>(cx<dfl>*, long long, long long, int, const double*, const double*, int);
 
 }  // namespace pgb

@@ -137,10 +137,14 @@ template <typename R> struct DeltaKernelCache {
   std::vector<int> out_elems;
   DBuf<int> ef, tb;
 };
+// Fbulk: F already in the bulk type (then F is not read; the parity factors
+// prt must be +-1)
 template <typename R>
 void mkdelta(const Geom& g, const Pairs& p, const double2* F, const cx<R>* Vd, const double* S,
              const double* C, const double* prt, bool singlet, double scale, double2* out,
-             DeltaKernelCache<R>* cache);
+             DeltaKernelCache<R>* cache, const cx<R>* Fbulk = nullptr);
+// F = -(G Delta) G^H in double-float (Norb <= 5; false otherwise)
+bool mkfk_df(cdf* F, const cdf* G, const double2* D, long long K, int Norb);
 void hermitize(double2* D, long long K, int Norb);
 void initial_delta(double2* D, const double* init, const double2* uni, int Nk, int Nw, int Norb,
                    int gap_sym);
