@@ -164,7 +164,16 @@ __host__ __device__ __forceinline__ dfl operator/(dfl a, dfl b) {
 }
 __host__ __device__ __forceinline__ float mad(float a, float b, float c) { return fmaf(a, b, c); }
 __host__ __device__ __forceinline__ double mad(double a, double b, double c) { return fma(a, b, c); }
-__host__ __device__ __forceinline__ dfl mad(dfl a, dfl b, dfl c) { return a * b + c; }
+// a*b + c with one renormalization: the double-word product's high word and
+// error term go straight into Dekker's sum with c (15 flops against 18 for
+// the renormalized product plus the sum; same error bound, a few 2^-47)
+__host__ __device__ __forceinline__ dfl mad(dfl a, dfl b, dfl c) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  const dfl s = two_sum(p, c.hi);
+  return fast_two_sum(s.hi, s.lo + (e + c.lo));
+}
 __host__ __device__ __forceinline__ dfl cabs1(cdf a) { return dabs(a.x) + dabs(a.y); }
 __host__ __device__ __forceinline__ cdf cdiv(cdf a, cdf b) {  // same scaling as the double version
   const dfl s = dabs(b.x) + dabs(b.y);
