@@ -138,8 +138,21 @@ __host__ __device__ __forceinline__ cdf mkc(dfl a, dfl b) {
 __host__ __device__ __forceinline__ cdf operator+(cdf a, cdf b) { return mkc(a.x + b.x, a.y + b.y); }
 __host__ __device__ __forceinline__ cdf operator-(cdf a, cdf b) { return mkc(a.x - b.x, a.y - b.y); }
 __host__ __device__ __forceinline__ cdf operator-(cdf a) { return mkc(-a.x, -a.y); }
+// a*b + c*d as one double-word sum of the two double-word products, with one
+// renormalization (19 flops against 25 for two renormalized products and
+// Dekker's sum); the complex product's two components
+__host__ __device__ __forceinline__ dfl dot2(dfl a, dfl b, dfl c, dfl d) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  const float q = c.hi * d.hi;
+  float f = fmaf(c.hi, d.hi, -q);
+  f = fmaf(c.hi, d.lo, fmaf(c.lo, d.hi, f));
+  const dfl s = two_sum(p, q);
+  return fast_two_sum(s.hi, s.lo + (e + f));
+}
 __host__ __device__ __forceinline__ cdf operator*(cdf a, cdf b) {
-  return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return mkc(dot2(a.x, b.x, -a.y, b.y), dot2(a.x, b.y, a.y, b.x));
 }
 __host__ __device__ __forceinline__ cdf operator*(dfl s, cdf b) { return mkc(s * b.x, s * b.y); }
 __host__ __device__ __forceinline__ cdf operator*(cdf b, dfl s) { return mkc(s * b.x, s * b.y); }

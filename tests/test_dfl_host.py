@@ -25,7 +25,7 @@ int main() {
   std::normal_distribution<double> nd(0.0, 1.0);
   std::uniform_real_distribution<double> ue(-4.0, 4.0);
   auto draw = [&]() { return (long double)nd(rng) * expl((long double)ue(rng)); };
-  long double e_add = 0, e_mul = 0, e_mad = 0, e_div = 0, e_rcp32 = 0, e_rcp64 = 0, e_rcpdf = 0;
+  long double e_add = 0, e_mul = 0, e_mad = 0, e_div = 0, e_rcp32 = 0, e_rcp64 = 0, e_rcpdf = 0, e_cmul = 0;
   for (int i = 0; i < 200000; ++i) {
     const long double x = draw(), y = draw(), z = draw();
     const dfl a = mk(x), b = mk(y), c = mk(z);
@@ -46,10 +46,18 @@ int main() {
     cdf bd;
     bd.x = mk(u);
     bd.y = mk(v);
+    // complex product, normwise: |ab - exact| / (|a| |b|)
+    cdf ad;
+    ad.x = a;
+    ad.y = b;
+    const cdf pr = ad * bd;
+    const long double px = ax * ld(bd.x) - by * ld(bd.y), py = ax * ld(bd.y) + by * ld(bd.x);
+    e_cmul = fmaxl(e_cmul, hypotl(ld(pr.x) - px, ld(pr.y) - py) /
+                               (hypotl(ax, by) * hypotl(ld(bd.x), ld(bd.y))));
     const cdf rd = crecip(bd);
     e_rcpdf = fmaxl(e_rcpdf, hypotl(ld(rd.x) - rx, ld(rd.y) - ry) / rn);
   }
-  printf("%Le %Le %Le %Le %Le %Le %Le\n", e_add, e_mul, e_mad, e_div, e_rcp32, e_rcp64, e_rcpdf);
+  printf("%Le %Le %Le %Le %Le %Le %Le %Le\n", e_add, e_mul, e_mad, e_div, e_rcp32, e_rcp64, e_rcpdf, e_cmul);
   return 0;
 }
 '''
@@ -66,7 +74,7 @@ def errors(tmp_path_factory):
     subprocess.run([nvcc, "-std=c++17", "-O2", "-I", str(ROOT / "pyrpa_gb300" / "csrc"), str(d / "t.cu"), "-o",
                     str(exe)], check=True, capture_output=True, text=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
-    return dict(zip(["add", "mul", "mad", "div", "rcp32", "rcp64", "rcpdf"], map(float, out)))
+    return dict(zip(["add", "mul", "mad", "div", "rcp32", "rcp64", "rcpdf", "cmul"], map(float, out)))
 
 
 def test_double_float_sum_product_mad_division(errors):
@@ -76,6 +84,7 @@ def test_double_float_sum_product_mad_division(errors):
     assert errors["mul"] < 6 * u
     assert errors["mad"] < 8 * u       # one renormalization for the product and the sum
     assert errors["div"] < 12 * u
+    assert errors["cmul"] < 8 * u      # complex product: one sum of two double-word products a component
 
 
 def test_complex_reciprocals(errors):
