@@ -30,7 +30,7 @@ extern "C" {
 #endif
 
 /* ------------------------------------------------------------ setup --- */
-/* fmod.f90:7-20 openmp_params: reports no OpenMP (0, false) in this build */
+/* fmod.f90:7-20 openmp_params: reports no OpenMP (0, false); this library runs on the GPU */
 void openmp_params(int64_t* omp_num, bool* omp_check);
 /* finv.f90:1-290 generate_irr_kpoint_inv: klist(3,Nk), kmap(3,Nkall), invk(3,Nkall) */
 void generate_irr_kpoint_inv(double* klist, int64_t* kmap, int64_t* invk, const int64_t* Nk,

@@ -609,7 +609,7 @@ void pyrpa_gb_device_info(int64_t* num_sms, int64_t* device) {
 
 // ================================================================ setup ==
 void openmp_params(int64_t* omp_num, bool* omp_check) {
-  // no OpenMP in this build: the work runs on the GPU
+  // no OpenMP in this library: the work runs on the GPU
   *omp_num = 0;
   *omp_check = false;
 }

@@ -16,7 +16,7 @@ ABI, at sizes the NumPy oracle finishes in about a minute each:
   this model: a 1e-13 change of G moves the oracle's lambda by 3e-12) are
   compared at the FP64 tolerances, lambda to 1e-8.  The fused fast form
   (coarse-mesh warm start, mixed FP32 / double-float schedule) is held to the
-  spec accuracy, lambda within 1e-6 of the oracle's.
+  benchmark's accuracy target, lambda within 1e-6 of the oracle's.
 * a 4096-point axis: a 3-orbital 16x16 model with 2048 frequencies, FP64
   chi0 (tail-corrected) and two FLEX iterations.
 * 3-D with radix 3: a 2-orbital 6x6x6 model with 256 frequencies, mkself to
